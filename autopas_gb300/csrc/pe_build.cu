@@ -1,0 +1,488 @@
+// pe_build.cu -- device rebuild of the cluster structure and the cluster-pair lists.
+//
+// Replaces VerletClusterLists::rebuildNeighborLists (src/autopas/containers/verletClusterLists/
+// VerletClusterLists.h:779-800 -> VerletClusterListsRebuilder.h:67-409):
+//   1. tower index of every particle            (ClusterTowerBlock2D.h:220-245)       k_bin
+//   2. one-digit radix (counting) sort on tower  (histogram, scan, scatter)            k_bin, k_scatter
+//   3. per-tower order by z, tie by particle index (ClusterTower::generateClusters sorts by z,
+//      ClusterTower.h:83-143; here the order is made deterministic), padding to whole clusters
+//                                                                                       k_tower_sort
+//   4. cluster bounding boxes in FP64             (Cluster::getBoundingBox, Cluster.h:135-149) k_cluster_bbox
+//   5. cluster-pair lists: B joins A's list iff the FP64 box distance^2 <= (rc+skin)^2, never halo-halo,
+//      forward-only for newton3  (VerletClusterListsRebuilder.h:237-409)                k_list_build
+// Every pass is a streaming pass over HBM except the on-chip bitonic sort of each tower.
+#include "pe_state.cuh"
+
+#include <cstdio>
+
+namespace pe {
+
+// ---------------------------------------------------------------------------------------------
+// 1. tower index + z key + histogram
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int tower_coord(double p, const SysDev &S, int d) {
+  // ClusterTowerBlock2D::getTowerIndex2DAtPosition (ClusterTowerBlock2D.h:220-245); for a periodic system the
+  // grid has no halo towers and covers exactly the box.
+  long long t = (long long)floor((p - S.bmin[d]) * S.inv_side[d]) + S.halo_towers;
+  if (t < 0) t = 0;
+  if (t > S.nt[d] - 1) t = S.nt[d] - 1;
+  if (!S.periodic) {
+    if (p >= S.halo_hi[d])
+      t = S.nt[d] - 1;
+    else if (p < S.halo_lo[d])
+      t = 0;
+  }
+  return (int)t;
+}
+
+__global__ void k_bin(DeviceState s, int64_t nslots_old, uint64_t *__restrict__ key, int32_t *__restrict__ tower_of) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nslots_old) return;
+  if (s.own[i] == 0) {
+    tower_of[i] = -1;
+    return;
+  }
+  const SysDev &S = s.sysd[s.sys[i]];
+  const int tx = tower_coord(s.x[i], S, 0);
+  const int ty = tower_coord(s.y[i], S, 1);
+  const int t = S.tower_base + ty * S.nt[0] + tx;
+  tower_of[i] = t;
+  key[i] = dbl_key(s.z[i]);
+  atomicAdd(&s.tw_count[t], 1);
+}
+
+void launch_bin(DeviceState &s, int64_t nslots_old, uint64_t *key, int32_t *tower_of, cudaStream_t st) {
+  cudaMemsetAsync(s.tw_count, 0, sizeof(int32_t) * s.ntowers, st);
+  const int64_t nb = (nslots_old + 255) / 256;
+  if (nb > 0) k_bin<<<(unsigned)nb, 256, 0, st>>>(s, nslots_old, key, tower_of);
+}
+
+__global__ void k_ncl(const int32_t *__restrict__ cnt, int32_t *__restrict__ ncl, int64_t nt, int C) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < nt) ncl[t] = (cnt[t] + C - 1) / C;
+}
+
+void launch_clusters_per_tower(DeviceState &s, int32_t *ncl, cudaStream_t st) {
+  const int64_t nb = (s.ntowers + 255) / 256;
+  if (nb > 0) k_ncl<<<(unsigned)nb, 256, 0, st>>>(s.tw_count, ncl, s.ntowers, s.C);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 2. scatter into tower segments (order inside a segment is fixed by the sort that follows)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_scatter(DeviceState s, int64_t nslots_old, const int32_t *__restrict__ tower_of,
+                          const uint64_t *__restrict__ key, int32_t *__restrict__ fill, uint64_t *__restrict__ skey,
+                          int32_t *__restrict__ sval) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nslots_old) return;
+  const int t = tower_of[i];
+  if (t < 0) return;
+  const int p = s.tw_start[t] + atomicAdd(&fill[t], 1);
+  skey[p] = key[i];
+  sval[p] = (int32_t)i;
+}
+
+void launch_scatter(DeviceState &s, int64_t nslots_old, const int32_t *tower_of, const uint64_t *key, int32_t *fill,
+                    uint64_t *skey, int32_t *sval, cudaStream_t st) {
+  cudaMemsetAsync(fill, 0, sizeof(int32_t) * s.ntowers, st);
+  const int64_t nb = (nslots_old + 255) / 256;
+  if (nb > 0) k_scatter<<<(unsigned)nb, 256, 0, st>>>(s, nslots_old, tower_of, key, fill, skey, sval);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 3. per-tower bitonic sort on (z key, particle index), cluster padding, tower xy bbox
+// ---------------------------------------------------------------------------------------------
+__global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, const int32_t *__restrict__ sval,
+                             int32_t *__restrict__ perm_src, int p2) {
+  extern __shared__ unsigned char smem[];
+  uint64_t *k = reinterpret_cast<uint64_t *>(smem);
+  int32_t *tie = reinterpret_cast<int32_t *>(k + p2);
+  int32_t *val = tie + p2;
+  __shared__ double red[4][32];
+
+  const int t = blockIdx.x;
+  const int n = s.tw_count[t];
+  const int base = s.tw_start[t];
+  const int clb = s.tw_cl_start[t];
+  const int cle = s.tw_cl_start[t + 1];
+  if (n > kTowerSortMax || n > p2) {
+    if (threadIdx.x == 0) atomicOr(s.err, kErrTowerOverflow);
+    return;
+  }
+  double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  for (int q = threadIdx.x; q < p2; q += blockDim.x) {
+    if (q < n) {
+      const int32_t v = sval[base + q];
+      k[q] = skey[base + q];
+      tie[q] = s.orig[v];
+      val[q] = v;
+      const double px = s.x[v], py = s.y[v];
+      mnx = fmin(mnx, px);
+      mxx = fmax(mxx, px);
+      mny = fmin(mny, py);
+      mxy = fmax(mxy, py);
+    } else {
+      k[q] = ~0ull;
+      tie[q] = 0x7fffffff;
+      val[q] = -1;
+    }
+  }
+  // tower bbox: warp then block reduction
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fmin(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (l == 0) {
+    red[0][w] = mnx;
+    red[1][w] = mny;
+    red[2][w] = mxx;
+    red[3][w] = mxy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < nw; ++q) {
+      mnx = fmin(mnx, red[0][q]);
+      mny = fmin(mny, red[1][q]);
+      mxx = fmax(mxx, red[2][q]);
+      mxy = fmax(mxy, red[3][q]);
+    }
+    s.tw_bb[4 * t + 0] = mnx;
+    s.tw_bb[4 * t + 1] = mny;
+    s.tw_bb[4 * t + 2] = mxx;
+    s.tw_bb[4 * t + 3] = mxy;
+  }
+  // bitonic sort, ascending on (k, tie)
+  for (int size = 2; size <= p2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < (p2 >> 1); q += blockDim.x) {
+        const int lo = 2 * q - (q & (stride - 1));
+        const int hi = lo + stride;
+        const bool asc = ((lo & size) == 0);
+        const uint64_t ka = k[lo], kb = k[hi];
+        const int32_t ta = tie[lo], tb = tie[hi];
+        const bool gt = (ka > kb) || (ka == kb && ta > tb);
+        if (gt == asc) {
+          k[lo] = kb;
+          k[hi] = ka;
+          tie[lo] = tb;
+          tie[hi] = ta;
+          const int32_t vt = val[lo];
+          val[lo] = val[hi];
+          val[hi] = vt;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const int C = s.C;
+  const int nsl = (cle - clb) * C;
+  for (int q = threadIdx.x; q < nsl; q += blockDim.x) perm_src[(int64_t)clb * C + q] = q < n ? val[q] : -1;
+  for (int c = clb + threadIdx.x; c < cle; c += blockDim.x) s.cl_tower[c] = t;
+}
+
+int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *perm_src, int max_tower,
+                      cudaStream_t st) {
+  if (max_tower > kTowerSortMax) return -1;
+  int p2 = 2;
+  while (p2 < max_tower) p2 <<= 1;
+  const size_t sm = (size_t)p2 * (8 + 4 + 4);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_tower_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, kTowerSortMax * 16);
+    attr_set = true;
+  }
+  if (s.ntowers > 0) k_tower_sort<<<(unsigned)s.ntowers, 256, sm, st>>>(s, skey, sval, perm_src, p2);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// 4. cluster bounding boxes and flags
+// ---------------------------------------------------------------------------------------------
+__global__ void k_cluster_bbox(DeviceState s) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= s.nclusters) return;
+  const int C = s.C;
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  int flags = 0;
+  for (int q = 0; q < C; ++q) {
+    const int64_t i = c * C + q;
+    const int o = s.own[i];
+    if (o == 0) continue;
+    flags |= 2;
+    if (o == 1) flags |= 1;
+    const double p[3] = {s.x[i], s.y[i], s.z[i]};
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fmin(lo[d], p[d]);
+      hi[d] = fmax(hi[d], p[d]);
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    s.cl_bb[6 * c + d] = lo[d];
+    s.cl_bb[6 * c + 3 + d] = hi[d];
+  }
+  s.cl_flags[c] = flags;
+  s.cl_sys[c] = s.sys[c * C];
+}
+
+void launch_cluster_bbox(DeviceState &s, cudaStream_t st) {
+  const int64_t nb = (s.nclusters + 127) / 128;
+  if (nb > 0) k_cluster_bbox<<<(unsigned)nb, 128, 0, st>>>(s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 5. cluster-pair lists, one warp per i-cluster
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double gap1(double alo, double ahi, double blo, double bhi) {
+  // boxDistanceSquared per dimension (ArrayMath.h:697-707): max(0, aMin-bMax) and max(0, bMin-aMax)
+  const double g1 = alo - bhi;
+  const double g2 = blo - ahi;
+  return fmax(0.0, fmax(g1, g2));
+}
+
+constexpr int kListWarps = 4;
+
+__global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
+  extern __shared__ uint32_t lbuf[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t A = blockIdx.x * (int64_t)kListWarps + warp;
+  if (A >= s.nclusters) return;
+  uint32_t *buf = lbuf + warp * kListBufPerWarp;
+  const int flagsA = s.cl_flags[A];
+  const bool aOwned = flagsA & 1;
+  if (!aOwned && !s.newton3) {
+    if (lane == 0) {
+      s.cp_count[A] = 0;
+      s.cp_start[A] = 0;
+    }
+    return;
+  }
+  const SysDev &S = s.sysd[s.cl_sys[A]];
+  double alo[3], ahi[3];
+  for (int d = 0; d < 3; ++d) {
+    alo[d] = s.cl_bb[6 * A + d];
+    ahi[d] = s.cl_bb[6 * A + 3 + d];
+  }
+  const double L = s.cutoff + s.skin;
+  const double L2 = L * L * (1.0 + 1e-12);
+  const double Lz = L * (1.0 + 1e-12);
+  const int tloc = s.cl_tower[A] - S.tower_base;
+  const int tx = tloc % S.nt[0], ty = tloc / S.nt[0];
+  int cnt = 0;
+  bool overflow = false;
+  if (aOwned) {  // self entry: pairs inside A
+    if (lane == 0) buf[0] = ((uint32_t)A << 5) | kShiftNone;
+    cnt = 1;
+  }
+  const int zlo_s = S.periodic ? -1 : 0, zhi_s = S.periodic ? 1 : 0;
+  for (int dy = -S.ky; dy <= S.ky && !overflow; ++dy) {
+    for (int dx = -S.kx; dx <= S.kx && !overflow; ++dx) {
+      int nx = tx + dx, ny = ty + dy, sx = 0, sy = 0;
+      if (S.periodic) {
+        while (nx < 0) { nx += S.nt[0]; sx -= 1; }
+        while (nx >= S.nt[0]) { nx -= S.nt[0]; sx += 1; }
+        while (ny < 0) { ny += S.nt[1]; sy -= 1; }
+        while (ny >= S.nt[1]) { ny -= S.nt[1]; sy += 1; }
+        if (sx < -1 || sx > 1 || sy < -1 || sy > 1) continue;
+      } else if (nx < 0 || ny < 0 || nx >= S.nt[0] || ny >= S.nt[1]) {
+        continue;
+      }
+      const int tB = S.tower_base + ny * S.nt[0] + nx;
+      const int c0 = s.tw_cl_start[tB], c1 = s.tw_cl_start[tB + 1];
+      if (c0 == c1) continue;
+      const double shx = sx == 0 ? 0.0 : (sx > 0 ? S.len[0] : -S.len[0]);
+      const double shy = sy == 0 ? 0.0 : (sy > 0 ? S.len[1] : -S.len[1]);
+      {
+        const double gx = gap1(alo[0], ahi[0], s.tw_bb[4 * tB + 0] + shx, s.tw_bb[4 * tB + 2] + shx);
+        const double gy = gap1(alo[1], ahi[1], s.tw_bb[4 * tB + 1] + shy, s.tw_bb[4 * tB + 3] + shy);
+        if (gx * gx + gy * gy > L2) continue;
+      }
+      for (int sz = zlo_s; sz <= zhi_s && !overflow; ++sz) {
+        const double shz = sz == 0 ? 0.0 : (sz > 0 ? S.len[2] : -S.len[2]);
+        const double zmin = alo[2] - Lz - shz;  // candidates need hi.z >= zmin
+        const double zmax = ahi[2] + Lz - shz;  // and lo.z <= zmax
+        // first cluster with hi.z >= zmin (hi.z is non-decreasing inside a tower)
+        int a = c0, b = c1;
+        while (a < b) {
+          const int m = (a + b) >> 1;
+          if (s.cl_bb[6 * (int64_t)m + 5] < zmin)
+            a = m + 1;
+          else
+            b = m;
+        }
+        const int code = shift_code(sx, sy, sz);
+        for (int cb = a; cb < c1; cb += 32) {
+          const int c = cb + lane;
+          bool inrange = false, accept = false;
+          if (c < c1) {
+            const double blz = s.cl_bb[6 * (int64_t)c + 2];
+            inrange = blz <= zmax;
+            if (inrange) {
+              const bool self = (c == A && code == kShiftNone);
+              bool canon = true;
+              if (s.newton3) canon = (c > A) || (c == A && code > kShiftNone);
+              const int fb = s.cl_flags[c];
+              const bool haloHalo = !aOwned && !(fb & 1);
+              if (!self && canon && !haloHalo && (fb & 2)) {
+                const double g0 = gap1(alo[0], ahi[0], s.cl_bb[6 * (int64_t)c + 0] + shx, s.cl_bb[6 * (int64_t)c + 3] + shx);
+                const double g1 = gap1(alo[1], ahi[1], s.cl_bb[6 * (int64_t)c + 1] + shy, s.cl_bb[6 * (int64_t)c + 4] + shy);
+                const double g2 = gap1(alo[2], ahi[2], blz + shz, s.cl_bb[6 * (int64_t)c + 5] + shz);
+                accept = (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
+              }
+            }
+          }
+          const unsigned am = __ballot_sync(0xffffffffu, accept);
+          const unsigned rm = __ballot_sync(0xffffffffu, inrange);
+          const int na = __popc(am);
+          if (cnt + na > kListBufPerWarp) {
+            overflow = true;
+            break;
+          }
+          if (accept) buf[cnt + __popc(am & ((1u << lane) - 1))] = ((uint32_t)c << 5) | (uint32_t)code;
+          cnt += na;
+          if (rm != 0xffffffffu) break;  // some lane left the z window (or the tower): later ones are out too
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (overflow) {
+    if (lane == 0) {
+      atomicOr(s.err, kErrListOverflow);
+      s.cp_count[A] = 0;
+      s.cp_start[A] = 0;
+    }
+    return;
+  }
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(s.cp_total, (unsigned long long)cnt);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (base + cnt > (unsigned long long)s.cp_cap) {
+    if (lane == 0) {
+      atomicOr(s.err, kErrListCapacity);
+      s.cp_count[A] = 0;
+      s.cp_start[A] = 0;
+    }
+    return;
+  }
+  for (int q = lane; q < cnt; q += 32) s.cp_list[base + q] = buf[q];
+  if (lane == 0) {
+    s.cp_start[A] = (int64_t)base;
+    s.cp_count[A] = cnt;
+  }
+}
+
+void launch_list_build(DeviceState &s, cudaStream_t st) {
+  static bool attr_set = false;
+  const size_t sm = (size_t)kListWarps * kListBufPerWarp * sizeof(uint32_t);
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_list_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr_set = true;
+  }
+  cudaMemsetAsync(s.cp_total, 0, sizeof(unsigned long long), st);
+  const int64_t nb = (s.nclusters + kListWarps - 1) / kListWarps;
+  if (nb > 0) k_list_build<<<(unsigned)nb, kListWarps * 32, sm, st>>>(s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// pair-set dump (verification): the particle pairs covered by the lists, evaluated in FP64
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool image_exists(const SysDev &S, const double *p, int sx, int sy, int sz) {
+  // md-flexible halo collection (RegularGridDecomposition.cpp:486-531): an image +len exists for a
+  // coordinate in [min, min+rc+skin), an image -len for one in [max-rc-skin, max).
+  const int sv[3] = {sx, sy, sz};
+  for (int d = 0; d < 3; ++d) {
+    if (sv[d] > 0 && !(p[d] < S.img_left[d])) return false;
+    if (sv[d] < 0 && !(p[d] >= S.img_right[d])) return false;
+  }
+  return true;
+}
+
+__global__ void k_pair_dump(DeviceState s, int which, int64_t cap, int64_t *__restrict__ oa, int64_t *__restrict__ ob,
+                            int32_t *__restrict__ oc, unsigned long long *__restrict__ count) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + warp;
+  if (A >= s.nclusters) return;
+  const int C = s.C;
+  const int n = s.cp_count[A];
+  const int64_t st = s.cp_start[A];
+  const SysDev &S = s.sysd[s.cl_sys[A]];
+  const double L = s.cutoff + s.skin;
+  const double lim = which == 0 ? L * L : s.cutoff * s.cutoff;
+  for (int e = 0; e < n; ++e) {
+    const uint32_t ent = s.cp_list[st + e];
+    const int64_t B = ent >> 5;
+    const int code = ent & 31;
+    int sx, sy, sz;
+    shift_of(code, sx, sy, sz);
+    for (int q = lane; q < C * C; q += 32) {
+      const int ii = q / C, jj = q % C;
+      const int64_t i = A * C + ii, j = B * C + jj;
+      const int oi = s.own[i], oj = s.own[j];
+      if (oi == 0 || oj == 0) continue;
+      if (oi == 2 && oj == 2) continue;
+      const double pi[3] = {s.x[i], s.y[i], s.z[i]};
+      const double pj[3] = {s.x[j], s.y[j], s.z[j]};
+      if (code == kShiftNone) {
+        // each unordered pair once: from the lower cluster, or from the only cluster that has a list
+        const bool bHasList = s.newton3 || (s.cl_flags[B] & 1);
+        if (!(A < B || (A == B && ii < jj) || (A > B && !bHasList))) continue;
+        const double d2 = dist2_mode(pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2], s.dist_mode);
+        const bool in = which == 0 ? (d2 < lim) : (d2 <= lim);
+        if (!in) continue;
+        const unsigned long long k = atomicAdd(count, 1ull);
+        if (k < (unsigned long long)cap) {
+          const int64_t ga = s.orig[i], gb = s.orig[j];
+          oa[k] = ga < gb ? ga : gb;
+          ob[k] = ga < gb ? gb : ga;
+          oc[k] = kShiftNone;
+        }
+        continue;
+      }
+      // (i, image of j with shift s): the halo copy of j seen by owned i
+      if (oi == 1 && image_exists(S, pj, sx, sy, sz)) {
+        const double q0 = image_coord(pj[0], sx, S.len[0]);
+        const double q1 = image_coord(pj[1], sy, S.len[1]);
+        const double q2 = image_coord(pj[2], sz, S.len[2]);
+        const double d2 = dist2_mode(pi[0] - q0, pi[1] - q1, pi[2] - q2, s.dist_mode);
+        const bool in = which == 0 ? (d2 < lim) : (d2 <= lim);
+        if (in) {
+          const unsigned long long k = atomicAdd(count, 1ull);
+          if (k < (unsigned long long)cap) {
+            oa[k] = s.orig[i];
+            ob[k] = s.orig[j];
+            oc[k] = code;
+          }
+        }
+      }
+      // with half lists the reverse view (j, image of i with -s) comes from the same entry
+      if (s.newton3 && oj == 1 && image_exists(S, pi, -sx, -sy, -sz)) {
+        const double q0 = image_coord(pi[0], -sx, S.len[0]);
+        const double q1 = image_coord(pi[1], -sy, S.len[1]);
+        const double q2 = image_coord(pi[2], -sz, S.len[2]);
+        const double d2 = dist2_mode(pj[0] - q0, pj[1] - q1, pj[2] - q2, s.dist_mode);
+        const bool in = which == 0 ? (d2 < lim) : (d2 <= lim);
+        if (in) {
+          const unsigned long long k = atomicAdd(count, 1ull);
+          if (k < (unsigned long long)cap) {
+            oa[k] = s.orig[j];
+            ob[k] = s.orig[i];
+            oc[k] = shift_code(-sx, -sy, -sz);
+          }
+        }
+      }
+    }
+  }
+}
+
+void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
+                      unsigned long long *count, cudaStream_t st) {
+  cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  const int64_t nb = (s.nclusters + 3) / 4;
+  if (nb > 0) k_pair_dump<<<(unsigned)nb, 128, 0, st>>>(s, which, cap, a, b, code, count);
+}
+
+}  // namespace pe

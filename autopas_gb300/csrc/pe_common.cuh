@@ -1,0 +1,88 @@
+// pe_common.cuh -- shared device structures of the GB300 pair-force engine.
+//
+// Data layout in HBM (all arrays in "slot order" after a rebuild):
+//   slots are grouped by system, then tower (2D xy column), then z; every tower is padded with
+//   dummy slots to a multiple of the cluster size C, so cluster c owns slots [c*C, c*C+C).
+//   FP64 SoA:   x y z  vx vy vz  fx fy fz  ofx ofy ofz         (master state, 96 B/particle)
+//   int SoA:    type(int32) own(int8) sys(int32) orig(int32) id(int64)
+//   packed:     pk_hi / pk_lo (float4): the position as an unevaluated sum hi+lo of two floats in a fixed
+//               binade [B, 2B) per system (w of pk_hi carries type | ownership<<16), 32 B/particle,
+//               read by the mixed-precision force kernel.
+//   clusters:   bbox (6 doubles), system, tower, flags; cluster-pair list entries are uint32
+//               (jcluster << 5 | image-shift code), one contiguous run per i-cluster.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pe {
+
+constexpr int kShiftNone = 13;      // code of the zero image shift ((0+1) + 3*(0+1) + 9*(0+1))
+constexpr int kMaxTypes = 16;       // type-table bound held in shared memory by the kernels
+constexpr int kTowerSortMax = 4096; // particles per tower sorted on chip
+constexpr int kListBufPerWarp = 2048;
+
+enum DeviceError : int {
+  kErrNone = 0,
+  kErrListOverflow = 1,   // a cluster list exceeded kListBufPerWarp entries
+  kErrListCapacity = 2,   // the global list buffer is too small (host regrows and retries)
+  kErrTowerOverflow = 4,  // a tower holds more than kTowerSortMax particles
+};
+
+// Per-system constants (device copy).
+struct SysDev {
+  double bmin[3], bmax[3], len[3];
+  double grid_lo[2];    // xy origin of tower (0,0)
+  double side[2];       // tower side length
+  double inv_side[2];   // 1/side
+  double halo_lo[2], halo_hi[2];  // halo box in xy (non-periodic), used by the tower-index sanity clamp
+  double img_left[3];   // image +len exists iff x <  bmin + rc + skin
+  double img_right[3];  // image -len exists iff x >= bmax - rc - skin
+  int nt[2];            // towers per dim
+  int halo_towers;      // towers added on each side (non-periodic) = towers per interaction length
+  int kx, ky;           // neighbour tower reach per dim (ceil(L/side))
+  int periodic;
+  int tower_base;       // first global tower index
+  // mixed-precision encoding: x' = (x - enc_o) + B in [B, 2B); len split as hi (multiple of ulp(B)) + lo
+  double enc_o[3];
+  double enc_B;
+  float len_hi[3], len_lo[3];
+};
+
+struct TypeTable {
+  int ntypes;
+  double eps24[kMaxTypes * kMaxTypes];
+  double sig2[kMaxTypes * kMaxTypes];
+  double shift6[kMaxTypes * kMaxTypes];
+};
+
+__host__ __device__ inline int shift_code(int sx, int sy, int sz) { return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1); }
+__host__ __device__ inline void shift_of(int code, int &sx, int &sy, int &sz) {
+  sx = code % 3 - 1;
+  sy = (code / 3) % 3 - 1;
+  sz = code / 9 - 1;
+}
+
+// FP64 squared distance with the selected contraction.  The explicit __dmul_rn/__dadd_rn/__fma_rn
+// intrinsics keep nvcc from fusing or reordering, so the bits equal those of the host expression.
+__device__ __forceinline__ double dist2_mode(double dx, double dy, double dz, int mode) {
+  if (mode == 1) return __fma_rn(dz, dz, __fma_rn(dx, dx, __dmul_rn(dy, dy)));
+  if (mode == 2) return __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// Position of the periodic image of x with shift s in {-1,0,1}: x + len or x + (-len), one rounding,
+// as md-flexible forms its halo copies (RegularGridDecomposition.cpp:219-228, 524-528).
+__device__ __forceinline__ double image_coord(double x, int s, double len) {
+  return s == 0 ? x : __dadd_rn(x, s > 0 ? len : -len);
+}
+
+// Monotone map of a double onto uint64 (for sorting by z).
+__device__ __forceinline__ uint64_t dbl_key(double v) {
+  uint64_t b = (uint64_t)__double_as_longlong(v);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// ---- launch wrappers implemented in the .cu files (all asynchronous on `st`) ----
+struct BuildArgs;  // defined in pe_engine.cu
+}  // namespace pe

@@ -1,0 +1,1019 @@
+// pe_engine.cu -- engine object, memory management, integrator kernels and the C ABI (include/pairengine.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pairengine.h"
+#include "pe_state.cuh"
+
+using namespace pe;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------------------------
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  bool ensure(size_t n) {
+    if (n <= cap && p) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    if (cudaMalloc(&p, want * sizeof(T)) != cudaSuccess) {
+      p = nullptr;
+      return false;
+    }
+    cap = want;
+    return true;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct ParticleArrays {
+  DBuf<double> x, y, z, vx, vy, vz, fx, fy, fz, ofx, ofy, ofz;
+  DBuf<int32_t> type, sys, orig;
+  DBuf<int8_t> own;
+  DBuf<int64_t> id;
+  bool ensure(size_t n) {
+    return x.ensure(n) && y.ensure(n) && z.ensure(n) && vx.ensure(n) && vy.ensure(n) && vz.ensure(n) &&
+           fx.ensure(n) && fy.ensure(n) && fz.ensure(n) && ofx.ensure(n) && ofy.ensure(n) && ofz.ensure(n) &&
+           type.ensure(n) && sys.ensure(n) && orig.ensure(n) && own.ensure(n) && id.ensure(n);
+  }
+  void release() {
+    x.release(); y.release(); z.release(); vx.release(); vy.release(); vz.release();
+    fx.release(); fy.release(); fz.release(); ofx.release(); ofy.release(); ofz.release();
+    type.release(); sys.release(); orig.release(); own.release(); id.release();
+  }
+  void bind(DeviceState &s) {
+    s.x = x.p; s.y = y.p; s.z = z.p; s.vx = vx.p; s.vy = vy.p; s.vz = vz.p;
+    s.fx = fx.p; s.fy = fy.p; s.fz = fz.p; s.ofx = ofx.p; s.ofy = ofy.p; s.ofz = ofz.p;
+    s.type = type.p; s.sys = sys.p; s.orig = orig.p; s.own = own.p; s.id = id.p;
+  }
+};
+
+struct SysHost {
+  pe_system_desc desc;
+  int64_t count = 0;  // real particles of this system
+  SysDev dev;
+  int64_t ntowers = 0;
+};
+
+}  // namespace
+
+struct pe_engine {
+  pe_config cfg;
+  std::vector<double> eps, sig, mass;
+  std::vector<SysHost> sys;
+  TypeTable table;
+  cudaStream_t st = nullptr;
+  int device = 0;
+  int C = 8;
+  int newton3 = 0;
+  int precision = PE_PRECISION_MIXED;
+  std::string err;
+
+  ParticleArrays A, Bk;  // current and gather target
+  DBuf<float4> pk_hi, pk_lo;
+  DBuf<int32_t> slot_of;
+  int64_t nuser = 0;     // particles of the last set_particles
+  int64_t nslots = 0;
+  int64_t pcap = 0;
+  bool have_particles = false;
+  bool lists_valid = false;
+  int steps_since_rebuild = 0;
+  bool forces_valid = false;
+
+  // towers / clusters
+  int64_t ntowers = 0, nclusters = 0;
+  DBuf<int32_t> tw_count, tw_start, tw_cl_start, tw_ncl, tw_fill;
+  DBuf<double> tw_bb;
+  DBuf<double> cl_bb;
+  DBuf<int32_t> cl_sys, cl_tower, cl_flags, cp_count;
+  DBuf<int64_t> cp_start;
+  DBuf<uint32_t> cp_list;
+  DBuf<unsigned long long> cp_total;
+  DBuf<double> cl_glob;
+  DBuf<unsigned long long> cl_hits;
+  DBuf<double> sys_glob;
+  DBuf<long long> sys_hits;
+  DBuf<int64_t> sys_cl_range;
+  DBuf<int32_t> sys_tower_base;
+  int64_t max_tower = 0;
+  int64_t num_cluster_pairs = 0;
+
+  // rebuild temporaries
+  DBuf<uint64_t> key, skey;
+  DBuf<int32_t> tower_of, sval, perm_src;
+  DBuf<int> derr;
+  DBuf<int> dmax;
+
+  // parameters on the device
+  DBuf<SysDev> sysd;
+  DBuf<TypeTable> types;
+  DBuf<double> dmass;
+
+  // transfer temporaries (user order)
+  DBuf<double> tmp3;
+  DBuf<int64_t> dump_a, dump_b;
+  DBuf<int32_t> dump_c;
+  DBuf<unsigned long long> dump_n;
+
+  // timing
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> force_ev;  // (start, end) indices into ev_pool
+  int ev_used = 0;
+  int64_t launches = 0;
+  int64_t force_launches = 0;
+
+  DeviceState state() {
+    DeviceState s;
+    s.nslots = nslots;
+    s.nreal = nuser;
+    A.bind(s);
+    s.pk_hi = pk_hi.p;
+    s.pk_lo = pk_lo.p;
+    s.slot_of = slot_of.p;
+    s.nsys = (int)sys.size();
+    s.ntowers = ntowers;
+    s.nclusters = nclusters;
+    s.C = C;
+    s.tw_count = tw_count.p;
+    s.tw_start = tw_start.p;
+    s.tw_cl_start = tw_cl_start.p;
+    s.tw_bb = tw_bb.p;
+    s.cl_bb = cl_bb.p;
+    s.cl_sys = cl_sys.p;
+    s.cl_tower = cl_tower.p;
+    s.cl_flags = cl_flags.p;
+    s.cp_start = cp_start.p;
+    s.cp_count = cp_count.p;
+    s.cp_list = cp_list.p;
+    s.cp_cap = (int64_t)cp_list.cap;
+    s.cp_total = cp_total.p;
+    s.newton3 = newton3;
+    s.sysd = sysd.p;
+    s.types = types.p;
+    s.mass = dmass.p;
+    s.cutoff = cfg.cutoff;
+    s.skin = cfg.skin;
+    s.dist_mode = cfg.dist_mode;
+    s.ntypes = table.ntypes;
+    s.cl_glob = cl_glob.p;
+    s.cl_hits = cl_hits.p;
+    s.sys_glob = sys_glob.p;
+    s.sys_hits = sys_hits.p;
+    s.err = derr.p;
+    return s;
+  }
+
+  int fail(int code, const char *fmt, ...) {
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    err = b;
+    return code;
+  }
+  int cuda_check(const char *where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(PE_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+    return PE_OK;
+  }
+  cudaEvent_t ev() {
+    if (ev_used == (int)ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+};
+
+#define PE_TRY(call)                      \
+  do {                                    \
+    int _rc = (call);                     \
+    if (_rc != PE_OK) return _rc;         \
+  } while (0)
+
+#define PE_CUDA(h, call)                                                                  \
+  do {                                                                                    \
+    cudaError_t _e = (call);                                                              \
+    if (_e != cudaSuccess) return (h)->fail(PE_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------------------------
+namespace pe {
+
+__global__ void k_scan_block(const int32_t *__restrict__ in, int32_t *__restrict__ out, int32_t *__restrict__ bsum,
+                             int64_t n) {
+  // exclusive scan of 1024-element tiles (256 threads x 4)
+  __shared__ int32_t sh[1024];
+  const int64_t base = blockIdx.x * 1024ll;
+  for (int q = threadIdx.x; q < 1024; q += 256) sh[q] = (base + q < n) ? in[base + q] : 0;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    int32_t v[4];
+    for (int r = 0; r < 4; ++r) {
+      const int q = threadIdx.x + 256 * r;
+      v[r] = q >= off ? sh[q - off] : 0;
+    }
+    __syncthreads();
+    for (int r = 0; r < 4; ++r) sh[threadIdx.x + 256 * r] += v[r];
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < 1024; q += 256) {
+    if (base + q < n) out[base + q] = sh[q] - ((base + q < n) ? in[base + q] : 0);
+  }
+  if (threadIdx.x == 0) bsum[blockIdx.x] = sh[1023];
+}
+
+__global__ void k_scan_add(int32_t *__restrict__ out, const int32_t *__restrict__ boff, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] += boff[i / 1024];
+}
+
+__global__ void k_set_total(int32_t *__restrict__ out, const int32_t *__restrict__ in, int64_t n) {
+  // out[n] = out[n-1] + in[n-1]
+  if (n > 0)
+    out[n] = out[n - 1] + in[n - 1];
+  else
+    out[0] = 0;
+}
+
+}  // namespace pe
+
+void pe::scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t st) {
+  // recursive tile scan; out must hold n+1 entries (out[n] = total)
+  if (n <= 0) {
+    cudaMemsetAsync(out, 0, sizeof(int32_t), st);
+    return;
+  }
+  const int64_t nb = (n + 1023) / 1024;
+  int32_t *bsum = nullptr, *boff = nullptr;
+  cudaMallocAsync(&bsum, sizeof(int32_t) * (nb + 1), st);
+  cudaMallocAsync(&boff, sizeof(int32_t) * (nb + 1), st);
+  k_scan_block<<<(unsigned)nb, 256, 0, st>>>(in, out, bsum, n);
+  if (nb > 1) {
+    scan_exclusive_i32(bsum, boff, nb, st);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, boff, n);
+  }
+  k_set_total<<<1, 1, 0, st>>>(out, in, n);
+  cudaFreeAsync(bsum, st);
+  cudaFreeAsync(boff, st);
+}
+
+namespace pe {
+
+// upload: user order -> slots 0..n-1
+__global__ void k_init_slots(DeviceState s, int64_t n, int has_type, int has_own, int has_id, int has_sys) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!has_type) s.type[i] = 0;
+  if (!has_own) s.own[i] = 1;
+  if (!has_id) s.id[i] = i;
+  if (!has_sys) s.sys[i] = 0;
+  s.orig[i] = (int32_t)i;
+  s.slot_of[i] = (int32_t)i;
+  s.fx[i] = s.fy[i] = s.fz[i] = 0;
+  s.ofx[i] = s.ofy[i] = s.ofz[i] = 0;
+}
+
+// periodic wrap of a coordinate that left the box (RegularGridDecomposition.cpp:555-590)
+__device__ __forceinline__ double wrap1(double x, double lo, double hi) {
+  const double len = hi - lo;
+  if (x < lo) {
+    const double p = x + len;
+    const double just = nextafter(hi, lo);
+    return p < just ? p : just;
+  }
+  if (x >= hi) {
+    const double p = x - len;
+    return lo > p ? lo : p;
+  }
+  return x;
+}
+
+__global__ void k_wrap(DeviceState s, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n || s.own[i] == 0) return;
+  const SysDev &S = s.sysd[s.sys[i]];
+  if (!S.periodic) return;
+  s.x[i] = wrap1(s.x[i], S.bmin[0], S.bmax[0]);
+  s.y[i] = wrap1(s.y[i], S.bmin[1], S.bmax[1]);
+  s.z[i] = wrap1(s.z[i], S.bmin[2], S.bmax[2]);
+}
+
+__device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) {
+  const int o = s.own[i];
+  const SysDev &S = s.sysd[s.sys[i]];
+  const double p[3] = {s.x[i], s.y[i], s.z[i]};
+  float h[3], l[3];
+  for (int d = 0; d < 3; ++d) {
+    const double xp = (p[d] - S.enc_o[d]) + S.enc_B;
+    h[d] = (float)xp;
+    l[d] = (float)(xp - (double)h[d]);
+  }
+  const int w = (s.type[i] & 0xffff) | (o << 16);
+  s.pk_hi[i] = make_float4(h[0], h[1], h[2], __int_as_float(w));
+  s.pk_lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
+__global__ void k_pack(DeviceState s, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) pack_one(s, i);
+}
+
+// gather into the new slot order; dummies fill the cluster padding
+__global__ void k_gather(DeviceState src, DeviceState dst, const int32_t *__restrict__ perm_src, int64_t nnew) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nnew) return;
+  const int32_t p = perm_src[q];
+  if (p >= 0) {
+    dst.x[q] = src.x[p]; dst.y[q] = src.y[p]; dst.z[q] = src.z[p];
+    dst.vx[q] = src.vx[p]; dst.vy[q] = src.vy[p]; dst.vz[q] = src.vz[p];
+    dst.fx[q] = src.fx[p]; dst.fy[q] = src.fy[p]; dst.fz[q] = src.fz[p];
+    dst.ofx[q] = src.ofx[p]; dst.ofy[q] = src.ofy[p]; dst.ofz[q] = src.ofz[p];
+    dst.type[q] = src.type[p]; dst.sys[q] = src.sys[p]; dst.own[q] = src.own[p];
+    dst.id[q] = src.id[p];
+    const int32_t o = src.orig[p];
+    dst.orig[q] = o;
+    dst.slot_of[o] = (int32_t)q;
+  } else {
+    // dummy: same system as the first slot of its cluster (always a real particle), parked far outside
+    const int64_t first = (q / dst.C) * dst.C;
+    const int32_t pf = perm_src[first];
+    const int32_t sy = src.sys[pf];
+    const SysDev &S = dst.sysd[sy];
+    dst.x[q] = S.bmin[0] - 1.0e4;
+    dst.y[q] = S.bmin[1] - 1.0e4;
+    dst.z[q] = S.bmin[2] - 1.0e4;
+    dst.vx[q] = dst.vy[q] = dst.vz[q] = 0;
+    dst.fx[q] = dst.fy[q] = dst.fz[q] = 0;
+    dst.ofx[q] = dst.ofy[q] = dst.ofz[q] = 0;
+    dst.type[q] = 0;
+    dst.sys[q] = sy;
+    dst.own[q] = 0;
+    dst.id[q] = -1;
+    dst.orig[q] = -1;
+  }
+}
+
+__global__ void k_max_i32(const int32_t *__restrict__ a, int64_t n, int *__restrict__ out) {
+  int m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, a[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int32_t *__restrict__ tower_base,
+                             int nsys, int64_t *__restrict__ range) {
+  const int sy = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sy >= nsys) return;
+  range[2 * sy] = tw_cl_start[tower_base[sy]];
+  range[2 * sy + 1] = tw_cl_start[tower_base[sy + 1]];
+}
+
+// velocity-Verlet position half (TimeDiscretization.cpp:17-66 with globalForce 0) fused with the re-encode
+__global__ void k_positions(DeviceState s, double dt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.nslots) return;
+  if (s.own[i] == 1) {
+    const double m = s.mass[s.type[i]];
+    const double c = __ddiv_rn(__dmul_rn(dt, dt), __dmul_rn(2.0, m));
+    const double fx = s.fx[i], fy = s.fy[i], fz = s.fz[i];
+    // displacement = v*dt + F*(dt*dt/(2m)), every operation rounded as written in the reference
+    s.x[i] = __dadd_rn(s.x[i], __dadd_rn(__dmul_rn(s.vx[i], dt), __dmul_rn(fx, c)));
+    s.y[i] = __dadd_rn(s.y[i], __dadd_rn(__dmul_rn(s.vy[i], dt), __dmul_rn(fy, c)));
+    s.z[i] = __dadd_rn(s.z[i], __dadd_rn(__dmul_rn(s.vz[i], dt), __dmul_rn(fz, c)));
+    s.ofx[i] = fx;
+    s.ofy[i] = fy;
+    s.ofz[i] = fz;
+    s.fx[i] = 0;
+    s.fy[i] = 0;
+    s.fz[i] = 0;
+  }
+  pack_one(s, i);
+}
+
+// velocity half when it is not fused into the force kernel
+__global__ void k_velocities(DeviceState s, double dt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.nslots || s.own[i] != 1) return;
+  const double m = s.mass[s.type[i]];
+  const double h = __ddiv_rn(dt, __dmul_rn(2.0, m));
+  s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(s.fx[i], s.ofx[i]), h));
+  s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(s.fy[i], s.ofy[i]), h));
+  s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(s.fz[i], s.ofz[i]), h));
+}
+
+// user-order extraction of a slot array
+__global__ void k_to_user(const double *__restrict__ a, const int32_t *__restrict__ slot_of,
+                          const int8_t *__restrict__ own, int only_owned, int64_t n, double *__restrict__ out) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int32_t q = slot_of[u];
+  out[u] = (only_owned && own[q] != 1) ? 0.0 : a[q];
+}
+
+__global__ void k_from_user(double *__restrict__ a, const int32_t *__restrict__ slot_of, int64_t n,
+                            const double *__restrict__ in) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u < n) a[slot_of[u]] = in[u];
+}
+
+}  // namespace pe
+
+// ---------------------------------------------------------------------------------------------
+// host-side geometry
+// ---------------------------------------------------------------------------------------------
+static double next_pow2(double v) {
+  double b = 1.0;
+  while (b < v) b *= 2.0;
+  return b;
+}
+
+// ClusterTowerBlock2D::estimateOptimalGridSideLength (ClusterTowerBlock2D.h:140-168) and resize() (:89-108).
+// A periodic system gets a grid that tiles exactly its box (no halo towers: images come from shifts).
+static void compute_grid(SysHost &S, int C, double L, int64_t count) {
+  SysDev &d = S.dev;
+  const double box[3] = {S.desc.box_max[0] - S.desc.box_min[0], S.desc.box_max[1] - S.desc.box_min[1],
+                         S.desc.box_max[2] - S.desc.box_min[2]};
+  for (int q = 0; q < 3; ++q) {
+    d.bmin[q] = S.desc.box_min[q];
+    d.bmax[q] = S.desc.box_max[q];
+    d.len[q] = box[q];
+  }
+  int64_t owned[2];
+  if (count == 0) {
+    for (int q = 0; q < 2; ++q) {
+      d.side[q] = box[q];
+      owned[q] = 1;
+    }
+  } else {
+    const double volume = box[0] * box[1] * box[2];
+    const double density = (double)count / volume;
+    const double opt = std::cbrt((double)C / density);
+    for (int q = 0; q < 2; ++q) {
+      const double no = std::ceil(box[q] / opt);
+      d.side[q] = box[q] / no;
+      owned[q] = (int64_t)no;
+    }
+  }
+  int h = 0;
+  for (int q = 0; q < 2; ++q) h = std::max(h, (int)std::ceil(L / d.side[q]));
+  d.periodic = S.desc.periodic;
+  for (int q = 0; q < 2; ++q) {
+    d.inv_side[q] = 1. / d.side[q];
+    if (d.periodic) {
+      d.nt[q] = (int)owned[q];
+    } else if (count == 0) {
+      d.nt[q] = 3;
+    } else {
+      d.nt[q] = (int)(owned[q] + (int64_t)std::ceil(L / d.side[q]) * 2);
+    }
+    d.halo_lo[q] = d.bmin[q] - L;
+    d.halo_hi[q] = d.bmax[q] + L;
+  }
+  d.halo_towers = d.periodic ? 0 : h;
+  for (int q = 0; q < 2; ++q) d.grid_lo[q] = d.bmin[q] - d.side[q] * d.halo_towers;
+  d.kx = (int)std::ceil(L / d.side[0]);
+  d.ky = (int)std::ceil(L / d.side[1]);
+  S.ntowers = (int64_t)d.nt[0] * d.nt[1];
+}
+
+static void compute_encoding(SysHost &S, double cutoff, double skin) {
+  SysDev &d = S.dev;
+  const double L = cutoff + skin;
+  for (int q = 0; q < 3; ++q) {
+    // image thresholds of md-flexible's halo collection (RegularGridDecomposition.cpp:188-196, 512-531)
+    d.img_left[q] = d.bmin[q] + cutoff + skin;
+    d.img_right[q] = d.bmax[q] - cutoff - skin;
+  }
+  const double M = L + 2.0;
+  double ext = 0;
+  for (int q = 0; q < 3; ++q) ext = std::max(ext, d.len[q]);
+  // x' = (x - o) + B must stay in [0, 2B) for x in [bmin - M, bmax + M] and for x' +- len (image shifts)
+  const double B = next_pow2(2.0 * ext + 2.0 * M + 4.0);
+  d.enc_B = B;
+  const double ulp = std::ldexp(B, -23);
+  for (int q = 0; q < 3; ++q) {
+    d.enc_o[q] = d.bmin[q] - M;
+    const double hi = std::nearbyint(d.len[q] / ulp) * ulp;  // a multiple of ulp(B): exact in float
+    d.len_hi[q] = (float)hi;
+    d.len_lo[q] = (float)(d.len[q] - hi);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// engine operations
+// ---------------------------------------------------------------------------------------------
+static int setup_grids(pe_engine *h) {
+  const double L = h->cfg.cutoff + h->cfg.skin;
+  int64_t base = 0;
+  std::vector<int32_t> tbase;
+  for (auto &S : h->sys) {
+    compute_grid(S, h->C, L, S.count);
+    compute_encoding(S, h->cfg.cutoff, h->cfg.skin);
+    if (S.desc.periodic) {
+      for (int q = 0; q < 3; ++q)
+        if (S.dev.len[q] < 2 * L)
+          return h->fail(PE_ERR_DOMAIN, "periodic box length %g in dim %d is shorter than 2*(rc+skin) = %g",
+                         S.dev.len[q], q, 2 * L);
+    }
+    S.dev.tower_base = (int)base;
+    tbase.push_back((int32_t)base);
+    base += S.ntowers;
+  }
+  tbase.push_back((int32_t)base);
+  h->ntowers = base;
+  std::vector<SysDev> sd;
+  for (auto &S : h->sys) sd.push_back(S.dev);
+  if (!h->sysd.ensure(sd.size()) || !h->sys_tower_base.ensure(tbase.size()))
+    return h->fail(PE_ERR_OOM, "system tables");
+  PE_CUDA(h, cudaMemcpyAsync(h->sysd.p, sd.data(), sizeof(SysDev) * sd.size(), cudaMemcpyHostToDevice, h->st));
+  PE_CUDA(h, cudaMemcpyAsync(h->sys_tower_base.p, tbase.data(), sizeof(int32_t) * tbase.size(),
+                             cudaMemcpyHostToDevice, h->st));
+  const size_t nt = (size_t)h->ntowers;
+  if (!h->tw_count.ensure(nt) || !h->tw_start.ensure(nt + 1) || !h->tw_cl_start.ensure(nt + 1) ||
+      !h->tw_ncl.ensure(nt) || !h->tw_fill.ensure(nt) || !h->tw_bb.ensure(4 * nt))
+    return h->fail(PE_ERR_OOM, "tower arrays (%lld towers)", (long long)nt);
+  // slot capacity: every tower can add at most C-1 padding dummies
+  h->pcap = h->nuser + (int64_t)nt * (h->C - 1) + 64;
+  return PE_OK;
+}
+
+static int ensure_particle_capacity(pe_engine *h) {
+  const size_t n = (size_t)h->pcap;
+  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pk_hi.ensure(n) || !h->pk_lo.ensure(n) ||
+      !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
+    return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
+  const size_t ncl = n / h->C + 1;
+  if (!h->cl_bb.ensure(6 * ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
+      !h->cp_count.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(4 * ncl) ||
+      !h->cl_hits.ensure(ncl) || !h->key.ensure(n) || !h->skey.ensure(n) || !h->tower_of.ensure(n) ||
+      !h->sval.ensure(n) || !h->perm_src.ensure(n) || !h->cp_total.ensure(1) || !h->derr.ensure(1) ||
+      !h->dmax.ensure(1) || !h->sys_glob.ensure(5 * h->sys.size()) || !h->sys_hits.ensure(h->sys.size()) ||
+      !h->sys_cl_range.ensure(2 * h->sys.size()))
+    return h->fail(PE_ERR_OOM, "cluster arrays");
+  return PE_OK;
+}
+
+static int do_rebuild(pe_engine *h) {
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "rebuild before pe_set_particles");
+  cudaStream_t st = h->st;
+  DeviceState s = h->state();
+  const int64_t nold = h->nslots;
+  h->launches += 1;
+  if (nold > 0) k_wrap<<<(unsigned)((nold + 255) / 256), 256, 0, st>>>(s, nold);
+  PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
+  launch_bin(s, nold, h->key.p, h->tower_of.p, st);
+  scan_exclusive_i32(h->tw_count.p, h->tw_start.p, h->ntowers, st);
+  launch_clusters_per_tower(s, h->tw_ncl.p, st);
+  scan_exclusive_i32(h->tw_ncl.p, h->tw_cl_start.p, h->ntowers, st);
+  PE_CUDA(h, cudaMemsetAsync(h->dmax.p, 0, sizeof(int), st));
+  if (h->ntowers > 0) k_max_i32<<<64, 256, 0, st>>>(h->tw_count.p, h->ntowers, h->dmax.p);
+  h->launches += 10;
+  int32_t total_cl = 0;
+  int maxt = 0;
+  PE_CUDA(h, cudaMemcpyAsync(&total_cl, h->tw_cl_start.p + h->ntowers, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  PE_CUDA(h, cudaMemcpyAsync(&maxt, h->dmax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PE_CUDA(h, cudaStreamSynchronize(st));
+  PE_TRY(h->cuda_check("binning"));
+  if (maxt > kTowerSortMax)
+    return h->fail(PE_ERR_TOWER_OVERFLOW, "a tower holds %d particles; the on-chip tower sort supports %d", maxt,
+                   kTowerSortMax);
+  h->max_tower = maxt;
+  h->nclusters = total_cl;
+  const int64_t nnew = (int64_t)total_cl * h->C;
+  if (nnew > h->pcap) return h->fail(PE_ERR_STATE, "slot capacity exceeded (%lld > %lld)", (long long)nnew,
+                                     (long long)h->pcap);
+  s = h->state();
+  launch_scatter(s, nold, h->tower_of.p, h->key.p, h->tw_fill.p, h->skey.p, h->sval.p, st);
+  if (launch_tower_sort(s, h->skey.p, h->sval.p, h->perm_src.p, std::max(maxt, 1), st) != 0)
+    return h->fail(PE_ERR_TOWER_OVERFLOW, "tower too large");
+  // gather into the second buffer set, then swap
+  DeviceState dst = s;
+  h->Bk.bind(dst);
+  dst.nslots = nnew;
+  if (nnew > 0) k_gather<<<(unsigned)((nnew + 255) / 256), 256, 0, st>>>(s, dst, h->perm_src.p, nnew);
+  std::swap(h->A, h->Bk);
+  h->nslots = nnew;
+  s = h->state();
+  if (nnew > 0) k_pack<<<(unsigned)((nnew + 255) / 256), 256, 0, st>>>(s, nnew);
+  launch_cluster_bbox(s, st);
+  h->launches += 5;
+  // cluster-pair lists (grow the buffer and retry when it is too small)
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    if (h->cp_list.cap == 0) {
+      const int64_t est = std::max<int64_t>(h->nclusters * (h->newton3 ? 48 : 96), 1024);
+      if (!h->cp_list.ensure((size_t)est)) return h->fail(PE_ERR_OOM, "cluster-pair list (%lld)", (long long)est);
+    }
+    s = h->state();
+    PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
+    launch_list_build(s, st);
+    h->launches += 1;
+    int e = 0;
+    unsigned long long tot = 0;
+    PE_CUDA(h, cudaMemcpyAsync(&e, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaMemcpyAsync(&tot, h->cp_total.p, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaStreamSynchronize(st));
+    PE_TRY(h->cuda_check("list build"));
+    if (e & kErrTowerOverflow) return h->fail(PE_ERR_TOWER_OVERFLOW, "tower overflow in sort");
+    if (e & kErrListOverflow)
+      return h->fail(PE_ERR_LIST_OVERFLOW, "a cluster list exceeded %d entries", kListBufPerWarp);
+    if (e & kErrListCapacity) {
+      const size_t want = (size_t)(tot * 1.25) + 1024;
+      h->cp_list.release();
+      if (!h->cp_list.ensure(want)) return h->fail(PE_ERR_OOM, "cluster-pair list (%zu)", want);
+      continue;
+    }
+    h->num_cluster_pairs = (int64_t)tot;
+    if (h->num_cluster_pairs * 2 + 1024 < (int64_t)h->cp_list.cap / 4) {
+      // keep the buffer within 4x of need
+    }
+    break;
+  }
+  const int ns = (int)h->sys.size();
+  k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
+  h->launches += 1;
+  PE_TRY(h->cuda_check("rebuild"));
+  h->lists_valid = true;
+  h->steps_since_rebuild = 0;
+  return PE_OK;
+}
+
+static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
+  DeviceState s = h->state();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int i0 = -1;
+  if (timed) {
+    i0 = h->ev_used;
+    e0 = h->ev();
+    e1 = h->ev();
+    cudaEventRecord(e0, h->st);
+  }
+  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st);
+  if (timed) {
+    cudaEventRecord(e1, h->st);
+    h->force_ev.push_back({i0, i0 + 1});
+  }
+  h->launches += 1;
+  h->force_launches += 1;
+  if (h->cfg.calc_globals) {
+    launch_reduce_globals_range(s, h->sys_cl_range.p, h->st);
+    h->launches += 1;
+  }
+  h->steps_since_rebuild += 1;
+  h->forces_valid = true;
+  return h->cuda_check("force kernel");
+}
+
+static int read_globals(pe_engine *h, pe_globals *g) {
+  if (!g) return PE_OK;
+  const int ns = (int)h->sys.size();
+  std::vector<double> v(5 * ns);
+  std::vector<long long> hits(ns);
+  if (h->cfg.calc_globals) {
+    PE_CUDA(h, cudaMemcpyAsync(v.data(), h->sys_glob.p, sizeof(double) * 5 * ns, cudaMemcpyDeviceToHost, h->st));
+    PE_CUDA(h, cudaMemcpyAsync(hits.data(), h->sys_hits.p, sizeof(long long) * ns, cudaMemcpyDeviceToHost, h->st));
+  }
+  PE_CUDA(h, cudaStreamSynchronize(h->st));
+  for (int q = 0; q < ns; ++q) {
+    g[q].upot = v[5 * q];
+    g[q].virial = v[5 * q + 1];
+    g[q].virial_xyz[0] = v[5 * q + 2];
+    g[q].virial_xyz[1] = v[5 * q + 3];
+    g[q].virial_xyz[2] = v[5 * q + 4];
+    g[q].num_pairs = h->cfg.calc_globals ? hits[q] : -1;
+  }
+  return PE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *systems, pe_engine **out) {
+  if (!out) return PE_ERR_ARG;
+  *out = nullptr;
+  if (!cfg || num_systems < 1 || !systems) return PE_ERR_ARG;
+  if (cfg->num_types < 1 || cfg->num_types > kMaxTypes || !cfg->epsilon || !cfg->sigma || !cfg->mass)
+    return PE_ERR_ARG;
+  if (!(cfg->cutoff > 0) || !(cfg->skin >= 0)) return PE_ERR_ARG;
+  if (cfg->precision != PE_PRECISION_FP64 && cfg->precision != PE_PRECISION_MIXED) return PE_ERR_ARG;
+  if (cfg->cluster_size != 0 && cfg->cluster_size != 4 && cfg->cluster_size != 8) return PE_ERR_ARG;
+  if (cfg->dist_mode < 0 || cfg->dist_mode > 2) return PE_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PE_ERR_NO_DEVICE;
+  pe_engine *h = new pe_engine();
+  h->cfg = *cfg;
+  h->eps.assign(cfg->epsilon, cfg->epsilon + cfg->num_types);
+  h->sig.assign(cfg->sigma, cfg->sigma + cfg->num_types);
+  h->mass.assign(cfg->mass, cfg->mass + cfg->num_types);
+  h->cfg.epsilon = h->eps.data();
+  h->cfg.sigma = h->sig.data();
+  h->cfg.mass = h->mass.data();
+  h->C = cfg->cluster_size == 0 ? 8 : cfg->cluster_size;
+  h->newton3 = cfg->newton3 == 1 ? 1 : 0;
+  h->precision = cfg->precision;
+  cudaGetDevice(&h->device);
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return PE_ERR_CUDA;
+  }
+  // ParticlePropertiesLibrary::calculateMixingCoefficients (ParticlePropertiesLibrary.h:444-473, 576-582)
+  TypeTable &t = h->table;
+  memset(&t, 0, sizeof t);
+  t.ntypes = cfg->num_types;
+  const double c2 = cfg->cutoff * cfg->cutoff;
+  for (int a = 0; a < t.ntypes; ++a)
+    for (int b = 0; b < t.ntypes; ++b) {
+      const int k = a * t.ntypes + b;
+      t.eps24[k] = 24 * std::sqrt(h->eps[a] * h->eps[b]);
+      const double sg = (h->sig[a] + h->sig[b]) / 2.0;
+      t.sig2[k] = sg * sg;
+      if (cfg->apply_shift) {
+        const double s2 = t.sig2[k] / c2;
+        const double s6 = s2 * s2 * s2;
+        t.shift6[k] = t.eps24[k] * (s6 - s6 * s6);
+      } else {
+        t.shift6[k] = 0.;
+      }
+    }
+  h->sys.resize(num_systems);
+  for (int q = 0; q < num_systems; ++q) {
+    h->sys[q].desc = systems[q];
+    for (int d = 0; d < 3; ++d)
+      if (!(systems[q].box_max[d] > systems[q].box_min[d])) {
+        pe_destroy(h);
+        return PE_ERR_ARG;
+      }
+  }
+  if (!h->types.ensure(1) || !h->dmass.ensure(t.ntypes)) {
+    pe_destroy(h);
+    return PE_ERR_OOM;
+  }
+  cudaMemcpy(h->types.p, &t, sizeof t, cudaMemcpyHostToDevice);
+  cudaMemcpy(h->dmass.p, h->mass.data(), sizeof(double) * t.ntypes, cudaMemcpyHostToDevice);
+  *out = h;
+  return PE_OK;
+}
+
+int pe_destroy(pe_engine *h) {
+  if (!h) return PE_ERR_ARG;
+  if (h->st) cudaStreamSynchronize(h->st);
+  h->A.release();
+  h->Bk.release();
+  for (auto *b : {&h->pk_hi, &h->pk_lo}) b->release();
+  for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
+                  &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
+                  &h->dump_c})
+    b->release();
+  for (auto *b : {&h->tw_bb, &h->cl_bb, &h->cl_glob, &h->sys_glob, &h->dmass, &h->tmp3}) b->release();
+  for (auto *b : {&h->cp_start, &h->sys_cl_range, &h->dump_a, &h->dump_b}) b->release();
+  h->cp_list.release();
+  h->cp_total.release();
+  h->cl_hits.release();
+  h->dump_n.release();
+  h->sys_hits.release();
+  h->key.release();
+  h->skey.release();
+  h->derr.release();
+  h->dmax.release();
+  h->sysd.release();
+  h->types.release();
+  for (auto e : h->ev_pool) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return PE_OK;
+}
+
+const char *pe_last_error(const pe_engine *h) { return h ? h->err.c_str() : "null engine"; }
+
+int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, const double *z, const double *vx,
+                     const double *vy, const double *vz, const int32_t *type, const int8_t *ownership,
+                     const int64_t *id, const int32_t *system) {
+  if (!h) return PE_ERR_ARG;
+  if (n < 0 || (n > 0 && (!x || !y || !z))) return h->fail(PE_ERR_ARG, "positions required");
+  if (n > (int64_t)0x3fffffff) return h->fail(PE_ERR_ARG, "too many particles (%lld)", (long long)n);
+  const int ns = (int)h->sys.size();
+  for (auto &S : h->sys) S.count = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int sy = system ? system[i] : 0;
+    if (sy < 0 || sy >= ns) return h->fail(PE_ERR_ARG, "particle %lld has system %d", (long long)i, sy);
+    if (type && (type[i] < 0 || type[i] >= h->table.ntypes))
+      return h->fail(PE_ERR_ARG, "particle %lld has type %d", (long long)i, type[i]);
+    if (ownership && (ownership[i] < 0 || ownership[i] > 2))
+      return h->fail(PE_ERR_ARG, "particle %lld has ownership %d", (long long)i, ownership[i]);
+    if (ownership && ownership[i] == PE_DUMMY) continue;
+    h->sys[sy].count++;
+  }
+  h->nuser = n;
+  PE_TRY(setup_grids(h));
+  PE_TRY(ensure_particle_capacity(h));
+  cudaStream_t st = h->st;
+  const size_t b8 = sizeof(double) * n;
+  if (n > 0) {
+    PE_CUDA(h, cudaMemcpyAsync(h->A.x.p, x, b8, cudaMemcpyHostToDevice, st));
+    PE_CUDA(h, cudaMemcpyAsync(h->A.y.p, y, b8, cudaMemcpyHostToDevice, st));
+    PE_CUDA(h, cudaMemcpyAsync(h->A.z.p, z, b8, cudaMemcpyHostToDevice, st));
+    if (vx && vy && vz) {
+      PE_CUDA(h, cudaMemcpyAsync(h->A.vx.p, vx, b8, cudaMemcpyHostToDevice, st));
+      PE_CUDA(h, cudaMemcpyAsync(h->A.vy.p, vy, b8, cudaMemcpyHostToDevice, st));
+      PE_CUDA(h, cudaMemcpyAsync(h->A.vz.p, vz, b8, cudaMemcpyHostToDevice, st));
+    } else {
+      PE_CUDA(h, cudaMemsetAsync(h->A.vx.p, 0, b8, st));
+      PE_CUDA(h, cudaMemsetAsync(h->A.vy.p, 0, b8, st));
+      PE_CUDA(h, cudaMemsetAsync(h->A.vz.p, 0, b8, st));
+    }
+    if (type) PE_CUDA(h, cudaMemcpyAsync(h->A.type.p, type, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    if (ownership) PE_CUDA(h, cudaMemcpyAsync(h->A.own.p, ownership, n, cudaMemcpyHostToDevice, st));
+    if (id) PE_CUDA(h, cudaMemcpyAsync(h->A.id.p, id, sizeof(int64_t) * n, cudaMemcpyHostToDevice, st));
+    if (system) PE_CUDA(h, cudaMemcpyAsync(h->A.sys.p, system, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    h->nslots = n;
+    DeviceState s = h->state();
+    k_init_slots<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, n, type != nullptr, ownership != nullptr,
+                                                               id != nullptr, system != nullptr);
+    k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, n);
+  }
+  h->nslots = n;
+  h->have_particles = true;
+  h->lists_valid = false;
+  h->forces_valid = false;
+  PE_CUDA(h, cudaStreamSynchronize(st));
+  return h->cuda_check("set_particles");
+}
+
+int pe_update_positions(pe_engine *h, const double *x, const double *y, const double *z) {
+  if (!h || !x || !y || !z) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  const int64_t n = h->nuser;
+  if (!h->tmp3.ensure(3 * (size_t)std::max<int64_t>(n, 1))) return h->fail(PE_ERR_OOM, "tmp");
+  cudaStream_t st = h->st;
+  const double *src[3] = {x, y, z};
+  double *dst[3] = {h->A.x.p, h->A.y.p, h->A.z.p};
+  for (int d = 0; d < 3; ++d) {
+    PE_CUDA(h, cudaMemcpyAsync(h->tmp3.p + d * n, src[d], sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    if (n > 0) k_from_user<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dst[d], h->slot_of.p, n, h->tmp3.p + d * n);
+  }
+  DeviceState s = h->state();
+  if (h->nslots > 0) k_pack<<<(unsigned)((h->nslots + 255) / 256), 256, 0, st>>>(s, h->nslots);
+  PE_CUDA(h, cudaStreamSynchronize(st));
+  return h->cuda_check("update_positions");
+}
+
+int pe_rebuild(pe_engine *h) {
+  if (!h) return PE_ERR_ARG;
+  return do_rebuild(h);
+}
+
+int pe_compute_forces(pe_engine *h, pe_globals *globals) {
+  if (!h) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "compute before pe_set_particles");
+  if (!h->lists_valid) PE_TRY(do_rebuild(h));
+  PE_TRY(force_eval(h, false, 0.0, true));
+  return read_globals(h, globals);
+}
+
+int pe_get_forces(pe_engine *h, double *fx, double *fy, double *fz) {
+  if (!h) return PE_ERR_ARG;
+  if (!h->forces_valid) return h->fail(PE_ERR_STATE, "no forces computed");
+  const int64_t n = h->nuser;
+  if (!h->tmp3.ensure(3 * (size_t)std::max<int64_t>(n, 1))) return h->fail(PE_ERR_OOM, "tmp");
+  double *outs[3] = {fx, fy, fz};
+  const double *src[3] = {h->A.fx.p, h->A.fy.p, h->A.fz.p};
+  for (int d = 0; d < 3; ++d) {
+    if (!outs[d] || n == 0) continue;
+    k_to_user<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(src[d], h->slot_of.p, h->A.own.p, 1, n,
+                                                                 h->tmp3.p + d * n);
+    PE_CUDA(h, cudaMemcpyAsync(outs[d], h->tmp3.p + d * n, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  }
+  PE_CUDA(h, cudaStreamSynchronize(h->st));
+  return h->cuda_check("get_forces");
+}
+
+int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, double *vy, double *vz) {
+  if (!h) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  const int64_t n = h->nuser;
+  if (!h->tmp3.ensure(3 * (size_t)std::max<int64_t>(n, 1))) return h->fail(PE_ERR_OOM, "tmp");
+  double *outs[6] = {x, y, z, vx, vy, vz};
+  const double *src[6] = {h->A.x.p, h->A.y.p, h->A.z.p, h->A.vx.p, h->A.vy.p, h->A.vz.p};
+  for (int d = 0; d < 6; ++d) {
+    if (!outs[d] || n == 0) continue;
+    k_to_user<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(src[d], h->slot_of.p, h->A.own.p, 0, n,
+                                                                 h->tmp3.p + (d % 3) * n);
+    PE_CUDA(h, cudaMemcpyAsync(outs[d], h->tmp3.p + (d % 3) * n, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    PE_CUDA(h, cudaStreamSynchronize(h->st));
+  }
+  return h->cuda_check("get_state");
+}
+
+int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals) {
+  if (!h || nsteps < 0) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "step before pe_set_particles");
+  if (!h->forces_valid) return h->fail(PE_ERR_STATE, "pe_step needs the forces of the current positions first");
+  const int freq = std::max(1, h->cfg.rebuild_frequency);
+  for (int k = 0; k < nsteps; ++k) {
+    DeviceState s = h->state();
+    if (h->nslots > 0) k_positions<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, dt);
+    h->launches += 1;
+    if (!h->lists_valid || h->steps_since_rebuild >= freq) PE_TRY(do_rebuild(h));
+    PE_TRY(force_eval(h, true, dt, true));
+  }
+  PE_TRY(h->cuda_check("step"));
+  if (globals) return read_globals(h, globals);
+  return PE_OK;
+}
+
+int pe_get_info(pe_engine *h, pe_info *info) {
+  if (!h || !info) return PE_ERR_ARG;
+  info->cluster_size = h->C;
+  info->newton3 = h->newton3;
+  info->precision = h->precision;
+  info->num_particles = h->nuser;
+  info->num_slots = h->nslots;
+  info->num_clusters = h->nclusters;
+  info->num_towers = h->ntowers;
+  info->num_cluster_pairs = h->num_cluster_pairs;
+  info->max_tower_size = h->max_tower;
+  return PE_OK;
+}
+
+int pe_get_tower_grid(pe_engine *h, int system, double *side, int64_t *num, int64_t *halo, double *origin) {
+  if (!h || system < 0 || system >= (int)h->sys.size()) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  const SysDev &d = h->sys[system].dev;
+  for (int q = 0; q < 2; ++q) {
+    if (side) side[q] = d.side[q];
+    if (num) num[q] = d.nt[q];
+    if (origin) origin[q] = d.grid_lo[q];
+  }
+  if (halo) *halo = d.halo_towers;
+  return PE_OK;
+}
+
+int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code, int64_t *count) {
+  if (!h || !count || cap < 0 || (cap > 0 && (!a || !b || !code))) return PE_ERR_ARG;
+  if (!h->lists_valid) PE_TRY(do_rebuild(h));
+  const size_t c = (size_t)std::max<int64_t>(cap, 1);
+  if (!h->dump_a.ensure(c) || !h->dump_b.ensure(c) || !h->dump_c.ensure(c) || !h->dump_n.ensure(1))
+    return h->fail(PE_ERR_OOM, "pair dump buffers");
+  DeviceState s = h->state();
+  launch_pair_dump(s, which, cap, h->dump_a.p, h->dump_b.p, h->dump_c.p, h->dump_n.p, h->st);
+  unsigned long long n = 0;
+  PE_CUDA(h, cudaMemcpyAsync(&n, h->dump_n.p, sizeof n, cudaMemcpyDeviceToHost, h->st));
+  PE_CUDA(h, cudaStreamSynchronize(h->st));
+  *count = (int64_t)n;
+  const int64_t m = std::min<int64_t>((int64_t)n, cap);
+  if (m > 0) {
+    PE_CUDA(h, cudaMemcpy(a, h->dump_a.p, sizeof(int64_t) * m, cudaMemcpyDeviceToHost));
+    PE_CUDA(h, cudaMemcpy(b, h->dump_b.p, sizeof(int64_t) * m, cudaMemcpyDeviceToHost));
+    PE_CUDA(h, cudaMemcpy(code, h->dump_c.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
+  }
+  return h->cuda_check("pair_set");
+}
+
+int pe_get_kernel_time(pe_engine *h, int reset, double *force_ms, int64_t *force_launches, double *total_ms,
+                       int64_t *total_launches) {
+  if (!h) return PE_ERR_ARG;
+  PE_CUDA(h, cudaStreamSynchronize(h->st));
+  double fm = 0;
+  for (auto &pr : h->force_ev) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev_pool[pr.first], h->ev_pool[pr.second]);
+    fm += ms;
+  }
+  if (force_ms) *force_ms = fm;
+  if (force_launches) *force_launches = h->force_launches;
+  if (total_ms) *total_ms = 0;
+  if (total_launches) *total_launches = h->launches;
+  if (reset) {
+    h->force_ev.clear();
+    h->ev_used = 0;
+    h->force_launches = 0;
+    h->launches = 0;
+  }
+  return PE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,383 @@
+// pe_force.cu -- Lennard-Jones cluster-pair force kernels and the globals reduction.
+//
+// Replaces the VCL traversal's SoAFunctorSingle / SoAFunctorPair calls on cluster views
+// (src/autopas/containers/verletClusterLists/traversals/VCLClusterFunctor.h:38-89) with the LJ arithmetic of
+// applicationLibrary/molecularDynamics/molecularDynamicsLibrary/LJFunctor.h:204-559 and the globals of
+// LJFunctor.h:641-720.
+//
+// Work decomposition: one warp per i-cluster.  lane = ii + C*jl with ii the i-particle (C of them) and
+// jl in [0, 32/C) a j-lane; the warp walks the i-cluster's list as a flat sequence of j-particles,
+// 32/C of them per step, so all lanes of a step read the same j-cluster (coalesced / broadcast loads).
+//
+//  * full lists (newton3 off): every pair is evaluated from both sides; the i-force is accumulated in
+//    registers (compensated FP32 for the mixed form) and written once -- no atomics, deterministic.
+//  * half lists (newton3 on): the j-force of a step is reduced across the C i-lanes with warp shuffles
+//    and added to j with one FP32 atomic per component per j.
+//
+// Precision forms:
+//  * FP64 ("plain FP64 GPU form"): positions, displacements and LJ arithmetic in FP64 with the reference's
+//    operation order; per-pair forces are bit-identical to LJFunctor's (strict evaluation).
+//  * MIXED: positions are stored as hi+lo float pairs inside one binade [B,2B) per system so that the
+//    hi difference is exact and the displacement is rounded once to FP32; the LJ arithmetic is FP32 and the
+//    i-force sum is Kahan-compensated.  Pairs within 2e-6 (relative) of the cutoff repeat the cutoff test in
+//    FP64 so that the interacting set equals the FP64 one.
+#include "pe_state.cuh"
+
+namespace pe {
+
+struct ForceArgs {
+  double rc2;
+  float rc2f;
+  double dt;
+  int fuse_velocity;
+  int calc_globals;
+};
+
+// Reciprocal: hardware approximation refined by one Newton-Raphson step r' = r + r(1 - x r).
+__device__ __forceinline__ float rcp_nr(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  const float e = fmaf(-x, r, 1.0f);
+  return fmaf(r, e, r);
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &c, float v) {
+  const float y = v - c;
+  const float t = sum + y;
+  c = (t - sum) - y;
+  sum = t;
+}
+
+// exact FP64 cutoff test of pair (i, image of j with shift code) -- used near the cutoff only
+__device__ __noinline__ bool exact_within(const DeviceState &s, const SysDev &S, int64_t i, int64_t j, int code,
+                                          double rc2) {
+  int sx, sy, sz;
+  shift_of(code, sx, sy, sz);
+  const double dx = s.x[i] - image_coord(s.x[j], sx, S.len[0]);
+  const double dy = s.y[i] - image_coord(s.y[j], sy, S.len[1]);
+  const double dz = s.z[i] - image_coord(s.z[j], sz, S.len[2]);
+  return dist2_mode(dx, dy, dz, s.dist_mode) <= rc2;
+}
+
+// ---------------------------------------------------------------------------------------------
+// mixed precision, full lists
+// ---------------------------------------------------------------------------------------------
+template <int C, bool GLOB, bool ONE_TYPE>
+__global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs fa) {
+  constexpr int JL = 32 / C;
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  const int T = s.types->ntypes;
+  if (!ONE_TYPE) {
+    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
+      tab[0][q] = (float)s.types->eps24[q];
+      tab[1][q] = (float)s.types->sig2[q];
+      tab[2][q] = (float)s.types->shift6[q];
+    }
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (A >= s.nclusters) return;
+  const int n = s.cp_count[A];
+  if (n == 0) return;
+  const int64_t lst = s.cp_start[A];
+  const int ii = lane % C, jl = lane / C;
+  const int64_t i = A * C + ii;
+  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const int wi = __float_as_int(hi_i.w);
+  const int ti = wi & 0xffff, oi = wi >> 16;
+  const SysDev &S = s.sysd[s.cl_sys[A]];
+  const float lhx = S.len_hi[0], lhy = S.len_hi[1], lhz = S.len_hi[2];
+  const float llx = S.len_lo[0], lly = S.len_lo[1], llz = S.len_lo[2];
+  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
+  if (ONE_TYPE) {
+    eps24 = (float)s.types->eps24[0];
+    sig2 = (float)s.types->sig2[0];
+    sh6 = (float)s.types->shift6[0];
+  }
+  const float rc2f = fa.rc2f;
+  const float nearband = rc2f * 2e-6f;
+
+  float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
+  float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+  int hits2 = 0;
+  const int total = n * C;
+#pragma unroll 2
+  for (int t = jl; t < total; t += JL) {
+    const int e = t / C, jj = t % C;
+    const uint32_t ent = __ldg(&s.cp_list[lst + e]);
+    const int64_t B = ent >> 5;
+    const int code = ent & 31;
+    const int64_t j = B * C + jj;
+    const float4 hj = __ldg(&s.pk_hi[j]);
+    const float4 lj = __ldg(&s.pk_lo[j]);
+    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+    if (code != kShiftNone) {
+      // the j image sits at x_j + s*len; shifting i by -s*len instead keeps the hi part exact
+      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      xh = fmaf(-sxf, lhx, xh);
+      yh = fmaf(-syf, lhy, yh);
+      zh = fmaf(-szf, lhz, zh);
+      xl = fmaf(-sxf, llx, xl);
+      yl = fmaf(-syf, lly, yl);
+      zl = fmaf(-szf, llz, zl);
+    }
+    const float dx = (xh - hj.x) + (xl - lj.x);
+    const float dy = (yh - hj.y) + (yl - lj.y);
+    const float dz = (zh - hj.z) + (zl - lj.z);
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const int wj = __float_as_int(hj.w);
+    const int oj = wj >> 16;
+    const bool valid = (oj != 0) && !(B == A && code == kShiftNone && jj == ii);
+    bool within = r2 <= rc2f;
+    if (valid && fabsf(r2 - rc2f) <= nearband) within = exact_within(s, S, i, j, code, fa.rc2);
+    const bool mask = valid && within;
+    if (!ONE_TYPE) {
+      const int k = ti * T + (wj & 0xffff);
+      eps24 = tab[0][k];
+      sig2 = tab[1][k];
+      sh6 = tab[2][k];
+    }
+    const float inv = rcp_nr(r2);
+    const float lj2 = sig2 * inv;
+    const float lj6 = lj2 * lj2 * lj2;
+    const float lj12 = lj6 * lj6;
+    const float lj12m6 = lj12 - lj6;
+    float fac = eps24 * (lj12 + lj12m6) * inv;
+    fac = mask ? fac : 0.f;
+    kahan_add(fxs, fxc, dx * fac);
+    kahan_add(fys, fyc, dy * fac);
+    kahan_add(fzs, fzc, dz * fac);
+    if (GLOB) {
+      pot += mask ? (eps24 * lj12m6 + sh6) : 0.f;
+      vx = fmaf(dx * fac, dx, vx);
+      vy = fmaf(dy * fac, dy, vy);
+      vz = fmaf(dz * fac, dz, vz);
+      hits2 += mask ? (oj == 1 ? 1 : 2) : 0;
+    }
+  }
+  // combine the j-lanes of each i (lanes ii, ii+C, ii+2C, ...) in FP64
+  double Fx = (double)fxs - (double)fxc, Fy = (double)fys - (double)fyc, Fz = (double)fzs - (double)fzc;
+#pragma unroll
+  for (int o = C; o < 32; o <<= 1) {
+    Fx += __shfl_xor_sync(0xffffffffu, Fx, o);
+    Fy += __shfl_xor_sync(0xffffffffu, Fy, o);
+    Fz += __shfl_xor_sync(0xffffffffu, Fz, o);
+  }
+  if (jl == 0 && oi == 1) {
+    s.fx[i] = Fx;
+    s.fy[i] = Fy;
+    s.fz[i] = Fz;
+    if (fa.fuse_velocity) {
+      // TimeDiscretization.cpp:152-164: v += (F + oldF) * (dt / (2m))
+      const double m = s.mass[ti];
+      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
+      s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
+      s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
+    }
+  }
+  if (GLOB) {
+    const double own_i = oi == 1 ? 1.0 : 0.0;  // energyFactor of the non-newton3 functor call
+    double g0 = own_i * pot, g1 = own_i * vx, g2 = own_i * vy, g3 = own_i * vz;
+    long long h = oi == 1 ? hits2 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+      g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+      g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      h += __shfl_xor_sync(0xffffffffu, h, o);
+    }
+    if (lane == 0) {
+      s.cl_glob[4 * A + 0] = g0;
+      s.cl_glob[4 * A + 1] = g1;
+      s.cl_glob[4 * A + 2] = g2;
+      s.cl_glob[4 * A + 3] = g3;
+      s.cl_hits[A] = (unsigned long long)h;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP64, full lists: the reference arithmetic, operation by operation
+// ---------------------------------------------------------------------------------------------
+template <int C, bool GLOB>
+__global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs fa) {
+  constexpr int JL = 32 / C;
+  const int lane = threadIdx.x & 31;
+  const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (A >= s.nclusters) return;
+  const int n = s.cp_count[A];
+  if (n == 0) return;
+  const int64_t lst = s.cp_start[A];
+  const int ii = lane % C, jl = lane / C;
+  const int64_t i = A * C + ii;
+  const double xi = s.x[i], yi = s.y[i], zi = s.z[i];
+  const int oi = s.own[i];
+  const int ti = s.type[i];
+  const int T = s.types->ntypes;
+  const SysDev &S = s.sysd[s.cl_sys[A]];
+  const double rc2 = fa.rc2;
+  double fx = 0, fy = 0, fz = 0, pot = 0, vx = 0, vy = 0, vz = 0;
+  long long hits2 = 0;
+  const int total = n * C;
+  for (int t = jl; t < total; t += JL) {
+    const int e = t / C, jj = t % C;
+    const uint32_t ent = __ldg(&s.cp_list[lst + e]);
+    const int64_t B = ent >> 5;
+    const int code = ent & 31;
+    const int64_t j = B * C + jj;
+    const int oj = s.own[j];
+    const bool valid = (oj != 0) && !(B == A && code == kShiftNone && jj == ii);
+    int sx, sy, sz;
+    shift_of(code, sx, sy, sz);
+    // LJFunctor.h:464-479: drx = x1 - x2 with x2 the (halo image) position
+    const double dx = __dsub_rn(xi, image_coord(s.x[j], sx, S.len[0]));
+    const double dy = __dsub_rn(yi, image_coord(s.y[j], sy, S.len[1]));
+    const double dz = __dsub_rn(zi, image_coord(s.z[j], sz, S.len[2]));
+    const double dr2 = dist2_mode(dx, dy, dz, s.dist_mode);
+    const bool mask = valid && dr2 <= rc2;
+    const int k = ti * T + s.type[j];
+    const double sig2 = s.types->sig2[k], eps24 = s.types->eps24[k], sh6 = s.types->shift6[k];
+    // LJFunctor.h:485-496
+    const double invdr2 = __ddiv_rn(1.0, dr2);
+    const double lj2 = __dmul_rn(sig2, invdr2);
+    const double lj6 = __dmul_rn(__dmul_rn(lj2, lj2), lj2);
+    const double lj12 = __dmul_rn(lj6, lj6);
+    const double lj12m6 = __dsub_rn(lj12, lj6);
+    double fac = __dmul_rn(__dmul_rn(eps24, __dadd_rn(lj12, lj12m6)), invdr2);
+    fac = mask ? fac : 0.0;
+    const double pfx = __dmul_rn(dx, fac), pfy = __dmul_rn(dy, fac), pfz = __dmul_rn(dz, fac);
+    fx = __dadd_rn(fx, pfx);
+    fy = __dadd_rn(fy, pfy);
+    fz = __dadd_rn(fz, pfz);
+    if (GLOB) {
+      pot = __dadd_rn(pot, mask ? __dadd_rn(__dmul_rn(eps24, lj12m6), sh6) : 0.0);
+      vx = __dadd_rn(vx, __dmul_rn(dx, pfx));
+      vy = __dadd_rn(vy, __dmul_rn(dy, pfy));
+      vz = __dadd_rn(vz, __dmul_rn(dz, pfz));
+      hits2 += mask ? (oj == 1 ? 1 : 2) : 0;
+    }
+  }
+#pragma unroll
+  for (int o = C; o < 32; o <<= 1) {
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+  }
+  if (jl == 0 && oi == 1) {
+    s.fx[i] = fx;
+    s.fy[i] = fy;
+    s.fz[i] = fz;
+    if (fa.fuse_velocity) {
+      const double m = s.mass[ti];
+      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(fx, s.ofx[i]), h));
+      s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(fy, s.ofy[i]), h));
+      s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(fz, s.ofz[i]), h));
+    }
+  }
+  if (GLOB) {
+    const double own_i = oi == 1 ? 1.0 : 0.0;
+    double g0 = own_i * pot, g1 = own_i * vx, g2 = own_i * vy, g3 = own_i * vz;
+    long long h = oi == 1 ? hits2 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+      g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+      g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      h += __shfl_xor_sync(0xffffffffu, h, o);
+    }
+    if (lane == 0) {
+      s.cl_glob[4 * A + 0] = g0;
+      s.cl_glob[4 * A + 1] = g1;
+      s.cl_glob[4 * A + 2] = g2;
+      s.cl_glob[4 * A + 3] = g3;
+      s.cl_hits[A] = (unsigned long long)h;
+    }
+  }
+}
+
+template <int C>
+static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st) {
+  const int64_t nb = (s.nclusters + 3) / 4;
+  if (nb == 0) return;
+  if (precision == 0) {
+    if (fa.calc_globals)
+      k_lj_fp64_full<C, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_fp64_full<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    return;
+  }
+  // the single-type specialisation keeps the LJ parameters in registers
+  const int T = s.ntypes;
+  if (T == 1) {
+    if (fa.calc_globals)
+      k_lj_mixed_full<C, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_full<C, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+  } else {
+    if (fa.calc_globals)
+      k_lj_mixed_full<C, true, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_full<C, false, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+  }
+}
+
+void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st) {
+  ForceArgs fa;
+  fa.rc2 = s.cutoff * s.cutoff;
+  fa.rc2f = (float)fa.rc2;
+  fa.dt = dt;
+  fa.fuse_velocity = fuse_velocity ? 1 : 0;
+  fa.calc_globals = calc_globals;
+  if (s.C == 4)
+    launch_force_c<4>(s, precision, fa, st);
+  else
+    launch_force_c<8>(s, precision, fa, st);
+}
+
+// ---------------------------------------------------------------------------------------------
+// per-system globals: deterministic block reduction over the system's clusters, then
+// LJFunctor::endTraversal post-processing (x0.5, /6; LJFunctor.h:661-685)
+// ---------------------------------------------------------------------------------------------
+__global__ void k_reduce_globals(DeviceState s, const int64_t *__restrict__ sys_cl_range) {
+  const int sy = blockIdx.x;
+  const int64_t c0 = sys_cl_range[2 * sy], c1 = sys_cl_range[2 * sy + 1];
+  double g[4] = {0, 0, 0, 0};
+  long long h = 0;
+  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+    for (int q = 0; q < 4; ++q) g[q] += s.cl_glob[4 * c + q];
+    h += (long long)s.cl_hits[c];
+  }
+  __shared__ double red[4][256];
+  __shared__ long long redh[256];
+  for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = g[q];
+  redh[threadIdx.x] = h;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+      redh[threadIdx.x] += redh[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double up = red[0][0] * 0.5 / 6.;
+    const double vx = red[1][0] * 0.5, vy = red[2][0] * 0.5, vz = red[3][0] * 0.5;
+    s.sys_glob[5 * sy + 0] = up;
+    s.sys_glob[5 * sy + 1] = vx + vy + vz;
+    s.sys_glob[5 * sy + 2] = vx;
+    s.sys_glob[5 * sy + 3] = vy;
+    s.sys_glob[5 * sy + 4] = vz;
+    s.sys_hits[sy] = redh[0] / 2;
+  }
+}
+
+void launch_reduce_globals_range(DeviceState &s, const int64_t *sys_cl_range, cudaStream_t st) {
+  if (s.nsys > 0) k_reduce_globals<<<s.nsys, 256, 0, st>>>(s, sys_cl_range);
+}
+
+}  // namespace pe

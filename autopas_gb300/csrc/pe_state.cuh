@@ -1,0 +1,81 @@
+// pe_state.cuh -- device-side state of one engine and the launchers shared by the .cu files.
+#pragma once
+
+#include "pe_common.cuh"
+
+namespace pe {
+
+// Plain pointer bundle; owned and sized by the engine (pe_engine.cu).
+struct DeviceState {
+  // ---- particles, slot order ----
+  int64_t nslots = 0;      // slots in use (real + padding dummies)
+  int64_t nreal = 0;       // real particles
+  double *x = nullptr, *y = nullptr, *z = nullptr;
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+  double *fx = nullptr, *fy = nullptr, *fz = nullptr;
+  double *ofx = nullptr, *ofy = nullptr, *ofz = nullptr;
+  int32_t *type = nullptr, *sys = nullptr, *orig = nullptr;
+  int8_t *own = nullptr;
+  int64_t *id = nullptr;
+  float4 *pk_hi = nullptr, *pk_lo = nullptr;
+  // inverse map: user index -> slot
+  int32_t *slot_of = nullptr;
+
+  // ---- towers / clusters ----
+  int nsys = 0;
+  int64_t ntowers = 0;
+  int64_t nclusters = 0;
+  int C = 8;
+  int32_t *tw_count = nullptr;     // [ntowers]
+  int32_t *tw_start = nullptr;     // [ntowers+1] exclusive scan of counts (compact order)
+  int32_t *tw_cl_start = nullptr;  // [ntowers+1] first cluster of each tower
+  double *tw_bb = nullptr;         // [ntowers*4] xy bbox of the tower's particles (minx,miny,maxx,maxy)
+  double *cl_bb = nullptr;         // [nclusters*6] lo xyz, hi xyz (real members only)
+  int32_t *cl_sys = nullptr;       // [nclusters]
+  int32_t *cl_tower = nullptr;     // [nclusters]
+  int32_t *cl_flags = nullptr;     // bit0: has owned member, bit1: has any real member
+  int64_t *cp_start = nullptr;     // [nclusters]
+  int32_t *cp_count = nullptr;     // [nclusters]
+  uint32_t *cp_list = nullptr;     // [cp_cap]
+  int64_t cp_cap = 0;
+  unsigned long long *cp_total = nullptr;  // device counter
+  int newton3 = 0;
+
+  // ---- systems and parameters ----
+  SysDev *sysd = nullptr;          // [nsys]
+  TypeTable *types = nullptr;      // device copy
+  double *mass = nullptr;          // [ntypes]
+  double cutoff = 0, skin = 0;
+  int dist_mode = 0;
+  int ntypes = 1;                  // host copy of types->ntypes
+
+  // ---- globals ----
+  double *cl_glob = nullptr;       // [nclusters*4]: 6*Upot, virial x,y,z partials (post energy factor)
+  unsigned long long *cl_hits = nullptr;  // [nclusters] interacting-pair counts (x2 for full lists)
+  double *sys_glob = nullptr;      // [nsys*5]
+  long long *sys_hits = nullptr;   // [nsys]
+
+  int *err = nullptr;              // device error flags (DeviceError bits)
+};
+
+// scan utilities (pe_engine.cu)
+void scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t st);  // out has n+1 entries
+
+// rebuild (pe_build.cu)
+void launch_bin(DeviceState &s, int64_t nslots_old, uint64_t *key, int32_t *tower_of, cudaStream_t st);
+void launch_clusters_per_tower(DeviceState &s, int32_t *ncl, cudaStream_t st);
+void launch_scatter(DeviceState &s, int64_t nslots_old, const int32_t *tower_of, const uint64_t *key,
+                    int32_t *fill, uint64_t *skey, int32_t *sval, cudaStream_t st);
+int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *perm_src, int max_tower,
+                      cudaStream_t st);
+void launch_cluster_bbox(DeviceState &s, cudaStream_t st);
+void launch_list_build(DeviceState &s, cudaStream_t st);
+void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
+                      unsigned long long *count, cudaStream_t st);
+
+// forces (pe_force.cu)
+void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt,
+                  cudaStream_t st);
+void launch_reduce_globals_range(DeviceState &s, const int64_t *sys_cl_range, cudaStream_t st);
+
+}  // namespace pe

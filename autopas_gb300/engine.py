@@ -1,0 +1,249 @@
+"""Python binding of the engine's C ABI (include/pairengine.h) over ctypes.
+
+This is a thin host wrapper for tests, benchmarks and scripting; the C++ mirror of the AutoPas container /
+traversal / functor interface lives in autopas_gb300/include/.  The library must have been built
+(``autopas_gb300.build.build()``); there is no fallback of any kind when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PE_OK = 0
+ERRORS = {
+    -1: "PE_ERR_ARG", -2: "PE_ERR_OOM", -3: "PE_ERR_CUDA", -4: "PE_ERR_LIST_OVERFLOW", -5: "PE_ERR_TOWER_OVERFLOW",
+    -6: "PE_ERR_STATE", -7: "PE_ERR_NO_DEVICE", -8: "PE_ERR_DOMAIN",
+}
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+DIST_STRICT, DIST_FMA_SOA, DIST_FMA_DOT = 0, 1, 2
+DUMMY, OWNED, HALO = 0, 1, 2
+
+# every symbol include/pairengine.h declares
+EXPORTS = [
+    "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
+    "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
+    "pe_pair_set", "pe_get_kernel_time",
+]
+
+
+class PeConfig(C.Structure):
+    _fields_ = [
+        ("cutoff", C.c_double), ("skin", C.c_double), ("num_types", C.c_int),
+        ("epsilon", C.POINTER(C.c_double)), ("sigma", C.POINTER(C.c_double)), ("mass", C.POINTER(C.c_double)),
+        ("apply_shift", C.c_int), ("precision", C.c_int), ("cluster_size", C.c_int), ("newton3", C.c_int),
+        ("dist_mode", C.c_int), ("rebuild_frequency", C.c_int), ("calc_globals", C.c_int),
+    ]
+
+
+class PeSystem(C.Structure):
+    _fields_ = [("box_min", C.c_double * 3), ("box_max", C.c_double * 3), ("periodic", C.c_int)]
+
+
+class PeGlobals(C.Structure):
+    _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("virial_xyz", C.c_double * 3),
+                ("num_pairs", C.c_int64)]
+
+
+class PeInfo(C.Structure):
+    _fields_ = [("cluster_size", C.c_int), ("newton3", C.c_int), ("precision", C.c_int),
+                ("num_particles", C.c_int64), ("num_slots", C.c_int64), ("num_clusters", C.c_int64),
+                ("num_towers", C.c_int64), ("num_cluster_pairs", C.c_int64), ("max_tower_size", C.c_int64)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(path: str | None = None):
+    """Load libpairengine.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or library_path()
+    if not os.path.exists(p):
+        raise RuntimeError(f"engine library {p} is missing; build it with autopas_gb300.build.build()")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    L.pe_create.argtypes = [C.POINTER(PeConfig), C.c_int, C.POINTER(PeSystem), C.POINTER(vp)]
+    L.pe_destroy.argtypes = [vp]
+    L.pe_last_error.argtypes = [vp]
+    L.pe_last_error.restype = C.c_char_p
+    L.pe_set_particles.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.pe_update_positions.argtypes = [vp, vp, vp, vp]
+    L.pe_rebuild.argtypes = [vp]
+    L.pe_compute_forces.argtypes = [vp, vp]
+    L.pe_get_forces.argtypes = [vp, vp, vp, vp]
+    L.pe_get_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.pe_step.argtypes = [vp, C.c_double, C.c_int, vp]
+    L.pe_get_info.argtypes = [vp, C.POINTER(PeInfo)]
+    L.pe_get_tower_grid.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), dp]
+    L.pe_pair_set.argtypes = [vp, C.c_int, C.c_int64, vp, vp, vp, C.POINTER(C.c_int64)]
+    L.pe_get_kernel_time.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_int64), dp, C.POINTER(C.c_int64)]
+    for name in EXPORTS:
+        if name != "pe_last_error":
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class PairEngine:
+    """One engine instance (one CUDA stream) holding one or more particle systems."""
+
+    def __init__(self, cutoff, skin, boxes, periodic=True, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,),
+                 shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_STRICT,
+                 rebuild_frequency=10, calc_globals=True):
+        L = load()
+        self._L = L
+        self._eps = np.ascontiguousarray(epsilon, np.float64)
+        self._sig = np.ascontiguousarray(sigma, np.float64)
+        self._mass = np.ascontiguousarray(mass, np.float64)
+        T = len(self._eps)
+        dp = C.POINTER(C.c_double)
+        cfg = PeConfig(cutoff, skin, T, self._eps.ctypes.data_as(dp), self._sig.ctypes.data_as(dp),
+                       self._mass.ctypes.data_as(dp), int(shift), int(precision), int(cluster_size), int(newton3),
+                       int(dist_mode), int(rebuild_frequency), int(calc_globals))
+        boxes = list(boxes)
+        if np.ndim(boxes[0]) == 1:  # single (bmin, bmax)
+            boxes = [boxes]
+        per = periodic if isinstance(periodic, (list, tuple)) else [periodic] * len(boxes)
+        arr = (PeSystem * len(boxes))()
+        for k, (bmin, bmax) in enumerate(boxes):
+            arr[k].box_min[:] = [float(v) for v in bmin]
+            arr[k].box_max[:] = [float(v) for v in bmax]
+            arr[k].periodic = int(per[k])
+        self.num_systems = len(boxes)
+        h = C.c_void_p()
+        rc = L.pe_create(C.byref(cfg), len(boxes), arr, C.byref(h))
+        if rc != PE_OK:
+            raise EngineError(rc, "pe_create failed")
+        self._h = h
+        self.n = 0
+
+    def _check(self, rc):
+        if rc != PE_OK:
+            raise EngineError(rc, self._L.pe_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.pe_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_particles(self, pos, vel=None, types=None, ownership=None, ids=None, system=None):
+        pos = np.asarray(pos, np.float64)
+        n = len(pos)
+        self._x, self._y, self._z = (np.ascontiguousarray(pos[:, d]) for d in range(3))
+        if vel is not None:
+            vel = np.asarray(vel, np.float64)
+            self._vx, self._vy, self._vz = (np.ascontiguousarray(vel[:, d]) for d in range(3))
+        else:
+            self._vx = self._vy = self._vz = None
+        t = None if types is None else np.ascontiguousarray(types, np.int32)
+        o = None if ownership is None else np.ascontiguousarray(ownership, np.int8)
+        i = None if ids is None else np.ascontiguousarray(ids, np.int64)
+        s = None if system is None else np.ascontiguousarray(system, np.int32)
+        self._check(self._L.pe_set_particles(self._h, n, _ptr(self._x), _ptr(self._y), _ptr(self._z),
+                                             _ptr(self._vx), _ptr(self._vy), _ptr(self._vz), _ptr(t), _ptr(o),
+                                             _ptr(i), _ptr(s)))
+        self.n = n
+
+    def set_particles_soa(self, x, y, z, vx=None, vy=None, vz=None, types=None, ownership=None, system=None):
+        """Zero-copy variant: the arrays (contiguous, possibly pinned) are passed as they are."""
+        self._check(self._L.pe_set_particles(self._h, len(x), _ptr(x), _ptr(y), _ptr(z), _ptr(vx), _ptr(vy),
+                                             _ptr(vz), _ptr(types), _ptr(ownership), None, _ptr(system)))
+        self.n = len(x)
+
+    def update_positions(self, pos):
+        pos = np.asarray(pos, np.float64)
+        x, y, z = (np.ascontiguousarray(pos[:, d]) for d in range(3))
+        self._check(self._L.pe_update_positions(self._h, _ptr(x), _ptr(y), _ptr(z)))
+
+    def rebuild(self):
+        self._check(self._L.pe_rebuild(self._h))
+
+    def compute_forces(self):
+        g = (PeGlobals * self.num_systems)()
+        self._check(self._L.pe_compute_forces(self._h, g))
+        return _globals(g)
+
+    def forces(self, out=None):
+        n = self.n
+        if out is None:
+            out = [np.empty(n), np.empty(n), np.empty(n)]
+        self._check(self._L.pe_get_forces(self._h, _ptr(out[0]), _ptr(out[1]), _ptr(out[2])))
+        return np.stack(out, 1)
+
+    def forces_into(self, fx, fy, fz):
+        self._check(self._L.pe_get_forces(self._h, _ptr(fx), _ptr(fy), _ptr(fz)))
+
+    def state(self):
+        n = self.n
+        a = [np.empty(n) for _ in range(6)]
+        self._check(self._L.pe_get_state(self._h, *[_ptr(v) for v in a]))
+        return np.stack(a[:3], 1), np.stack(a[3:], 1)
+
+    def step(self, dt, nsteps, want_globals=True):
+        g = (PeGlobals * self.num_systems)() if want_globals else None
+        self._check(self._L.pe_step(self._h, float(dt), int(nsteps), g))
+        return _globals(g) if want_globals else None
+
+    def info(self):
+        i = PeInfo()
+        self._check(self._L.pe_get_info(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in PeInfo._fields_}
+
+    def tower_grid(self, system=0):
+        side = (C.c_double * 2)()
+        num = (C.c_int64 * 2)()
+        halo = C.c_int64()
+        origin = (C.c_double * 2)()
+        self._check(self._L.pe_get_tower_grid(self._h, system, side, num, C.byref(halo), origin))
+        return np.array(side[:]), np.array(num[:]), int(halo.value), np.array(origin[:])
+
+    def pair_set(self, which=0):
+        """(a, b, code) of the covered pairs within rc+skin (which=0) or rc (which=1)."""
+        cnt = C.c_int64()
+        self._check(self._L.pe_pair_set(self._h, int(which), 0, None, None, None, C.byref(cnt)))
+        cap = int(cnt.value)
+        a = np.empty(max(cap, 1), np.int64)
+        b = np.empty(max(cap, 1), np.int64)
+        c = np.empty(max(cap, 1), np.int32)
+        self._check(self._L.pe_pair_set(self._h, int(which), cap, _ptr(a), _ptr(b), _ptr(c), C.byref(cnt)))
+        return a[:cap], b[:cap], c[:cap]
+
+    def kernel_time(self, reset=True):
+        fm = C.c_double()
+        fl = C.c_int64()
+        tm = C.c_double()
+        tl = C.c_int64()
+        self._check(self._L.pe_get_kernel_time(self._h, int(reset), C.byref(fm), C.byref(fl), C.byref(tm),
+                                               C.byref(tl)))
+        return {"force_ms": fm.value, "force_launches": fl.value, "total_launches": tl.value}
+
+
+def _globals(g):
+    return [{"upot": x.upot, "virial": x.virial, "virial_xyz": tuple(x.virial_xyz), "num_pairs": x.num_pairs}
+            for x in g]

@@ -1,0 +1,166 @@
+/*
+ * pairengine.h -- C ABI of the GB300 short-range pair-force engine for AutoPas.
+ *
+ * The engine replaces, for the Lennard-Jones path, what AutoPas runs under
+ * autopas::AutoPas<Particle>::computeInteractions(&functor)  (src/autopas/AutoPasImpl.h:116-137):
+ *   container rebuild  -> LogicHandler::computeInteractions (src/autopas/LogicHandler.h:1095-1108)
+ *                         calling ParticleContainerInterface::rebuildNeighborLists
+ *                         (src/autopas/containers/ParticleContainerInterface.h:75-404)
+ *   force traversal    -> container->computeInteractions(&traversal) (LogicHandler.h:1113),
+ *                         the traversal's TraversalInterface (src/autopas/containers/TraversalInterface.h:18-83)
+ *                         and the functor's SoAFunctorPair/Single
+ *                         (applicationLibrary/molecularDynamics/molecularDynamicsLibrary/LJFunctor.h:204-559)
+ *   globals            -> functor.initTraversal / endTraversal / getPotentialEnergy / getVirial (LJFunctor.h:641-720)
+ *   integration        -> md-flexible TimeDiscretization (examples/md-flexible/src/TimeDiscretization.cpp:17-164)
+ *
+ * Only plain C types cross this boundary.  The engine owns all device memory; host arrays passed in
+ * are borrowed for the duration of the call.  Every call returns a status (PE_OK = 0, negative on error);
+ * pe_last_error() gives the message.  One engine = one CUDA stream; an engine must not be used from two
+ * threads at once (AutoPas calls computeInteractions outside OpenMP regions, LogicHandler.h:1113).
+ *
+ * An engine holds one or more independent particle systems ("ensemble"): each system has its own box,
+ * tower grid and cluster lists; all systems share the cutoff, skin and the type table, and every
+ * kernel processes all systems in one launch.
+ */
+#ifndef AUTOPAS_GB300_PAIRENGINE_H
+#define AUTOPAS_GB300_PAIRENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PE_OK 0
+#define PE_ERR_ARG (-1)           /* invalid argument */
+#define PE_ERR_OOM (-2)           /* device allocation failed */
+#define PE_ERR_CUDA (-3)          /* a CUDA call failed */
+#define PE_ERR_LIST_OVERFLOW (-4) /* a cluster's neighbour list exceeded the per-cluster bound */
+#define PE_ERR_TOWER_OVERFLOW (-5)/* a tower holds more particles than the on-chip sort supports */
+#define PE_ERR_STATE (-6)         /* call order violated (e.g. compute before set_particles) */
+#define PE_ERR_NO_DEVICE (-7)     /* no CUDA device or not an sm_103 device */
+#define PE_ERR_DOMAIN (-8)        /* periodic box shorter than twice the interaction length */
+
+/* ---- option values ---- */
+#define PE_PRECISION_FP64 0   /* plain FP64 form: FP64 positions, FP64 LJ arithmetic, FP64 sums */
+#define PE_PRECISION_MIXED 1  /* FP64 state, FP32 LJ on hi/lo-split displacements, compensated FP32 sums */
+
+#define PE_DIST_STRICT 0   /* dr2 = (dx*dx + dy*dy) + dz*dz, every operation rounded (source semantics) */
+#define PE_DIST_FMA_SOA 1  /* dr2 = fma(dz,dz, fma(dx,dx, dy*dy)) (GCC -O3 -march=native contraction) */
+#define PE_DIST_FMA_DOT 2  /* dr2 = fma(dz,dz, fma(dy,dy, dx*dx)) (contracted ArrayMath::dot) */
+
+/* OwnershipState values (src/autopas/particles/OwnershipState.h:20-29) */
+#define PE_DUMMY 0
+#define PE_OWNED 1
+#define PE_HALO 2
+
+typedef struct pe_engine pe_engine;
+
+/* Engine-wide options; the counterpart of the LJFunctor template/constructor arguments
+ * (LJFunctor.h:39-117: applyShift, useMixing, useNewton3, calculateGlobals, cutoff, ParticlePropertiesLibrary)
+ * plus the container options (cutoff, skin, verletClusterSize, rebuild frequency) of AutoPasDecl.h:552-1151. */
+typedef struct {
+  double cutoff;           /* rc */
+  double skin;             /* Verlet skin; lists hold pairs within rc+skin */
+  int num_types;           /* >= 1 */
+  const double *epsilon;   /* [num_types] */
+  const double *sigma;     /* [num_types] */
+  const double *mass;      /* [num_types], used by the integrator */
+  int apply_shift;         /* truncated-shifted potential (applyShift) */
+  int precision;           /* PE_PRECISION_* */
+  int cluster_size;        /* 4 or 8; 0 lets the engine's tuner decide */
+  int newton3;             /* 0: full lists, each pair evaluated from both sides; 1: half lists + j-force reduction;
+                              -1: tuner decides */
+  int dist_mode;           /* PE_DIST_* for every FP64 distance test */
+  int rebuild_frequency;   /* steps between list rebuilds inside pe_step (verletRebuildFrequency) */
+  int calc_globals;        /* compute Upot and virial with every force evaluation */
+} pe_config;
+
+/* One particle system of the ensemble. */
+typedef struct {
+  double box_min[3];
+  double box_max[3];
+  int periodic;  /* 1: the engine forms the periodic images itself, with the positions md-flexible gives its
+                    halo copies (RegularGridDecomposition.cpp:159-236); 0: the caller supplies halo particles
+                    (ownership PE_HALO) as AutoPas containers receive them through addHaloParticle */
+} pe_system_desc;
+
+/* Per-system results of the last force evaluation (LJFunctor::getPotentialEnergy / getVirial). */
+typedef struct {
+  double upot;
+  double virial;       /* sum of the three components, as LJFunctor::getVirial returns */
+  double virial_xyz[3];
+  int64_t num_pairs;   /* interacting pairs (dr2 <= rc^2), each unordered pair once; -1 if not counted */
+} pe_globals;
+
+/* Replaces: constructing the container + functor (ContainerSelector.h:38-113, LJFunctor constructors). */
+int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *systems, pe_engine **out);
+/* Replaces: container destruction. */
+int pe_destroy(pe_engine *h);
+const char *pe_last_error(const pe_engine *h);
+
+/* Replaces: AutoPas::addParticle / addHaloParticle + the functor's SoALoader (Functor.h:112-129,217-279)
+ * for all particles at once.  Positions/velocities are SoA; type/ownership/id/system may be NULL
+ * (type 0, owned, id = index, system 0).  Invalidates the lists. */
+int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, const double *z,
+                     const double *vx, const double *vy, const double *vz, const int32_t *type,
+                     const int8_t *ownership, const int64_t *id, const int32_t *system);
+/* Updates positions (and optionally velocities) of the particles last set, in the same order, without
+ * invalidating the lists (particles must not have moved more than skin/2 since the last rebuild). */
+int pe_update_positions(pe_engine *h, const double *x, const double *y, const double *z);
+
+/* Replaces: VerletClusterLists::rebuildNeighborLists (VerletClusterLists.h:779-800) -- binning by radix
+ * sort on tower index, per-tower z order, clusters, bounding boxes and the cluster-pair lists. */
+int pe_rebuild(pe_engine *h);
+
+/* Replaces: functor.initTraversal(); container->computeInteractions(&traversal); functor.endTraversal()
+ * (LogicHandler.h:1092-1122).  Forces are overwritten.  globals: [num_systems] or NULL. */
+int pe_compute_forces(pe_engine *h, pe_globals *globals);
+
+/* Forces in the order of the last pe_set_particles (halo/dummy entries: 0).  Any pointer may be NULL. */
+int pe_get_forces(pe_engine *h, double *fx, double *fy, double *fz);
+/* Positions and velocities in the order of the last pe_set_particles. */
+int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, double *vy, double *vz);
+
+/* nsteps velocity-Verlet steps on the device with md-flexible's step order
+ * (Simulation.cpp:230-346 with TimeDiscretization.cpp:17-164): position update, list rebuild when due
+ * (every rebuild_frequency steps), forces, velocity update.  Requires forces of the current positions
+ * (pe_compute_forces) before the first step.  globals of the last step: [num_systems] or NULL. */
+int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals);
+
+/* ---- introspection / verification ---- */
+typedef struct {
+  int cluster_size;
+  int newton3;
+  int precision;
+  int64_t num_particles;     /* real particles (owned + halo) */
+  int64_t num_slots;         /* particles + padding dummies */
+  int64_t num_clusters;
+  int64_t num_towers;
+  int64_t num_cluster_pairs; /* entries in all cluster-pair lists */
+  int64_t max_tower_size;
+} pe_info;
+int pe_get_info(pe_engine *h, pe_info *info);
+
+/* Tower grid of one system (ClusterTowerBlock2D::estimateOptimalGridSideLength):
+ * side[2], num[2] (towers per dim), halo = towers per interaction length, origin[2]. */
+int pe_get_tower_grid(pe_engine *h, int system, double *side, int64_t *num, int64_t *halo, double *origin);
+
+/* The particle-pair set covered by the cluster-pair lists, evaluated in FP64 with dist_mode:
+ * entries (a, b, code) with a, b indices of the last pe_set_particles and code = image shift of b
+ * ((sx+1) + 3(sy+1) + 9(sz+1) form, 13 = no shift).  Pairs without shift are reported once with a < b;
+ * periodic-image pairs are reported once per (owned particle, image) as md-flexible's halo copies form them.
+ * which = 0: dr2 < (rc+skin)^2 (the Verlet pair rule), 1: dr2 <= rc^2 (the interacting set).
+ * Writes up to cap entries and returns the total count in *count. */
+int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code, int64_t *count);
+
+/* CUDA-event timing of the last pe_compute_forces / pe_step force kernels (ms, summed over launches) and
+ * launch count; reset with reset != 0. */
+int pe_get_kernel_time(pe_engine *h, int reset, double *force_ms, int64_t *force_launches, double *total_ms,
+                       int64_t *total_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

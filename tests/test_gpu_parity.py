@@ -1,0 +1,222 @@
+"""Parity of the CUDA engine (through the C ABI) with the CPU oracle.
+
+Tolerances:
+* FP64 form: forces within 1e-12 of the largest force magnitude (the per-pair arithmetic is the reference's
+  operation order; only the summation order differs), Upot and virial within 1e-12 relative.
+* mixed form: force RMS error relative to the RMS force <= 1e-6 (the spec bar), Upot within 1e-6.
+* pair sets (rc+skin Verlet rule and the rc interacting set): bit-exact set equality.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng_mod():
+    from autopas_gb300.build import build
+    build()
+    from autopas_gb300 import engine
+    return engine
+
+
+def liquid(n_cells=6, rho=0.8442, seed=0, jitter=0.08):
+    from autopas_gb300 import workloads
+    pos, vel, bmin, bmax = workloads.fcc_lj(n_cells, rho, 0.72, seed=seed)
+    rng = np.random.default_rng(seed)
+    pos = np.mod(pos + rng.normal(0, jitter, pos.shape), bmax)
+    return pos, vel, bmin, bmax
+
+
+def canonical_oracle_pairs(orc, pos, bmin, bmax, rc, skin, which, dist_mode=0):
+    allpos, own, allt, owner, code = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    n = len(pos)
+    if which == 0:
+        a, b = orc.pair_set(allpos, rc + skin, own=own, dist_mode=dist_mode)
+    else:
+        a, b = orc.interacting_set(allpos, rc, own=own, dist_mode=dist_mode)
+    halo_b = b >= n
+    bb = np.where(halo_b, owner[np.where(halo_b, b - n, 0)], b)
+    cc = np.where(halo_b, code[np.where(halo_b, b - n, 0)], 13)
+    return np.unique(np.stack([a, bb, cc], 1), axis=0)
+
+
+def rel_rms(F, R):
+    return float(np.sqrt(((F - R) ** 2).sum(1).mean()) / np.sqrt((R ** 2).sum(1).mean()))
+
+
+@pytest.mark.parametrize("C", [4, 8])
+def test_fp64_periodic_forces_match_oracle(eng_mod, orc, C):
+    pos, vel, bmin, bmax = liquid()
+    rc, skin = 2.5, 0.3
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_FP64,
+                           cluster_size=C)
+    e.set_particles(pos, vel)
+    g = e.compute_forces()[0]
+    F = e.forces()
+    lj = orc.LJ(rc)
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.lj_forces(allpos, lj, own=own)
+    R = R[: len(pos)]
+    scale = np.abs(R).max()
+    np.testing.assert_allclose(F, R, rtol=0, atol=1e-12 * scale)
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-12)
+    assert g["virial"] == pytest.approx(glob[1], rel=1e-12)
+    ia, ib = orc.interacting_set(allpos, rc, own=own)
+    n = len(pos)
+    # unique physical pairs: owned-owned once, owned-halo pairs come in mirrored couples
+    n_oo = int(np.sum(ib < n))
+    n_oh = int(np.sum(ib >= n))
+    assert g["num_pairs"] == n_oo + n_oh // 2
+
+
+def test_fp64_explicit_halo_forces_match_oracle(eng_mod, orc):
+    """Container mode: the caller hands owned + halo particles (AutoPas addHaloParticle semantics)."""
+    pos, vel, bmin, bmax = liquid(5, seed=3)
+    rc, skin = 2.5, 0.3
+    allpos, own, allt, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, precision=eng_mod.PRECISION_FP64)
+    e.set_particles(allpos, ownership=own)
+    g = e.compute_forces()[0]
+    F = e.forces()
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+    n = len(pos)
+    scale = np.abs(R[:n]).max()
+    np.testing.assert_allclose(F[:n], R[:n], rtol=0, atol=1e-12 * scale)
+    assert np.all(F[n:] == 0)
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-12)
+    assert g["virial"] == pytest.approx(glob[1], rel=1e-12)
+    ia, ib = orc.interacting_set(allpos, rc, own=own)
+    assert g["num_pairs"] == len(ia)
+
+
+@pytest.mark.parametrize("dist_mode", [0, 1])
+@pytest.mark.parametrize("C", [4, 8])
+def test_pair_set_bit_exact_periodic(eng_mod, orc, dist_mode, C):
+    pos, vel, bmin, bmax = liquid(6, seed=5)
+    rc, skin = 2.5, 0.3
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, cluster_size=C, dist_mode=dist_mode)
+    e.set_particles(pos, vel)
+    e.rebuild()
+    for which in (0, 1):
+        a, b, c = e.pair_set(which)
+        dev = np.unique(np.stack([a, b, c], 1), axis=0)
+        assert len(dev) == len(a), "device reported a pair twice"
+        ref = canonical_oracle_pairs(orc, pos, bmin, bmax, rc, skin, which, dist_mode)
+        assert len(dev) == len(ref)
+        assert np.array_equal(dev, ref)
+
+
+def test_pair_set_bit_exact_explicit_halo(eng_mod, orc):
+    pos, vel, bmin, bmax = liquid(5, seed=9)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False)
+    e.set_particles(allpos, ownership=own)
+    e.rebuild()
+    a, b, c = e.pair_set(0)
+    assert np.all(c == 13)
+    dev = np.unique(np.stack([a, b], 1), axis=0)
+    ra, rb = orc.pair_set(allpos, rc + skin, own=own)
+    ref = np.unique(np.stack([ra, rb], 1), axis=0)
+    assert np.array_equal(dev, ref)
+
+
+@pytest.mark.parametrize("C", [4, 8])
+def test_mixed_precision_error_bound(eng_mod, orc, C):
+    pos, vel, bmin, bmax = liquid(8, seed=11)
+    rc, skin = 2.5, 0.3
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_MIXED, cluster_size=C)
+    e.set_particles(pos, vel)
+    g = e.compute_forces()[0]
+    F = e.forces()
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+    R = R[: len(pos)]
+    err = rel_rms(F, R)
+    assert err <= 1e-6, err
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
+    assert g["virial"] == pytest.approx(glob[1], rel=1e-6)
+    # the interacting set of the mixed kernel equals the FP64 one (near-cutoff pairs are re-tested in FP64)
+    ia, ib = orc.interacting_set(allpos, rc, own=own)
+    n = len(pos)
+    assert g["num_pairs"] == int(np.sum(ib < n)) + int(np.sum(ib >= n)) // 2
+
+
+def test_multi_type_mixing_and_shift(eng_mod, orc):
+    rng = np.random.default_rng(21)
+    from autopas_gb300 import workloads
+    bmin, bmax = np.zeros(3), np.full(3, 14.0)
+    pos = workloads.rsa(1800, bmin, bmax, bmin, bmax, 0.85, seed=5)
+    types = rng.choice(4, size=len(pos), p=[0.4, 0.3, 0.2, 0.1]).astype(np.int32)
+    eps, sig = [1.0, 0.8, 1.2, 0.6], [1.0, 1.1, 0.9, 1.2]
+    rc, skin = 3.0, 0.3
+    lj = orc.LJ(rc, epsilon=eps, sigma=sig, shift=True)
+    allpos, own, allt, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin, types=types)
+    R, glob, _ = orc.lj_forces(allpos, lj, own=own, types=allt)
+    R = R[: len(pos)]
+    for prec, tol in ((eng_mod.PRECISION_FP64, 1e-12), (eng_mod.PRECISION_MIXED, 1e-6)):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=eps, sigma=sig, mass=[1, 1, 1, 1],
+                               shift=True, precision=prec)
+        e.set_particles(pos, types=types)
+        g = e.compute_forces()[0]
+        F = e.forces()
+        if prec == eng_mod.PRECISION_FP64:
+            np.testing.assert_allclose(F, R, rtol=0, atol=tol * np.abs(R).max())
+        else:
+            assert rel_rms(F, R) <= tol
+        assert g["upot"] == pytest.approx(glob[0], rel=tol)
+
+
+def test_md_trajectory_fp64_matches_oracle(eng_mod, orc):
+    pos, vel, bmin, bmax = liquid(5, seed=13, jitter=0.02)
+    rc, skin, dt, nsteps = 2.5, 0.3, 0.002, 40
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_FP64,
+                           rebuild_frequency=10)
+    e.set_particles(pos, vel)
+    e.compute_forces()
+    g = e.step(dt, nsteps)[0]
+    P, V = e.state()
+    lj = orc.LJ(rc)
+    rp, rv, rf, en = orc.md_run(pos, vel, None, [1.0], bmin, bmax, skin, lj, dt, nsteps)
+    d = P - rp
+    d -= (bmax - bmin) * np.round(d / (bmax - bmin))
+    assert np.abs(d).max() < 1e-9
+    assert np.abs(V - rv).max() < 1e-8
+    assert g["upot"] == pytest.approx(en[-1, 0], rel=1e-9)
+
+
+def test_ensemble_systems_are_independent(eng_mod, orc):
+    from autopas_gb300 import workloads
+    systems = workloads.ensemble(3, nmin=600, nmax=3000, seed=4)
+    rc, skin = 2.5, 0.3
+    boxes = [(s["bmin"], s["bmax"]) for s in systems]
+    pos = np.concatenate([s["pos"] for s in systems])
+    sysid = np.concatenate([np.full(len(s["pos"]), k, np.int32) for k, s in enumerate(systems)])
+    for prec in (eng_mod.PRECISION_FP64, eng_mod.PRECISION_MIXED):
+        e = eng_mod.PairEngine(rc, skin, boxes, periodic=True, precision=prec)
+        e.set_particles(pos, system=sysid)
+        gs = e.compute_forces()
+        F = e.forces()
+        for k, s in enumerate(systems):
+            allpos, own, _, _, _ = orc.periodic_system(s["pos"], s["bmin"], s["bmax"], rc, skin)
+            R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+            R = R[: len(s["pos"])]
+            Fk = F[sysid == k]
+            if prec == eng_mod.PRECISION_FP64:
+                np.testing.assert_allclose(Fk, R, rtol=0, atol=1e-12 * np.abs(R).max())
+                assert gs[k]["upot"] == pytest.approx(glob[0], rel=1e-12)
+            else:
+                assert rel_rms(Fk, R) <= 1e-6
+                assert gs[k]["upot"] == pytest.approx(glob[0], rel=1e-6)
+
+
+def test_errors_are_reported_not_hidden(eng_mod):
+    with pytest.raises(eng_mod.EngineError) as ei:
+        eng_mod.PairEngine(2.5, 0.3, ([0, 0, 0], [4.0, 20, 20]), periodic=True).set_particles(
+            np.random.default_rng(0).uniform(0, 4, (100, 3)))
+    assert ei.value.code == -8  # periodic box shorter than 2(rc+skin)
+    e = eng_mod.PairEngine(2.5, 0.3, ([0, 0, 0], [10, 10, 10]))
+    with pytest.raises(eng_mod.EngineError) as ei:
+        e.compute_forces()
+    assert ei.value.code == -6
