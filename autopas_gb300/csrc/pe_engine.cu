@@ -138,6 +138,9 @@ struct pe_engine {
   int ev_used = 0;
   int64_t launches = 0;
   int64_t force_launches = 0;
+  int64_t rebuilds = 0;
+  cudaEvent_t timer_ev[2] = {nullptr, nullptr};
+  DBuf<long long> pairs_acc;  // interacting pairs summed over force evaluations
 
   DeviceState state() {
     DeviceState s;
@@ -176,6 +179,7 @@ struct pe_engine {
     s.cl_hits = cl_hits.p;
     s.sys_glob = sys_glob.p;
     s.sys_hits = sys_hits.p;
+    s.pairs_acc = pairs_acc.p;
     s.err = derr.p;
     return s;
   }
@@ -657,6 +661,7 @@ static int do_rebuild(pe_engine *h) {
   PE_TRY(h->cuda_check("rebuild"));
   h->lists_valid = true;
   h->steps_since_rebuild = 0;
+  h->rebuilds += 1;
   return PE_OK;
 }
 
@@ -768,12 +773,13 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
         return PE_ERR_ARG;
       }
   }
-  if (!h->types.ensure(1) || !h->dmass.ensure(t.ntypes)) {
+  if (!h->types.ensure(1) || !h->dmass.ensure(t.ntypes) || !h->pairs_acc.ensure(1)) {
     pe_destroy(h);
     return PE_ERR_OOM;
   }
   cudaMemcpy(h->types.p, &t, sizeof t, cudaMemcpyHostToDevice);
   cudaMemcpy(h->dmass.p, h->mass.data(), sizeof(double) * t.ntypes, cudaMemcpyHostToDevice);
+  cudaMemset(h->pairs_acc.p, 0, sizeof(long long));
   *out = h;
   return PE_OK;
 }
@@ -802,6 +808,9 @@ int pe_destroy(pe_engine *h) {
   h->sysd.release();
   h->types.release();
   for (auto e : h->ev_pool) cudaEventDestroy(e);
+  for (auto e : h->timer_ev)
+    if (e) cudaEventDestroy(e);
+  h->pairs_acc.release();
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return PE_OK;
@@ -993,9 +1002,8 @@ int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, in
   return h->cuda_check("pair_set");
 }
 
-int pe_get_kernel_time(pe_engine *h, int reset, double *force_ms, int64_t *force_launches, double *total_ms,
-                       int64_t *total_launches) {
-  if (!h) return PE_ERR_ARG;
+int pe_get_stats(pe_engine *h, int reset, pe_stats *out) {
+  if (!h || !out) return PE_ERR_ARG;
   PE_CUDA(h, cudaStreamSynchronize(h->st));
   double fm = 0;
   for (auto &pr : h->force_ev) {
@@ -1003,16 +1011,39 @@ int pe_get_kernel_time(pe_engine *h, int reset, double *force_ms, int64_t *force
     cudaEventElapsedTime(&ms, h->ev_pool[pr.first], h->ev_pool[pr.second]);
     fm += ms;
   }
-  if (force_ms) *force_ms = fm;
-  if (force_launches) *force_launches = h->force_launches;
-  if (total_ms) *total_ms = 0;
-  if (total_launches) *total_launches = h->launches;
+  long long pairs = 0;
+  if (h->pairs_acc.p) PE_CUDA(h, cudaMemcpy(&pairs, h->pairs_acc.p, sizeof(long long), cudaMemcpyDeviceToHost));
+  out->force_ms = fm;
+  out->force_launches = h->force_launches;
+  out->kernel_launches = h->launches;
+  out->pairs_total = pairs;
+  out->rebuilds = h->rebuilds;
   if (reset) {
     h->force_ev.clear();
     h->ev_used = 0;
     h->force_launches = 0;
     h->launches = 0;
+    h->rebuilds = 0;
+    if (h->pairs_acc.p) PE_CUDA(h, cudaMemset(h->pairs_acc.p, 0, sizeof(long long)));
   }
+  return PE_OK;
+}
+
+int pe_device_timer(pe_engine *h, int op, double *ms) {
+  if (!h || (op != 0 && op != 1)) return PE_ERR_ARG;
+  if (!h->timer_ev[0]) {
+    PE_CUDA(h, cudaEventCreate(&h->timer_ev[0]));
+    PE_CUDA(h, cudaEventCreate(&h->timer_ev[1]));
+  }
+  if (op == 0) {
+    PE_CUDA(h, cudaEventRecord(h->timer_ev[0], h->st));
+    return PE_OK;
+  }
+  PE_CUDA(h, cudaEventRecord(h->timer_ev[1], h->st));
+  PE_CUDA(h, cudaEventSynchronize(h->timer_ev[1]));
+  float m = 0;
+  PE_CUDA(h, cudaEventElapsedTime(&m, h->timer_ev[0], h->timer_ev[1]));
+  if (ms) *ms = m;
   return PE_OK;
 }
 

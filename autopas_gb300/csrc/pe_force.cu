@@ -373,6 +373,7 @@ __global__ void k_reduce_globals(DeviceState s, const int64_t *__restrict__ sys_
     s.sys_glob[5 * sy + 3] = vy;
     s.sys_glob[5 * sy + 4] = vz;
     s.sys_hits[sy] = redh[0] / 2;
+    atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)(redh[0] / 2));
   }
 }
 

@@ -54,6 +54,7 @@ struct DeviceState {
   unsigned long long *cl_hits = nullptr;  // [nclusters] interacting-pair counts (x2 for full lists)
   double *sys_glob = nullptr;      // [nsys*5]
   long long *sys_hits = nullptr;   // [nsys]
+  long long *pairs_acc = nullptr;  // running sum of interacting pairs over force evaluations
 
   int *err = nullptr;              // device error flags (DeviceError bits)
 };

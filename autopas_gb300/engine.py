@@ -26,7 +26,7 @@ DUMMY, OWNED, HALO = 0, 1, 2
 EXPORTS = [
     "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
-    "pe_pair_set", "pe_get_kernel_time",
+    "pe_pair_set", "pe_get_stats", "pe_device_timer",
 ]
 
 
@@ -46,6 +46,11 @@ class PeSystem(C.Structure):
 class PeGlobals(C.Structure):
     _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("virial_xyz", C.c_double * 3),
                 ("num_pairs", C.c_int64)]
+
+
+class PeStats(C.Structure):
+    _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_int64), ("kernel_launches", C.c_int64),
+                ("pairs_total", C.c_int64), ("rebuilds", C.c_int64)]
 
 
 class PeInfo(C.Structure):
@@ -86,7 +91,8 @@ def load(path: str | None = None):
     L.pe_get_info.argtypes = [vp, C.POINTER(PeInfo)]
     L.pe_get_tower_grid.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), dp]
     L.pe_pair_set.argtypes = [vp, C.c_int, C.c_int64, vp, vp, vp, C.POINTER(C.c_int64)]
-    L.pe_get_kernel_time.argtypes = [vp, C.c_int, dp, C.POINTER(C.c_int64), dp, C.POINTER(C.c_int64)]
+    L.pe_get_stats.argtypes = [vp, C.c_int, C.POINTER(PeStats)]
+    L.pe_device_timer.argtypes = [vp, C.c_int, dp]
     for name in EXPORTS:
         if name != "pe_last_error":
             getattr(L, name).restype = C.c_int
@@ -234,14 +240,18 @@ class PairEngine:
         self._check(self._L.pe_pair_set(self._h, int(which), cap, _ptr(a), _ptr(b), _ptr(c), C.byref(cnt)))
         return a[:cap], b[:cap], c[:cap]
 
-    def kernel_time(self, reset=True):
-        fm = C.c_double()
-        fl = C.c_int64()
-        tm = C.c_double()
-        tl = C.c_int64()
-        self._check(self._L.pe_get_kernel_time(self._h, int(reset), C.byref(fm), C.byref(fl), C.byref(tm),
-                                               C.byref(tl)))
-        return {"force_ms": fm.value, "force_launches": fl.value, "total_launches": tl.value}
+    def stats(self, reset=True):
+        st = PeStats()
+        self._check(self._L.pe_get_stats(self._h, int(reset), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in PeStats._fields_}
+
+    def timer_start(self):
+        self._check(self._L.pe_device_timer(self._h, 0, None))
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._check(self._L.pe_device_timer(self._h, 1, C.byref(ms)))
+        return ms.value
 
 
 def _globals(g):

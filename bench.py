@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 LJ pair-force engine: pair interactions/s and MD steps/s, FP32-mixed vs FP64.
+
+Workload (one GPU): a vapour-liquid slab of 2,000,000 LJ particles in a 3:1:1 periodic box, liquid (density
+0.75) in the middle third, vapour (0.02) elsewhere, positions uniform within each region with minimum pair
+distance 0.8, T* = 0.8, cutoff 3.0, skin 0.4, lists rebuilt every 20 steps, velocity Verlet dt = 0.002,
+truncated (unshifted) potential, single type (eps = sigma = m = 1).  Seeded synthetic data.
+
+A step is one full MD step on the device (position update, list rebuild when due, forces + globals, velocity
+update).  value = interacting pairs (dr2 <= rc^2, each unordered pair once) summed over the timed steps /
+device time of those steps (CUDA events on the engine's stream).  The working set (~0.5 GB) exceeds the 129 MB
+L2, so no flush is needed between steps.
+
+--impl reference times the reference's CPU path restated in the oracle (LinkedCells + c08 colouring + SoA LJ
+functor with newton3, OpenMP on all host cores) on a 250,000-particle slab of the same densities and shape.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RC, SKIN, DT, REBUILD = 3.0, 0.4, 0.002, 20
+FLOP_PER_PAIR = 38  # 8 distance + 18 newton3 kernel + 12 globals (unshifted), LJFunctor.h:722-789
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=2_000_000, help="particles of the slab workload")
+    p.add_argument("--fp64-steps", type=int, default=10)
+    p.add_argument("--cluster-size", type=int, default=8)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------------------------- distributed
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        # replicas only: each rank drives its own GPU; gloo carries the barrier and the max-over-ranks time
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if not pg:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if not pg:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------- workload
+def make_slab(n, seed=7):
+    from autopas_gb300 import workloads
+    return workloads.slab(n_total=n, seed=seed)
+
+
+def cpu_reference_rate(n_sample, nthreads, budget_s, max_evals=None):
+    """Pair interactions/s of the c08 CPU path (oracle restatement) on a slab sample."""
+    from oracle import oracle as orc
+    pos, vel, bmin, bmax = make_slab(n_sample, seed=17)
+    allpos, own, allt, _, _ = orc.periodic_system(pos, bmin, bmax, RC, SKIN)
+    lj = orc.LJ(RC)
+    ia, ib = orc.interacting_set(allpos, RC, own=own)
+    n = len(pos)
+    pairs = int((ib < n).sum()) + int((ib >= n).sum()) // 2
+    evals, t_total = 0, 0.0
+    while True:
+        t0 = time.perf_counter()
+        orc.cpu_lc_c08(allpos, lj, SKIN, own=own, nthreads=nthreads)
+        t_total += time.perf_counter() - t0
+        evals += 1
+        if t_total >= budget_s or (max_evals and evals >= max_evals):
+            break
+    return pairs * evals / t_total, pairs, evals, t_total
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    orc.build()
+    nthreads = os.cpu_count() or 1
+    n_sample = 250_000
+    from oracle import oracle as o2  # noqa: F401
+    pos, vel, bmin, bmax = make_slab(n_sample, seed=17)
+    allpos, own, allt, _, _ = orc.periodic_system(pos, bmin, bmax, RC, SKIN)
+    lj = orc.LJ(RC)
+    ia, ib = orc.interacting_set(allpos, RC, own=own)
+    n = len(pos)
+    pairs = int((ib < n).sum()) + int((ib >= n).sum()) // 2
+    for _ in range(max(args.warmup, 0)):
+        orc.cpu_lc_c08(allpos, lj, SKIN, own=own, nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.cpu_lc_c08(allpos, lj, SKIN, own=own, nthreads=nthreads)
+    t = time.perf_counter() - t0
+    value = pairs * args.steps / t
+    sample = (f"one step = one force evaluation (lc_c08, newton3, SoA, FP64) of a {n_sample}-particle slab with the "
+              f"workload's densities and box shape plus its periodic halo copies; {pairs} interacting pairs")
+    line = {
+        "impl": "reference", "metric": metric_name(), "value": value, "unit": "pair interactions/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(args),
+        "cpu_baseline": {"value": value, "unit": "pair interactions/s", "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "pair interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def metric_name():
+    return "pair interactions/s & MD steps/s on 1 GB300: FP32-mixed vs FP64 GPU at stated error"
+
+
+def config_dict(args):
+    return {"workload": f"LJ vapour-liquid slab: {args.n} particles, 3:1:1 periodic box, liquid 0.75 in the middle "
+                        f"third / vapour 0.02, dmin 0.8, T* 0.8, rc {RC}, skin {SKIN}, rebuild every {REBUILD} "
+                        f"steps, dt {DT}, truncated LJ, eps=sigma=m=1",
+            "particles": args.n, "cutoff": RC, "skin": SKIN, "rebuild_frequency": REBUILD,
+            "cluster_size": args.cluster_size, "newton3": False, "l2_policy": "inputs larger than L2 (no flush)"}
+
+
+# ---------------------------------------------------------------------------------------------- our arm
+def run_ours(args):
+    world, rank, local, pg = dist_setup(args)
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    from autopas_gb300 import engine as E
+
+    pos, vel, bmin, bmax = make_slab(args.n, seed=7 + rank)
+    n = len(pos)
+
+    def new_engine(prec):
+        e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
+                         newton3=0, rebuild_frequency=REBUILD, calc_globals=True)
+        e.set_particles(pos, vel)
+        return e
+
+    # ---- force error of the mixed form against the FP64 form on the initial configuration
+    err = None
+    if not args.profile:
+        e64 = new_engine(E.PRECISION_FP64)
+        g64 = e64.compute_forces()[0]
+        F64 = e64.forces()
+        e64.close()
+        em = new_engine(E.PRECISION_MIXED)
+        gm = em.compute_forces()[0]
+        Fm = em.forces()
+        em.close()
+        d = Fm - F64
+        fr = np.sqrt((F64 ** 2).sum(1))
+        frms = float(np.sqrt((fr ** 2).mean()))
+        err = {"rms_rel": float(np.sqrt((d ** 2).sum(1).mean()) / frms),
+               "max_rel": float((np.sqrt((d ** 2).sum(1)) / np.maximum(fr, frms)).max()),
+               "upot_rel": abs(gm["upot"] - g64["upot"]) / abs(g64["upot"]),
+               "virial_rel": abs(gm["virial"] - g64["virial"]) / abs(g64["virial"]),
+               "pairs_equal": gm["num_pairs"] == g64["num_pairs"],
+               "against": "this engine's FP64 form (checked against the CPU oracle to 1e-12 in tests)",
+               "definition": "rms_rel = sqrt(mean|dF|^2)/sqrt(mean|F|^2); max_rel = max |dF|/max(|F|, F_rms)"}
+        del F64, Fm
+
+    # ---- mixed MD steps (the headline)
+    e = new_engine(E.PRECISION_MIXED)
+    e.compute_forces()
+    e.step(DT, args.warmup, want_globals=False)
+    e.stats(reset=True)
+    info = e.info()
+    barrier(pg)
+    clk = ClockSampler(local) if rank == 0 else None
+    if clk:
+        clk.start()
+    e.timer_start()
+    g_last = e.step(DT, args.steps, want_globals=True)[0]
+    ms = e.timer_stop()
+    clocks = clk.stop() if clk else None
+    st = e.stats(reset=True)
+    ms_max = max_over_ranks(pg, ms)
+    pairs_total = st["pairs_total"]
+    pairs_all = sum_over_ranks(pg, pairs_total)
+    value = pairs_all / (ms_max * 1e-3)
+    steps_per_s = args.steps / (ms_max * 1e-3)
+    force_ms_per_launch = st["force_ms"] / max(st["force_launches"], 1)
+    pairs_per_launch = pairs_total / max(st["force_launches"], 1)
+
+    # ---- FP64 form on the same workload
+    fp64 = None
+    if not args.profile and args.fp64_steps > 0:
+        e2 = new_engine(E.PRECISION_FP64)
+        e2.compute_forces()
+        e2.step(DT, 1, want_globals=False)
+        e2.stats(reset=True)
+        e2.timer_start()
+        e2.step(DT, args.fp64_steps, want_globals=True)
+        ms2 = e2.timer_stop()
+        st2 = e2.stats(reset=True)
+        e2.close()
+        fp64 = {"value": st2["pairs_total"] / (ms2 * 1e-3), "unit": "pair interactions/s",
+                "md_steps_per_s": args.fp64_steps / (ms2 * 1e-3), "ms_per_step": ms2 / args.fp64_steps,
+                "steps": args.fp64_steps,
+                "force_kernel_ms": st2["force_ms"] / max(st2["force_launches"], 1)}
+
+    # ---- end to end through the C ABI with host buffers (pinned when torch is present)
+    e2e = None
+    if not args.no_e2e and not args.profile:
+        try:
+            import torch
+            pin = lambda k: torch.empty(k, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+        except Exception:
+            pin = lambda k: np.empty(k)  # noqa: E731
+        hx, hy, hz = pin(n), pin(n), pin(n)
+        hx[:], hy[:], hz[:] = pos[:, 0], pos[:, 1], pos[:, 2]
+        fx, fy, fz = pin(n), pin(n), pin(n)
+        ee = new_engine(E.PRECISION_MIXED)
+        ee.compute_forces()
+        nst = max(min(args.steps, 40), 5)
+        for k in range(3):
+            ee.update_positions(pos)
+            ee.compute_forces()
+            ee.forces_into(fx, fy, fz)
+        ee.stats(reset=True)
+        barrier(pg)
+        t0 = time.perf_counter()
+        for k in range(nst):
+            if k % REBUILD == 0:
+                ee.rebuild()
+            ee._check(ee._L.pe_update_positions(ee._h, hx.ctypes.data, hy.ctypes.data, hz.ctypes.data))
+            ee.compute_forces()
+            ee.forces_into(fx, fy, fz)
+        t_e2e = time.perf_counter() - t0
+        st3 = ee.stats(reset=True)
+        ee.close()
+        t_e2e = max_over_ranks(pg, t_e2e)
+        e2e = {"value": sum_over_ranks(pg, st3["pairs_total"]) / t_e2e, "unit": "pair interactions/s",
+               "h2d_bytes_per_step": 3 * 8 * n, "d2h_bytes_per_step": 3 * 8 * n + 48,
+               "steps": nst, "ms_per_step": 1e3 * t_e2e / nst,
+               "what": "per step: pe_update_positions from pinned host x,y,z + pe_compute_forces (pe_rebuild every "
+                       f"{REBUILD} steps) + pe_get_forces into pinned host fx,fy,fz; host wall clock"}
+
+    # ---- CPU baseline (rank 0, N = 1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
+        nthreads = os.cpu_count() or 1
+        rate, pairs_s, evals, tt = cpu_reference_rate(250_000, nthreads, budget_s=15.0, max_evals=20)
+        cpu = {"value": rate, "unit": "pair interactions/s", "cores": nthreads, "kind": "port",
+               "sample": f"{evals} force evaluations (lc_c08 + SoA LJ, newton3, FP64, OpenMP) of a 250,000-particle "
+                         f"slab with the workload's densities and shape ({pairs_s} interacting pairs), {tt:.1f} s"}
+
+    if rank != 0:
+        return 0
+    peaks = measured_peaks()
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = FLOP_PER_PAIR * pairs_per_launch / (force_ms_per_launch * 1e-3) / 1e12
+    line = {
+        "metric": metric_name(), "value": value, "unit": "pair interactions/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 LJ arithmetic on f64 state", "data": "synthetic",
+        "config": config_dict(args),
+        "md_steps_per_s": steps_per_s,
+        "force_kernel": {"ms_per_launch": force_ms_per_launch, "pairs_per_launch": pairs_per_launch,
+                         "pair_interactions_per_s": pairs_per_launch / (force_ms_per_launch * 1e-3)},
+        "fp64_gpu": fp64,
+        "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+        "force_error": err,
+        "upot_last_step": g_last["upot"], "rebuilds_in_timed_region": st["rebuilds"],
+        "engine": {k: info[k] for k in ("num_clusters", "num_cluster_pairs", "max_tower_size", "num_towers")},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "kernel": "k_lj_mixed_full<8>",
+                     "algorithmic": f"{FLOP_PER_PAIR} FLOP per interacting pair (reference convention)",
+                     "peak_source": f"nominal CUDA-core FP32: 152 SM x 128 lanes x 2 FLOP x {sm_max:.0f} MHz "
+                                    "(MEASURED_PEAKS.json holds no CUDA-core figure; hbm/bf16 peaks do not bound "
+                                    "this kernel)"},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["kernel_launches"], "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

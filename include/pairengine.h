@@ -155,10 +155,21 @@ int pe_get_tower_grid(pe_engine *h, int system, double *side, int64_t *num, int6
  * Writes up to cap entries and returns the total count in *count. */
 int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code, int64_t *count);
 
-/* CUDA-event timing of the last pe_compute_forces / pe_step force kernels (ms, summed over launches) and
- * launch count; reset with reset != 0. */
-int pe_get_kernel_time(pe_engine *h, int reset, double *force_ms, int64_t *force_launches, double *total_ms,
-                       int64_t *total_launches);
+/* Counters of the engine since the last reset: CUDA-event time of the force kernels (recorded on the engine's
+ * stream around every force launch), launches of the engine's own kernels, interacting pairs summed over all
+ * force evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds. */
+typedef struct {
+  double force_ms;
+  int64_t force_launches;
+  int64_t kernel_launches;
+  int64_t pairs_total;
+  int64_t rebuilds;
+} pe_stats;
+int pe_get_stats(pe_engine *h, int reset, pe_stats *out);
+
+/* Device timer on the engine's stream: op 0 records a start event; op 1 records a stop event, waits for it and
+ * returns the elapsed milliseconds between the two in *ms. */
+int pe_device_timer(pe_engine *h, int op, double *ms);
 
 #ifdef __cplusplus
 }

@@ -37,6 +37,8 @@ typedef struct {
 static void soa_single(const soa_t *s, int64_t b, int64_t e, const orc_lj_params *p, tglob_t *g) {
   const double c2 = p->cutoff * p->cutoff;
   const int T = p->ntypes;
+  /* single-type functor (useMixing = false): constants, no table lookups in the vector loop */
+  const double sig2c = p->sig2[0], eps24c = p->eps24[0], sh6c = p->shift6[0];
   for (int64_t i = b; i < e; ++i) {
     if (s->o[i] == ORC_DUMMY) continue;
     double fxa = 0, fya = 0, fza = 0, up = 0, vx = 0, vy = 0, vz = 0;
@@ -46,8 +48,9 @@ static void soa_single(const soa_t *s, int64_t b, int64_t e, const orc_lj_params
     const double oi = s->o[i] == ORC_OWNED ? 1. : 0.;
 #pragma omp simd reduction(+ : fxa, fya, fza, up, vx, vy, vz, hits)
     for (int64_t j = i + 1; j < e; ++j) {
-      const int k = ti * T + s->t[j];
-      const double sig2 = p->sig2[k], eps24 = p->eps24[k], sh6 = p->shift6[k];
+      const int k = T == 1 ? 0 : ti * T + s->t[j];
+      const double sig2 = T == 1 ? sig2c : p->sig2[k], eps24 = T == 1 ? eps24c : p->eps24[k],
+                   sh6 = T == 1 ? sh6c : p->shift6[k];
       const double dx = xi - s->x[j], dy = yi - s->y[j], dz = zi - s->z[j];
       const double dr2 = dx * dx + dy * dy + dz * dz;
       const int mask = dr2 <= c2 && s->o[j] != ORC_DUMMY;
@@ -86,6 +89,8 @@ static void soa_pair(const soa_t *s, int64_t b1, int64_t e1, int64_t b2, int64_t
                      tglob_t *g) {
   const double c2 = p->cutoff * p->cutoff;
   const int T = p->ntypes;
+  /* single-type functor (useMixing = false): constants, no table lookups in the vector loop */
+  const double sig2c = p->sig2[0], eps24c = p->eps24[0], sh6c = p->shift6[0];
   for (int64_t i = b1; i < e1; ++i) {
     if (s->o[i] == ORC_DUMMY) continue;
     double fxa = 0, fya = 0, fza = 0, up = 0, vx = 0, vy = 0, vz = 0;
@@ -95,8 +100,9 @@ static void soa_pair(const soa_t *s, int64_t b1, int64_t e1, int64_t b2, int64_t
     const double oi = s->o[i] == ORC_OWNED ? 1. : 0.;
 #pragma omp simd reduction(+ : fxa, fya, fza, up, vx, vy, vz, hits)
     for (int64_t j = b2; j < e2; ++j) {
-      const int k = ti * T + s->t[j];
-      const double sig2 = p->sig2[k], eps24 = p->eps24[k], sh6 = p->shift6[k];
+      const int k = T == 1 ? 0 : ti * T + s->t[j];
+      const double sig2 = T == 1 ? sig2c : p->sig2[k], eps24 = T == 1 ? eps24c : p->eps24[k],
+                   sh6 = T == 1 ? sh6c : p->shift6[k];
       const double dx = xi - s->x[j], dy = yi - s->y[j], dz = zi - s->z[j];
       const double dr2 = dx * dx + dy * dy + dz * dz;
       const int mask = dr2 <= c2 && s->o[j] != ORC_DUMMY;
