@@ -245,6 +245,59 @@ __device__ __forceinline__ double gap1(double alo, double ahi, double blo, doubl
 
 constexpr int kListWarps = 4;
 
+// Candidate segments of an i-cluster: for every neighbour tower (xy offset within the tower reach, wrapped
+// with an image shift for periodic systems) and z image shift, the run of the tower's clusters whose z-range
+// can come within L.  Lanes find the runs of 32 segments at once (two binary searches each, since lo.z and
+// hi.z are non-decreasing inside a tower); the runs are then walked in segment order, so the list order is
+// deterministic.
+__device__ __forceinline__ void segment_run(const DeviceState &s, const SysDev &S, int tx, int ty, int seg,
+                                            int nseg_z, const double *alo, const double *ahi, double L2, double Lz,
+                                            int &c_first, int &c_end, int &code, double &shx, double &shy,
+                                            double &shz) {
+  c_first = c_end = 0;
+  const int side_x = 2 * S.kx + 1;
+  const int sz = (seg % nseg_z) - (nseg_z > 1 ? 1 : 0);
+  const int txy = seg / nseg_z;
+  const int dx = txy % side_x - S.kx, dy = txy / side_x - S.ky;
+  int nx = tx + dx, ny = ty + dy, sx = 0, sy = 0;
+  if (S.periodic) {
+    if (nx < 0) { nx += S.nt[0]; sx = -1; }
+    else if (nx >= S.nt[0]) { nx -= S.nt[0]; sx = 1; }
+    if (ny < 0) { ny += S.nt[1]; sy = -1; }
+    else if (ny >= S.nt[1]) { ny -= S.nt[1]; sy = 1; }
+    if (nx < 0 || ny < 0 || nx >= S.nt[0] || ny >= S.nt[1]) return;
+  } else if (nx < 0 || ny < 0 || nx >= S.nt[0] || ny >= S.nt[1]) {
+    return;
+  }
+  shx = sx == 0 ? 0.0 : (sx > 0 ? S.len[0] : -S.len[0]);
+  shy = sy == 0 ? 0.0 : (sy > 0 ? S.len[1] : -S.len[1]);
+  shz = sz == 0 ? 0.0 : (sz > 0 ? S.len[2] : -S.len[2]);
+  // an image shifted in z can only matter for an i-cluster near the opposite face
+  if (sz > 0 && S.bmin[2] + shz > ahi[2] + Lz) return;
+  if (sz < 0 && S.bmax[2] + shz < alo[2] - Lz) return;
+  const int tB = S.tower_base + ny * S.nt[0] + nx;
+  const int c0 = s.tw_cl_start[tB], c1 = s.tw_cl_start[tB + 1];
+  if (c0 == c1) return;
+  const double gx = gap1(alo[0], ahi[0], s.tw_bb[4 * tB + 0] + shx, s.tw_bb[4 * tB + 2] + shx);
+  const double gy = gap1(alo[1], ahi[1], s.tw_bb[4 * tB + 1] + shy, s.tw_bb[4 * tB + 3] + shy);
+  if (gx * gx + gy * gy > L2) return;
+  const double zmin = alo[2] - Lz - shz;  // candidates need hi.z >= zmin
+  const double zmax = ahi[2] + Lz - shz;  // and lo.z <= zmax
+  int a = c0, b = c1;
+  while (a < b) {
+    const int m = (a + b) >> 1;
+    if (s.cl_bb[6 * (int64_t)m + 5] < zmin) a = m + 1; else b = m;
+  }
+  int a2 = a, b2 = c1;
+  while (a2 < b2) {
+    const int m = (a2 + b2) >> 1;
+    if (s.cl_bb[6 * (int64_t)m + 2] <= zmax) a2 = m + 1; else b2 = m;
+  }
+  c_first = a;
+  c_end = a2;
+  code = shift_code(sx, sy, sz);
+}
+
 __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
   extern __shared__ uint32_t lbuf[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -277,74 +330,45 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     if (lane == 0) buf[0] = ((uint32_t)A << 5) | kShiftNone;
     cnt = 1;
   }
-  const int zlo_s = S.periodic ? -1 : 0, zhi_s = S.periodic ? 1 : 0;
-  for (int dy = -S.ky; dy <= S.ky && !overflow; ++dy) {
-    for (int dx = -S.kx; dx <= S.kx && !overflow; ++dx) {
-      int nx = tx + dx, ny = ty + dy, sx = 0, sy = 0;
-      if (S.periodic) {
-        while (nx < 0) { nx += S.nt[0]; sx -= 1; }
-        while (nx >= S.nt[0]) { nx -= S.nt[0]; sx += 1; }
-        while (ny < 0) { ny += S.nt[1]; sy -= 1; }
-        while (ny >= S.nt[1]) { ny -= S.nt[1]; sy += 1; }
-        if (sx < -1 || sx > 1 || sy < -1 || sy > 1) continue;
-      } else if (nx < 0 || ny < 0 || nx >= S.nt[0] || ny >= S.nt[1]) {
-        continue;
-      }
-      const int tB = S.tower_base + ny * S.nt[0] + nx;
-      const int c0 = s.tw_cl_start[tB], c1 = s.tw_cl_start[tB + 1];
-      if (c0 == c1) continue;
-      const double shx = sx == 0 ? 0.0 : (sx > 0 ? S.len[0] : -S.len[0]);
-      const double shy = sy == 0 ? 0.0 : (sy > 0 ? S.len[1] : -S.len[1]);
-      {
-        const double gx = gap1(alo[0], ahi[0], s.tw_bb[4 * tB + 0] + shx, s.tw_bb[4 * tB + 2] + shx);
-        const double gy = gap1(alo[1], ahi[1], s.tw_bb[4 * tB + 1] + shy, s.tw_bb[4 * tB + 3] + shy);
-        if (gx * gx + gy * gy > L2) continue;
-      }
-      for (int sz = zlo_s; sz <= zhi_s && !overflow; ++sz) {
-        const double shz = sz == 0 ? 0.0 : (sz > 0 ? S.len[2] : -S.len[2]);
-        const double zmin = alo[2] - Lz - shz;  // candidates need hi.z >= zmin
-        const double zmax = ahi[2] + Lz - shz;  // and lo.z <= zmax
-        // first cluster with hi.z >= zmin (hi.z is non-decreasing inside a tower)
-        int a = c0, b = c1;
-        while (a < b) {
-          const int m = (a + b) >> 1;
-          if (s.cl_bb[6 * (int64_t)m + 5] < zmin)
-            a = m + 1;
-          else
-            b = m;
-        }
-        const int code = shift_code(sx, sy, sz);
-        for (int cb = a; cb < c1; cb += 32) {
-          const int c = cb + lane;
-          bool inrange = false, accept = false;
-          if (c < c1) {
-            const double blz = s.cl_bb[6 * (int64_t)c + 2];
-            inrange = blz <= zmax;
-            if (inrange) {
-              const bool self = (c == A && code == kShiftNone);
-              bool canon = true;
-              if (s.newton3) canon = (c > A) || (c == A && code > kShiftNone);
-              const int fb = s.cl_flags[c];
-              const bool haloHalo = !aOwned && !(fb & 1);
-              if (!self && canon && !haloHalo && (fb & 2)) {
-                const double g0 = gap1(alo[0], ahi[0], s.cl_bb[6 * (int64_t)c + 0] + shx, s.cl_bb[6 * (int64_t)c + 3] + shx);
-                const double g1 = gap1(alo[1], ahi[1], s.cl_bb[6 * (int64_t)c + 1] + shy, s.cl_bb[6 * (int64_t)c + 4] + shy);
-                const double g2 = gap1(alo[2], ahi[2], blz + shz, s.cl_bb[6 * (int64_t)c + 5] + shz);
-                accept = (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
-              }
-            }
+  const int nseg_z = S.periodic ? 3 : 1;
+  const int nseg = (2 * S.kx + 1) * (2 * S.ky + 1) * nseg_z;
+  for (int sb = 0; sb < nseg && !overflow; sb += 32) {
+    int cf = 0, ce = 0, code = kShiftNone;
+    double shx = 0, shy = 0, shz = 0;
+    if (sb + lane < nseg) segment_run(s, S, tx, ty, sb + lane, nseg_z, alo, ahi, L2, Lz, cf, ce, code, shx, shy, shz);
+    unsigned live = __ballot_sync(0xffffffffu, ce > cf);
+    while (live && !overflow) {
+      const int src = __ffs(live) - 1;
+      live &= live - 1;
+      const int f = __shfl_sync(0xffffffffu, cf, src), e = __shfl_sync(0xffffffffu, ce, src);
+      const int cd = __shfl_sync(0xffffffffu, code, src);
+      const double hx = __shfl_sync(0xffffffffu, shx, src), hy = __shfl_sync(0xffffffffu, shy, src);
+      const double hz = __shfl_sync(0xffffffffu, shz, src);
+      for (int cb = f; cb < e; cb += 32) {
+        const int c = cb + lane;
+        bool accept = false;
+        if (c < e) {
+          const bool self = (c == A && cd == kShiftNone);
+          bool canon = true;
+          if (s.newton3) canon = (c > A) || (c == A && cd > kShiftNone);
+          const int fb = s.cl_flags[c];
+          const bool haloHalo = !aOwned && !(fb & 1);
+          if (!self && canon && !haloHalo && (fb & 2)) {
+            const double *bb = s.cl_bb + 6 * (int64_t)c;
+            const double g0 = gap1(alo[0], ahi[0], bb[0] + hx, bb[3] + hx);
+            const double g1 = gap1(alo[1], ahi[1], bb[1] + hy, bb[4] + hy);
+            const double g2 = gap1(alo[2], ahi[2], bb[2] + hz, bb[5] + hz);
+            accept = (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
           }
-          const unsigned am = __ballot_sync(0xffffffffu, accept);
-          const unsigned rm = __ballot_sync(0xffffffffu, inrange);
-          const int na = __popc(am);
-          if (cnt + na > kListBufPerWarp) {
-            overflow = true;
-            break;
-          }
-          if (accept) buf[cnt + __popc(am & ((1u << lane) - 1))] = ((uint32_t)c << 5) | (uint32_t)code;
-          cnt += na;
-          if (rm != 0xffffffffu) break;  // some lane left the z window (or the tower): later ones are out too
         }
+        const unsigned am = __ballot_sync(0xffffffffu, accept);
+        const int na = __popc(am);
+        if (cnt + na > kListBufPerWarp) {
+          overflow = true;
+          break;
+        }
+        if (accept) buf[cnt + __popc(am & ((1u << lane) - 1))] = ((uint32_t)c << 5) | (uint32_t)cd;
+        cnt += na;
       }
     }
   }

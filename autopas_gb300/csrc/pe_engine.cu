@@ -68,6 +68,10 @@ struct ParticleArrays {
 struct SysHost {
   pe_system_desc desc;
   int64_t count = 0;  // real particles of this system
+  double density = 0; // density used to size the towers (0: box average)
+  std::vector<int64_t> hist;
+  int64_t hist_cells = 0, hist_nc[3] = {1, 1, 1};
+  double hist_inv[3] = {1, 1, 1};
   SysDev dev;
   int64_t ntowers = 0;
 };
@@ -111,6 +115,10 @@ struct pe_engine {
   DBuf<double> sys_glob;
   DBuf<long long> sys_hits;
   DBuf<int64_t> sys_cl_range;
+  DBuf<int64_t> chunks;        // (system, first cluster, end cluster) per reduction chunk
+  DBuf<int32_t> sys_chunk0;    // first chunk of each system, [nsys+1]
+  DBuf<double> chunk_part;     // [nchunks*5]
+  int nchunks = 0;
   DBuf<int32_t> sys_tower_base;
   int64_t max_tower = 0;
   int64_t num_cluster_pairs = 0;
@@ -456,7 +464,7 @@ static double next_pow2(double v) {
 
 // ClusterTowerBlock2D::estimateOptimalGridSideLength (ClusterTowerBlock2D.h:140-168) and resize() (:89-108).
 // A periodic system gets a grid that tiles exactly its box (no halo towers: images come from shifts).
-static void compute_grid(SysHost &S, int C, double L, int64_t count) {
+static void compute_grid(SysHost &S, int C, double L, int64_t count, double density_override) {
   SysDev &d = S.dev;
   const double box[3] = {S.desc.box_max[0] - S.desc.box_min[0], S.desc.box_max[1] - S.desc.box_min[1],
                          S.desc.box_max[2] - S.desc.box_min[2]};
@@ -473,7 +481,7 @@ static void compute_grid(SysHost &S, int C, double L, int64_t count) {
     }
   } else {
     const double volume = box[0] * box[1] * box[2];
-    const double density = (double)count / volume;
+    const double density = density_override > 0 ? density_override : (double)count / volume;
     const double opt = std::cbrt((double)C / density);
     for (int q = 0; q < 2; ++q) {
       const double no = std::ceil(box[q] / opt);
@@ -526,6 +534,67 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
   }
 }
 
+// Local density per system for tower sizing: particles are histogrammed on a coarse grid (cells of about
+// rc+skin, at most 64 per dimension); the result is the cell density below which 90% of the particles lie.
+static void estimate_densities(pe_engine *h, int64_t n, const double *x, const double *y, const double *z,
+                               const int8_t *own, const int32_t *system) {
+  const double L = h->cfg.cutoff + h->cfg.skin;
+  const int ns = (int)h->sys.size();
+  for (int q = 0; q < ns; ++q) {
+    SysHost &S = h->sys[q];
+    S.density = 0;
+    int64_t nc[3];
+    double inv[3];
+    for (int d = 0; d < 3; ++d) {
+      const double len = S.desc.box_max[d] - S.desc.box_min[d];
+      nc[d] = std::max<int64_t>(1, std::min<int64_t>(64, (int64_t)(len / L)));
+      inv[d] = nc[d] / len;
+    }
+    S.hist_cells = nc[0] * nc[1] * nc[2];
+    S.hist.assign((size_t)S.hist_cells, 0);
+    S.hist_nc[0] = nc[0];
+    S.hist_nc[1] = nc[1];
+    S.hist_nc[2] = nc[2];
+    S.hist_inv[0] = inv[0];
+    S.hist_inv[1] = inv[1];
+    S.hist_inv[2] = inv[2];
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    if (own && own[i] == PE_DUMMY) continue;
+    SysHost &S = h->sys[system ? system[i] : 0];
+    const double p[3] = {x[i], y[i], z[i]};
+    int64_t c[3];
+    bool inside = true;
+    for (int d = 0; d < 3; ++d) {
+      const double u = (p[d] - S.desc.box_min[d]) * S.hist_inv[d];
+      if (!(u >= 0 && u < (double)S.hist_nc[d])) inside = false;
+      c[d] = (int64_t)u;
+    }
+    if (!inside) continue;
+    S.hist[(size_t)((c[2] * S.hist_nc[1] + c[1]) * S.hist_nc[0] + c[0])]++;
+  }
+  for (int q = 0; q < ns; ++q) {
+    SysHost &S = h->sys[q];
+    std::vector<int64_t> v(S.hist);
+    std::sort(v.begin(), v.end());
+    int64_t total = 0;
+    for (auto c : v) total += c;
+    if (total == 0) continue;
+    double cellvol = 1;
+    for (int d = 0; d < 3; ++d) cellvol *= (S.desc.box_max[d] - S.desc.box_min[d]) / S.hist_nc[d];
+    int64_t acc = 0;
+    for (auto c : v) {
+      acc += c;
+      if (acc >= 0.9 * total) {
+        S.density = std::max((double)c / cellvol, (double)total / (cellvol * S.hist_cells));
+        break;
+      }
+    }
+    S.hist.clear();
+    S.hist.shrink_to_fit();
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // engine operations
 // ---------------------------------------------------------------------------------------------
@@ -534,7 +603,7 @@ static int setup_grids(pe_engine *h) {
   int64_t base = 0;
   std::vector<int32_t> tbase;
   for (auto &S : h->sys) {
-    compute_grid(S, h->C, L, S.count);
+    compute_grid(S, h->C, L, S.count, h->cfg.tower_sizing == 1 ? S.density : 0.0);
     compute_encoding(S, h->cfg.cutoff, h->cfg.skin);
     if (S.desc.periodic) {
       for (int q = 0; q < 3; ++q)
@@ -658,6 +727,32 @@ static int do_rebuild(pe_engine *h) {
   const int ns = (int)h->sys.size();
   k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
   h->launches += 1;
+  {
+    // reduction chunks for the per-system globals
+    std::vector<int64_t> rng(2 * ns);
+    PE_CUDA(h, cudaMemcpyAsync(rng.data(), h->sys_cl_range.p, sizeof(int64_t) * 2 * ns, cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaStreamSynchronize(st));
+    std::vector<int64_t> ch;
+    std::vector<int32_t> c0(ns + 1);
+    int k = 0;
+    for (int q = 0; q < ns; ++q) {
+      c0[q] = k;
+      for (int64_t a = rng[2 * q]; a < rng[2 * q + 1]; a += kChunk, ++k) {
+        ch.push_back(q);
+        ch.push_back(a);
+        ch.push_back(std::min<int64_t>(a + kChunk, rng[2 * q + 1]));
+      }
+    }
+    c0[ns] = k;
+    h->nchunks = k;
+    if (!h->chunks.ensure(std::max<size_t>(ch.size(), 3)) || !h->sys_chunk0.ensure(ns + 1) ||
+        !h->chunk_part.ensure(5 * (size_t)std::max(k, 1)))
+      return h->fail(PE_ERR_OOM, "reduction chunks");
+    if (!ch.empty())
+      PE_CUDA(h, cudaMemcpyAsync(h->chunks.p, ch.data(), sizeof(int64_t) * ch.size(), cudaMemcpyHostToDevice, st));
+    PE_CUDA(h, cudaMemcpyAsync(h->sys_chunk0.p, c0.data(), sizeof(int32_t) * (ns + 1), cudaMemcpyHostToDevice, st));
+    PE_CUDA(h, cudaStreamSynchronize(st));
+  }
   PE_TRY(h->cuda_check("rebuild"));
   h->lists_valid = true;
   h->steps_since_rebuild = 0;
@@ -683,8 +778,8 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
   h->launches += 1;
   h->force_launches += 1;
   if (h->cfg.calc_globals) {
-    launch_reduce_globals_range(s, h->sys_cl_range.p, h->st);
-    h->launches += 1;
+    launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->st);
+    h->launches += 2;
   }
   h->steps_since_rebuild += 1;
   h->forces_valid = true;
@@ -727,6 +822,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->precision != PE_PRECISION_FP64 && cfg->precision != PE_PRECISION_MIXED) return PE_ERR_ARG;
   if (cfg->cluster_size != 0 && cfg->cluster_size != 4 && cfg->cluster_size != 8) return PE_ERR_ARG;
   if (cfg->dist_mode < 0 || cfg->dist_mode > 2) return PE_ERR_ARG;
+  if (cfg->tower_sizing < 0 || cfg->tower_sizing > 1) return PE_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PE_ERR_NO_DEVICE;
   pe_engine *h = new pe_engine();
@@ -795,7 +891,9 @@ int pe_destroy(pe_engine *h) {
                   &h->dump_c})
     b->release();
   for (auto *b : {&h->tw_bb, &h->cl_bb, &h->cl_glob, &h->sys_glob, &h->dmass, &h->tmp3}) b->release();
-  for (auto *b : {&h->cp_start, &h->sys_cl_range, &h->dump_a, &h->dump_b}) b->release();
+  for (auto *b : {&h->cp_start, &h->sys_cl_range, &h->dump_a, &h->dump_b, &h->chunks}) b->release();
+  h->sys_chunk0.release();
+  h->chunk_part.release();
   h->cp_list.release();
   h->cp_total.release();
   h->cl_hits.release();
@@ -837,6 +935,7 @@ int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, 
     h->sys[sy].count++;
   }
   h->nuser = n;
+  if (h->cfg.tower_sizing == 1) estimate_densities(h, n, x, y, z, ownership, system);
   PE_TRY(setup_grids(h));
   PE_TRY(ensure_particle_capacity(h));
   cudaStream_t st = h->st;

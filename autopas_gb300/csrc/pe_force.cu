@@ -49,7 +49,7 @@ __device__ __forceinline__ void kahan_add(float &sum, float &c, float v) {
 }
 
 // exact FP64 cutoff test of pair (i, image of j with shift code) -- used near the cutoff only
-__device__ __noinline__ bool exact_within(const DeviceState &s, const SysDev &S, int64_t i, int64_t j, int code,
+__device__ __forceinline__ bool exact_within(const DeviceState &s, const SysDev &S, int64_t i, int64_t j, int code,
                                           double rc2) {
   int sx, sy, sz;
   shift_of(code, sx, sy, sz);
@@ -61,12 +61,18 @@ __device__ __noinline__ bool exact_within(const DeviceState &s, const SysDev &S,
 
 // ---------------------------------------------------------------------------------------------
 // mixed precision, full lists
+//
+// Each lane evaluates two pairs per iteration: flat j-slot f = jl + p*JL (p = 0, 1) of the iteration's
+// 64/C^2 list entries (C = 8: one entry, j = jl and jl+4; C = 4: four entries, one j each).  Dummy slots sit
+// far outside every box and the self pair has r2 == 0, so the mask is just 0 < r2 <= rc2: no ownership load
+// for j unless the system carries halo particles.
 // ---------------------------------------------------------------------------------------------
-template <int C, bool GLOB, bool ONE_TYPE>
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN>
 __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs fa) {
   constexpr int JL = 32 / C;
+  constexpr int EPI = 64 / (C * C);  // list entries per iteration
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
-  const int T = s.types->ntypes;
+  const int T = s.ntypes;
   if (!ONE_TYPE) {
     for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
       tab[0][q] = (float)s.types->eps24[q];
@@ -80,15 +86,14 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
   if (A >= s.nclusters) return;
   const int n = s.cp_count[A];
   if (n == 0) return;
-  const int64_t lst = s.cp_start[A];
+  const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
   const int ii = lane % C, jl = lane / C;
   const int64_t i = A * C + ii;
   const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
   const int wi = __float_as_int(hi_i.w);
   const int ti = wi & 0xffff, oi = wi >> 16;
   const SysDev &S = s.sysd[s.cl_sys[A]];
-  const float lhx = S.len_hi[0], lhy = S.len_hi[1], lhz = S.len_hi[2];
-  const float llx = S.len_lo[0], lly = S.len_lo[1], llz = S.len_lo[2];
+  const bool halos = !S.periodic;
   float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
   if (ONE_TYPE) {
     eps24 = (float)s.types->eps24[0];
@@ -96,64 +101,72 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
     sh6 = (float)s.types->shift6[0];
   }
   const float rc2f = fa.rc2f;
-  const float nearband = rc2f * 2e-6f;
+  const float band = rc2f * 2e-6f;
 
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
-  int hits2 = 0;
-  const int total = n * C;
-#pragma unroll 2
-  for (int t = jl; t < total; t += JL) {
-    const int e = t / C, jj = t % C;
-    const uint32_t ent = __ldg(&s.cp_list[lst + e]);
-    const int64_t B = ent >> 5;
-    const int code = ent & 31;
-    const int64_t j = B * C + jj;
-    const float4 hj = __ldg(&s.pk_hi[j]);
-    const float4 lj = __ldg(&s.pk_lo[j]);
-    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-    if (code != kShiftNone) {
-      // the j image sits at x_j + s*len; shifting i by -s*len instead keeps the hi part exact
-      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
-      xh = fmaf(-sxf, lhx, xh);
-      yh = fmaf(-syf, lhy, yh);
-      zh = fmaf(-szf, lhz, zh);
-      xl = fmaf(-sxf, llx, xl);
-      yl = fmaf(-syf, lly, yl);
-      zl = fmaf(-szf, llz, zl);
-    }
-    const float dx = (xh - hj.x) + (xl - lj.x);
-    const float dy = (yh - hj.y) + (yl - lj.y);
-    const float dz = (zh - hj.z) + (zl - lj.z);
-    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const int wj = __float_as_int(hj.w);
-    const int oj = wj >> 16;
-    const bool valid = (oj != 0) && !(B == A && code == kShiftNone && jj == ii);
-    bool within = r2 <= rc2f;
-    if (valid && fabsf(r2 - rc2f) <= nearband) within = exact_within(s, S, i, j, code, fa.rc2);
-    const bool mask = valid && within;
-    if (!ONE_TYPE) {
-      const int k = ti * T + (wj & 0xffff);
-      eps24 = tab[0][k];
-      sig2 = tab[1][k];
-      sh6 = tab[2][k];
-    }
-    const float inv = rcp_nr(r2);
-    const float lj2 = sig2 * inv;
-    const float lj6 = lj2 * lj2 * lj2;
-    const float lj12 = lj6 * lj6;
-    const float lj12m6 = lj12 - lj6;
-    float fac = eps24 * (lj12 + lj12m6) * inv;
-    fac = mask ? fac : 0.f;
-    kahan_add(fxs, fxc, dx * fac);
-    kahan_add(fys, fyc, dy * fac);
-    kahan_add(fzs, fzc, dz * fac);
-    if (GLOB) {
-      pot += mask ? (eps24 * lj12m6 + sh6) : 0.f;
-      vx = fmaf(dx * fac, dx, vx);
-      vy = fmaf(dy * fac, dy, vy);
-      vz = fmaf(dz * fac, dz, vz);
-      hits2 += mask ? (oj == 1 ? 1 : 2) : 0;
+  int hits = 0, hhalo = 0;
+
+  for (int e = 0; e < n; e += EPI) {
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const int f = jl + p * JL;
+      const int ee = e + f / C;
+      const int jj = f % C;
+      if (EPI > 1 && ee >= n) continue;
+      const uint32_t ent = __ldg(lst + ee);
+      const int64_t j = (int64_t)(ent >> 5) * C + jj;
+      const int code = ent & 31;
+      const float4 hj = __ldg(&s.pk_hi[j]);
+      const float4 lj = __ldg(&s.pk_lo[j]);
+      float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+      if (code != kShiftNone) {
+        // the j image sits at x_j + s*len; moving i by -s*len instead keeps the hi difference exact
+        const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+        xh = fmaf(-sxf, S.len_hi[0], xh);
+        yh = fmaf(-syf, S.len_hi[1], yh);
+        zh = fmaf(-szf, S.len_hi[2], zh);
+        xl = fmaf(-sxf, S.len_lo[0], xl);
+        yl = fmaf(-syf, S.len_lo[1], yl);
+        zl = fmaf(-szf, S.len_lo[2], zl);
+      }
+      const float dx = (xh - hj.x) + (xl - lj.x);
+      const float dy = (yh - hj.y) + (yl - lj.y);
+      const float dz = (zh - hj.z) + (zl - lj.z);
+      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      bool mask = (r2 <= rc2f) && (r2 > 0.f);
+      if (fabsf(r2 - rc2f) <= band) mask = (r2 > 0.f) && exact_within(s, S, i, j, code, fa.rc2);
+      if (!ONE_TYPE) {
+        const int k = ti * T + (__float_as_int(hj.w) & 0xffff);
+        eps24 = tab[0][k];
+        sig2 = tab[1][k];
+        sh6 = tab[2][k];
+      }
+      const float inv = rcp_nr(r2);
+      const float lj2 = sig2 * inv;
+      const float lj6 = lj2 * lj2 * lj2;
+      const float lj12 = lj6 * lj6;
+      const float lj12m6 = lj12 - lj6;
+      float fac = eps24 * (lj12 + lj12m6) * inv;
+      fac = mask ? fac : 0.f;
+      const float px = dx * fac, py = dy * fac, pz = dz * fac;
+      if (KAHAN) {
+        kahan_add(fxs, fxc, px);
+        kahan_add(fys, fyc, py);
+        kahan_add(fzs, fzc, pz);
+      } else {
+        fxs += px;
+        fys += py;
+        fzs += pz;
+      }
+      if (GLOB) {
+        pot += mask ? fmaf(eps24, lj12m6, sh6) : 0.f;
+        vx = fmaf(px, dx, vx);
+        vy = fmaf(py, dy, vy);
+        vz = fmaf(pz, dz, vz);
+        hits += mask ? 1 : 0;
+        if (halos) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
+      }
     }
   }
   // combine the j-lanes of each i (lanes ii, ii+C, ii+2C, ...) in FP64
@@ -178,9 +191,11 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
     }
   }
   if (GLOB) {
-    const double own_i = oi == 1 ? 1.0 : 0.0;  // energyFactor of the non-newton3 functor call
-    double g0 = own_i * pot, g1 = own_i * vx, g2 = own_i * vy, g3 = own_i * vz;
-    long long h = oi == 1 ? hits2 : 0;
+    const bool owned = oi == 1;  // energyFactor of the non-newton3 functor call
+    double g0 = owned ? (double)pot : 0.0, g1 = owned ? (double)vx : 0.0;
+    double g2 = owned ? (double)vy : 0.0, g3 = owned ? (double)vz : 0.0;
+    // unique pairs x2: owned-owned pairs are seen from both sides, owned-halo ones once
+    long long h = owned ? (long long)(hits + hhalo) : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       g0 += __shfl_xor_sync(0xffffffffu, g0, o);
@@ -315,14 +330,14 @@ static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, c
   const int T = s.ntypes;
   if (T == 1) {
     if (fa.calc_globals)
-      k_lj_mixed_full<C, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      k_lj_mixed_full<C, true, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     else
-      k_lj_mixed_full<C, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      k_lj_mixed_full<C, false, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
   } else {
     if (fa.calc_globals)
-      k_lj_mixed_full<C, true, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      k_lj_mixed_full<C, true, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     else
-      k_lj_mixed_full<C, false, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      k_lj_mixed_full<C, false, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
   }
 }
 
@@ -340,15 +355,17 @@ void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_vel
 }
 
 // ---------------------------------------------------------------------------------------------
-// per-system globals: deterministic block reduction over the system's clusters, then
-// LJFunctor::endTraversal post-processing (x0.5, /6; LJFunctor.h:661-685)
+// per-system globals: the clusters of each system are cut into chunks of at most kChunk clusters; one block
+// reduces each chunk (fixed thread assignment and tree), then one thread per system adds its chunks in
+// order, so the result is bitwise reproducible.  LJFunctor::endTraversal post-processing (x0.5, /6;
+// LJFunctor.h:661-685) is applied at the end.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_reduce_globals(DeviceState s, const int64_t *__restrict__ sys_cl_range) {
-  const int sy = blockIdx.x;
-  const int64_t c0 = sys_cl_range[2 * sy], c1 = sys_cl_range[2 * sy + 1];
+__global__ void k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, double *__restrict__ cpart) {
+  const int64_t c0 = chunks[3 * blockIdx.x + 1], c1 = chunks[3 * blockIdx.x + 2];
   double g[4] = {0, 0, 0, 0};
   long long h = 0;
   for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+#pragma unroll
     for (int q = 0; q < 4; ++q) g[q] += s.cl_glob[4 * c + q];
     h += (long long)s.cl_hits[c];
   }
@@ -365,20 +382,36 @@ __global__ void k_reduce_globals(DeviceState s, const int64_t *__restrict__ sys_
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double up = red[0][0] * 0.5 / 6.;
-    const double vx = red[1][0] * 0.5, vy = red[2][0] * 0.5, vz = red[3][0] * 0.5;
-    s.sys_glob[5 * sy + 0] = up;
-    s.sys_glob[5 * sy + 1] = vx + vy + vz;
-    s.sys_glob[5 * sy + 2] = vx;
-    s.sys_glob[5 * sy + 3] = vy;
-    s.sys_glob[5 * sy + 4] = vz;
-    s.sys_hits[sy] = redh[0] / 2;
-    atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)(redh[0] / 2));
+    for (int q = 0; q < 4; ++q) cpart[5 * blockIdx.x + q] = red[q][0];
+    cpart[5 * blockIdx.x + 4] = (double)redh[0];
   }
 }
 
-void launch_reduce_globals_range(DeviceState &s, const int64_t *sys_cl_range, cudaStream_t st) {
-  if (s.nsys > 0) k_reduce_globals<<<s.nsys, 256, 0, st>>>(s, sys_cl_range);
+__global__ void k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0, const double *__restrict__ cpart) {
+  const int sy = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sy >= s.nsys) return;
+  double g[4] = {0, 0, 0, 0};
+  double h = 0;
+  for (int k = sys_chunk0[sy]; k < sys_chunk0[sy + 1]; ++k) {
+    for (int q = 0; q < 4; ++q) g[q] += cpart[5 * k + q];
+    h += cpart[5 * k + 4];
+  }
+  const double up = g[0] * 0.5 / 6.;
+  const double vx = g[1] * 0.5, vy = g[2] * 0.5, vz = g[3] * 0.5;
+  s.sys_glob[5 * sy + 0] = up;
+  s.sys_glob[5 * sy + 1] = vx + vy + vz;
+  s.sys_glob[5 * sy + 2] = vx;
+  s.sys_glob[5 * sy + 3] = vy;
+  s.sys_glob[5 * sy + 4] = vz;
+  const long long pairs = (long long)(h + 0.5) / 2;
+  s.sys_hits[sy] = pairs;
+  atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)pairs);
+}
+
+void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
+                           double *cpart, cudaStream_t st) {
+  if (nchunks > 0) k_reduce_chunks<<<nchunks, 256, 0, st>>>(s, chunks, cpart);
+  if (s.nsys > 0) k_reduce_systems<<<(s.nsys + 127) / 128, 128, 0, st>>>(s, sys_chunk0, cpart);
 }
 
 }  // namespace pe

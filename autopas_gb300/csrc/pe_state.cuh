@@ -77,6 +77,8 @@ void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_
 // forces (pe_force.cu)
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt,
                   cudaStream_t st);
-void launch_reduce_globals_range(DeviceState &s, const int64_t *sys_cl_range, cudaStream_t st);
+constexpr int kChunk = 4096;  // clusters per globals-reduction chunk
+void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
+                           double *cpart, cudaStream_t st);
 
 }  // namespace pe

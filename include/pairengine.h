@@ -75,6 +75,10 @@ typedef struct {
   int dist_mode;           /* PE_DIST_* for every FP64 distance test */
   int rebuild_frequency;   /* steps between list rebuilds inside pe_step (verletRebuildFrequency) */
   int calc_globals;        /* compute Upot and virial with every force evaluation */
+  int tower_sizing;        /* 0: tower side from the box-average density, as VerletClusterLists does
+                              (ClusterTowerBlock2D.h:140-168); 1: from the density that 90% of the particles
+                              are at or below (coarse histogram), which keeps clusters compact in inhomogeneous
+                              systems.  Only the cluster shapes differ; the pair set is the same. */
 } pe_config;
 
 /* One particle system of the ensemble. */

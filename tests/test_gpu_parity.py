@@ -220,3 +220,36 @@ def test_errors_are_reported_not_hidden(eng_mod):
     with pytest.raises(eng_mod.EngineError) as ei:
         e.compute_forces()
     assert ei.value.code == -6
+
+
+@pytest.mark.parametrize("C", [4, 8])
+def test_tower_grid_matches_reference_formula(eng_mod, orc, C):
+    """Reference tower sizing (ClusterTowerBlock2D::estimateOptimalGridSideLength) in container mode."""
+    pos, vel, bmin, bmax = liquid(5, seed=2)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, cluster_size=C, tower_sizing=0)
+    e.set_particles(allpos, ownership=own)
+    side, num, halo, origin = e.tower_grid(0)
+    rside, rnum, rhalo = orc.tower_grid(bmin, bmax, len(allpos), C, rc + skin)
+    assert np.array_equal(side, rside)
+    assert np.array_equal(num, rnum)
+    assert halo == rhalo
+    np.testing.assert_array_equal(origin, bmin[:2] - side * halo)
+
+
+def test_local_density_towers_keep_pair_set(eng_mod, orc):
+    """Tower sizing changes only the cluster shapes: the pair set of a slab is the same either way."""
+    from autopas_gb300 import workloads
+    pos, vel, bmin, bmax = workloads.slab(n_total=20000, seed=3)
+    rc, skin = 3.0, 0.4
+    sets = []
+    for ts in (0, 1):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, tower_sizing=ts)
+        e.set_particles(pos, vel)
+        e.rebuild()
+        a, b, c = e.pair_set(0)
+        sets.append(np.unique(np.stack([a, b, c], 1), axis=0))
+    assert np.array_equal(sets[0], sets[1])
+    ref = canonical_oracle_pairs(orc, pos, bmin, bmax, rc, skin, 0)
+    assert np.array_equal(sets[1], ref)
