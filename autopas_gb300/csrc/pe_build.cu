@@ -412,6 +412,85 @@ void launch_list_build(DeviceState &s, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// 6. particle neighbour lists from the (full) cluster-pair lists: every j within rc+skin of an owned i,
+//    tested on the hi/lo float positions with a relative margin of 1e-5 on (rc+skin)^2 (the float distance is
+//    within ~1e-7 of the FP64 one, so the list is a superset of the FP64 rc+skin pair set).  Lanes append in
+//    (entry, j-lane) order via ballots, so every list has a deterministic order.
+// ---------------------------------------------------------------------------------------------
+template <int C>
+__global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
+  constexpr int JL = 32 / C;
+  constexpr int EPI = 64 / (C * C);
+  const int lane = threadIdx.x & 31;
+  const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (A >= s.nclusters) return;
+  const int n = s.cp_count[A];
+  const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
+  const int ii = lane % C, jl = lane / C;
+  const int64_t i = A * C + ii;
+  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const int oi = __float_as_int(hi_i.w) >> 16;
+  const SysDev &S = s.sysd[s.cl_sys[A]];
+  const unsigned same_i = (C == 8 ? 0x01010101u : 0x11111111u) << ii;
+  const unsigned lt = (1u << lane) - 1;
+  const int cap = s.pl_cap;
+  int cnt = 0;
+  for (int e = 0; e < n; e += EPI) {
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const int f = jl + p * JL;
+      const int ee = e + f / C;
+      const int jj = f % C;
+      bool keep = false;
+      uint32_t ent = 0;
+      if (ee < n && oi == 1) {
+        ent = __ldg(lst + ee);
+        const int64_t j = (int64_t)(ent >> 5) * C + jj;
+        const int code = ent & 31;
+        const float4 hj = __ldg(&s.pk_hi[j]);
+        const float4 lj = __ldg(&s.pk_lo[j]);
+        float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+        if (code != kShiftNone) {
+          const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+          xh = fmaf(-sxf, S.len_hi[0], xh);
+          yh = fmaf(-syf, S.len_hi[1], yh);
+          zh = fmaf(-szf, S.len_hi[2], zh);
+          xl = fmaf(-sxf, S.len_lo[0], xl);
+          yl = fmaf(-syf, S.len_lo[1], yl);
+          zl = fmaf(-szf, S.len_lo[2], zl);
+        }
+        const float dx = (xh - hj.x) + (xl - lj.x);
+        const float dy = (yh - hj.y) + (yl - lj.y);
+        const float dz = (zh - hj.z) + (zl - lj.z);
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        keep = (r2 > 0.f) && (r2 <= L2f) && ((__float_as_int(hj.w) >> 16) != 0);
+        ent = ((uint32_t)j << 5) | (uint32_t)code;
+      }
+      const unsigned mine = __ballot_sync(0xffffffffu, keep) & same_i;
+      const int k = cnt + __popc(mine & lt);
+      if (keep && k < cap) s.pl_list[(int64_t)k * s.pl_stride + i] = ent;
+      cnt += __popc(mine);
+    }
+  }
+  if (jl == 0) {
+    s.pl_count[i] = cnt;
+    if (cnt > 0) atomicMax(s.pl_max, cnt);
+  }
+}
+
+void launch_plist_build(DeviceState &s, cudaStream_t st) {
+  const double L = s.cutoff + s.skin;
+  const float L2f = (float)(L * L * (1.0 + 1e-5));
+  cudaMemsetAsync(s.pl_max, 0, sizeof(int), st);
+  const int64_t nb = (s.nclusters + 3) / 4;
+  if (nb == 0) return;
+  if (s.C == 4)
+    k_plist_build<4><<<(unsigned)nb, 128, 0, st>>>(s, L2f);
+  else
+    k_plist_build<8><<<(unsigned)nb, 128, 0, st>>>(s, L2f);
+}
+
+// ---------------------------------------------------------------------------------------------
 // pair-set dump (verification): the particle pairs covered by the lists, evaluated in FP64
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ bool image_exists(const SysDev &S, const double *p, int sx, int sy, int sz) {
@@ -502,9 +581,60 @@ __global__ void k_pair_dump(DeviceState s, int which, int64_t cap, int64_t *__re
   }
 }
 
+// the pairs covered by the particle lists: i's list holds every j (image) it sees, so an owned-owned pair
+// without shift is reported from the particle with the lower user index, an owned-halo pair from the owned one
+__global__ void k_pair_dump_plist(DeviceState s, int which, int64_t cap, int64_t *__restrict__ oa,
+                                  int64_t *__restrict__ ob, int32_t *__restrict__ oc,
+                                  unsigned long long *__restrict__ count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.nslots || s.own[i] != 1) return;
+  const SysDev &S = s.sysd[s.sys[i]];
+  const double L = s.cutoff + s.skin;
+  const double lim = which == 0 ? L * L : s.cutoff * s.cutoff;
+  const int n = min(s.pl_count[i], s.pl_cap);
+  const double pi[3] = {s.x[i], s.y[i], s.z[i]};
+  for (int k = 0; k < n; ++k) {
+    const uint32_t ent = s.pl_list[(int64_t)k * s.pl_stride + i];
+    const int64_t j = ent >> 5;
+    const int code = ent & 31;
+    int sx, sy, sz;
+    shift_of(code, sx, sy, sz);
+    const int oj = s.own[j];
+    const double pj[3] = {s.x[j], s.y[j], s.z[j]};
+    if (code == kShiftNone) {
+      if (oj == 1 && !(s.orig[i] < s.orig[j])) continue;
+    } else if (!image_exists(S, pj, sx, sy, sz)) {
+      continue;
+    }
+    const double q0 = image_coord(pj[0], sx, S.len[0]);
+    const double q1 = image_coord(pj[1], sy, S.len[1]);
+    const double q2 = image_coord(pj[2], sz, S.len[2]);
+    const double d2 = dist2_mode(pi[0] - q0, pi[1] - q1, pi[2] - q2, s.dist_mode);
+    const bool in = which == 0 ? (d2 < lim) : (d2 <= lim);
+    if (!in) continue;
+    const unsigned long long k2 = atomicAdd(count, 1ull);
+    if (k2 < (unsigned long long)cap) {
+      int64_t ga = s.orig[i], gb = s.orig[j];
+      if (code == kShiftNone && gb < ga) {
+        const int64_t t = ga;
+        ga = gb;
+        gb = t;
+      }
+      oa[k2] = ga;
+      ob[k2] = gb;
+      oc[k2] = code;
+    }
+  }
+}
+
 void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
                       unsigned long long *count, cudaStream_t st) {
   cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  if (s.traversal == 1) {
+    const int64_t nb = (s.nslots + 127) / 128;
+    if (nb > 0) k_pair_dump_plist<<<(unsigned)nb, 128, 0, st>>>(s, which, cap, a, b, code, count);
+    return;
+  }
   const int64_t nb = (s.nclusters + 3) / 4;
   if (nb > 0) k_pair_dump<<<(unsigned)nb, 128, 0, st>>>(s, which, cap, a, b, code, count);
 }

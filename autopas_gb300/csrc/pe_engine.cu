@@ -88,6 +88,7 @@ struct pe_engine {
   int C = 8;
   int newton3 = 0;
   int precision = PE_PRECISION_MIXED;
+  int traversal = 1;
   std::string err;
 
   ParticleArrays A, Bk;  // current and gather target
@@ -122,6 +123,12 @@ struct pe_engine {
   DBuf<int32_t> sys_tower_base;
   int64_t max_tower = 0;
   int64_t num_cluster_pairs = 0;
+  // particle lists
+  DBuf<uint32_t> pl_list;
+  DBuf<int32_t> pl_count;
+  DBuf<int> pl_max;
+  int pl_cap = 0;
+  int64_t pl_entries = 0;
 
   // rebuild temporaries
   DBuf<uint64_t> key, skey;
@@ -176,6 +183,12 @@ struct pe_engine {
     s.cp_cap = (int64_t)cp_list.cap;
     s.cp_total = cp_total.p;
     s.newton3 = newton3;
+    s.traversal = traversal;
+    s.pl_list = pl_list.p;
+    s.pl_count = pl_count.p;
+    s.pl_cap = pl_cap;
+    s.pl_stride = pcap;
+    s.pl_max = pl_max.p;
     s.sysd = sysd.p;
     s.types = types.p;
     s.mass = dmass.p;
@@ -649,6 +662,40 @@ static int ensure_particle_capacity(pe_engine *h) {
   return PE_OK;
 }
 
+// particle lists filtered from the full cluster-pair lists; the per-particle capacity grows when exceeded
+static int build_particle_lists(pe_engine *h) {
+  cudaStream_t st = h->st;
+  if (!h->pl_count.ensure((size_t)h->pcap) || !h->pl_max.ensure(1)) return h->fail(PE_ERR_OOM, "particle lists");
+  if (h->pl_cap == 0) {
+    double rho = 0;
+    for (auto &S : h->sys) {
+      double vol = 1;
+      for (int d = 0; d < 3; ++d) vol *= S.desc.box_max[d] - S.desc.box_min[d];
+      rho = std::max(rho, std::max(S.density, (double)S.count / vol));
+    }
+    const double L = h->cfg.cutoff + h->cfg.skin;
+    h->pl_cap = (int)std::min(4096.0, 4.18879 * L * L * L * rho * 1.4 + 32);
+  }
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    const size_t need = (size_t)h->pl_cap * (size_t)h->pcap;
+    if (!h->pl_list.ensure(need)) return h->fail(PE_ERR_OOM, "particle lists (%zu entries)", need);
+    DeviceState s = h->state();
+    launch_plist_build(s, st);
+    h->launches += 1;
+    int mx = 0;
+    PE_CUDA(h, cudaMemcpyAsync(&mx, h->pl_max.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaStreamSynchronize(st));
+    PE_TRY(h->cuda_check("particle list build"));
+    if (mx <= h->pl_cap) {
+      h->pl_entries = 0;
+      return PE_OK;
+    }
+    h->pl_cap = (int)(mx * 1.2) + 8;
+    h->pl_list.release();
+  }
+  return h->fail(PE_ERR_LIST_OVERFLOW, "particle lists kept overflowing");
+}
+
 static int do_rebuild(pe_engine *h) {
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "rebuild before pe_set_particles");
   cudaStream_t st = h->st;
@@ -724,6 +771,7 @@ static int do_rebuild(pe_engine *h) {
     }
     break;
   }
+  if (h->traversal == 1) PE_TRY(build_particle_lists(h));
   const int ns = (int)h->sys.size();
   k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
   h->launches += 1;
@@ -823,6 +871,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->cluster_size != 0 && cfg->cluster_size != 4 && cfg->cluster_size != 8) return PE_ERR_ARG;
   if (cfg->dist_mode < 0 || cfg->dist_mode > 2) return PE_ERR_ARG;
   if (cfg->tower_sizing < 0 || cfg->tower_sizing > 1) return PE_ERR_ARG;
+  if (cfg->traversal < -1 || cfg->traversal > 1) return PE_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PE_ERR_NO_DEVICE;
   pe_engine *h = new pe_engine();
@@ -834,7 +883,8 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   h->cfg.sigma = h->sig.data();
   h->cfg.mass = h->mass.data();
   h->C = cfg->cluster_size == 0 ? 8 : cfg->cluster_size;
-  h->newton3 = cfg->newton3 == 1 ? 1 : 0;
+  h->traversal = cfg->traversal == 0 ? 0 : 1;
+  h->newton3 = (cfg->newton3 == 1 && h->traversal == 0) ? 1 : 0;
   h->precision = cfg->precision;
   cudaGetDevice(&h->device);
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
@@ -909,6 +959,9 @@ int pe_destroy(pe_engine *h) {
   for (auto e : h->timer_ev)
     if (e) cudaEventDestroy(e);
   h->pairs_acc.release();
+  h->pl_list.release();
+  h->pl_count.release();
+  h->pl_max.release();
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return PE_OK;
@@ -1058,6 +1111,9 @@ int pe_get_info(pe_engine *h, pe_info *info) {
   info->cluster_size = h->C;
   info->newton3 = h->newton3;
   info->precision = h->precision;
+  info->traversal = h->traversal;
+  info->num_list_entries = h->pl_entries;
+  info->list_capacity = h->pl_cap;
   info->num_particles = h->nuser;
   info->num_slots = h->nslots;
   info->num_clusters = h->nclusters;

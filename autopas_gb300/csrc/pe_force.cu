@@ -315,8 +315,258 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// particle-list kernels: one thread per slot, full neighbour list (each pair evaluated from both sides),
+// entries read column-major so that a warp's list reads are coalesced.  Globals are reduced per cluster
+// (C consecutive lanes) to match the chunked system reduction.
+// ---------------------------------------------------------------------------------------------
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN>
+__global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  const int T = s.ntypes;
+  if (!ONE_TYPE) {
+    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
+      tab[0][q] = (float)s.types->eps24[q];
+      tab[1][q] = (float)s.types->sig2[q];
+      tab[2][q] = (float)s.types->shift6[q];
+    }
+    __syncthreads();
+  }
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool inrange = i < s.nslots;
+  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+  int n = 0, ti = 0, oi = 0;
+  if (inrange) {
+    hi_i = s.pk_hi[i];
+    lo_i = s.pk_lo[i];
+    const int wi = __float_as_int(hi_i.w);
+    ti = wi & 0xffff;
+    oi = wi >> 16;
+    if (oi == 1) n = s.pl_count[i];
+  }
+  const int sy = inrange ? s.sys[i] : 0;
+  const SysDev &S = s.sysd[sy];
+  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
+  if (ONE_TYPE) {
+    eps24 = (float)s.types->eps24[0];
+    sig2 = (float)s.types->sig2[0];
+    sh6 = (float)s.types->shift6[0];
+  }
+  const float rc2f = fa.rc2f;
+  const float band = rc2f * 2e-6f;
+  float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
+  float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+  int hits = 0, hhalo = 0;
+  const uint32_t *__restrict__ lp = s.pl_list + i;
+  const int64_t stride = s.pl_stride;
+#pragma unroll 2
+  for (int k = 0; k < n; ++k) {
+    const uint32_t ent = __ldg(lp + (int64_t)k * stride);
+    const int64_t j = ent >> 5;
+    const int code = ent & 31;
+    const float4 hj = __ldg(&s.pk_hi[j]);
+    const float4 lj = __ldg(&s.pk_lo[j]);
+    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+    if (code != kShiftNone) {
+      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      xh = fmaf(-sxf, S.len_hi[0], xh);
+      yh = fmaf(-syf, S.len_hi[1], yh);
+      zh = fmaf(-szf, S.len_hi[2], zh);
+      xl = fmaf(-sxf, S.len_lo[0], xl);
+      yl = fmaf(-syf, S.len_lo[1], yl);
+      zl = fmaf(-szf, S.len_lo[2], zl);
+    }
+    const float dx = (xh - hj.x) + (xl - lj.x);
+    const float dy = (yh - hj.y) + (yl - lj.y);
+    const float dz = (zh - hj.z) + (zl - lj.z);
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    bool mask = (r2 <= rc2f);
+    if (fabsf(r2 - rc2f) <= band) mask = exact_within(s, S, i, j, code, fa.rc2);
+    if (!ONE_TYPE) {
+      const int kk = ti * T + (__float_as_int(hj.w) & 0xffff);
+      eps24 = tab[0][kk];
+      sig2 = tab[1][kk];
+      sh6 = tab[2][kk];
+    }
+    const float inv = rcp_nr(r2);
+    const float lj2 = sig2 * inv;
+    const float lj6 = lj2 * lj2 * lj2;
+    const float lj12 = lj6 * lj6;
+    const float lj12m6 = lj12 - lj6;
+    float fac = eps24 * (lj12 + lj12m6) * inv;
+    fac = mask ? fac : 0.f;
+    const float px = dx * fac, py = dy * fac, pz = dz * fac;
+    if (KAHAN) {
+      kahan_add(fxs, fxc, px);
+      kahan_add(fys, fyc, py);
+      kahan_add(fzs, fzc, pz);
+    } else {
+      fxs += px;
+      fys += py;
+      fzs += pz;
+    }
+    if (GLOB) {
+      pot += mask ? fmaf(eps24, lj12m6, sh6) : 0.f;
+      vx = fmaf(px, dx, vx);
+      vy = fmaf(py, dy, vy);
+      vz = fmaf(pz, dz, vz);
+      hits += mask ? 1 : 0;
+      if (!S.periodic) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
+    }
+  }
+  const double Fx = (double)fxs - (double)fxc, Fy = (double)fys - (double)fyc, Fz = (double)fzs - (double)fzc;
+  if (oi == 1) {
+    s.fx[i] = Fx;
+    s.fy[i] = Fy;
+    s.fz[i] = Fz;
+    if (fa.fuse_velocity) {
+      const double m = s.mass[ti];
+      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
+      s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
+      s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
+    }
+  }
+  if (GLOB) {
+    const bool owned = oi == 1;
+    double g0 = owned ? (double)pot : 0.0, g1 = owned ? (double)vx : 0.0;
+    double g2 = owned ? (double)vy : 0.0, g3 = owned ? (double)vz : 0.0;
+    long long h = owned ? (long long)(hits + hhalo) : 0;
+#pragma unroll
+    for (int o = 1; o < C; o <<= 1) {
+      g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+      g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+      g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      h += __shfl_xor_sync(0xffffffffu, h, o);
+    }
+    if (inrange && (i % C) == 0) {
+      const int64_t cl = i / C;
+      s.cl_glob[4 * cl + 0] = g0;
+      s.cl_glob[4 * cl + 1] = g1;
+      s.cl_glob[4 * cl + 2] = g2;
+      s.cl_glob[4 * cl + 3] = g3;
+      s.cl_hits[cl] = (unsigned long long)h;
+    }
+  }
+}
+
+template <int C, bool GLOB>
+__global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs fa) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool inrange = i < s.nslots;
+  int n = 0, oi = 0, ti = 0;
+  double xi = 0, yi = 0, zi = 0;
+  if (inrange) {
+    oi = s.own[i];
+    ti = s.type[i];
+    xi = s.x[i];
+    yi = s.y[i];
+    zi = s.z[i];
+    if (oi == 1) n = s.pl_count[i];
+  }
+  const SysDev &S = s.sysd[inrange ? s.sys[i] : 0];
+  const int T = s.ntypes;
+  const double rc2 = fa.rc2;
+  double fx = 0, fy = 0, fz = 0, pot = 0, vx = 0, vy = 0, vz = 0;
+  long long hits2 = 0;
+  for (int k = 0; k < n; ++k) {
+    const uint32_t ent = __ldg(s.pl_list + (int64_t)k * s.pl_stride + i);
+    const int64_t j = ent >> 5;
+    const int code = ent & 31;
+    int sx, sy, sz;
+    shift_of(code, sx, sy, sz);
+    const double dx = __dsub_rn(xi, image_coord(s.x[j], sx, S.len[0]));
+    const double dy = __dsub_rn(yi, image_coord(s.y[j], sy, S.len[1]));
+    const double dz = __dsub_rn(zi, image_coord(s.z[j], sz, S.len[2]));
+    const double dr2 = dist2_mode(dx, dy, dz, s.dist_mode);
+    const bool mask = dr2 <= rc2;
+    const int kk = ti * T + s.type[j];
+    const double sig2 = s.types->sig2[kk], eps24 = s.types->eps24[kk], sh6 = s.types->shift6[kk];
+    const double invdr2 = __ddiv_rn(1.0, dr2);
+    const double lj2 = __dmul_rn(sig2, invdr2);
+    const double lj6 = __dmul_rn(__dmul_rn(lj2, lj2), lj2);
+    const double lj12 = __dmul_rn(lj6, lj6);
+    const double lj12m6 = __dsub_rn(lj12, lj6);
+    double fac = __dmul_rn(__dmul_rn(eps24, __dadd_rn(lj12, lj12m6)), invdr2);
+    fac = mask ? fac : 0.0;
+    const double pfx = __dmul_rn(dx, fac), pfy = __dmul_rn(dy, fac), pfz = __dmul_rn(dz, fac);
+    fx = __dadd_rn(fx, pfx);
+    fy = __dadd_rn(fy, pfy);
+    fz = __dadd_rn(fz, pfz);
+    if (GLOB) {
+      pot = __dadd_rn(pot, mask ? __dadd_rn(__dmul_rn(eps24, lj12m6), sh6) : 0.0);
+      vx = __dadd_rn(vx, __dmul_rn(dx, pfx));
+      vy = __dadd_rn(vy, __dmul_rn(dy, pfy));
+      vz = __dadd_rn(vz, __dmul_rn(dz, pfz));
+      hits2 += mask ? (s.own[j] == 1 ? 1 : 2) : 0;
+    }
+  }
+  if (oi == 1) {
+    s.fx[i] = fx;
+    s.fy[i] = fy;
+    s.fz[i] = fz;
+    if (fa.fuse_velocity) {
+      const double m = s.mass[ti];
+      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(fx, s.ofx[i]), h));
+      s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(fy, s.ofy[i]), h));
+      s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(fz, s.ofz[i]), h));
+    }
+  }
+  if (GLOB) {
+    const bool owned = oi == 1;
+    double g0 = owned ? pot : 0.0, g1 = owned ? vx : 0.0, g2 = owned ? vy : 0.0, g3 = owned ? vz : 0.0;
+    long long h = owned ? hits2 : 0;
+#pragma unroll
+    for (int o = 1; o < C; o <<= 1) {
+      g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+      g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+      g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      h += __shfl_xor_sync(0xffffffffu, h, o);
+    }
+    if (inrange && (i % C) == 0) {
+      const int64_t cl = i / C;
+      s.cl_glob[4 * cl + 0] = g0;
+      s.cl_glob[4 * cl + 1] = g1;
+      s.cl_glob[4 * cl + 2] = g2;
+      s.cl_glob[4 * cl + 3] = g3;
+      s.cl_hits[cl] = (unsigned long long)h;
+    }
+  }
+}
+
+template <int C>
+static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st) {
+  const int64_t nb = (s.nslots + 127) / 128;
+  if (nb == 0) return;
+  if (precision == 0) {
+    if (fa.calc_globals)
+      k_lj_fp64_plist<C, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_fp64_plist<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    return;
+  }
+  if (s.ntypes == 1) {
+    if (fa.calc_globals)
+      k_lj_mixed_plist<C, true, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_plist<C, false, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+  } else {
+    if (fa.calc_globals)
+      k_lj_mixed_plist<C, true, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_plist<C, false, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+  }
+}
+
 template <int C>
 static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st) {
+  if (s.traversal == 1) {
+    launch_force_plist<C>(s, precision, fa, st);
+    return;
+  }
   const int64_t nb = (s.nclusters + 3) / 4;
   if (nb == 0) return;
   if (precision == 0) {

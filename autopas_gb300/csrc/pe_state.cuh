@@ -41,6 +41,15 @@ struct DeviceState {
   unsigned long long *cp_total = nullptr;  // device counter
   int newton3 = 0;
 
+  // particle neighbour lists (traversal 1): entry k of slot i at pl_list[k * pl_stride + i],
+  // (j slot << 5 | image-shift code), every j within rc+skin of i (FP32 test with a safety margin)
+  int traversal = 0;               // 0: cluster-pair lists, 1: particle lists
+  uint32_t *pl_list = nullptr;
+  int32_t *pl_count = nullptr;     // [nslots]
+  int pl_cap = 0;
+  int64_t pl_stride = 0;
+  int *pl_max = nullptr;           // device max of pl_count
+
   // ---- systems and parameters ----
   SysDev *sysd = nullptr;          // [nsys]
   TypeTable *types = nullptr;      // device copy
@@ -71,6 +80,7 @@ int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *pe
                       cudaStream_t st);
 void launch_cluster_bbox(DeviceState &s, cudaStream_t st);
 void launch_list_build(DeviceState &s, cudaStream_t st);
+void launch_plist_build(DeviceState &s, cudaStream_t st);
 void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
                       unsigned long long *count, cudaStream_t st);
 

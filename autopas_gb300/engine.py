@@ -36,7 +36,7 @@ class PeConfig(C.Structure):
         ("epsilon", C.POINTER(C.c_double)), ("sigma", C.POINTER(C.c_double)), ("mass", C.POINTER(C.c_double)),
         ("apply_shift", C.c_int), ("precision", C.c_int), ("cluster_size", C.c_int), ("newton3", C.c_int),
         ("dist_mode", C.c_int), ("rebuild_frequency", C.c_int), ("calc_globals", C.c_int),
-        ("tower_sizing", C.c_int),
+        ("tower_sizing", C.c_int), ("traversal", C.c_int),
     ]
 
 
@@ -55,9 +55,10 @@ class PeStats(C.Structure):
 
 
 class PeInfo(C.Structure):
-    _fields_ = [("cluster_size", C.c_int), ("newton3", C.c_int), ("precision", C.c_int),
+    _fields_ = [("cluster_size", C.c_int), ("newton3", C.c_int), ("precision", C.c_int), ("traversal", C.c_int),
                 ("num_particles", C.c_int64), ("num_slots", C.c_int64), ("num_clusters", C.c_int64),
-                ("num_towers", C.c_int64), ("num_cluster_pairs", C.c_int64), ("max_tower_size", C.c_int64)]
+                ("num_towers", C.c_int64), ("num_cluster_pairs", C.c_int64), ("max_tower_size", C.c_int64),
+                ("num_list_entries", C.c_int64), ("list_capacity", C.c_int64)]
 
 
 _lib = None
@@ -116,7 +117,7 @@ class PairEngine:
 
     def __init__(self, cutoff, skin, boxes, periodic=True, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,),
                  shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_STRICT,
-                 rebuild_frequency=10, calc_globals=True, tower_sizing=1):
+                 rebuild_frequency=10, calc_globals=True, tower_sizing=1, traversal=1):
         L = load()
         self._L = L
         self._eps = np.ascontiguousarray(epsilon, np.float64)
@@ -126,7 +127,8 @@ class PairEngine:
         dp = C.POINTER(C.c_double)
         cfg = PeConfig(cutoff, skin, T, self._eps.ctypes.data_as(dp), self._sig.ctypes.data_as(dp),
                        self._mass.ctypes.data_as(dp), int(shift), int(precision), int(cluster_size), int(newton3),
-                       int(dist_mode), int(rebuild_frequency), int(calc_globals), int(tower_sizing))
+                       int(dist_mode), int(rebuild_frequency), int(calc_globals), int(tower_sizing),
+                       int(traversal))
         boxes = list(boxes)
         if np.ndim(boxes[0]) == 1:  # single (bmin, bmax)
             boxes = [boxes]

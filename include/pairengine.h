@@ -79,6 +79,10 @@ typedef struct {
                               (ClusterTowerBlock2D.h:140-168); 1: from the density that 90% of the particles
                               are at or below (coarse histogram), which keeps clusters compact in inhomogeneous
                               systems.  Only the cluster shapes differ; the pair set is the same. */
+  int traversal;           /* 0: cluster-pair lists (VerletClusterLists traversal, vcl_cluster_iteration);
+                              1: per-particle lists filtered from the cluster pairs on the device (VerletLists
+                              traversal, vl_list_iteration); -1: the engine's tuner times both and keeps the
+                              faster */
 } pe_config;
 
 /* One particle system of the ensemble. */
@@ -138,12 +142,15 @@ typedef struct {
   int cluster_size;
   int newton3;
   int precision;
+  int traversal;
   int64_t num_particles;     /* real particles (owned + halo) */
   int64_t num_slots;         /* particles + padding dummies */
   int64_t num_clusters;
   int64_t num_towers;
   int64_t num_cluster_pairs; /* entries in all cluster-pair lists */
   int64_t max_tower_size;
+  int64_t num_list_entries;  /* particle-list entries (traversal 1) */
+  int64_t list_capacity;     /* particle-list entries reserved per particle */
 } pe_info;
 int pe_get_info(pe_engine *h, pe_info *info);
 

@@ -45,12 +45,13 @@ def rel_rms(F, R):
     return float(np.sqrt(((F - R) ** 2).sum(1).mean()) / np.sqrt((R ** 2).sum(1).mean()))
 
 
+@pytest.mark.parametrize("traversal", [0, 1])
 @pytest.mark.parametrize("C", [4, 8])
-def test_fp64_periodic_forces_match_oracle(eng_mod, orc, C):
+def test_fp64_periodic_forces_match_oracle(eng_mod, orc, C, traversal):
     pos, vel, bmin, bmax = liquid()
     rc, skin = 2.5, 0.3
     e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_FP64,
-                           cluster_size=C)
+                           cluster_size=C, traversal=traversal)
     e.set_particles(pos, vel)
     g = e.compute_forces()[0]
     F = e.forces()
@@ -70,12 +71,14 @@ def test_fp64_periodic_forces_match_oracle(eng_mod, orc, C):
     assert g["num_pairs"] == n_oo + n_oh // 2
 
 
-def test_fp64_explicit_halo_forces_match_oracle(eng_mod, orc):
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_fp64_explicit_halo_forces_match_oracle(eng_mod, orc, traversal):
     """Container mode: the caller hands owned + halo particles (AutoPas addHaloParticle semantics)."""
     pos, vel, bmin, bmax = liquid(5, seed=3)
     rc, skin = 2.5, 0.3
     allpos, own, allt, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
-    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, precision=eng_mod.PRECISION_FP64)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, precision=eng_mod.PRECISION_FP64,
+                           traversal=traversal)
     e.set_particles(allpos, ownership=own)
     g = e.compute_forces()[0]
     F = e.forces()
@@ -90,12 +93,14 @@ def test_fp64_explicit_halo_forces_match_oracle(eng_mod, orc):
     assert g["num_pairs"] == len(ia)
 
 
+@pytest.mark.parametrize("traversal", [0, 1])
 @pytest.mark.parametrize("dist_mode", [0, 1])
 @pytest.mark.parametrize("C", [4, 8])
-def test_pair_set_bit_exact_periodic(eng_mod, orc, dist_mode, C):
+def test_pair_set_bit_exact_periodic(eng_mod, orc, dist_mode, C, traversal):
     pos, vel, bmin, bmax = liquid(6, seed=5)
     rc, skin = 2.5, 0.3
-    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, cluster_size=C, dist_mode=dist_mode)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, cluster_size=C, dist_mode=dist_mode,
+                           traversal=traversal)
     e.set_particles(pos, vel)
     e.rebuild()
     for which in (0, 1):
@@ -107,11 +112,12 @@ def test_pair_set_bit_exact_periodic(eng_mod, orc, dist_mode, C):
         assert np.array_equal(dev, ref)
 
 
-def test_pair_set_bit_exact_explicit_halo(eng_mod, orc):
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_pair_set_bit_exact_explicit_halo(eng_mod, orc, traversal):
     pos, vel, bmin, bmax = liquid(5, seed=9)
     rc, skin = 2.5, 0.3
     allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
-    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, traversal=traversal)
     e.set_particles(allpos, ownership=own)
     e.rebuild()
     a, b, c = e.pair_set(0)
@@ -122,11 +128,13 @@ def test_pair_set_bit_exact_explicit_halo(eng_mod, orc):
     assert np.array_equal(dev, ref)
 
 
+@pytest.mark.parametrize("traversal", [0, 1])
 @pytest.mark.parametrize("C", [4, 8])
-def test_mixed_precision_error_bound(eng_mod, orc, C):
+def test_mixed_precision_error_bound(eng_mod, orc, C, traversal):
     pos, vel, bmin, bmax = liquid(8, seed=11)
     rc, skin = 2.5, 0.3
-    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_MIXED, cluster_size=C)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_MIXED, cluster_size=C,
+                           traversal=traversal)
     e.set_particles(pos, vel)
     g = e.compute_forces()[0]
     F = e.forces()
@@ -186,7 +194,8 @@ def test_md_trajectory_fp64_matches_oracle(eng_mod, orc):
     assert g["upot"] == pytest.approx(en[-1, 0], rel=1e-9)
 
 
-def test_ensemble_systems_are_independent(eng_mod, orc):
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_ensemble_systems_are_independent(eng_mod, orc, traversal):
     from autopas_gb300 import workloads
     systems = workloads.ensemble(3, nmin=600, nmax=3000, seed=4)
     rc, skin = 2.5, 0.3
@@ -194,7 +203,7 @@ def test_ensemble_systems_are_independent(eng_mod, orc):
     pos = np.concatenate([s["pos"] for s in systems])
     sysid = np.concatenate([np.full(len(s["pos"]), k, np.int32) for k, s in enumerate(systems)])
     for prec in (eng_mod.PRECISION_FP64, eng_mod.PRECISION_MIXED):
-        e = eng_mod.PairEngine(rc, skin, boxes, periodic=True, precision=prec)
+        e = eng_mod.PairEngine(rc, skin, boxes, periodic=True, precision=prec, traversal=traversal)
         e.set_particles(pos, system=sysid)
         gs = e.compute_forces()
         F = e.forces()
@@ -228,7 +237,7 @@ def test_tower_grid_matches_reference_formula(eng_mod, orc, C):
     pos, vel, bmin, bmax = liquid(5, seed=2)
     rc, skin = 2.5, 0.3
     allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
-    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, cluster_size=C, tower_sizing=0)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, cluster_size=C, tower_sizing=0, traversal=0)
     e.set_particles(allpos, ownership=own)
     side, num, halo, origin = e.tower_grid(0)
     rside, rnum, rhalo = orc.tower_grid(bmin, bmax, len(allpos), C, rc + skin)
