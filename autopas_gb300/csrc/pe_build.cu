@@ -336,40 +336,57 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     int cf = 0, ce = 0, code = kShiftNone;
     double shx = 0, shy = 0, shz = 0;
     if (sb + lane < nseg) segment_run(s, S, tx, ty, sb + lane, nseg_z, alo, ahi, L2, Lz, cf, ce, code, shx, shy, shz);
-    unsigned live = __ballot_sync(0xffffffffu, ce > cf);
-    while (live && !overflow) {
-      const int src = __ffs(live) - 1;
-      live &= live - 1;
-      const int f = __shfl_sync(0xffffffffu, cf, src), e = __shfl_sync(0xffffffffu, ce, src);
+    // flatten the runs of the 32 segments into one candidate index space (exclusive prefix over lanes)
+    const int len = ce - cf;
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - len;
+    for (int base = 0; base < total; base += 32) {
+      const int t = base + lane;
+      // segment of candidate t: the last lane whose exclusive offset is <= t (binary search over lanes)
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int it = 0; it < 5; ++it) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int om = __shfl_sync(0xffffffffu, excl, mid);
+        if (om <= t) lo = mid; else hi = mid - 1;
+      }
+      // lanes with empty runs share offsets with the next non-empty one; step forward to a run holding t
+      const int src = lo;
+      const int f = __shfl_sync(0xffffffffu, cf, src), e0 = __shfl_sync(0xffffffffu, excl, src);
       const int cd = __shfl_sync(0xffffffffu, code, src);
       const double hx = __shfl_sync(0xffffffffu, shx, src), hy = __shfl_sync(0xffffffffu, shy, src);
       const double hz = __shfl_sync(0xffffffffu, shz, src);
-      for (int cb = f; cb < e; cb += 32) {
-        const int c = cb + lane;
-        bool accept = false;
-        if (c < e) {
-          const bool self = (c == A && cd == kShiftNone);
-          bool canon = true;
-          if (s.newton3) canon = (c > A) || (c == A && cd > kShiftNone);
-          const int fb = s.cl_flags[c];
-          const bool haloHalo = !aOwned && !(fb & 1);
-          if (!self && canon && !haloHalo && (fb & 2)) {
-            const double *bb = s.cl_bb + 6 * (int64_t)c;
-            const double g0 = gap1(alo[0], ahi[0], bb[0] + hx, bb[3] + hx);
-            const double g1 = gap1(alo[1], ahi[1], bb[1] + hy, bb[4] + hy);
-            const double g2 = gap1(alo[2], ahi[2], bb[2] + hz, bb[5] + hz);
-            accept = (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
-          }
+      bool accept = false;
+      int c = 0;
+      if (t < total) {
+        c = f + (t - e0);
+        const bool self = (c == A && cd == kShiftNone);
+        bool canon = true;
+        if (s.newton3) canon = (c > A) || (c == A && cd > kShiftNone);
+        const int fb = s.cl_flags[c];
+        const bool haloHalo = !aOwned && !(fb & 1);
+        if (!self && canon && !haloHalo && (fb & 2)) {
+          const double *bb = s.cl_bb + 6 * (int64_t)c;
+          const double g0 = gap1(alo[0], ahi[0], bb[0] + hx, bb[3] + hx);
+          const double g1 = gap1(alo[1], ahi[1], bb[1] + hy, bb[4] + hy);
+          const double g2 = gap1(alo[2], ahi[2], bb[2] + hz, bb[5] + hz);
+          accept = (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
         }
-        const unsigned am = __ballot_sync(0xffffffffu, accept);
-        const int na = __popc(am);
-        if (cnt + na > kListBufPerWarp) {
-          overflow = true;
-          break;
-        }
-        if (accept) buf[cnt + __popc(am & ((1u << lane) - 1))] = ((uint32_t)c << 5) | (uint32_t)cd;
-        cnt += na;
       }
+      const unsigned am = __ballot_sync(0xffffffffu, accept);
+      const int na = __popc(am);
+      if (cnt + na > kListBufPerWarp) {
+        overflow = true;
+        break;
+      }
+      if (accept) buf[cnt + __popc(am & ((1u << lane) - 1))] = ((uint32_t)c << 5) | (uint32_t)cd;
+      cnt += na;
     }
   }
   __syncwarp();

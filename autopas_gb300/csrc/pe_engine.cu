@@ -89,6 +89,10 @@ struct pe_engine {
   int newton3 = 0;
   int precision = PE_PRECISION_MIXED;
   int traversal = 1;
+  int variant = 0;
+  bool tuned = false;
+  std::vector<pe_tuning_entry> tune_log;
+  int tune_chosen = -1;
   std::string err;
 
   ParticleArrays A, Bk;  // current and gather target
@@ -184,6 +188,7 @@ struct pe_engine {
     s.cp_total = cp_total.p;
     s.newton3 = newton3;
     s.traversal = traversal;
+    s.variant = variant;
     s.pl_list = pl_list.p;
     s.pl_count = pl_count.p;
     s.pl_cap = pl_cap;
@@ -856,6 +861,66 @@ static int read_globals(pe_engine *h, pe_globals *g) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// tuner: full search over (cluster size, traversal, kernel variant), timing force evaluations
+// ---------------------------------------------------------------------------------------------
+static int apply_config(pe_engine *h, int C, int traversal, int variant) {
+  const bool regrid = C != h->C;
+  const bool relist = regrid || traversal != h->traversal;
+  h->C = C;
+  h->traversal = traversal;
+  h->variant = variant;
+  h->newton3 = (h->cfg.newton3 == 1 && traversal == 0) ? 1 : 0;
+  if (regrid) {
+    PE_TRY(setup_grids(h));
+    PE_TRY(ensure_particle_capacity(h));
+    h->cp_list.release();
+  }
+  if (relist || !h->lists_valid) PE_TRY(do_rebuild(h));
+  return PE_OK;
+}
+
+static int tune(pe_engine *h, int samples) {
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "tuning needs particles");
+  samples = std::max(1, samples);
+  std::vector<int> Cs = h->cfg.cluster_size == 0 ? std::vector<int>{4, 8} : std::vector<int>{h->cfg.cluster_size};
+  std::vector<int> Ts = h->cfg.traversal == -1 ? std::vector<int>{0, 1} : std::vector<int>{h->traversal};
+  h->tune_log.clear();
+  const int rebuilds = (int)h->rebuilds;
+  for (int C : Cs)
+    for (int T : Ts) {
+      const int nv = T == 1 ? 2 : 1;
+      for (int v = 0; v < nv; ++v) {
+        PE_TRY(apply_config(h, C, T, v));
+        std::vector<float> t;
+        for (int k = 0; k < samples + 1; ++k) {
+          cudaEvent_t a = h->ev(), b = h->ev();
+          cudaEventRecord(a, h->st);
+          DeviceState ds = h->state();
+          launch_force(ds, h->precision, h->cfg.calc_globals, false, 0.0, h->st);
+          cudaEventRecord(b, h->st);
+          PE_CUDA(h, cudaEventSynchronize(b));
+          float ms = 0;
+          cudaEventElapsedTime(&ms, a, b);
+          if (k > 0) t.push_back(ms);  // the first launch warms caches
+        }
+        h->ev_used -= 2 * (samples + 1);
+        std::sort(t.begin(), t.end());
+        h->tune_log.push_back({C, T, v, (double)t[t.size() / 2]});
+      }
+    }
+  int best = 0;
+  for (int k = 1; k < (int)h->tune_log.size(); ++k)
+    if (h->tune_log[k].ms < h->tune_log[best].ms) best = k;
+  h->tune_chosen = best;
+  const auto &b = h->tune_log[best];
+  PE_TRY(apply_config(h, b.cluster_size, b.traversal, b.variant));
+  h->rebuilds = rebuilds;
+  h->tuned = true;
+  PE_TRY(h->cuda_check("tuning"));
+  return PE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------------------
 extern "C" {
@@ -1050,6 +1115,7 @@ int pe_rebuild(pe_engine *h) {
 int pe_compute_forces(pe_engine *h, pe_globals *globals) {
   if (!h) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "compute before pe_set_particles");
+  if (!h->tuned && (h->cfg.cluster_size == 0 || h->cfg.traversal == -1)) PE_TRY(tune(h, 3));
   if (!h->lists_valid) PE_TRY(do_rebuild(h));
   PE_TRY(force_eval(h, false, 0.0, true));
   return read_globals(h, globals);
@@ -1181,6 +1247,20 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out) {
     h->rebuilds = 0;
     if (h->pairs_acc.p) PE_CUDA(h, cudaMemset(h->pairs_acc.p, 0, sizeof(long long)));
   }
+  return PE_OK;
+}
+
+int pe_tune(pe_engine *h, int samples) {
+  if (!h) return PE_ERR_ARG;
+  return tune(h, samples);
+}
+
+int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, int *chosen) {
+  if (!h || cap < 0 || (cap > 0 && !entries)) return PE_ERR_ARG;
+  const int n = (int)h->tune_log.size();
+  for (int k = 0; k < std::min(cap, n); ++k) entries[k] = h->tune_log[k];
+  if (count) *count = n;
+  if (chosen) *chosen = h->tune_chosen;
   return PE_OK;
 }
 

@@ -320,52 +320,18 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
 // entries read column-major so that a warp's list reads are coalesced.  Globals are reduced per cluster
 // (C consecutive lanes) to match the chunked system reduction.
 // ---------------------------------------------------------------------------------------------
-template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN>
-__global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
-  __shared__ float tab[3][kMaxTypes * kMaxTypes];
-  const int T = s.ntypes;
-  if (!ONE_TYPE) {
-    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
-      tab[0][q] = (float)s.types->eps24[q];
-      tab[1][q] = (float)s.types->sig2[q];
-      tab[2][q] = (float)s.types->shift6[q];
-    }
-    __syncthreads();
-  }
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool inrange = i < s.nslots;
-  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
-  int n = 0, ti = 0, oi = 0;
-  if (inrange) {
-    hi_i = s.pk_hi[i];
-    lo_i = s.pk_lo[i];
-    const int wi = __float_as_int(hi_i.w);
-    ti = wi & 0xffff;
-    oi = wi >> 16;
-    if (oi == 1) n = s.pl_count[i];
-  }
-  const int sy = inrange ? s.sys[i] : 0;
-  const SysDev &S = s.sysd[sy];
-  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
-  if (ONE_TYPE) {
-    eps24 = (float)s.types->eps24[0];
-    sig2 = (float)s.types->sig2[0];
-    sh6 = (float)s.types->shift6[0];
-  }
-  const float rc2f = fa.rc2f;
-  const float band = rc2f * 2e-6f;
+// one pair of the mixed kernels: displacement from the hi/lo positions, LJ in FP32, compensated sums
+template <bool GLOB, bool ONE_TYPE, bool KAHAN>
+struct MixedAcc {
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
   int hits = 0, hhalo = 0;
-  const uint32_t *__restrict__ lp = s.pl_list + i;
-  const int64_t stride = s.pl_stride;
-#pragma unroll 2
-  for (int k = 0; k < n; ++k) {
-    const uint32_t ent = __ldg(lp + (int64_t)k * stride);
-    const int64_t j = ent >> 5;
+
+  __device__ __forceinline__ void pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                       const float4 &hi_i, const float4 &lo_i, int ti, uint32_t ent,
+                                       const float4 &hj, const float4 &lj, float eps24, float sig2, float sh6,
+                                       const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
     const int code = ent & 31;
-    const float4 hj = __ldg(&s.pk_hi[j]);
-    const float4 lj = __ldg(&s.pk_lo[j]);
     float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
     if (code != kShiftNone) {
       const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
@@ -380,8 +346,8 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
     const float dy = (yh - hj.y) + (yl - lj.y);
     const float dz = (zh - hj.z) + (zl - lj.z);
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    bool mask = (r2 <= rc2f);
-    if (fabsf(r2 - rc2f) <= band) mask = exact_within(s, S, i, j, code, fa.rc2);
+    bool mask = (r2 <= fa.rc2f);
+    if (fabsf(r2 - fa.rc2f) <= band) mask = exact_within(s, S, i, (int64_t)(ent >> 5), code, fa.rc2);
     if (!ONE_TYPE) {
       const int kk = ti * T + (__float_as_int(hj.w) & 0xffff);
       eps24 = tab[0][kk];
@@ -414,7 +380,68 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
       if (!S.periodic) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
     }
   }
-  const double Fx = (double)fxs - (double)fxc, Fy = (double)fys - (double)fyc, Fz = (double)fzs - (double)fzc;
+};
+
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL>
+__global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  const int T = s.ntypes;
+  if (!ONE_TYPE) {
+    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
+      tab[0][q] = (float)s.types->eps24[q];
+      tab[1][q] = (float)s.types->sig2[q];
+      tab[2][q] = (float)s.types->shift6[q];
+    }
+    __syncthreads();
+  }
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool inrange = i < s.nslots;
+  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+  int n = 0, ti = 0, oi = 0;
+  if (inrange) {
+    hi_i = s.pk_hi[i];
+    lo_i = s.pk_lo[i];
+    const int wi = __float_as_int(hi_i.w);
+    ti = wi & 0xffff;
+    oi = wi >> 16;
+    if (oi == 1) n = s.pl_count[i];
+  }
+  const int sy = inrange ? s.sys[i] : 0;
+  const SysDev &S = s.sysd[sy];
+  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
+  if (ONE_TYPE) {
+    eps24 = (float)s.types->eps24[0];
+    sig2 = (float)s.types->sig2[0];
+    sh6 = (float)s.types->shift6[0];
+  }
+  const float band = fa.rc2f * 2e-6f;
+  MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
+  const uint32_t *__restrict__ lp = s.pl_list + i;
+  const int64_t stride = s.pl_stride;
+  int k = 0;
+  // batches of UNROLL entries: all list and position loads of a batch are issued before its arithmetic
+  for (; k + UNROLL <= n; k += UNROLL) {
+    uint32_t ent[UNROLL];
+    float4 hj[UNROLL], lj[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) ent[u] = __ldg(lp + (int64_t)(k + u) * stride);
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      hj[u] = __ldg(&s.pk_hi[ent[u] >> 5]);
+      lj[u] = __ldg(&s.pk_lo[ent[u] >> 5]);
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u)
+      acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
+  }
+  for (; k < n; ++k) {
+    const uint32_t ent = __ldg(lp + (int64_t)k * stride);
+    const float4 hj = __ldg(&s.pk_hi[ent >> 5]);
+    const float4 lj = __ldg(&s.pk_lo[ent >> 5]);
+    acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent, hj, lj, eps24, sig2, sh6, tab, T, band);
+  }
+  const double Fx = (double)acc.fxs - (double)acc.fxc, Fy = (double)acc.fys - (double)acc.fyc,
+               Fz = (double)acc.fzs - (double)acc.fzc;
   if (oi == 1) {
     s.fx[i] = Fx;
     s.fy[i] = Fy;
@@ -429,9 +456,9 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
   }
   if (GLOB) {
     const bool owned = oi == 1;
-    double g0 = owned ? (double)pot : 0.0, g1 = owned ? (double)vx : 0.0;
-    double g2 = owned ? (double)vy : 0.0, g3 = owned ? (double)vz : 0.0;
-    long long h = owned ? (long long)(hits + hhalo) : 0;
+    double g0 = owned ? (double)acc.pot : 0.0, g1 = owned ? (double)acc.vx : 0.0;
+    double g2 = owned ? (double)acc.vy : 0.0, g3 = owned ? (double)acc.vz : 0.0;
+    long long h = owned ? (long long)(acc.hits + acc.hhalo) : 0;
 #pragma unroll
     for (int o = 1; o < C; o <<= 1) {
       g0 += __shfl_xor_sync(0xffffffffu, g0, o);
@@ -548,17 +575,27 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
       k_lj_fp64_plist<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     return;
   }
+  // kernel variant (loads batched per 2 or 4 list entries), chosen by the engine's tuner
+  const bool u4 = s.variant == 1;
+#define PE_PLIST(G, O)                                                                   \
+  do {                                                                                   \
+    if (u4)                                                                              \
+      k_lj_mixed_plist<C, G, O, true, 4><<<(unsigned)nb, 128, 0, st>>>(s, fa);           \
+    else                                                                                 \
+      k_lj_mixed_plist<C, G, O, true, 2><<<(unsigned)nb, 128, 0, st>>>(s, fa);           \
+  } while (0)
   if (s.ntypes == 1) {
     if (fa.calc_globals)
-      k_lj_mixed_plist<C, true, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      PE_PLIST(true, true);
     else
-      k_lj_mixed_plist<C, false, true, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      PE_PLIST(false, true);
   } else {
     if (fa.calc_globals)
-      k_lj_mixed_plist<C, true, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      PE_PLIST(true, false);
     else
-      k_lj_mixed_plist<C, false, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+      PE_PLIST(false, false);
   }
+#undef PE_PLIST
 }
 
 template <int C>

@@ -44,6 +44,7 @@ struct DeviceState {
   // particle neighbour lists (traversal 1): entry k of slot i at pl_list[k * pl_stride + i],
   // (j slot << 5 | image-shift code), every j within rc+skin of i (FP32 test with a safety margin)
   int traversal = 0;               // 0: cluster-pair lists, 1: particle lists
+  int variant = 0;                 // kernel variant inside a traversal (tuner dimension)
   uint32_t *pl_list = nullptr;
   int32_t *pl_count = nullptr;     // [nslots]
   int pl_cap = 0;

@@ -26,7 +26,7 @@ DUMMY, OWNED, HALO = 0, 1, 2
 EXPORTS = [
     "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
-    "pe_pair_set", "pe_get_stats", "pe_device_timer",
+    "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning",
 ]
 
 
@@ -52,6 +52,10 @@ class PeGlobals(C.Structure):
 class PeStats(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_int64), ("kernel_launches", C.c_int64),
                 ("pairs_total", C.c_int64), ("rebuilds", C.c_int64)]
+
+
+class PeTuningEntry(C.Structure):
+    _fields_ = [("cluster_size", C.c_int), ("traversal", C.c_int), ("variant", C.c_int), ("ms", C.c_double)]
 
 
 class PeInfo(C.Structure):
@@ -95,6 +99,8 @@ def load(path: str | None = None):
     L.pe_pair_set.argtypes = [vp, C.c_int, C.c_int64, vp, vp, vp, C.POINTER(C.c_int64)]
     L.pe_get_stats.argtypes = [vp, C.c_int, C.POINTER(PeStats)]
     L.pe_device_timer.argtypes = [vp, C.c_int, dp]
+    L.pe_tune.argtypes = [vp, C.c_int]
+    L.pe_get_tuning.argtypes = [vp, C.c_int, C.POINTER(PeTuningEntry), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     for name in EXPORTS:
         if name != "pe_last_error":
             getattr(L, name).restype = C.c_int
@@ -247,6 +253,18 @@ class PairEngine:
         st = PeStats()
         self._check(self._L.pe_get_stats(self._h, int(reset), C.byref(st)))
         return {k: getattr(st, k) for k, _ in PeStats._fields_}
+
+    def tune(self, samples=3):
+        self._check(self._L.pe_tune(self._h, int(samples)))
+        return self.tuning()
+
+    def tuning(self):
+        arr = (PeTuningEntry * 64)()
+        cnt = C.c_int()
+        chosen = C.c_int()
+        self._check(self._L.pe_get_tuning(self._h, 64, arr, C.byref(cnt), C.byref(chosen)))
+        return {"candidates": [{"cluster_size": a.cluster_size, "traversal": a.traversal, "variant": a.variant,
+                                "ms": a.ms} for a in arr[:cnt.value]], "chosen": chosen.value}
 
     def timer_start(self):
         self._check(self._L.pe_device_timer(self._h, 0, None))

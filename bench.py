@@ -42,7 +42,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=2_000_000, help="particles of the slab workload")
     p.add_argument("--fp64-steps", type=int, default=10)
-    p.add_argument("--cluster-size", type=int, default=8)
+    p.add_argument("--cluster-size", type=int, default=0, help="0: the engine's tuner picks 4 or 8")
+    p.add_argument("--traversal", type=int, default=-1, help="-1: tuner; 0 cluster pairs; 1 particle lists")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
@@ -215,7 +216,8 @@ def config_dict(args):
                         f"third / vapour 0.02, dmin 0.8, T* 0.8, rc {RC}, skin {SKIN}, rebuild every {REBUILD} "
                         f"steps, dt {DT}, truncated LJ, eps=sigma=m=1",
             "particles": args.n, "cutoff": RC, "skin": SKIN, "rebuild_frequency": REBUILD,
-            "cluster_size": args.cluster_size, "newton3": False, "l2_policy": "inputs larger than L2 (no flush)"}
+            "cluster_size": args.cluster_size or "tuned", "traversal": "tuned" if args.traversal < 0 else args.traversal,
+            "newton3": False, "l2_policy": "inputs larger than L2 (no flush)"}
 
 
 # ---------------------------------------------------------------------------------------------- our arm
@@ -231,7 +233,7 @@ def run_ours(args):
 
     def new_engine(prec):
         e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
-                         newton3=0, rebuild_frequency=REBUILD, calc_globals=True)
+                         newton3=0, rebuild_frequency=REBUILD, calc_globals=True, traversal=args.traversal)
         e.set_particles(pos, vel)
         return e
 
@@ -261,6 +263,7 @@ def run_ours(args):
     # ---- mixed MD steps (the headline)
     e = new_engine(E.PRECISION_MIXED)
     e.compute_forces()
+    tuning = e.tuning()
     e.step(DT, args.warmup, want_globals=False)
     e.stats(reset=True)
     info = e.info()
@@ -362,10 +365,13 @@ def run_ours(args):
         "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
         "force_error": err,
         "upot_last_step": g_last["upot"], "rebuilds_in_timed_region": st["rebuilds"],
-        "engine": {k: info[k] for k in ("num_clusters", "num_cluster_pairs", "max_tower_size", "num_towers")},
+        "engine": {k: info[k] for k in ("cluster_size", "traversal", "num_clusters", "num_cluster_pairs",
+                                        "max_tower_size", "num_towers", "list_capacity")},
+        "tuning": tuning,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": None,
-                     "kernel": "k_lj_mixed_full<8>",
+                     "kernel": ("k_lj_mixed_plist" if info["traversal"] == 1 else "k_lj_mixed_full") +
+                               f"<{info['cluster_size']}>",
                      "algorithmic": f"{FLOP_PER_PAIR} FLOP per interacting pair (reference convention)",
                      "peak_source": f"nominal CUDA-core FP32: 152 SM x 128 lanes x 2 FLOP x {sm_max:.0f} MHz "
                                     "(MEASURED_PEAKS.json holds no CUDA-core figure; hbm/bf16 peaks do not bound "

@@ -178,6 +178,22 @@ typedef struct {
 } pe_stats;
 int pe_get_stats(pe_engine *h, int reset, pe_stats *out);
 
+/* The engine's tuner (the counterpart of AutoPas's AutoTuner full search, tuning/AutoTuner.cpp:85-175, over
+ * the engine-internal dimensions that AutoPas does not tune): every candidate (cluster size 4/8 when
+ * cluster_size == 0, traversal 0/1 when traversal == -1, kernel variant) is applied, the lists rebuilt, and
+ * `samples` force evaluations timed with CUDA events; the fastest candidate (median time) is kept.  It runs
+ * by itself at the first pe_compute_forces when cluster_size == 0 or traversal == -1.  The evidence of the
+ * last tuning is returned by pe_get_tuning: up to cap entries of {cluster_size, traversal, variant, ms};
+ * *count receives the number of candidates and *chosen the index of the kept one. */
+typedef struct {
+  int cluster_size;
+  int traversal;
+  int variant;
+  double ms;
+} pe_tuning_entry;
+int pe_tune(pe_engine *h, int samples);
+int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, int *chosen);
+
 /* Device timer on the engine's stream: op 0 records a start event; op 1 records a stop event, waits for it and
  * returns the elapsed milliseconds between the two in *ms. */
 int pe_device_timer(pe_engine *h, int op, double *ms);

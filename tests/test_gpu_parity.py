@@ -262,3 +262,27 @@ def test_local_density_towers_keep_pair_set(eng_mod, orc):
     assert np.array_equal(sets[0], sets[1])
     ref = canonical_oracle_pairs(orc, pos, bmin, bmax, rc, skin, 0)
     assert np.array_equal(sets[1], ref)
+
+
+def test_tuner_full_search_keeps_results(eng_mod, orc):
+    """The engine tuner times every (cluster size, traversal, variant) candidate and keeps the fastest;
+    whatever it picks, the forces stay those of the oracle."""
+    pos, vel, bmin, bmax = liquid(7, seed=17)
+    rc, skin = 2.5, 0.3
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_MIXED, cluster_size=0,
+                           traversal=-1)
+    e.set_particles(pos, vel)
+    g = e.compute_forces()[0]
+    tun = e.tuning()
+    assert len(tun["candidates"]) == 6
+    assert 0 <= tun["chosen"] < 6
+    best = tun["candidates"][tun["chosen"]]
+    assert best["ms"] == min(c["ms"] for c in tun["candidates"])
+    info = e.info()
+    assert (info["cluster_size"], info["traversal"]) == (best["cluster_size"], best["traversal"])
+    F = e.forces()
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+    assert rel_rms(F, R[: len(pos)]) <= 1e-6
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
+    e.step(0.002, 5)
