@@ -224,6 +224,7 @@ __global__ void k_cluster_bbox(DeviceState s) {
     s.cl_bb[6 * c + d] = lo[d];
     s.cl_bb[6 * c + 3 + d] = hi[d];
   }
+  s.cl_z[c] = make_float2(__double2float_rd(lo[2]), __double2float_ru(hi[2]));
   s.cl_flags[c] = flags;
   s.cl_sys[c] = s.sys[c * C];
 }
@@ -281,20 +282,24 @@ __device__ __forceinline__ void segment_run(const DeviceState &s, const SysDev &
   const double gx = gap1(alo[0], ahi[0], s.tw_bb[4 * tB + 0] + shx, s.tw_bb[4 * tB + 2] + shx);
   const double gy = gap1(alo[1], ahi[1], s.tw_bb[4 * tB + 1] + shy, s.tw_bb[4 * tB + 3] + shy);
   if (gx * gx + gy * gy > L2) return;
-  const double zmin = alo[2] - Lz - shz;  // candidates need hi.z >= zmin
-  const double zmax = ahi[2] + Lz - shz;  // and lo.z <= zmax
-  int a = c0, b = c1;
-  while (a < b) {
-    const int m = (a + b) >> 1;
-    if (s.cl_bb[6 * (int64_t)m + 5] < zmin) a = m + 1; else b = m;
-  }
-  int a2 = a, b2 = c1;
-  while (a2 < b2) {
-    const int m = (a2 + b2) >> 1;
-    if (s.cl_bb[6 * (int64_t)m + 2] <= zmax) a2 = m + 1; else b2 = m;
-  }
+  // window of clusters with hi.z >= zmin and lo.z <= zmax, on the float z ranges (rounded outwards, so the
+  // window can only be wider than the FP64 one; the FP64 box test decides).  Clusters of a tower are
+  // z-ordered and nearly uniform in z: an interpolated first guess plus a short walk finds the bounds.
+  const float zmin = __double2float_rd(alo[2] - Lz - shz);
+  const float zmax = __double2float_ru(ahi[2] + Lz - shz);
+  const float z0 = s.cl_z[c0].x, z1 = s.cl_z[c1 - 1].y;
+  if (z1 < zmin || z0 > zmax) return;
+  const float span = fmaxf(z1 - z0, 1e-30f);
+  int a = c0 + (int)((float)(c1 - c0) * fminf(fmaxf((zmin - z0) / span, 0.f), 1.f));
+  a = min(max(a, c0), c1 - 1);
+  while (a > c0 && s.cl_z[a - 1].y >= zmin) --a;
+  while (a < c1 && s.cl_z[a].y < zmin) ++a;
+  int b = c0 + (int)((float)(c1 - c0) * fminf(fmaxf((zmax - z0) / span, 0.f), 1.f));
+  b = min(max(b, a), c1);
+  while (b > a && s.cl_z[b - 1].x > zmax) --b;
+  while (b < c1 && s.cl_z[b].x <= zmax) ++b;
   c_first = a;
-  c_end = a2;
+  c_end = b;
   code = shift_code(sx, sy, sz);
 }
 
@@ -330,7 +335,9 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     if (lane == 0) buf[0] = ((uint32_t)A << 5) | kShiftNone;
     cnt = 1;
   }
-  const int nseg_z = S.periodic ? 3 : 1;
+  // z images only matter for an i-cluster within L of a z face
+  const bool zface = S.periodic && (alo[2] - Lz < S.bmin[2] || ahi[2] + Lz > S.bmax[2]);
+  const int nseg_z = zface ? 3 : 1;
   const int nseg = (2 * S.kx + 1) * (2 * S.ky + 1) * nseg_z;
   for (int sb = 0; sb < nseg && !overflow; sb += 32) {
     int cf = 0, ce = 0, code = kShiftNone;

@@ -111,6 +111,7 @@ struct pe_engine {
   DBuf<int32_t> tw_count, tw_start, tw_cl_start, tw_ncl, tw_fill;
   DBuf<double> tw_bb;
   DBuf<double> cl_bb;
+  DBuf<float2> cl_z;
   DBuf<int32_t> cl_sys, cl_tower, cl_flags, cp_count;
   DBuf<int64_t> cp_start;
   DBuf<uint32_t> cp_list;
@@ -178,6 +179,7 @@ struct pe_engine {
     s.tw_cl_start = tw_cl_start.p;
     s.tw_bb = tw_bb.p;
     s.cl_bb = cl_bb.p;
+    s.cl_z = cl_z.p;
     s.cl_sys = cl_sys.p;
     s.cl_tower = cl_tower.p;
     s.cl_flags = cl_flags.p;
@@ -657,7 +659,7 @@ static int ensure_particle_capacity(pe_engine *h) {
       !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
-  if (!h->cl_bb.ensure(6 * ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
+  if (!h->cl_bb.ensure(6 * ncl) || !h->cl_z.ensure(ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
       !h->cp_count.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(4 * ncl) ||
       !h->cl_hits.ensure(ncl) || !h->key.ensure(n) || !h->skey.ensure(n) || !h->tower_of.ensure(n) ||
       !h->sval.ensure(n) || !h->perm_src.ensure(n) || !h->cp_total.ensure(1) || !h->derr.ensure(1) ||
@@ -1010,6 +1012,7 @@ int pe_destroy(pe_engine *h) {
   h->sys_chunk0.release();
   h->chunk_part.release();
   h->cp_list.release();
+  h->cl_z.release();
   h->cp_total.release();
   h->cl_hits.release();
   h->dump_n.release();

@@ -324,6 +324,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
 template <bool GLOB, bool ONE_TYPE, bool KAHAN>
 struct MixedAcc {
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
+  float bx = 0.f, by = 0.f, bz = 0.f;  // plain sum of the current batch, Kahan-added by flush()
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
   int hits = 0, hhalo = 0;
 
@@ -362,15 +363,9 @@ struct MixedAcc {
     float fac = eps24 * (lj12 + lj12m6) * inv;
     fac = mask ? fac : 0.f;
     const float px = dx * fac, py = dy * fac, pz = dz * fac;
-    if (KAHAN) {
-      kahan_add(fxs, fxc, px);
-      kahan_add(fys, fyc, py);
-      kahan_add(fzs, fzc, pz);
-    } else {
-      fxs += px;
-      fys += py;
-      fzs += pz;
-    }
+    bx += px;
+    by += py;
+    bz += pz;
     if (GLOB) {
       pot += mask ? fmaf(eps24, lj12m6, sh6) : 0.f;
       vx = fmaf(px, dx, vx);
@@ -379,6 +374,19 @@ struct MixedAcc {
       hits += mask ? 1 : 0;
       if (!S.periodic) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
     }
+  }
+
+  __device__ __forceinline__ void flush() {
+    if (KAHAN) {
+      kahan_add(fxs, fxc, bx);
+      kahan_add(fys, fyc, by);
+      kahan_add(fzs, fzc, bz);
+    } else {
+      fxs += bx;
+      fys += by;
+      fzs += bz;
+    }
+    bx = by = bz = 0.f;
   }
 };
 
@@ -433,6 +441,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u)
       acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
+    acc.flush();
   }
   for (; k < n; ++k) {
     const uint32_t ent = __ldg(lp + (int64_t)k * stride);
@@ -440,6 +449,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
     const float4 lj = __ldg(&s.pk_lo[ent >> 5]);
     acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent, hj, lj, eps24, sig2, sh6, tab, T, band);
   }
+  acc.flush();
   const double Fx = (double)acc.fxs - (double)acc.fxc, Fy = (double)acc.fys - (double)acc.fyc,
                Fz = (double)acc.fzs - (double)acc.fzc;
   if (oi == 1) {

@@ -31,6 +31,7 @@ struct DeviceState {
   int32_t *tw_cl_start = nullptr;  // [ntowers+1] first cluster of each tower
   double *tw_bb = nullptr;         // [ntowers*4] xy bbox of the tower's particles (minx,miny,maxx,maxy)
   double *cl_bb = nullptr;         // [nclusters*6] lo xyz, hi xyz (real members only)
+  float2 *cl_z = nullptr;          // [nclusters] z range rounded outwards to float (window search only)
   int32_t *cl_sys = nullptr;       // [nclusters]
   int32_t *cl_tower = nullptr;     // [nclusters]
   int32_t *cl_flags = nullptr;     // bit0: has owned member, bit1: has any real member
