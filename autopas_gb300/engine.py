@@ -16,8 +16,9 @@ from . import build as _build
 PE_OK = 0
 ERRORS = {
     -1: "PE_ERR_ARG", -2: "PE_ERR_OOM", -3: "PE_ERR_CUDA", -4: "PE_ERR_LIST_OVERFLOW", -5: "PE_ERR_TOWER_OVERFLOW",
-    -6: "PE_ERR_STATE", -7: "PE_ERR_NO_DEVICE", -8: "PE_ERR_DOMAIN",
+    -6: "PE_ERR_STATE", -7: "PE_ERR_NO_DEVICE", -8: "PE_ERR_DOMAIN", -9: "PE_ERR_TOO_LARGE",
 }
+NOALLOC_MAX_PARTICLES = 16384
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 DIST_STRICT, DIST_FMA_SOA, DIST_FMA_DOT = 0, 1, 2
 DUMMY, OWNED, HALO = 0, 1, 2
@@ -26,7 +27,7 @@ DUMMY, OWNED, HALO = 0, 1, 2
 EXPORTS = [
     "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
-    "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning",
+    "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning", "pe_lj_forces_noalloc",
 ]
 
 
@@ -100,6 +101,7 @@ def load(path: str | None = None):
     L.pe_get_stats.argtypes = [vp, C.c_int, C.POINTER(PeStats)]
     L.pe_device_timer.argtypes = [vp, C.c_int, dp]
     L.pe_tune.argtypes = [vp, C.c_int]
+    L.pe_lj_forces_noalloc.argtypes = [C.POINTER(PeConfig), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pe_get_tuning.argtypes = [vp, C.c_int, C.POINTER(PeTuningEntry), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     for name in EXPORTS:
         if name != "pe_last_error":
@@ -273,6 +275,25 @@ class PairEngine:
         ms = C.c_double()
         self._check(self._L.pe_device_timer(self._h, 1, C.byref(ms)))
         return ms.value
+
+
+def make_config(cutoff, skin=0.0, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,), shift=False, dist_mode=DIST_STRICT):
+    """A PeConfig for calls that take one without an engine (pe_lj_forces_noalloc).  Returns (cfg, keepalive)."""
+    eps = np.ascontiguousarray(epsilon, np.float64)
+    sig = np.ascontiguousarray(sigma, np.float64)
+    ms = np.ascontiguousarray(mass, np.float64)
+    dp = C.POINTER(C.c_double)
+    cfg = PeConfig(cutoff, skin, len(eps), eps.ctypes.data_as(dp), sig.ctypes.data_as(dp), ms.ctypes.data_as(dp),
+                   int(shift), PRECISION_FP64, 8, 0, int(dist_mode), 1, 1, 1, 1)
+    return cfg, (eps, sig, ms)
+
+
+def lj_forces_noalloc(cfg, n, x, y, z, type_ptr, own_ptr, fx, fy, fz, globals_ptr, stream=None):
+    """Direct call of pe_lj_forces_noalloc with device addresses (ints); raises on a non-zero status."""
+    L = load()
+    rc = L.pe_lj_forces_noalloc(C.byref(cfg), int(n), x, y, z, type_ptr, own_ptr, fx, fy, fz, globals_ptr, stream)
+    if rc != PE_OK:
+        raise EngineError(rc, "pe_lj_forces_noalloc failed")
 
 
 def _globals(g):

@@ -41,6 +41,7 @@ extern "C" {
 #define PE_ERR_STATE (-6)         /* call order violated (e.g. compute before set_particles) */
 #define PE_ERR_NO_DEVICE (-7)     /* no CUDA device or not an sm_103 device */
 #define PE_ERR_DOMAIN (-8)        /* periodic box shorter than twice the interaction length */
+#define PE_ERR_TOO_LARGE (-9)     /* more particles than pe_lj_forces_noalloc accepts */
 
 /* ---- option values ---- */
 #define PE_PRECISION_FP64 0   /* plain FP64 form: FP64 positions, FP64 LJ arithmetic, FP64 sums */
@@ -193,6 +194,25 @@ typedef struct {
 } pe_tuning_entry;
 int pe_tune(pe_engine *h, int samples);
 int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, int *chosen);
+
+/* Forces without any memory allocation.  This entry point has no counterpart in the reference: it exists
+ * for callers that cannot allocate device memory where they need forces -- code running while a stream is
+ * captured into a CUDA graph, hosts whose device memory is all handed out by a framework's pool, loops that
+ * must not block in an allocator.  It computes, in the plain FP64 form, the forces on the owned particles of
+ * one small non-periodic set (owned + halo, AutoPas container semantics; every pair with dr2 <= rc^2 from both
+ * sides, reference LJ arithmetic) and writes globals[0..5] = {Upot, virial, virial_x, virial_y, virial_z,
+ * interacting pairs}.  All arrays are device memory owned by the caller (type and ownership may be NULL:
+ * type 0, owned); cfg supplies cutoff, types, epsilon, sigma, apply_shift and dist_mode; stream is a
+ * cudaStream_t (NULL: the default stream).  The call is asynchronous on that stream.
+ * Limits: n <= PE_NOALLOC_MAX_PARTICLES, else PE_ERR_TOO_LARGE.  The only scratch is a fixed 5 KB array of
+ * per-block partial sums in the library's device memory, shared by every call on a device and held by every
+ * device that loads the library until the process exits; calls that overlap on the GPU race on it, so issue
+ * them on one stream or wait for one before the next.  The first call on a device looks up that array's
+ * device address (with the device current) and caches it: make that first call before any stream capture. */
+#define PE_NOALLOC_MAX_PARTICLES 16384
+int pe_lj_forces_noalloc(const pe_config *cfg, int64_t n, const double *x, const double *y, const double *z,
+                         const int32_t *type, const int8_t *ownership, double *fx, double *fy, double *fz,
+                         double *globals, void *stream);
 
 /* Device timer on the engine's stream: op 0 records a start event; op 1 records a stop event, waits for it and
  * returns the elapsed milliseconds between the two in *ms. */
