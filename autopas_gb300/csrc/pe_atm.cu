@@ -1,0 +1,205 @@
+// pe_atm.cu -- Axilrod-Teller-Muto three-body forces on the particle lists.
+//
+// Replaces AxilrodTellerMutoFunctor::AoSFunctor under the triwise traversals
+// (applicationLibrary/molecularDynamics/molecularDynamicsLibrary/AxilrodTellerMutoFunctor.h:186-293, 360-385).
+//
+// One warp per owned particle i.  The warp first gathers the neighbours of i within the triplet cutoff from i's
+// particle list (displacements d = r_i - r_j from the hi/lo positions, so each is rounded once to FP32) into
+// shared memory, then the lanes walk the pairs (j, k) of that set; every triplet with all three distances within
+// the cutoff contributes the reference's force on i (forceI, :231-240) and 3*Upot (:268).  Each triplet is thus
+// evaluated once from each of its vertices and no atomics are needed.  Near-cutoff distances repeat the test in
+// FP64 on the positions the reference would use (halo images formed as x + s*len).  Force and energy sums are
+// compensated FP32 per lane and FP64 across lanes; the virial of i is F_i . r_i in FP64, which summed over the
+// owned particles equals the reference's per-triplet sum of F . r over owned vertices (:272-286).
+#include "pe_state.cuh"
+
+namespace pe {
+
+constexpr int kAtmWarps = 4;
+constexpr int kAtmMaxNeigh = 256;
+
+struct AtmArgs {
+  float nu;
+  float rc2f;
+  double rc2;
+};
+
+__device__ __forceinline__ void kahan(float &s, float &c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// exact FP64 squared distance between two particle images as the reference sees them
+__device__ __forceinline__ double img_dist2(const DeviceState &s, const SysDev &S, int64_t a, int ca, int64_t b,
+                                            int cb) {
+  int ax, ay, az, bx, by, bz;
+  shift_of(ca, ax, ay, az);
+  shift_of(cb, bx, by, bz);
+  const double dx = image_coord(s.x[b], bx, S.len[0]) - image_coord(s.x[a], ax, S.len[0]);
+  const double dy = image_coord(s.y[b], by, S.len[1]) - image_coord(s.y[a], ay, S.len[1]);
+  const double dz = image_coord(s.z[b], bz, S.len[2]) - image_coord(s.z[a], az, S.len[2]);
+  return dist2_mode(dx, dy, dz, 0);
+}
+
+__global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs aa, double *__restrict__ slot_glob,
+                                                         int *__restrict__ err) {
+  __shared__ float4 nb[kAtmWarps][kAtmMaxNeigh];
+  __shared__ uint32_t ne[kAtmWarps][kAtmMaxNeigh];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = blockIdx.x * (int64_t)kAtmWarps + w;
+  if (i >= s.nslots) return;
+  const int oi = s.own[i];
+  if (oi != 1) {
+    if (lane == 0) {
+      slot_glob[3 * i] = 0;
+      slot_glob[3 * i + 1] = 0;
+      slot_glob[3 * i + 2] = 0;
+    }
+    return;
+  }
+  const SysDev &S = s.sysd[s.sys[i]];
+  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const int n = min(s.pl_count[i], s.pl_cap);
+  const float band = aa.rc2f * 2e-6f;
+  // phase 1: neighbours within the triplet cutoff, in list order
+  int m = 0;
+  bool overflow = false;
+  for (int base = 0; base < n; base += 32) {
+    const int k = base + lane;
+    bool keep = false;
+    float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t ent = 0;
+    if (k < n) {
+      ent = s.pl_list[(int64_t)k * s.pl_stride + i];
+      const int64_t j = ent >> 5;
+      const int code = ent & 31;
+      const float4 hj = s.pk_hi[j], lj = s.pk_lo[j];
+      float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+      if (code != kShiftNone) {
+        const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+        xh = fmaf(-sxf, S.len_hi[0], xh);
+        yh = fmaf(-syf, S.len_hi[1], yh);
+        zh = fmaf(-szf, S.len_hi[2], zh);
+        xl = fmaf(-sxf, S.len_lo[0], xl);
+        yl = fmaf(-syf, S.len_lo[1], yl);
+        zl = fmaf(-szf, S.len_lo[2], zl);
+      }
+      d.x = (xh - hj.x) + (xl - lj.x);
+      d.y = (yh - hj.y) + (yl - lj.y);
+      d.z = (zh - hj.z) + (zl - lj.z);
+      d.w = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+      keep = d.w <= aa.rc2f;
+      if (fabsf(d.w - aa.rc2f) <= band) keep = img_dist2(s, S, i, kShiftNone, j, code) <= aa.rc2;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    const int pos = m + __popc(bal & ((1u << lane) - 1));
+    if (keep) {
+      if (pos < kAtmMaxNeigh) {
+        nb[w][pos] = d;
+        ne[w][pos] = ent;
+      } else {
+        overflow = true;
+      }
+    }
+    m += __popc(bal);
+  }
+  if (__any_sync(0xffffffffu, overflow)) {
+    if (lane == 0) atomicOr(err, 1);
+    return;
+  }
+  __syncwarp();
+  // phase 2: pairs (a, b), a < b, of the neighbour set
+  float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f, ps = 0.f, pc = 0.f;
+  int trip = 0;
+  const float nu3 = 3.0f * aa.nu;
+  for (int a = 0; a < m; ++a) {
+    const float4 dj = nb[w][a];
+    for (int b = a + 1 + lane; b < m; b += 32) {
+      const float4 dk = nb[w][b];
+      // reference vectors: IJ = r_j - r_i = -d_j, KI = r_i - r_k = d_k, JK = r_k - r_j = d_j - d_k
+      const float IJx = -dj.x, IJy = -dj.y, IJz = -dj.z;
+      const float KIx = dk.x, KIy = dk.y, KIz = dk.z;
+      const float JKx = dj.x - dk.x, JKy = dj.y - dk.y, JKz = dj.z - dk.z;
+      const float d2IJ = dj.w, d2KI = dk.w;
+      float d2JK = fmaf(JKz, JKz, fmaf(JKy, JKy, JKx * JKx));
+      bool in = d2JK <= aa.rc2f;
+      if (fabsf(d2JK - aa.rc2f) <= band) {
+        const uint32_t ej = ne[w][a], ek = ne[w][b];
+        in = img_dist2(s, S, (int64_t)(ej >> 5), ej & 31, (int64_t)(ek >> 5), ek & 31) <= aa.rc2;
+      }
+      if (!in) continue;
+      const float all2 = d2IJ * d2JK * d2KI;
+      const float all5 = all2 * all2 * sqrtf(all2);
+      const float factor = nu3 / all5;
+      const float IJdotKI = IJx * KIx + IJy * KIy + IJz * KIz;
+      const float IJdotJK = IJx * JKx + IJy * JKy + IJz * JKz;
+      const float JKdotKI = JKx * KIx + JKy * KIy + JKz * KIz;
+      const float allDots = IJdotKI * IJdotJK * JKdotKI;
+      const float cJK = IJdotKI * (IJdotJK - JKdotKI);
+      const float cIJ = IJdotJK * JKdotKI - d2JK * d2KI + 5.0f * allDots / d2IJ;
+      const float cKI = -IJdotJK * JKdotKI + d2IJ * d2JK - 5.0f * allDots / d2KI;
+      kahan(fxs, fxc, (JKx * cJK + IJx * cIJ + KIx * cKI) * factor);
+      kahan(fys, fyc, (JKy * cJK + IJy * cIJ + KIy * cKI) * factor);
+      kahan(fzs, fzc, (JKz * cJK + IJz * cIJ + KIz * cKI) * factor);
+      kahan(ps, pc, factor * (all2 - 3.0f * allDots));
+      ++trip;
+    }
+  }
+  double Fx = (double)fxs - (double)fxc, Fy = (double)fys - (double)fyc, Fz = (double)fzs - (double)fzc;
+  double P = (double)ps - (double)pc;
+  long long T = trip;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Fx += __shfl_xor_sync(0xffffffffu, Fx, o);
+    Fy += __shfl_xor_sync(0xffffffffu, Fy, o);
+    Fz += __shfl_xor_sync(0xffffffffu, Fz, o);
+    P += __shfl_xor_sync(0xffffffffu, P, o);
+    T += __shfl_xor_sync(0xffffffffu, T, o);
+  }
+  if (lane == 0) {
+    s.fx[i] += Fx;
+    s.fy[i] += Fy;
+    s.fz[i] += Fz;
+    slot_glob[3 * i] = P;
+    slot_glob[3 * i + 1] = Fx * s.x[i] + Fy * s.y[i] + Fz * s.z[i];
+    slot_glob[3 * i + 2] = (double)T;
+  }
+}
+
+// per-system sums over the system's slots in a fixed order, endTraversal post-processing (/3/3)
+__global__ void k_reduce_atm(DeviceState s, const int64_t *__restrict__ sys_cl_range, const double *__restrict__ slot_glob,
+                             double *__restrict__ out) {
+  const int sy = blockIdx.x;
+  const int64_t a = sys_cl_range[2 * sy] * s.C, b = sys_cl_range[2 * sy + 1] * s.C;
+  double g[3] = {0, 0, 0};
+  for (int64_t q = a + threadIdx.x; q < b; q += blockDim.x)
+    for (int c = 0; c < 3; ++c) g[c] += slot_glob[3 * q + c];
+  __shared__ double red[3][256];
+  for (int c = 0; c < 3; ++c) red[c][threadIdx.x] = g[c];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int c = 0; c < 3; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[3 * sy] = red[0][0] / 3. / 3.;
+    out[3 * sy + 1] = red[1][0];
+    out[3 * sy + 2] = red[2][0];
+  }
+}
+
+void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, const int64_t *sys_cl_range, double *out,
+                int *err, cudaStream_t st) {
+  AtmArgs aa;
+  aa.nu = (float)nu;
+  aa.rc2 = cutoff * cutoff;
+  aa.rc2f = (float)aa.rc2;
+  const int64_t nb = (s.nslots + kAtmWarps - 1) / kAtmWarps;
+  if (nb > 0) k_atm<<<(unsigned)nb, kAtmWarps * 32, 0, st>>>(s, aa, slot_glob, err);
+  if (s.nsys > 0) k_reduce_atm<<<s.nsys, 256, 0, st>>>(s, sys_cl_range, slot_glob, out);
+}
+
+}  // namespace pe

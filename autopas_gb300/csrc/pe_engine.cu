@@ -134,6 +134,9 @@ struct pe_engine {
   DBuf<int> pl_max;
   int pl_cap = 0;
   int64_t pl_entries = 0;
+  bool need_plist = false;       // particle lists needed besides the force traversal (three-body forces)
+  DBuf<double> atm_slot, atm_out;
+  DBuf<int> atm_err;
 
   // rebuild temporaries
   DBuf<uint64_t> key, skey;
@@ -778,7 +781,7 @@ static int do_rebuild(pe_engine *h) {
     }
     break;
   }
-  if (h->traversal == 1) PE_TRY(build_particle_lists(h));
+  if (h->traversal == 1 || h->need_plist) PE_TRY(build_particle_lists(h));
   const int ns = (int)h->sys.size();
   k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
   h->launches += 1;
@@ -839,6 +842,18 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
   h->steps_since_rebuild += 1;
   h->forces_valid = true;
   return h->cuda_check("force kernel");
+}
+
+static int atm_eval(pe_engine *h, double nu, double cutoff3) {
+  const int ns = (int)h->sys.size();
+  if (!h->atm_slot.ensure(3 * (size_t)std::max<int64_t>(h->pcap, 1)) || !h->atm_out.ensure(3 * (size_t)ns) ||
+      !h->atm_err.ensure(1))
+    return h->fail(PE_ERR_OOM, "three-body buffers");
+  DeviceState s = h->state();
+  PE_CUDA(h, cudaMemsetAsync(h->atm_err.p, 0, sizeof(int), h->st));
+  launch_atm(s, nu, cutoff3, h->atm_slot.p, h->sys_cl_range.p, h->atm_out.p, h->atm_err.p, h->st);
+  h->launches += 2;
+  return h->cuda_check("three-body kernel");
 }
 
 static int read_globals(pe_engine *h, pe_globals *g) {
@@ -939,6 +954,9 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->dist_mode < 0 || cfg->dist_mode > 2) return PE_ERR_ARG;
   if (cfg->tower_sizing < 0 || cfg->tower_sizing > 1) return PE_ERR_ARG;
   if (cfg->traversal < -1 || cfg->traversal > 1) return PE_ERR_ARG;
+  if (cfg->atm_nu > 0 && !(cfg->atm_cutoff > 0 && cfg->atm_cutoff <= cfg->cutoff + cfg->skin)) return PE_ERR_ARG;
+  // every force kernel evaluates each pair from both sides (full lists); half lists are not offered
+  if (cfg->newton3 == 1) return PE_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PE_ERR_NO_DEVICE;
   pe_engine *h = new pe_engine();
@@ -951,6 +969,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   h->cfg.mass = h->mass.data();
   h->C = cfg->cluster_size == 0 ? 8 : cfg->cluster_size;
   h->traversal = cfg->traversal == 0 ? 0 : 1;
+  h->need_plist = cfg->atm_nu > 0;
   h->newton3 = (cfg->newton3 == 1 && h->traversal == 0) ? 1 : 0;
   h->precision = cfg->precision;
   cudaGetDevice(&h->device);
@@ -1030,6 +1049,9 @@ int pe_destroy(pe_engine *h) {
   h->pl_list.release();
   h->pl_count.release();
   h->pl_max.release();
+  h->atm_slot.release();
+  h->atm_out.release();
+  h->atm_err.release();
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return PE_OK;
@@ -1168,10 +1190,46 @@ int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals) {
     if (h->nslots > 0) k_positions<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, dt);
     h->launches += 1;
     if (!h->lists_valid || h->steps_since_rebuild >= freq) PE_TRY(do_rebuild(h));
-    PE_TRY(force_eval(h, true, dt, true));
+    if (h->cfg.atm_nu > 0) {
+      // the velocity update needs the total force: pair forces, then three-body forces, then velocities
+      PE_TRY(force_eval(h, false, dt, true));
+      PE_TRY(atm_eval(h, h->cfg.atm_nu, h->cfg.atm_cutoff));
+      DeviceState s2 = h->state();
+      if (h->nslots > 0) k_velocities<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s2, dt);
+      h->launches += 1;
+    } else {
+      PE_TRY(force_eval(h, true, dt, true));
+    }
   }
   PE_TRY(h->cuda_check("step"));
   if (globals) return read_globals(h, globals);
+  return PE_OK;
+}
+
+int pe_compute_atm(pe_engine *h, double nu, double cutoff3, pe_globals *globals) {
+  if (!h) return PE_ERR_ARG;
+  if (!(cutoff3 > 0) || cutoff3 > h->cfg.cutoff + h->cfg.skin) return h->fail(PE_ERR_ARG, "ATM cutoff %g", cutoff3);
+  if (!h->forces_valid) return h->fail(PE_ERR_STATE, "pe_compute_atm adds to the forces of pe_compute_forces");
+  if (!h->need_plist && h->traversal != 1) {
+    h->need_plist = true;
+    PE_TRY(build_particle_lists(h));
+  }
+  h->need_plist = true;
+  PE_TRY(atm_eval(h, nu, cutoff3));
+  const int ns = (int)h->sys.size();
+  std::vector<double> v(3 * ns);
+  int e = 0;
+  PE_CUDA(h, cudaMemcpyAsync(v.data(), h->atm_out.p, sizeof(double) * 3 * ns, cudaMemcpyDeviceToHost, h->st));
+  PE_CUDA(h, cudaMemcpyAsync(&e, h->atm_err.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  PE_CUDA(h, cudaStreamSynchronize(h->st));
+  if (e) return h->fail(PE_ERR_LIST_OVERFLOW, "more than 256 neighbours within the triplet cutoff");
+  if (globals)
+    for (int q = 0; q < ns; ++q) {
+      globals[q].upot = v[3 * q];
+      globals[q].virial = v[3 * q + 1];
+      globals[q].virial_xyz[0] = globals[q].virial_xyz[1] = globals[q].virial_xyz[2] = 0;
+      globals[q].num_pairs = (int64_t)(v[3 * q + 2] + 0.5) / 3;
+    }
   return PE_OK;
 }
 

@@ -11,8 +11,7 @@
 //
 //  * full lists (newton3 off): every pair is evaluated from both sides; the i-force is accumulated in
 //    registers (compensated FP32 for the mixed form) and written once -- no atomics, deterministic.
-//  * half lists (newton3 on): the j-force of a step is reduced across the C i-lanes with warp shuffles
-//    and added to j with one FP32 atomic per component per j.
+//    This is the only list mode the kernels implement.
 //
 // Precision forms:
 //  * FP64 ("plain FP64 GPU form"): positions, displacements and LJ arithmetic in FP64 with the reference's

@@ -86,6 +86,10 @@ void launch_plist_build(DeviceState &s, cudaStream_t st);
 void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
                       unsigned long long *count, cudaStream_t st);
 
+// three-body forces (pe_atm.cu)
+void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, const int64_t *sys_cl_range, double *out,
+                int *err, cudaStream_t st);
+
 // forces (pe_force.cu)
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt,
                   cudaStream_t st);

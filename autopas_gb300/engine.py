@@ -28,6 +28,7 @@ EXPORTS = [
     "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
     "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning", "pe_lj_forces_noalloc",
+    "pe_compute_atm",
 ]
 
 
@@ -37,7 +38,7 @@ class PeConfig(C.Structure):
         ("epsilon", C.POINTER(C.c_double)), ("sigma", C.POINTER(C.c_double)), ("mass", C.POINTER(C.c_double)),
         ("apply_shift", C.c_int), ("precision", C.c_int), ("cluster_size", C.c_int), ("newton3", C.c_int),
         ("dist_mode", C.c_int), ("rebuild_frequency", C.c_int), ("calc_globals", C.c_int),
-        ("tower_sizing", C.c_int), ("traversal", C.c_int),
+        ("tower_sizing", C.c_int), ("traversal", C.c_int), ("atm_nu", C.c_double), ("atm_cutoff", C.c_double),
     ]
 
 
@@ -101,6 +102,7 @@ def load(path: str | None = None):
     L.pe_get_stats.argtypes = [vp, C.c_int, C.POINTER(PeStats)]
     L.pe_device_timer.argtypes = [vp, C.c_int, dp]
     L.pe_tune.argtypes = [vp, C.c_int]
+    L.pe_compute_atm.argtypes = [vp, C.c_double, C.c_double, vp]
     L.pe_lj_forces_noalloc.argtypes = [C.POINTER(PeConfig), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pe_get_tuning.argtypes = [vp, C.c_int, C.POINTER(PeTuningEntry), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     for name in EXPORTS:
@@ -125,7 +127,7 @@ class PairEngine:
 
     def __init__(self, cutoff, skin, boxes, periodic=True, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,),
                  shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_STRICT,
-                 rebuild_frequency=10, calc_globals=True, tower_sizing=1, traversal=1):
+                 rebuild_frequency=10, calc_globals=True, tower_sizing=1, traversal=1, atm_nu=0.0, atm_cutoff=0.0):
         L = load()
         self._L = L
         self._eps = np.ascontiguousarray(epsilon, np.float64)
@@ -136,7 +138,7 @@ class PairEngine:
         cfg = PeConfig(cutoff, skin, T, self._eps.ctypes.data_as(dp), self._sig.ctypes.data_as(dp),
                        self._mass.ctypes.data_as(dp), int(shift), int(precision), int(cluster_size), int(newton3),
                        int(dist_mode), int(rebuild_frequency), int(calc_globals), int(tower_sizing),
-                       int(traversal))
+                       int(traversal), float(atm_nu), float(atm_cutoff))
         boxes = list(boxes)
         if np.ndim(boxes[0]) == 1:  # single (bmin, bmax)
             boxes = [boxes]
@@ -204,6 +206,12 @@ class PairEngine:
     def compute_forces(self):
         g = (PeGlobals * self.num_systems)()
         self._check(self._L.pe_compute_forces(self._h, g))
+        return _globals(g)
+
+    def compute_atm(self, nu, cutoff3):
+        """Adds Axilrod-Teller-Muto forces to the current forces; returns per-system ATM globals."""
+        g = (PeGlobals * self.num_systems)()
+        self._check(self._L.pe_compute_atm(self._h, float(nu), float(cutoff3), g))
         return _globals(g)
 
     def forces(self, out=None):
@@ -284,7 +292,7 @@ def make_config(cutoff, skin=0.0, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,), shi
     ms = np.ascontiguousarray(mass, np.float64)
     dp = C.POINTER(C.c_double)
     cfg = PeConfig(cutoff, skin, len(eps), eps.ctypes.data_as(dp), sig.ctypes.data_as(dp), ms.ctypes.data_as(dp),
-                   int(shift), PRECISION_FP64, 8, 0, int(dist_mode), 1, 1, 1, 1)
+                   int(shift), PRECISION_FP64, 8, 0, int(dist_mode), 1, 1, 1, 1, 0.0, 0.0)
     return cfg, (eps, sig, ms)
 
 

@@ -71,8 +71,8 @@ typedef struct {
   int apply_shift;         /* truncated-shifted potential (applyShift) */
   int precision;           /* PE_PRECISION_* */
   int cluster_size;        /* 4 or 8; 0 lets the engine's tuner decide */
-  int newton3;             /* 0: full lists, each pair evaluated from both sides; 1: half lists + j-force reduction;
-                              -1: tuner decides */
+  int newton3;             /* 0 or -1: full lists, each pair evaluated from both sides (the only mode the force
+                              kernels implement; 1 is rejected with PE_ERR_ARG) */
   int dist_mode;           /* PE_DIST_* for every FP64 distance test */
   int rebuild_frequency;   /* steps between list rebuilds inside pe_step (verletRebuildFrequency) */
   int calc_globals;        /* compute Upot and virial with every force evaluation */
@@ -84,6 +84,8 @@ typedef struct {
                               1: per-particle lists filtered from the cluster pairs on the device (VerletLists
                               traversal, vl_list_iteration); -1: the engine's tuner times both and keeps the
                               faster */
+  double atm_nu;           /* > 0: pe_step adds Axilrod-Teller-Muto three-body forces with this nu */
+  double atm_cutoff;       /* triplet cutoff for ATM (all three distances); <= cutoff + skin */
 } pe_config;
 
 /* One particle system of the ensemble. */
@@ -137,6 +139,14 @@ int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, doub
  * (every rebuild_frequency steps), forces, velocity update.  Requires forces of the current positions
  * (pe_compute_forces) before the first step.  globals of the last step: [num_systems] or NULL. */
 int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals);
+
+/* Replaces: computeInteractions(&atmFunctor) for AxilrodTellerMutoFunctor (AxilrodTellerMutoFunctor.h:186-385):
+ * adds the three-body forces of every triplet with all distances <= cutoff3 to the current forces (call after
+ * pe_compute_forces) and returns per system {Upot_ATM, virial_ATM = sum over owned i of F_i . r_i, -, -, -,
+ * num_pairs = triplets counted once per owned vertex / 3}.  The triplet arithmetic is FP32 on displacements
+ * rounded once from the FP64 positions; sums are compensated FP32 per lane and FP64 beyond.  cutoff3 must not
+ * exceed cutoff + skin (the particle lists supply the candidates). */
+int pe_compute_atm(pe_engine *h, double nu, double cutoff3, pe_globals *globals);
 
 /* ---- introspection / verification ---- */
 typedef struct {

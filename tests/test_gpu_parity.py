@@ -286,3 +286,56 @@ def test_tuner_full_search_keeps_results(eng_mod, orc):
     assert rel_rms(F, R[: len(pos)]) <= 1e-6
     assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
     e.step(0.002, 5)
+
+
+# ------------------------------------------------------------------------------------------- three-body (ATM)
+# The triplet arithmetic is FP32 (on displacements rounded once from FP64), so the ATM checks use a relative
+# tolerance of 1e-5 on forces and energies instead of the reference's FP64 absolute 1e-7.
+def test_atm_known_answer_through_engine(eng_mod):
+    """ATMFunctorTestNoGlobals.h:19-32 (cutoff 1, nu 1) with the pair term switched off (epsilon 0)."""
+    pos = np.array([[0.0, 0.0, 0.0], [0.1, 0.2, 0.3], [0.3, 0.2, 0.1]])
+    e = eng_mod.PairEngine(1.0, 0.3, ([-1, -1, -1], [2, 2, 2]), periodic=False, epsilon=[0.0], sigma=[1.0],
+                           precision=eng_mod.PRECISION_MIXED)
+    e.set_particles(pos)
+    e.compute_forces()
+    g = e.compute_atm(1.0, 1.0)[0]
+    F = e.forces()
+    exp = np.array([[-188761.250385809] * 3, [-95789.2912405596, 94380.6251929043, 284550.541626368],
+                    [284550.541626368, 94380.6251929043, -95789.2912405596]])
+    np.testing.assert_allclose(F, exp, rtol=1e-5, atol=1e-5 * np.abs(exp).max())
+    assert g["num_pairs"] == 1
+
+
+def test_atm_globals_known_answer(eng_mod):
+    """ATMFunctorTestGlobals.cpp:12-78 (cutoff 5, nu 0.7), all three particles owned."""
+    import math
+    p = np.array([[0.0, 0.0, 0.0], [0.1, 0.0, 0.0], [0.0, 0.2, 0.3]])
+    e = eng_mod.PairEngine(5.0, 0.3, ([-1, -1, -1], [2, 2, 2]), periodic=False, epsilon=[0.0], sigma=[1.0])
+    e.set_particles(p)
+    e.compute_forces()
+    g = e.compute_atm(0.7, 5.0)[0]
+    ij, ik, jk = p[0] - p[1], p[0] - p[2], p[1] - p[2]
+    dij, dik, djk = (math.sqrt(float(v @ v)) for v in (ij, ik, jk))
+    ci = float(ik @ ij) / (dik * dij)
+    cj = -float(jk @ ij) / (djk * dij)
+    ck = float(ik @ jk) / (dik * djk)
+    expected = 0.7 * (3 * ci * cj * ck + 1.0) / (dij * djk * dik) ** 3
+    assert g["upot"] == pytest.approx(expected, rel=1e-5)
+
+
+def test_atm_periodic_liquid_matches_oracle(eng_mod, orc):
+    from autopas_gb300 import workloads
+    pos, vel, bmin, bmax = workloads.fcc_lj(4, 0.8, 1.0, seed=2)
+    rng = np.random.default_rng(2)
+    pos = np.mod(pos + rng.normal(0, 0.07, pos.shape), bmax)
+    rc, skin, nu = 2.5, 0.3, 0.073
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=[0.0], sigma=[1.0])
+    e.set_particles(pos, vel)
+    e.compute_forces()
+    g = e.compute_atm(nu, rc)[0]
+    F = e.forces()
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, hits = orc.atm_forces(allpos, nu, rc, own=own)
+    R = R[: len(pos)]
+    assert rel_rms(F, R) <= 1e-5
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-5)
