@@ -49,6 +49,13 @@ struct SysDev {
   float len_hi[3], len_lo[3];
 };
 
+// Velocity-Verlet factors per type, computed on the host with the reference's operation order
+// (TimeDiscretization.cpp:42: dt*dt/(2*m); :160: dt/(2*m)) so that no kernel divides in FP64.
+struct VVFactors {
+  double c[kMaxTypes];  // dt*dt / (2 m)
+  double h[kMaxTypes];  // dt / (2 m)
+};
+
 struct TypeTable {
   int ntypes;
   double eps24[kMaxTypes * kMaxTypes];

@@ -163,6 +163,11 @@ struct pe_engine {
   int64_t force_launches = 0;
   int64_t rebuilds = 0;
   cudaEvent_t timer_ev[2] = {nullptr, nullptr};
+  // CUDA graph of one step without list rebuild, captured once per rebuild
+  cudaGraphExec_t step_graph = nullptr;
+  bool step_graph_valid = false;
+  double step_graph_dt = 0;
+  int step_graph_launches = 0;
   DBuf<long long> pairs_acc;  // interacting pairs summed over force evaluations
 
   DeviceState state() {
@@ -427,12 +432,11 @@ __global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int3
 }
 
 // velocity-Verlet position half (TimeDiscretization.cpp:17-66 with globalForce 0) fused with the re-encode
-__global__ void k_positions(DeviceState s, double dt) {
+__global__ void k_positions(DeviceState s, double dt, VVFactors vv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= s.nslots) return;
   if (s.own[i] == 1) {
-    const double m = s.mass[s.type[i]];
-    const double c = __ddiv_rn(__dmul_rn(dt, dt), __dmul_rn(2.0, m));
+    const double c = vv.c[s.type[i]];
     const double fx = s.fx[i], fy = s.fy[i], fz = s.fz[i];
     // displacement = v*dt + F*(dt*dt/(2m)), every operation rounded as written in the reference
     s.x[i] = __dadd_rn(s.x[i], __dadd_rn(__dmul_rn(s.vx[i], dt), __dmul_rn(fx, c)));
@@ -449,11 +453,10 @@ __global__ void k_positions(DeviceState s, double dt) {
 }
 
 // velocity half when it is not fused into the force kernel
-__global__ void k_velocities(DeviceState s, double dt) {
+__global__ void k_velocities(DeviceState s, VVFactors vv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= s.nslots || s.own[i] != 1) return;
-  const double m = s.mass[s.type[i]];
-  const double h = __ddiv_rn(dt, __dmul_rn(2.0, m));
+  const double h = vv.h[s.type[i]];
   s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(s.fx[i], s.ofx[i]), h));
   s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(s.fy[i], s.ofy[i]), h));
   s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(s.fz[i], s.ofz[i]), h));
@@ -815,7 +818,18 @@ static int do_rebuild(pe_engine *h) {
   h->lists_valid = true;
   h->steps_since_rebuild = 0;
   h->rebuilds += 1;
+  h->step_graph_valid = false;  // sizes and buffers may have changed
   return PE_OK;
+}
+
+static VVFactors vv_factors(const pe_engine *h, double dt) {
+  VVFactors v{};
+  for (int t = 0; t < h->table.ntypes; ++t) {
+    const double m = h->mass[t];
+    v.c[t] = dt * dt / (2 * m);
+    v.h[t] = dt / (2 * m);
+  }
+  return v;
 }
 
 static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
@@ -828,13 +842,14 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
     e1 = h->ev();
     cudaEventRecord(e0, h->st);
   }
-  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st);
+  const VVFactors vv = vv_factors(h, dt);
+  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st, &vv);
   if (timed) {
     cudaEventRecord(e1, h->st);
     h->force_ev.push_back({i0, i0 + 1});
   }
   h->launches += 1;
-  h->force_launches += 1;
+  if (timed) h->force_launches += 1;
   if (h->cfg.calc_globals) {
     launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->st);
     h->launches += 2;
@@ -1045,6 +1060,7 @@ int pe_destroy(pe_engine *h) {
   for (auto e : h->ev_pool) cudaEventDestroy(e);
   for (auto e : h->timer_ev)
     if (e) cudaEventDestroy(e);
+  if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
   h->pairs_acc.release();
   h->pl_list.release();
   h->pl_count.release();
@@ -1180,26 +1196,70 @@ int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, doub
   return h->cuda_check("get_state");
 }
 
+// The launches of one step after the position update: forces (+ three-body forces and the velocity half when
+// ATM is on, else the velocity half is fused into the force kernel) and the globals reduction.
+static int step_forces(pe_engine *h, double dt, const VVFactors &vv, bool timed) {
+  if (h->cfg.atm_nu > 0) {
+    // the velocity update needs the total force: pair forces, then three-body forces, then velocities
+    PE_TRY(force_eval(h, false, dt, timed));
+    PE_TRY(atm_eval(h, h->cfg.atm_nu, h->cfg.atm_cutoff));
+    DeviceState s2 = h->state();
+    if (h->nslots > 0) k_velocities<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s2, vv);
+    h->launches += 1;
+    return PE_OK;
+  }
+  return force_eval(h, true, dt, timed);
+}
+
+static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
+  if (h->step_graph) {
+    cudaGraphExecDestroy(h->step_graph);
+    h->step_graph = nullptr;
+  }
+  h->step_graph_valid = false;
+  const int64_t launches0 = h->launches;
+  const int steps0 = h->steps_since_rebuild;
+  PE_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  DeviceState s = h->state();
+  if (h->nslots > 0) k_positions<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, dt, vv);
+  h->launches += 1;
+  const int rc = step_forces(h, dt, vv, false);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(h->st, &g);
+  if (rc != PE_OK) return rc;
+  if (ce != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  const cudaError_t ie = cudaGraphInstantiate(&h->step_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+  h->step_graph_launches = (int)(h->launches - launches0);
+  h->launches = launches0;
+  h->steps_since_rebuild = steps0;
+  h->step_graph_dt = dt;
+  h->step_graph_valid = true;
+  return PE_OK;
+}
+
 int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals) {
   if (!h || nsteps < 0) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "step before pe_set_particles");
   if (!h->forces_valid) return h->fail(PE_ERR_STATE, "pe_step needs the forces of the current positions first");
   const int freq = std::max(1, h->cfg.rebuild_frequency);
+  const VVFactors vv = vv_factors(h, dt);
   for (int k = 0; k < nsteps; ++k) {
-    DeviceState s = h->state();
-    if (h->nslots > 0) k_positions<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, dt);
-    h->launches += 1;
-    if (!h->lists_valid || h->steps_since_rebuild >= freq) PE_TRY(do_rebuild(h));
-    if (h->cfg.atm_nu > 0) {
-      // the velocity update needs the total force: pair forces, then three-body forces, then velocities
-      PE_TRY(force_eval(h, false, dt, true));
-      PE_TRY(atm_eval(h, h->cfg.atm_nu, h->cfg.atm_cutoff));
-      DeviceState s2 = h->state();
-      if (h->nslots > 0) k_velocities<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s2, dt);
-      h->launches += 1;
-    } else {
-      PE_TRY(force_eval(h, true, dt, true));
+    const bool rebuild_due = !h->lists_valid || h->steps_since_rebuild >= freq;
+    if (!rebuild_due && h->cfg.use_graphs) {
+      if (!h->step_graph_valid || h->step_graph_dt != dt) PE_TRY(capture_step_graph(h, dt, vv));
+      PE_CUDA(h, cudaGraphLaunch(h->step_graph, h->st));
+      h->launches += h->step_graph_launches;
+      h->steps_since_rebuild += 1;
+      h->forces_valid = true;
+      continue;
     }
+    DeviceState s = h->state();
+    if (h->nslots > 0) k_positions<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, dt, vv);
+    h->launches += 1;
+    if (rebuild_due) PE_TRY(do_rebuild(h));
+    PE_TRY(step_forces(h, dt, vv, true));
   }
   PE_TRY(h->cuda_check("step"));
   if (globals) return read_globals(h, globals);

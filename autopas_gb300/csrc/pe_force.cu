@@ -30,6 +30,7 @@ struct ForceArgs {
   double dt;
   int fuse_velocity;
   int calc_globals;
+  VVFactors vv;
 };
 
 // Reciprocal: hardware approximation refined by one Newton-Raphson step r' = r + r(1 - x r).
@@ -182,8 +183,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
     s.fz[i] = Fz;
     if (fa.fuse_velocity) {
       // TimeDiscretization.cpp:152-164: v += (F + oldF) * (dt / (2m))
-      const double m = s.mass[ti];
-      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      const double h = fa.vv.h[ti];
       s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
@@ -285,8 +285,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
     s.fy[i] = fy;
     s.fz[i] = fz;
     if (fa.fuse_velocity) {
-      const double m = s.mass[ti];
-      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      const double h = fa.vv.h[ti];
       s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(fx, s.ofx[i]), h));
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(fz, s.ofz[i]), h));
@@ -456,8 +455,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
     s.fy[i] = Fy;
     s.fz[i] = Fz;
     if (fa.fuse_velocity) {
-      const double m = s.mass[ti];
-      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      const double h = fa.vv.h[ti];
       s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
@@ -543,8 +541,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
     s.fy[i] = fy;
     s.fz[i] = fz;
     if (fa.fuse_velocity) {
-      const double m = s.mass[ti];
-      const double h = __ddiv_rn(fa.dt, __dmul_rn(2.0, m));
+      const double h = fa.vv.h[ti];
       s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(fx, s.ofx[i]), h));
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(fz, s.ofz[i]), h));
@@ -637,8 +634,10 @@ static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, c
   }
 }
 
-void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st) {
+void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
+                  const VVFactors *vv) {
   ForceArgs fa;
+  if (vv) fa.vv = *vv;
   fa.rc2 = s.cutoff * s.cutoff;
   fa.rc2f = (float)fa.rc2;
   fa.dt = dt;

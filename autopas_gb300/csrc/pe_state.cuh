@@ -92,7 +92,7 @@ void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, con
 
 // forces (pe_force.cu)
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt,
-                  cudaStream_t st);
+                  cudaStream_t st, const VVFactors *vv = nullptr);
 constexpr int kChunk = 4096;  // clusters per globals-reduction chunk
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
                            double *cpart, cudaStream_t st);

@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
+    p.add_argument("--workload", default="slab", choices=["slab", "ensemble"],
+                   help="slab: the headline 2M-particle system; ensemble: 512 independent systems in one engine")
+    p.add_argument("--systems", type=int, default=512)
     return p.parse_args()
 
 
@@ -382,10 +385,71 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------------------------- ensemble
+def run_ensemble(args):
+    """512 independent periodic LJ systems (sizes log-uniform in 500-50,000, densities 0.3-0.9, T* 0.7-1.5,
+    rc 2.5, skin 0.3, rebuild every 10) stepped together by one engine with CUDA-graph replay, against the same
+    systems run one engine at a time in the FP64 form (a sample of systems spanning the size range)."""
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    from autopas_gb300 import engine as E, workloads
+    rc, skin, reb = 2.5, 0.3, 10
+    systems = workloads.ensemble(args.systems, seed=11)
+    boxes = [(s_["bmin"], s_["bmax"]) for s_ in systems]
+    pos = np.concatenate([s_["pos"] for s_ in systems])
+    vel = np.concatenate([s_["vel"] for s_ in systems])
+    sysid = np.concatenate([np.full(len(s_["pos"]), k, np.int32) for k, s_ in enumerate(systems)])
+    e = E.PairEngine(rc, skin, boxes, periodic=True, precision=E.PRECISION_MIXED, cluster_size=0, traversal=-1,
+                     rebuild_frequency=reb, use_graphs=True)
+    e.set_particles(pos, vel, system=sysid)
+    e.compute_forces()
+    tuning = e.tuning()
+    e.step(0.002, args.warmup, want_globals=False)
+    e.stats(reset=True)
+    e.timer_start()
+    e.step(0.002, args.steps, want_globals=True)
+    ms = e.timer_stop()
+    st = e.stats(reset=True)
+    value = st["pairs_total"] / (ms * 1e-3)
+    # one at a time, FP64 form, on a sample of 8 systems spread over the size range
+    order = np.argsort([len(s_["pos"]) for s_ in systems])
+    sample = order[np.linspace(0, len(order) - 1, 8).astype(int)]
+    pairs1 = 0
+    ms1 = 0.0
+    for k in sample:
+        s_ = systems[k]
+        e1 = E.PairEngine(rc, skin, (s_["bmin"], s_["bmax"]), periodic=True, precision=E.PRECISION_FP64,
+                          cluster_size=8, traversal=1, rebuild_frequency=reb, use_graphs=False)
+        e1.set_particles(s_["pos"], s_["vel"])
+        e1.compute_forces()
+        e1.stats(reset=True)
+        e1.timer_start()
+        e1.step(0.002, 10, want_globals=True)
+        ms1 += e1.timer_stop()
+        pairs1 += e1.stats(reset=True)["pairs_total"]
+        e1.close()
+    one = pairs1 / (ms1 * 1e-3)
+    line = {"metric": "pair interactions/s, batched ensemble (FP32-mixed, one engine, CUDA graph) vs one-at-a-time FP64",
+            "value": value, "unit": "pair interactions/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 LJ arithmetic on f64 state", "data": "synthetic",
+            "config": {"workload": f"{len(systems)} periodic LJ systems, sizes log-uniform 500-50,000 "
+                                   f"({len(pos)} particles), densities U(0.3,0.9), T* U(0.7,1.5), rc {rc}, skin {skin}, "
+                                   f"rebuild every {reb}", "particles": int(len(pos)), "systems": len(systems)},
+            "one_at_a_time_fp64": {"value": one, "unit": "pair interactions/s",
+                                   "sample": "8 systems spanning the size range, each in its own engine, 10 steps"},
+            "speedup_vs_one_at_a_time_fp64": value / one, "tuning": tuning, "gpu_launches": st["kernel_launches"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
     return run_ours(args)
 
 

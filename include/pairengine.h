@@ -86,6 +86,8 @@ typedef struct {
                               faster */
   double atm_nu;           /* > 0: pe_step adds Axilrod-Teller-Muto three-body forces with this nu */
   double atm_cutoff;       /* triplet cutoff for ATM (all three distances); <= cutoff + skin */
+  int use_graphs;          /* 1: pe_step captures the launches of a step without list rebuild into a CUDA graph
+                              once per rebuild and replays it; 0: every step is launched kernel by kernel */
 } pe_config;
 
 /* One particle system of the ensemble. */
@@ -177,9 +179,10 @@ int pe_get_tower_grid(pe_engine *h, int system, double *side, int64_t *num, int6
  * Writes up to cap entries and returns the total count in *count. */
 int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code, int64_t *count);
 
-/* Counters of the engine since the last reset: CUDA-event time of the force kernels (recorded on the engine's
- * stream around every force launch), launches of the engine's own kernels, interacting pairs summed over all
- * force evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds. */
+/* Counters of the engine since the last reset: CUDA-event time of the force kernels launched outside CUDA
+ * graphs (force_ms) and the number of launches it covers (force_launches), launches of the engine's own
+ * kernels including those inside graph replays (kernel_launches), interacting pairs summed over all force
+ * evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds. */
 typedef struct {
   double force_ms;
   int64_t force_launches;
