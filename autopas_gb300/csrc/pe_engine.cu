@@ -666,10 +666,10 @@ static int ensure_particle_capacity(pe_engine *h) {
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
   if (!h->cl_bb.ensure(6 * ncl) || !h->cl_z.ensure(ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
-      !h->cp_count.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(4 * ncl) ||
+      !h->cp_count.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(kGlob * ncl) ||
       !h->cl_hits.ensure(ncl) || !h->key.ensure(n) || !h->skey.ensure(n) || !h->tower_of.ensure(n) ||
       !h->sval.ensure(n) || !h->perm_src.ensure(n) || !h->cp_total.ensure(1) || !h->derr.ensure(1) ||
-      !h->dmax.ensure(1) || !h->sys_glob.ensure(5 * h->sys.size()) || !h->sys_hits.ensure(h->sys.size()) ||
+      !h->dmax.ensure(1) || !h->sys_glob.ensure(kSysGlob * h->sys.size()) || !h->sys_hits.ensure(h->sys.size()) ||
       !h->sys_cl_range.ensure(2 * h->sys.size()))
     return h->fail(PE_ERR_OOM, "cluster arrays");
   return PE_OK;
@@ -807,7 +807,7 @@ static int do_rebuild(pe_engine *h) {
     c0[ns] = k;
     h->nchunks = k;
     if (!h->chunks.ensure(std::max<size_t>(ch.size(), 3)) || !h->sys_chunk0.ensure(ns + 1) ||
-        !h->chunk_part.ensure(5 * (size_t)std::max(k, 1)))
+        !h->chunk_part.ensure((kGlob + 1) * (size_t)std::max(k, 1)))
       return h->fail(PE_ERR_OOM, "reduction chunks");
     if (!ch.empty())
       PE_CUDA(h, cudaMemcpyAsync(h->chunks.p, ch.data(), sizeof(int64_t) * ch.size(), cudaMemcpyHostToDevice, st));
@@ -874,19 +874,21 @@ static int atm_eval(pe_engine *h, double nu, double cutoff3) {
 static int read_globals(pe_engine *h, pe_globals *g) {
   if (!g) return PE_OK;
   const int ns = (int)h->sys.size();
-  std::vector<double> v(5 * ns);
+  std::vector<double> v(kSysGlob * ns);
   std::vector<long long> hits(ns);
   if (h->cfg.calc_globals) {
-    PE_CUDA(h, cudaMemcpyAsync(v.data(), h->sys_glob.p, sizeof(double) * 5 * ns, cudaMemcpyDeviceToHost, h->st));
+    PE_CUDA(h, cudaMemcpyAsync(v.data(), h->sys_glob.p, sizeof(double) * kSysGlob * ns, cudaMemcpyDeviceToHost,
+                               h->st));
     PE_CUDA(h, cudaMemcpyAsync(hits.data(), h->sys_hits.p, sizeof(long long) * ns, cudaMemcpyDeviceToHost, h->st));
   }
   PE_CUDA(h, cudaStreamSynchronize(h->st));
   for (int q = 0; q < ns; ++q) {
-    g[q].upot = v[5 * q];
-    g[q].virial = v[5 * q + 1];
-    g[q].virial_xyz[0] = v[5 * q + 2];
-    g[q].virial_xyz[1] = v[5 * q + 3];
-    g[q].virial_xyz[2] = v[5 * q + 4];
+    g[q].upot = v[kSysGlob * q];
+    g[q].virial = v[kSysGlob * q + 1];
+    g[q].virial_xyz[0] = v[kSysGlob * q + 2];
+    g[q].virial_xyz[1] = v[kSysGlob * q + 3];
+    g[q].virial_xyz[2] = v[kSysGlob * q + 4];
+    g[q].ekin = v[kSysGlob * q + 5];
     g[q].num_pairs = h->cfg.calc_globals ? hits[q] : -1;
   }
   return PE_OK;
@@ -1288,6 +1290,7 @@ int pe_compute_atm(pe_engine *h, double nu, double cutoff3, pe_globals *globals)
       globals[q].upot = v[3 * q];
       globals[q].virial = v[3 * q + 1];
       globals[q].virial_xyz[0] = globals[q].virial_xyz[1] = globals[q].virial_xyz[2] = 0;
+      globals[q].ekin = 0;
       globals[q].num_pairs = (int64_t)(v[3 * q + 2] + 0.5) / 3;
     }
   return PE_OK;

@@ -48,6 +48,12 @@ __device__ __forceinline__ void kahan_add(float &sum, float &c, float v) {
   sum = t;
 }
 
+// kinetic energy 0.5 m v^2 of slot i (FP64)
+__device__ __forceinline__ double kinetic(const DeviceState &s, int64_t i, int ti) {
+  const double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+  return 0.5 * s.mass[ti] * (vx * vx + vy * vy + vz * vz);
+}
+
 // exact FP64 cutoff test of pair (i, image of j with shift code) -- used near the cutoff only
 __device__ __forceinline__ bool exact_within(const DeviceState &s, const SysDev &S, int64_t i, int64_t j, int code,
                                           double rc2) {
@@ -177,6 +183,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
     Fy += __shfl_xor_sync(0xffffffffu, Fy, o);
     Fz += __shfl_xor_sync(0xffffffffu, Fz, o);
   }
+  double ek = 0.0;
   if (jl == 0 && oi == 1) {
     s.fx[i] = Fx;
     s.fy[i] = Fy;
@@ -188,6 +195,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
     }
+    if (GLOB) ek = kinetic(s, i, ti);
   }
   if (GLOB) {
     const bool owned = oi == 1;  // energyFactor of the non-newton3 functor call
@@ -201,13 +209,15 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
       g1 += __shfl_xor_sync(0xffffffffu, g1, o);
       g2 += __shfl_xor_sync(0xffffffffu, g2, o);
       g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      ek += __shfl_xor_sync(0xffffffffu, ek, o);
       h += __shfl_xor_sync(0xffffffffu, h, o);
     }
     if (lane == 0) {
-      s.cl_glob[4 * A + 0] = g0;
-      s.cl_glob[4 * A + 1] = g1;
-      s.cl_glob[4 * A + 2] = g2;
-      s.cl_glob[4 * A + 3] = g3;
+      s.cl_glob[kGlob * A + 0] = g0;
+      s.cl_glob[kGlob * A + 1] = g1;
+      s.cl_glob[kGlob * A + 2] = g2;
+      s.cl_glob[kGlob * A + 3] = g3;
+      s.cl_glob[kGlob * A + 4] = ek;
       s.cl_hits[A] = (unsigned long long)h;
     }
   }
@@ -280,6 +290,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
     fy += __shfl_xor_sync(0xffffffffu, fy, o);
     fz += __shfl_xor_sync(0xffffffffu, fz, o);
   }
+  double ek = 0.0;
   if (jl == 0 && oi == 1) {
     s.fx[i] = fx;
     s.fy[i] = fy;
@@ -290,6 +301,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(fz, s.ofz[i]), h));
     }
+    if (GLOB) ek = kinetic(s, i, ti);
   }
   if (GLOB) {
     const double own_i = oi == 1 ? 1.0 : 0.0;
@@ -301,13 +313,15 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
       g1 += __shfl_xor_sync(0xffffffffu, g1, o);
       g2 += __shfl_xor_sync(0xffffffffu, g2, o);
       g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      ek += __shfl_xor_sync(0xffffffffu, ek, o);
       h += __shfl_xor_sync(0xffffffffu, h, o);
     }
     if (lane == 0) {
-      s.cl_glob[4 * A + 0] = g0;
-      s.cl_glob[4 * A + 1] = g1;
-      s.cl_glob[4 * A + 2] = g2;
-      s.cl_glob[4 * A + 3] = g3;
+      s.cl_glob[kGlob * A + 0] = g0;
+      s.cl_glob[kGlob * A + 1] = g1;
+      s.cl_glob[kGlob * A + 2] = g2;
+      s.cl_glob[kGlob * A + 3] = g3;
+      s.cl_glob[kGlob * A + 4] = ek;
       s.cl_hits[A] = (unsigned long long)h;
     }
   }
@@ -450,6 +464,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
   acc.flush();
   const double Fx = (double)acc.fxs - (double)acc.fxc, Fy = (double)acc.fys - (double)acc.fyc,
                Fz = (double)acc.fzs - (double)acc.fzc;
+  double ek = 0.0;
   if (oi == 1) {
     s.fx[i] = Fx;
     s.fy[i] = Fy;
@@ -460,6 +475,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
     }
+    if (GLOB) ek = kinetic(s, i, ti);
   }
   if (GLOB) {
     const bool owned = oi == 1;
@@ -472,14 +488,16 @@ __global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs
       g1 += __shfl_xor_sync(0xffffffffu, g1, o);
       g2 += __shfl_xor_sync(0xffffffffu, g2, o);
       g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      ek += __shfl_xor_sync(0xffffffffu, ek, o);
       h += __shfl_xor_sync(0xffffffffu, h, o);
     }
     if (inrange && (i % C) == 0) {
       const int64_t cl = i / C;
-      s.cl_glob[4 * cl + 0] = g0;
-      s.cl_glob[4 * cl + 1] = g1;
-      s.cl_glob[4 * cl + 2] = g2;
-      s.cl_glob[4 * cl + 3] = g3;
+      s.cl_glob[kGlob * cl + 0] = g0;
+      s.cl_glob[kGlob * cl + 1] = g1;
+      s.cl_glob[kGlob * cl + 2] = g2;
+      s.cl_glob[kGlob * cl + 3] = g3;
+      s.cl_glob[kGlob * cl + 4] = ek;
       s.cl_hits[cl] = (unsigned long long)h;
     }
   }
@@ -536,6 +554,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
       hits2 += mask ? (s.own[j] == 1 ? 1 : 2) : 0;
     }
   }
+  double ek = 0.0;
   if (oi == 1) {
     s.fx[i] = fx;
     s.fy[i] = fy;
@@ -546,6 +565,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
       s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(fy, s.ofy[i]), h));
       s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(fz, s.ofz[i]), h));
     }
+    if (GLOB) ek = kinetic(s, i, ti);
   }
   if (GLOB) {
     const bool owned = oi == 1;
@@ -557,14 +577,16 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
       g1 += __shfl_xor_sync(0xffffffffu, g1, o);
       g2 += __shfl_xor_sync(0xffffffffu, g2, o);
       g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      ek += __shfl_xor_sync(0xffffffffu, ek, o);
       h += __shfl_xor_sync(0xffffffffu, h, o);
     }
     if (inrange && (i % C) == 0) {
       const int64_t cl = i / C;
-      s.cl_glob[4 * cl + 0] = g0;
-      s.cl_glob[4 * cl + 1] = g1;
-      s.cl_glob[4 * cl + 2] = g2;
-      s.cl_glob[4 * cl + 3] = g3;
+      s.cl_glob[kGlob * cl + 0] = g0;
+      s.cl_glob[kGlob * cl + 1] = g1;
+      s.cl_glob[kGlob * cl + 2] = g2;
+      s.cl_glob[kGlob * cl + 3] = g3;
+      s.cl_glob[kGlob * cl + 4] = ek;
       s.cl_hits[cl] = (unsigned long long)h;
     }
   }
@@ -657,47 +679,48 @@ void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_vel
 // ---------------------------------------------------------------------------------------------
 __global__ void k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, double *__restrict__ cpart) {
   const int64_t c0 = chunks[3 * blockIdx.x + 1], c1 = chunks[3 * blockIdx.x + 2];
-  double g[4] = {0, 0, 0, 0};
+  double g[kGlob] = {0, 0, 0, 0, 0};
   long long h = 0;
   for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) g[q] += s.cl_glob[4 * c + q];
+    for (int q = 0; q < kGlob; ++q) g[q] += s.cl_glob[kGlob * c + q];
     h += (long long)s.cl_hits[c];
   }
-  __shared__ double red[4][256];
+  __shared__ double red[kGlob][256];
   __shared__ long long redh[256];
-  for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = g[q];
+  for (int q = 0; q < kGlob; ++q) red[q][threadIdx.x] = g[q];
   redh[threadIdx.x] = h;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
-      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+      for (int q = 0; q < kGlob; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
       redh[threadIdx.x] += redh[threadIdx.x + o];
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    for (int q = 0; q < 4; ++q) cpart[5 * blockIdx.x + q] = red[q][0];
-    cpart[5 * blockIdx.x + 4] = (double)redh[0];
+    for (int q = 0; q < kGlob; ++q) cpart[(kGlob + 1) * blockIdx.x + q] = red[q][0];
+    cpart[(kGlob + 1) * blockIdx.x + kGlob] = (double)redh[0];
   }
 }
 
 __global__ void k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0, const double *__restrict__ cpart) {
   const int sy = blockIdx.x * blockDim.x + threadIdx.x;
   if (sy >= s.nsys) return;
-  double g[4] = {0, 0, 0, 0};
+  double g[kGlob] = {0, 0, 0, 0, 0};
   double h = 0;
   for (int k = sys_chunk0[sy]; k < sys_chunk0[sy + 1]; ++k) {
-    for (int q = 0; q < 4; ++q) g[q] += cpart[5 * k + q];
-    h += cpart[5 * k + 4];
+    for (int q = 0; q < kGlob; ++q) g[q] += cpart[(kGlob + 1) * k + q];
+    h += cpart[(kGlob + 1) * k + kGlob];
   }
   const double up = g[0] * 0.5 / 6.;
   const double vx = g[1] * 0.5, vy = g[2] * 0.5, vz = g[3] * 0.5;
-  s.sys_glob[5 * sy + 0] = up;
-  s.sys_glob[5 * sy + 1] = vx + vy + vz;
-  s.sys_glob[5 * sy + 2] = vx;
-  s.sys_glob[5 * sy + 3] = vy;
-  s.sys_glob[5 * sy + 4] = vz;
+  s.sys_glob[kSysGlob * sy + 0] = up;
+  s.sys_glob[kSysGlob * sy + 1] = vx + vy + vz;
+  s.sys_glob[kSysGlob * sy + 2] = vx;
+  s.sys_glob[kSysGlob * sy + 3] = vy;
+  s.sys_glob[kSysGlob * sy + 4] = vz;
+  s.sys_glob[kSysGlob * sy + 5] = g[4];
   const long long pairs = (long long)(h + 0.5) / 2;
   s.sys_hits[sy] = pairs;
   atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)pairs);

@@ -61,7 +61,7 @@ struct DeviceState {
   int ntypes = 1;                  // host copy of types->ntypes
 
   // ---- globals ----
-  double *cl_glob = nullptr;       // [nclusters*4]: 6*Upot, virial x,y,z partials (post energy factor)
+  double *cl_glob = nullptr;       // [nclusters*kGlob]: 6*Upot, virial x,y,z (post energy factor), kinetic
   unsigned long long *cl_hits = nullptr;  // [nclusters] interacting-pair counts (x2 for full lists)
   double *sys_glob = nullptr;      // [nsys*5]
   long long *sys_hits = nullptr;   // [nsys]
@@ -94,6 +94,8 @@ void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, con
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt,
                   cudaStream_t st, const VVFactors *vv = nullptr);
 constexpr int kChunk = 4096;  // clusters per globals-reduction chunk
+constexpr int kGlob = 5;      // per-cluster partials: 6*Upot, virial x, y, z, kinetic energy
+constexpr int kSysGlob = 6;   // per system: Upot, virial, virial x, y, z, kinetic energy
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
                            double *cpart, cudaStream_t st);
 

@@ -49,7 +49,7 @@ class PeSystem(C.Structure):
 
 class PeGlobals(C.Structure):
     _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("virial_xyz", C.c_double * 3),
-                ("num_pairs", C.c_int64)]
+                ("num_pairs", C.c_int64), ("ekin", C.c_double)]
 
 
 class PeStats(C.Structure):
@@ -307,5 +307,5 @@ def lj_forces_noalloc(cfg, n, x, y, z, type_ptr, own_ptr, fx, fy, fz, globals_pt
 
 
 def _globals(g):
-    return [{"upot": x.upot, "virial": x.virial, "virial_xyz": tuple(x.virial_xyz), "num_pairs": x.num_pairs}
-            for x in g]
+    return [{"upot": x.upot, "virial": x.virial, "virial_xyz": tuple(x.virial_xyz), "num_pairs": x.num_pairs,
+             "ekin": x.ekin} for x in g]

@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
-    p.add_argument("--workload", default="slab", choices=["slab", "ensemble"],
+    p.add_argument("--workload", default="slab", choices=["slab", "ensemble", "drift"],
                    help="slab: the headline 2M-particle system; ensemble: 512 independent systems in one engine")
     p.add_argument("--systems", type=int, default=512)
     return p.parse_args()
@@ -456,8 +456,49 @@ def run_ensemble(args):
     return 0
 
 
+# ---------------------------------------------------------------------------------------------- energy drift
+def run_drift(args):
+    """Energy drift of the FP32-mixed and FP64 forms over --steps steps (default 10^4) on the FCC case:
+    20^3 unit cells (32,000 particles), density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, rebuild every 10."""
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    from autopas_gb300 import engine as E, workloads
+    pos, vel, bmin, bmax = workloads.fcc_lj(20, 0.8442, 0.72, seed=1)
+    nsteps = args.steps if args.steps >= 1000 else 10000
+    out = {}
+    for name, prec in (("fp64", E.PRECISION_FP64), ("mixed", E.PRECISION_MIXED)):
+        e = E.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10)
+        e.set_particles(pos, vel)
+        g = e.compute_forces()[0]
+        E0 = g["upot"] + g["ekin"]
+        series = []
+        t0 = time.perf_counter()
+        for _ in range(nsteps // 100):
+            g = e.step(0.002, 100)[0]
+            series.append(g["upot"] + g["ekin"])
+        wall = time.perf_counter() - t0
+        s_ = np.array(series)
+        slope = np.polyfit(np.arange(1, len(s_) + 1) * 100 * 0.002, s_ / len(pos), 1)[0]
+        out[name] = {"E0_per_particle": E0 / len(pos), "drift_rel": float((s_[-1] - E0) / abs(E0)),
+                     "max_dev_rel": float(np.abs(s_ - E0).max() / abs(E0)),
+                     "slope_per_particle_per_time": float(slope), "steps": nsteps,
+                     "steps_per_s": nsteps / wall}
+        e.close()
+    line = {"metric": "energy drift over MD steps, FP32-mixed vs FP64 (32,000-particle FCC LJ)",
+            "value": out["mixed"]["drift_rel"], "unit": "relative total-energy change", "n_gpus": 1,
+            "steps": nsteps, "warmup": 0, "higher_is_better": False, "data": "synthetic",
+            "config": {"workload": "FCC 20^3 unit cells, density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, "
+                                   "rebuild every 10, truncated LJ"},
+            "mixed": out["mixed"], "fp64": out["fp64"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "drift" and args.impl != "reference":
+        return run_drift(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "ensemble":

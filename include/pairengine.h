@@ -105,6 +105,7 @@ typedef struct {
   double virial;       /* sum of the three components, as LJFunctor::getVirial returns */
   double virial_xyz[3];
   int64_t num_pairs;   /* interacting pairs (dr2 <= rc^2), each unordered pair once; -1 if not counted */
+  double ekin;         /* kinetic energy sum 0.5 m v^2 of the owned particles (after the step's velocity update) */
 } pe_globals;
 
 /* Replaces: constructing the container + functor (ContainerSelector.h:38-113, LJFunctor constructors). */

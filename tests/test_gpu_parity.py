@@ -355,3 +355,33 @@ def test_graph_replay_matches_eager_steps(eng_mod):
     for a, b in zip(out[0][:3], out[1][:3]):
         assert np.array_equal(a, b)
     assert out[0][3] == out[1][3]
+
+
+def test_fcc_32000_trajectory_matches_oracle(eng_mod, orc):
+    """Full-size FCC case: 20^3 unit cells (32,000 particles) at density 0.8442, T* 0.72, rc 2.5, skin 0.3,
+    velocity Verlet dt 0.002 for 100 steps with a rebuild every 10.  The FP64 form follows the oracle's
+    md-flexible trajectory to 1e-9 (positions) and the mixed form conserves energy as well as FP64 does."""
+    from autopas_gb300 import workloads
+    pos, vel, bmin, bmax = workloads.fcc_lj(20, 0.8442, 0.72, seed=1)
+    rc, skin, dt, nsteps = 2.5, 0.3, 0.002, 100
+    rp, rv, rf, en = orc.md_run(pos, vel, None, [1.0], bmin, bmax, skin, orc.LJ(rc), dt, nsteps)
+    res = {}
+    for prec in (eng_mod.PRECISION_FP64, eng_mod.PRECISION_MIXED):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10)
+        e.set_particles(pos, vel)
+        g0 = e.compute_forces()[0]
+        g = e.step(dt, nsteps)[0]
+        P, V = e.state()
+        res[prec] = (P, V, g0, g)
+    P, V, g0, g = res[eng_mod.PRECISION_FP64]
+    d = P - rp
+    d -= (bmax - bmin) * np.round(d / (bmax - bmin))
+    assert np.abs(d).max() < 1e-9
+    assert np.abs(V - rv).max() < 1e-8
+    assert g["upot"] == pytest.approx(en[-1, 0], rel=1e-10)
+    assert g["ekin"] == pytest.approx(en[-1, 1], rel=1e-10)
+    e0_ref = res[eng_mod.PRECISION_FP64][2]["upot"] + 0.5 * float((vel ** 2).sum())
+    drift64 = abs(g["upot"] + g["ekin"] - e0_ref)
+    gm = res[eng_mod.PRECISION_MIXED][3]
+    driftm = abs(gm["upot"] + gm["ekin"] - e0_ref)
+    assert driftm <= max(2 * drift64, 1e-6 * abs(e0_ref))
