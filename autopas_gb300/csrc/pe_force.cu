@@ -402,8 +402,9 @@ struct MixedAcc {
   }
 };
 
-template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL>
-__global__ void __launch_bounds__(128) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
+// MINB: minimum resident blocks per SM requested from the compiler (caps registers for more warps in flight)
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
   const int T = s.ntypes;
   if (!ONE_TYPE) {
@@ -603,14 +604,23 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
       k_lj_fp64_plist<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     return;
   }
-  // kernel variant (loads batched per 2 or 4 list entries), chosen by the engine's tuner
-  const bool u4 = s.variant == 1;
+  // kernel variants, chosen by the engine's tuner: list loads batched per 1, 2 or 4 entries under register
+  // caps of 64 (8 blocks of 128 threads per SM), 85 (6 blocks), 40 (12 blocks) or 51 (10 blocks)
 #define PE_PLIST(G, O)                                                                   \
   do {                                                                                   \
-    if (u4)                                                                              \
-      k_lj_mixed_plist<C, G, O, true, 4><<<(unsigned)nb, 128, 0, st>>>(s, fa);           \
-    else                                                                                 \
-      k_lj_mixed_plist<C, G, O, true, 2><<<(unsigned)nb, 128, 0, st>>>(s, fa);           \
+    switch (s.variant) {                                                                 \
+      case 1:                                                                            \
+        k_lj_mixed_plist<C, G, O, true, 4, 6><<<(unsigned)nb, 128, 0, st>>>(s, fa);      \
+        break;                                                                           \
+      case 2:                                                                            \
+        k_lj_mixed_plist<C, G, O, true, 2, 12><<<(unsigned)nb, 128, 0, st>>>(s, fa);     \
+        break;                                                                           \
+      case 3:                                                                            \
+        k_lj_mixed_plist<C, G, O, true, 1, 10><<<(unsigned)nb, 128, 0, st>>>(s, fa);     \
+        break;                                                                           \
+      default:                                                                           \
+        k_lj_mixed_plist<C, G, O, true, 2, 8><<<(unsigned)nb, 128, 0, st>>>(s, fa);      \
+    }                                                                                    \
   } while (0)
   if (s.ntypes == 1) {
     if (fa.calc_globals)
