@@ -274,8 +274,12 @@ def test_tuner_full_search_keeps_results(eng_mod, orc):
     e.set_particles(pos, vel)
     g = e.compute_forces()[0]
     tun = e.tuning()
-    assert len(tun["candidates"]) == 6
-    assert 0 <= tun["chosen"] < 6
+    cands = tun["candidates"]
+    # cluster sizes 4 and 8, each with the cluster-pair traversal and every particle-list kernel variant
+    assert {c["cluster_size"] for c in cands} == {4, 8}
+    assert {c["traversal"] for c in cands} == {0, 1}
+    assert len(cands) == 2 * (1 + len({c["variant"] for c in cands if c["traversal"] == 1}))
+    assert 0 <= tun["chosen"] < len(cands)
     best = tun["candidates"][tun["chosen"]]
     assert best["ms"] == min(c["ms"] for c in tun["candidates"])
     info = e.info()
