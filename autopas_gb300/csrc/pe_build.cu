@@ -13,6 +13,7 @@
 // Every pass is a streaming pass over HBM except the on-chip bitonic sort of each tower.
 #include "pe_state.cuh"
 
+#include <algorithm>
 #include <cstdio>
 
 namespace pe {
@@ -512,6 +513,98 @@ void launch_plist_build(DeviceState &s, cudaStream_t st) {
     k_plist_build<4><<<(unsigned)nb, 128, 0, st>>>(s, L2f);
   else
     k_plist_build<8><<<(unsigned)nb, 128, 0, st>>>(s, L2f);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 7. rolling pruning (the inner lists the force kernels read)
+//    Invariant: every pair within rc at a force evaluation is in the inner list.  It holds because (a) the
+//    inner list holds every pair within rc + b at the last prune, b the prune buffer, and (b) no particle has
+//    moved b/2 since then (otherwise the prune kernel refreshes the inner list first).  (a) needs the outer
+//    list to hold every pair within rc + b at the prune, which is the case while no particle has moved
+//    (skin - b)/2 since the rebuild; beyond that the prune copies the whole outer list (radius rc + skin), so
+//    the guarantee falls back to the reference's own skin contract.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_prune_reset_refs(DeviceState s) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i == 0) {
+    s.disp_bits[0] = 0x7f800000u;  // +inf: the next prune check fires
+    s.disp_bits[1] = 0u;
+  }
+  if (i >= s.nslots) return;
+  const double x = s.x[i], y = s.y[i], z = s.z[i];
+  s.x_prune[3 * i] = x;
+  s.x_prune[3 * i + 1] = y;
+  s.x_prune[3 * i + 2] = z;
+  s.x_reb[3 * i] = x;
+  s.x_reb[3 * i + 1] = y;
+  s.x_reb[3 * i + 2] = z;
+}
+
+void launch_prune_reset_refs(DeviceState &s, cudaStream_t st) {
+  const int64_t nb = (std::max<int64_t>(s.nslots, 1) + 255) / 256;
+  k_prune_reset_refs<<<(unsigned)nb, 256, 0, st>>>(s);
+}
+
+__global__ void k_displacement(DeviceState s) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool in = i < s.nslots;
+  track_displacement(s, in ? i : 0, in && s.own[i] != 0);
+}
+
+void launch_displacement(DeviceState &s, cudaStream_t st) {
+  const int64_t nb = (std::max<int64_t>(s.nslots, 1) + 255) / 256;
+  k_displacement<<<(unsigned)nb, 256, 0, st>>>(s);
+}
+
+__global__ void __launch_bounds__(128) k_prune(DeviceState s) {
+  if (s.disp_bits[0] < f2bits(s.prune_half2)) return;  // nobody moved half the buffer: nothing to do
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.nslots) return;
+  if (s.own[i] != 1) {
+    s.pi_count[i] = 0;
+    return;
+  }
+  // whole outer list when particles have used up the skin beyond the buffer since the rebuild
+  const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
+  const SysDev &S = s.sysd[s.sys[i]];
+  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const int n = min(s.pl_count[i], s.pl_cap);
+  int m = 0;
+  for (int k = 0; k < n; ++k) {
+    const uint32_t ent = __ldg(s.pl_list + (int64_t)k * s.pl_stride + i);
+    const int64_t j = ent >> 5;
+    const int code = ent & 31;
+    const float4 hj = __ldg(&s.pk_hi[j]), lj = __ldg(&s.pk_lo[j]);
+    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+    if (code != kShiftNone) {
+      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      xh = fmaf(-sxf, S.len_hi[0], xh);
+      yh = fmaf(-syf, S.len_hi[1], yh);
+      zh = fmaf(-szf, S.len_hi[2], zh);
+      xl = fmaf(-sxf, S.len_lo[0], xl);
+      yl = fmaf(-syf, S.len_lo[1], yl);
+      zl = fmaf(-szf, S.len_lo[2], zl);
+    }
+    const float dx = (xh - hj.x) + (xl - lj.x);
+    const float dy = (yh - hj.y) + (yl - lj.y);
+    const float dz = (zh - hj.z) + (zl - lj.z);
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    if (r2 <= lim) s.pi_list[(int64_t)(m++) * s.pl_stride + i] = ent;
+  }
+  s.pi_count[i] = m;
+  s.x_prune[3 * i] = s.x[i];
+  s.x_prune[3 * i + 1] = s.y[i];
+  s.x_prune[3 * i + 2] = s.z[i];
+}
+
+__global__ void k_prune_clear(DeviceState s) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && s.disp_bits[0] >= f2bits(s.prune_half2)) s.disp_bits[0] = 0u;
+}
+
+void launch_prune(DeviceState &s, cudaStream_t st) {
+  const int64_t nb = (std::max<int64_t>(s.nslots, 1) + 127) / 128;
+  k_prune<<<(unsigned)nb, 128, 0, st>>>(s);
+  k_prune_clear<<<1, 32, 0, st>>>(s);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -135,6 +135,10 @@ struct pe_engine {
   int pl_cap = 0;
   int64_t pl_entries = 0;
   bool need_plist = false;       // particle lists needed besides the force traversal (three-body forces)
+  DBuf<uint32_t> pi_list;        // pruned inner lists
+  DBuf<int32_t> pi_count;
+  DBuf<double> x_prune, x_reb;
+  DBuf<unsigned int> disp_bits;
   DBuf<double> atm_slot, atm_out;
   DBuf<int> atm_err;
 
@@ -204,6 +208,22 @@ struct pe_engine {
     s.pl_cap = pl_cap;
     s.pl_stride = pcap;
     s.pl_max = pl_max.p;
+    s.prune = (cfg.prune_buffer > 0 && traversal == 1) ? 1 : 0;
+    s.pi_list = pi_list.p;
+    s.pi_count = pi_count.p;
+    s.x_prune = x_prune.p;
+    s.x_reb = x_reb.p;
+    s.disp_bits = disp_bits.p;
+    s.fl_list = s.prune ? pi_list.p : pl_list.p;
+    s.fl_count = s.prune ? pi_count.p : pl_count.p;
+    {
+      const double b = cfg.prune_buffer, rc = cfg.cutoff, sk = cfg.skin;
+      s.prune_half2 = (float)(0.25 * b * b * (1.0 - 1e-6));
+      const double lim = 0.5 * (sk - b);
+      s.reb_limit2 = lim > 0 ? (float)(lim * lim * (1.0 - 1e-6)) : 0.f;
+      s.r_in2f = (float)((rc + b) * (rc + b) * (1.0 + 1e-5));
+      s.r_out2f = (float)((rc + sk) * (rc + sk) * (1.0 + 1e-5));
+    }
     s.sysd = sysd.p;
     s.types = types.p;
     s.mass = dmass.p;
@@ -434,7 +454,10 @@ __global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int3
 // velocity-Verlet position half (TimeDiscretization.cpp:17-66 with globalForce 0) fused with the re-encode
 __global__ void k_positions(DeviceState s, double dt, VVFactors vv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= s.nslots) return;
+  if (i >= s.nslots) {
+    if (s.prune) track_displacement(s, 0, false);
+    return;
+  }
   if (s.own[i] == 1) {
     const double c = vv.c[s.type[i]];
     const double fx = s.fx[i], fy = s.fy[i], fz = s.fz[i];
@@ -450,6 +473,7 @@ __global__ void k_positions(DeviceState s, double dt, VVFactors vv) {
     s.fz[i] = 0;
   }
   pack_one(s, i);
+  if (s.prune) track_displacement(s, i, s.own[i] != 0);
 }
 
 // velocity half when it is not fused into the force kernel
@@ -701,6 +725,17 @@ static int build_particle_lists(pe_engine *h) {
     PE_TRY(h->cuda_check("particle list build"));
     if (mx <= h->pl_cap) {
       h->pl_entries = 0;
+      if (h->cfg.prune_buffer > 0 && h->traversal == 1) {
+        const size_t cap = (size_t)h->pl_cap * (size_t)h->pcap;
+        if (!h->pi_list.ensure(cap) || !h->pi_count.ensure((size_t)h->pcap) || !h->x_prune.ensure(3 * (size_t)h->pcap) ||
+            !h->x_reb.ensure(3 * (size_t)h->pcap) || !h->disp_bits.ensure(2))
+          return h->fail(PE_ERR_OOM, "pruned lists");
+        DeviceState s2 = h->state();
+        launch_prune_reset_refs(s2, st);
+        launch_prune(s2, st);
+        h->launches += 3;
+        PE_TRY(h->cuda_check("prune"));
+      }
       return PE_OK;
     }
     h->pl_cap = (int)(mx * 1.2) + 8;
@@ -821,6 +856,8 @@ static int do_rebuild(pe_engine *h) {
   h->step_graph_valid = false;  // sizes and buffers may have changed
   return PE_OK;
 }
+
+static bool pruning(const pe_engine *h) { return h->cfg.prune_buffer > 0 && h->traversal == 1; }
 
 static VVFactors vv_factors(const pe_engine *h, double dt) {
   VVFactors v{};
@@ -972,6 +1009,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->tower_sizing < 0 || cfg->tower_sizing > 1) return PE_ERR_ARG;
   if (cfg->traversal < -1 || cfg->traversal > 1) return PE_ERR_ARG;
   if (cfg->atm_nu > 0 && !(cfg->atm_cutoff > 0 && cfg->atm_cutoff <= cfg->cutoff + cfg->skin)) return PE_ERR_ARG;
+  if (cfg->prune_buffer < 0 || cfg->prune_buffer > cfg->skin) return PE_ERR_ARG;
   // every force kernel evaluates each pair from both sides (full lists); half lists are not offered
   if (cfg->newton3 == 1) return PE_ERR_ARG;
   int ndev = 0;
@@ -1068,6 +1106,11 @@ int pe_destroy(pe_engine *h) {
   h->pl_count.release();
   h->pl_max.release();
   h->atm_slot.release();
+  h->pi_list.release();
+  h->pi_count.release();
+  h->x_prune.release();
+  h->x_reb.release();
+  h->disp_bits.release();
   h->atm_out.release();
   h->atm_err.release();
   if (h->st) cudaStreamDestroy(h->st);
@@ -1160,6 +1203,12 @@ int pe_compute_forces(pe_engine *h, pe_globals *globals) {
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "compute before pe_set_particles");
   if (!h->tuned && (h->cfg.cluster_size == 0 || h->cfg.traversal == -1)) PE_TRY(tune(h, 3));
   if (!h->lists_valid) PE_TRY(do_rebuild(h));
+  if (pruning(h)) {
+    DeviceState s = h->state();
+    launch_displacement(s, h->st);  // positions may have been set from the host since the last prune
+    launch_prune(s, h->st);
+    h->launches += 3;
+  }
   PE_TRY(force_eval(h, false, 0.0, true));
   return read_globals(h, globals);
 }
@@ -1201,6 +1250,11 @@ int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, doub
 // The launches of one step after the position update: forces (+ three-body forces and the velocity half when
 // ATM is on, else the velocity half is fused into the force kernel) and the globals reduction.
 static int step_forces(pe_engine *h, double dt, const VVFactors &vv, bool timed) {
+  if (pruning(h)) {
+    DeviceState s = h->state();
+    launch_prune(s, h->st);  // positions were tracked by k_positions
+    h->launches += 2;
+  }
   if (h->cfg.atm_nu > 0) {
     // the velocity update needs the total force: pair forces, then three-body forces, then velocities
     PE_TRY(force_eval(h, false, dt, timed));

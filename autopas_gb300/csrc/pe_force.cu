@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     const int wi = __float_as_int(hi_i.w);
     ti = wi & 0xffff;
     oi = wi >> 16;
-    if (oi == 1) n = s.pl_count[i];
+    if (oi == 1) n = s.fl_count[i];
   }
   const int sy = inrange ? s.sys[i] : 0;
   const SysDev &S = s.sysd[sy];
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   }
   const float band = fa.rc2f * 2e-6f;
   MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
-  const uint32_t *__restrict__ lp = s.pl_list + i;
+  const uint32_t *__restrict__ lp = s.fl_list + i;
   const int64_t stride = s.pl_stride;
   int k = 0;
   // batches of UNROLL entries: all list and position loads of a batch are issued before its arithmetic
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
     xi = s.x[i];
     yi = s.y[i];
     zi = s.z[i];
-    if (oi == 1) n = s.pl_count[i];
+    if (oi == 1) n = s.fl_count[i];
   }
   const SysDev &S = s.sysd[inrange ? s.sys[i] : 0];
   const int T = s.ntypes;
@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
   double fx = 0, fy = 0, fz = 0, pot = 0, vx = 0, vy = 0, vz = 0;
   long long hits2 = 0;
   for (int k = 0; k < n; ++k) {
-    const uint32_t ent = __ldg(s.pl_list + (int64_t)k * s.pl_stride + i);
+    const uint32_t ent = __ldg(s.fl_list + (int64_t)k * s.pl_stride + i);
     const int64_t j = ent >> 5;
     const int code = ent & 31;
     int sx, sy, sz;

@@ -51,6 +51,21 @@ struct DeviceState {
   int pl_cap = 0;
   int64_t pl_stride = 0;
   int *pl_max = nullptr;           // device max of pl_count
+  // lists the force kernels read: the particle lists themselves, or the pruned inner lists
+  uint32_t *fl_list = nullptr;
+  int32_t *fl_count = nullptr;
+  // rolling pruning: inner lists within rc + prune buffer, refreshed from the outer lists on the device when
+  // a particle has moved half the buffer since the last prune (see launch_prune)
+  int prune = 0;
+  uint32_t *pi_list = nullptr;
+  int32_t *pi_count = nullptr;
+  double *x_prune = nullptr;       // [3 * slots] positions at the last prune
+  double *x_reb = nullptr;         // [3 * slots] positions at the last rebuild
+  unsigned int *disp_bits = nullptr;  // [2] max squared displacement (float bits) since prune / since rebuild
+  float prune_half2 = 0;           // (buffer/2)^2: a larger displacement since the last prune forces a prune
+  float reb_limit2 = 0;            // ((skin - buffer)/2)^2: beyond it a prune keeps the whole outer list
+  float r_in2f = 0;                // (rc + buffer)^2 with a relative margin of 1e-5
+  float r_out2f = 0;               // (rc + skin)^2 with the same margin
 
   // ---- systems and parameters ----
   SysDev *sysd = nullptr;          // [nsys]
@@ -70,6 +85,30 @@ struct DeviceState {
   int *err = nullptr;              // device error flags (DeviceError bits)
 };
 
+__device__ __forceinline__ unsigned int f2bits(float v) { return __float_as_uint(v); }
+
+// warp maximum of a non-negative float, folded into *addr (float bits compare as unsigned integers)
+__device__ __forceinline__ void warp_max_atomic(unsigned int *addr, float v) {
+  unsigned int b = f2bits(v);
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(addr, b);
+}
+
+// squared displacement of slot i since the last prune and since the last rebuild, rounded up, into
+// disp_bits (all lanes of the warp must call it)
+__device__ __forceinline__ void track_displacement(const DeviceState &s, int64_t i, bool real) {
+  float dp = 0.f, dr = 0.f;
+  if (real) {
+    const double x = s.x[i], y = s.y[i], z = s.z[i];
+    const double a = x - s.x_prune[3 * i], b = y - s.x_prune[3 * i + 1], c = z - s.x_prune[3 * i + 2];
+    const double d = x - s.x_reb[3 * i], e = y - s.x_reb[3 * i + 1], f = z - s.x_reb[3 * i + 2];
+    dp = __double2float_ru(a * a + b * b + c * c);
+    dr = __double2float_ru(d * d + e * e + f * f);
+  }
+  warp_max_atomic(&s.disp_bits[0], dp);
+  warp_max_atomic(&s.disp_bits[1], dr);
+}
+
 // scan utilities (pe_engine.cu)
 void scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t st);  // out has n+1 entries
 
@@ -83,6 +122,9 @@ int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *pe
 void launch_cluster_bbox(DeviceState &s, cudaStream_t st);
 void launch_list_build(DeviceState &s, cudaStream_t st);
 void launch_plist_build(DeviceState &s, cudaStream_t st);
+void launch_prune_reset_refs(DeviceState &s, cudaStream_t st);   // x_prune = x_reb = x, force the next prune
+void launch_displacement(DeviceState &s, cudaStream_t st);       // update disp_bits from the current positions
+void launch_prune(DeviceState &s, cudaStream_t st);              // prune if needed, then clear the flag
 void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
                       unsigned long long *count, cudaStream_t st);
 

@@ -44,6 +44,7 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=10)
     p.add_argument("--cluster-size", type=int, default=0, help="0: the engine's tuner picks 4 or 8")
     p.add_argument("--traversal", type=int, default=-1, help="-1: tuner; 0 cluster pairs; 1 particle lists")
+    p.add_argument("--prune", type=float, default=0.1, help="rolling-prune buffer of the particle lists (0: off)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
@@ -200,6 +201,7 @@ def config_dict(args):
                         f"steps, dt {DT}, truncated LJ, eps=sigma=m=1",
             "particles": args.n, "cutoff": RC, "skin": SKIN, "rebuild_frequency": REBUILD,
             "cluster_size": args.cluster_size or "tuned", "traversal": "tuned" if args.traversal < 0 else args.traversal,
+            "prune_buffer": args.prune,
             "newton3": False, "l2_policy": "inputs larger than L2 (no flush)"}
 
 
@@ -216,7 +218,8 @@ def run_ours(args):
 
     def new_engine(prec):
         e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
-                         newton3=0, rebuild_frequency=REBUILD, calc_globals=True, traversal=args.traversal)
+                         newton3=0, rebuild_frequency=REBUILD, calc_globals=True, traversal=args.traversal,
+                         prune_buffer=args.prune)
         e.set_particles(pos, vel)
         return e
 

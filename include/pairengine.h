@@ -88,6 +88,9 @@ typedef struct {
   double atm_cutoff;       /* triplet cutoff for ATM (all three distances); <= cutoff + skin */
   int use_graphs;          /* 1: pe_step captures the launches of a step without list rebuild into a CUDA graph
                               once per rebuild and replays it; 0: every step is launched kernel by kernel */
+  double prune_buffer;     /* > 0 (particle lists only): the force kernels read inner lists holding the pairs within
+                              cutoff + prune_buffer, refreshed on the device from the rc+skin lists whenever a
+                              particle has moved prune_buffer/2 since the last refresh; 0: off */
 } pe_config;
 
 /* One particle system of the ensemble. */

@@ -389,3 +389,32 @@ def test_fcc_32000_trajectory_matches_oracle(eng_mod, orc):
     gm = res[eng_mod.PRECISION_MIXED][3]
     driftm = abs(gm["upot"] + gm["ekin"] - e0_ref)
     assert driftm <= max(2 * drift64, 1e-6 * abs(e0_ref))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_pruned_lists_keep_the_interacting_set(eng_mod, orc, prec):
+    """With rolling pruning the force kernels read lists at rc + buffer, refreshed on the device; the interacting
+    set of every step stays the FP64 one and the trajectory stays that of the unpruned engine."""
+    pos, vel, bmin, bmax = liquid(7, seed=31, jitter=0.05)
+    vel = vel * 2.0  # fast particles: several prunes between rebuilds
+    runs = []
+    for buf in (0.0, 0.08):
+        e = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10,
+                               prune_buffer=buf)
+        e.set_particles(pos, vel)
+        g0 = e.compute_forces()[0]
+        pairs = [g0["num_pairs"]]
+        for _ in range(6):
+            g = e.step(0.002, 5)[0]
+            pairs.append(g["num_pairs"])
+        P, V = e.state()
+        runs.append((pairs, P, e.forces(), g))
+    assert runs[0][0] == runs[1][0]
+    tol = 1e-9 if prec == 0 else 1e-5
+    np.testing.assert_allclose(runs[1][1], runs[0][1], rtol=0, atol=tol)
+    assert runs[1][3]["upot"] == pytest.approx(runs[0][3]["upot"], rel=1e-7)
+    # and the pruned forces of the final state are the oracle's
+    P = np.mod(runs[1][1], bmax)
+    allpos, own, _, _, _ = orc.periodic_system(P, bmin, bmax, 2.5, 0.3)
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(2.5), own=own)
+    assert rel_rms(runs[1][2], R[: len(P)]) <= (1e-12 if prec == 0 else 1e-6)
