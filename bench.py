@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=10)
     p.add_argument("--cluster-size", type=int, default=0, help="0: the engine's tuner picks 4 or 8")
     p.add_argument("--traversal", type=int, default=-1, help="-1: tuner; 0 cluster pairs; 1 particle lists")
-    p.add_argument("--prune", type=float, default=0.1, help="rolling-prune buffer of the particle lists (0: off)")
+    p.add_argument("--prune", type=float, default=0.0, help="rolling-prune buffer of the particle lists (0: off)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "autopas_gb300/Checkpoint.h"
 #include "autopas_gb300/GPUClusterLists.h"
 
 using namespace autopas_gb300;
@@ -27,7 +28,27 @@ static int failures = 0;
 
 using Functor = LJFunctorGPU<MoleculeLJ, false, false, true>;
 
+static void checkpoint_roundtrip() {
+  ParticleRecord r;
+  std::mt19937_64 rng(3);
+  std::normal_distribution<double> g(0.0, 5.0);
+  for (int i = 0; i < 40; ++i) {
+    for (auto *v : {&r.x, &r.y, &r.z, &r.vx, &r.vy, &r.vz, &r.fx, &r.fy, &r.fz}) v->push_back(g(rng));
+    r.typeId.push_back(i % 3);
+    r.id.push_back(1000 + i);
+  }
+  const std::string fn = "/tmp/autopas_gb300_ckpt_test.vtu";
+  writeRankRecord(fn, r);
+  const ParticleRecord q = readRankRecord(fn);
+  CHECK(q.size() == r.size(), "checkpoint size");
+  bool same = q.x == r.x && q.y == r.y && q.z == r.z && q.vx == r.vx && q.vy == r.vy && q.vz == r.vz &&
+              q.fx == r.fx && q.fy == r.fy && q.fz == r.fz && q.typeId == r.typeId && q.id == r.id;
+  CHECK(same, "checkpoint round trip must restore every value exactly");
+  std::remove(fn.c_str());
+}
+
 static void cpu_tests() {
+  checkpoint_roundtrip();
   CHECK(toString(ContainerOption::gpuClusterLists) == "GPUClusterLists", "container name");
   CHECK(toString(TraversalOption::gpu_particle_lists) == "gpu_particle_lists", "traversal name");
   CHECK(toEngineTraversal(TraversalOption::gpu_tuned) == -1, "tuned traversal");

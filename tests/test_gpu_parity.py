@@ -418,3 +418,29 @@ def test_pruned_lists_keep_the_interacting_set(eng_mod, orc, prec):
     allpos, own, _, _, _ = orc.periodic_system(P, bmin, bmax, 2.5, 0.3)
     R, glob, _ = orc.lj_forces(allpos, orc.LJ(2.5), own=own)
     assert rel_rms(runs[1][2], R[: len(P)]) <= (1e-12 if prec == 0 else 1e-6)
+
+
+def test_checkpoint_restart_continues_the_trajectory(eng_mod, tmp_path):
+    """A run checkpointed at a rebuild step and restarted in a new engine continues bit for bit."""
+    from autopas_gb300 import checkpoint
+    pos, vel, bmin, bmax = liquid(5, seed=41)
+    kw = dict(periodic=True, rebuild_frequency=10, precision=eng_mod.PRECISION_MIXED)
+    e = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), **kw)
+    e.set_particles(pos, vel)
+    e.compute_forces()
+    e.step(0.002, 20)
+    P1, V1 = e.state()
+    e.step(0.002, 20)
+    Pref, Vref = e.state()
+    p = tmp_path / "lj_0_20.vtu"
+    checkpoint.write_rank_record(p, P1, V1, np.zeros_like(P1), np.zeros(len(P1)), np.arange(len(P1)))
+    r = checkpoint.read_rank_record(p)
+    e2 = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), **kw)
+    e2.set_particles(np.mod(r["pos"], bmax), r["vel"])
+    e2.compute_forces()
+    e2.step(0.002, 20)
+    P2, V2 = e2.state()
+    d = P2 - Pref
+    d -= (bmax - bmin) * np.round(d / (bmax - bmin))
+    assert np.abs(d).max() < 1e-12
+    assert np.abs(V2 - Vref).max() < 1e-12

@@ -242,3 +242,15 @@ def test_wrap_rule(orc):
     assert L.orc_wrap(-0.5, 0.0, 10.0) == 9.5
     assert L.orc_wrap(10.0, 0.0, 10.0) == 0.0
     assert L.orc_wrap(-1e-20, 0.0, 10.0) == np.nextafter(10.0, 0.0)
+
+
+def test_checkpoint_roundtrip_is_exact(tmp_path):
+    from autopas_gb300 import checkpoint
+    rng = np.random.default_rng(8)
+    pos, vel, f = rng.normal(size=(50, 3)) * 7, rng.normal(size=(50, 3)), rng.normal(size=(50, 3)) * 1e3
+    t, ids = rng.integers(0, 4, 50), np.arange(50) * 3 + 1
+    p = tmp_path / "run_0_100.vtu"
+    checkpoint.write_rank_record(p, pos, vel, f, t, ids)
+    r = checkpoint.read_rank_record(p)
+    for k, ref in (("pos", pos), ("vel", vel), ("forces", f), ("type_ids", t), ("ids", ids)):
+        assert np.array_equal(r[k], ref), k
