@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
     return;
   }
   const SysDev &S = s.sysd[s.sys[i]];
-  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
   const int n = min(s.pl_count[i], s.pl_cap);
   const float band = aa.rc2f * 2e-6f;
   // phase 1: neighbours within the triplet cutoff, in list order
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
       ent = s.pl_list[(int64_t)k * s.pl_stride + i];
       const int64_t j = ent >> 5;
       const int code = ent & 31;
-      const float4 hj = s.pk_hi[j], lj = s.pk_lo[j];
+      const float4 hj = s.pk[2 * (j)], lj = s.pk[2 * (j) + 1];
       float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
       if (code != kShiftNone) {
         const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);

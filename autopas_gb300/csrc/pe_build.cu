@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
   const int ii = lane % C, jl = lane / C;
   const int64_t i = A * C + ii;
-  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
   const int oi = __float_as_int(hi_i.w) >> 16;
   const SysDev &S = s.sysd[s.cl_sys[A]];
   const unsigned same_i = (C == 8 ? 0x01010101u : 0x11111111u) << ii;
@@ -472,8 +472,8 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
         ent = __ldg(lst + ee);
         const int64_t j = (int64_t)(ent >> 5) * C + jj;
         const int code = ent & 31;
-        const float4 hj = __ldg(&s.pk_hi[j]);
-        const float4 lj = __ldg(&s.pk_lo[j]);
+        const float4 hj = __ldg(&s.pk[2 * (j)]);
+        const float4 lj = __ldg(&s.pk[2 * (j) + 1]);
         float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
         if (code != kShiftNone) {
           const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
@@ -567,14 +567,14 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
   // whole outer list when particles have used up the skin beyond the buffer since the rebuild
   const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
   const SysDev &S = s.sysd[s.sys[i]];
-  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
   const int n = min(s.pl_count[i], s.pl_cap);
   int m = 0;
   for (int k = 0; k < n; ++k) {
     const uint32_t ent = __ldg(s.pl_list + (int64_t)k * s.pl_stride + i);
     const int64_t j = ent >> 5;
     const int code = ent & 31;
-    const float4 hj = __ldg(&s.pk_hi[j]), lj = __ldg(&s.pk_lo[j]);
+    const float4 hj = __ldg(&s.pk[2 * (j)]), lj = __ldg(&s.pk[2 * (j) + 1]);
     float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
     if (code != kShiftNone) {
       const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);

@@ -5,9 +5,9 @@
 //   dummy slots to a multiple of the cluster size C, so cluster c owns slots [c*C, c*C+C).
 //   FP64 SoA:   x y z  vx vy vz  fx fy fz  ofx ofy ofz         (master state, 96 B/particle)
 //   int SoA:    type(int32) own(int8) sys(int32) orig(int32) id(int64)
-//   packed:     pk_hi / pk_lo (float4): the position as an unevaluated sum hi+lo of two floats in a fixed
-//               binade [B, 2B) per system (w of pk_hi carries type | ownership<<16), 32 B/particle,
-//               read by the mixed-precision force kernel.
+//   packed:     pk (2 float4 per slot, hi then lo): the position as an unevaluated sum hi+lo of two floats in a
+//               fixed binade [B, 2B) per system (w of hi carries type | ownership<<16), 32 B/particle in one
+//               sector, read by the mixed-precision kernels.
 //   clusters:   bbox (6 doubles), system, tower, flags; cluster-pair list entries are uint32
 //               (jcluster << 5 | image-shift code), one contiguous run per i-cluster.
 #pragma once

@@ -96,7 +96,7 @@ struct pe_engine {
   std::string err;
 
   ParticleArrays A, Bk;  // current and gather target
-  DBuf<float4> pk_hi, pk_lo;
+  DBuf<float4> pk;
   DBuf<int32_t> slot_of;
   int64_t nuser = 0;     // particles of the last set_particles
   int64_t nslots = 0;
@@ -179,8 +179,7 @@ struct pe_engine {
     s.nslots = nslots;
     s.nreal = nuser;
     A.bind(s);
-    s.pk_hi = pk_hi.p;
-    s.pk_lo = pk_lo.p;
+    s.pk = pk.p;
     s.slot_of = slot_of.p;
     s.nsys = (int)sys.size();
     s.ntowers = ntowers;
@@ -391,8 +390,8 @@ __device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) {
     l[d] = (float)(xp - (double)h[d]);
   }
   const int w = (s.type[i] & 0xffff) | (o << 16);
-  s.pk_hi[i] = make_float4(h[0], h[1], h[2], __int_as_float(w));
-  s.pk_lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+  s.pk[2 * (i)] = make_float4(h[0], h[1], h[2], __int_as_float(w));
+  s.pk[2 * (i) + 1] = make_float4(l[0], l[1], l[2], 0.f);
 }
 
 __global__ void k_pack(DeviceState s, int64_t n) {
@@ -685,7 +684,7 @@ static int setup_grids(pe_engine *h) {
 
 static int ensure_particle_capacity(pe_engine *h) {
   const size_t n = (size_t)h->pcap;
-  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pk_hi.ensure(n) || !h->pk_lo.ensure(n) ||
+  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pk.ensure(2 * n) ||
       !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
@@ -1076,7 +1075,7 @@ int pe_destroy(pe_engine *h) {
   if (h->st) cudaStreamSynchronize(h->st);
   h->A.release();
   h->Bk.release();
-  for (auto *b : {&h->pk_hi, &h->pk_lo}) b->release();
+  h->pk.release();
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})

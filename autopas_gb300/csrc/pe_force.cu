@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
   const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
   const int ii = lane % C, jl = lane / C;
   const int64_t i = A * C + ii;
-  const float4 hi_i = s.pk_hi[i], lo_i = s.pk_lo[i];
+  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
   const int wi = __float_as_int(hi_i.w);
   const int ti = wi & 0xffff, oi = wi >> 16;
   const SysDev &S = s.sysd[s.cl_sys[A]];
@@ -123,8 +123,8 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
       const uint32_t ent = __ldg(lst + ee);
       const int64_t j = (int64_t)(ent >> 5) * C + jj;
       const int code = ent & 31;
-      const float4 hj = __ldg(&s.pk_hi[j]);
-      const float4 lj = __ldg(&s.pk_lo[j]);
+      const float4 hj = __ldg(&s.pk[2 * (j)]);
+      const float4 lj = __ldg(&s.pk[2 * (j) + 1]);
       float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
       if (code != kShiftNone) {
         // the j image sits at x_j + s*len; moving i by -s*len instead keeps the hi difference exact
@@ -420,8 +420,8 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
   int n = 0, ti = 0, oi = 0;
   if (inrange) {
-    hi_i = s.pk_hi[i];
-    lo_i = s.pk_lo[i];
+    hi_i = s.pk[2 * (i)];
+    lo_i = s.pk[2 * (i) + 1];
     const int wi = __float_as_int(hi_i.w);
     ti = wi & 0xffff;
     oi = wi >> 16;
@@ -440,26 +440,36 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   const uint32_t *__restrict__ lp = s.fl_list + i;
   const int64_t stride = s.pl_stride;
   int k = 0;
-  // batches of UNROLL entries: all list and position loads of a batch are issued before its arithmetic
+  // batches of UNROLL entries: the list entries of the next batch are loaded while the current batch's
+  // positions are gathered and evaluated, so the dependent list -> position load chain overlaps arithmetic
+  uint32_t ent[UNROLL];
+  if (UNROLL <= n) {
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) ent[u] = __ldg(lp + (int64_t)u * stride);
+  }
   for (; k + UNROLL <= n; k += UNROLL) {
-    uint32_t ent[UNROLL];
     float4 hj[UNROLL], lj[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) ent[u] = __ldg(lp + (int64_t)(k + u) * stride);
-#pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      hj[u] = __ldg(&s.pk_hi[ent[u] >> 5]);
-      lj[u] = __ldg(&s.pk_lo[ent[u] >> 5]);
+      const float4 *q = s.pk + 2 * (int64_t)(ent[u] >> 5);
+      hj[u] = __ldg(q);
+      lj[u] = __ldg(q + 1);
     }
+    uint32_t nxt[UNROLL];
+    const bool more = k + 2 * UNROLL <= n;
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) nxt[u] = more ? __ldg(lp + (int64_t)(k + UNROLL + u) * stride) : 0u;
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u)
       acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
     acc.flush();
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) ent[u] = nxt[u];
   }
   for (; k < n; ++k) {
     const uint32_t ent = __ldg(lp + (int64_t)k * stride);
-    const float4 hj = __ldg(&s.pk_hi[ent >> 5]);
-    const float4 lj = __ldg(&s.pk_lo[ent >> 5]);
+    const float4 hj = __ldg(&s.pk[2 * (ent >> 5)]);
+    const float4 lj = __ldg(&s.pk[2 * (ent >> 5) + 1]);
     acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent, hj, lj, eps24, sig2, sh6, tab, T, band);
   }
   acc.flush();

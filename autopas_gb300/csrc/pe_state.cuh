@@ -17,7 +17,7 @@ struct DeviceState {
   int32_t *type = nullptr, *sys = nullptr, *orig = nullptr;
   int8_t *own = nullptr;
   int64_t *id = nullptr;
-  float4 *pk_hi = nullptr, *pk_lo = nullptr;
+  float4 *pk = nullptr;  // [2 * slots]: hi at 2i, lo at 2i+1 (one 32-byte sector per particle)
   // inverse map: user index -> slot
   int32_t *slot_of = nullptr;
 
