@@ -560,8 +560,14 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
   if (s.disp_bits[0] < f2bits(s.prune_half2)) return;  // nobody moved half the buffer: nothing to do
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= s.nslots) return;
-  if (s.own[i] != 1) {
+  const int oi = s.own[i];
+  if (oi != 1) {
     s.pi_count[i] = 0;
+    if (oi != 0) {  // halo particles are list partners: their displacement counts from this prune too
+      s.x_prune[3 * i] = s.x[i];
+      s.x_prune[3 * i + 1] = s.y[i];
+      s.x_prune[3 * i + 2] = s.z[i];
+    }
     return;
   }
   // whole outer list when particles have used up the skin beyond the buffer since the rebuild
@@ -597,8 +603,12 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
   s.x_prune[3 * i + 2] = s.z[i];
 }
 
+// after a launch that pruned: the displacement since the prune starts again from zero; counts the prunes
 __global__ void k_prune_clear(DeviceState s) {
-  if (threadIdx.x == 0 && blockIdx.x == 0 && s.disp_bits[0] >= f2bits(s.prune_half2)) s.disp_bits[0] = 0u;
+  if (threadIdx.x == 0 && blockIdx.x == 0 && s.disp_bits[0] >= f2bits(s.prune_half2)) {
+    s.disp_bits[0] = 0u;
+    s.disp_bits[2] += 1u;
+  }
 }
 
 void launch_prune(DeviceState &s, cudaStream_t st) {
@@ -606,6 +616,8 @@ void launch_prune(DeviceState &s, cudaStream_t st) {
   k_prune<<<(unsigned)nb, 128, 0, st>>>(s);
   k_prune_clear<<<1, 32, 0, st>>>(s);
 }
+
+void launch_prune_clear(DeviceState &s, cudaStream_t st) { k_prune_clear<<<1, 32, 0, st>>>(s); }
 
 // ---------------------------------------------------------------------------------------------
 // pair-set dump (verification): the particle pairs covered by the lists, evaluated in FP64

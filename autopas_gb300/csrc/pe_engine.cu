@@ -726,13 +726,14 @@ static int build_particle_lists(pe_engine *h) {
       h->pl_entries = 0;
       if (h->cfg.prune_buffer > 0 && h->traversal == 1) {
         const size_t cap = (size_t)h->pl_cap * (size_t)h->pcap;
+        const bool fresh = h->disp_bits.p == nullptr;
         if (!h->pi_list.ensure(cap) || !h->pi_count.ensure((size_t)h->pcap) || !h->x_prune.ensure(3 * (size_t)h->pcap) ||
-            !h->x_reb.ensure(3 * (size_t)h->pcap) || !h->disp_bits.ensure(2))
+            !h->x_reb.ensure(3 * (size_t)h->pcap) || !h->disp_bits.ensure(3))
           return h->fail(PE_ERR_OOM, "pruned lists");
+        if (fresh) PE_CUDA(h, cudaMemsetAsync(h->disp_bits.p, 0, 3 * sizeof(unsigned int), st));
         DeviceState s2 = h->state();
-        launch_prune_reset_refs(s2, st);
-        launch_prune(s2, st);
-        h->launches += 3;
+        launch_prune_reset_refs(s2, st);  // the next force evaluation prunes from the new lists
+        h->launches += 1;
         PE_TRY(h->cuda_check("prune"));
       }
       return PE_OK;
@@ -870,6 +871,14 @@ static VVFactors vv_factors(const pe_engine *h, double dt) {
 
 static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
   DeviceState s = h->state();
+  // rolling pruning: the FP64 form prunes in a kernel of its own before the force kernel; the mixed kernel
+  // prunes by itself while it walks the outer lists, and the flag is cleared after it
+  const bool prune_fp64 = pruning(h) && h->precision == PE_PRECISION_FP64;
+  const bool prune_fused = pruning(h) && h->precision != PE_PRECISION_FP64;
+  if (prune_fp64) {
+    launch_prune(s, h->st);
+    h->launches += 2;
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int i0 = -1;
   if (timed) {
@@ -883,6 +892,10 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
   if (timed) {
     cudaEventRecord(e1, h->st);
     h->force_ev.push_back({i0, i0 + 1});
+  }
+  if (prune_fused) {
+    launch_prune_clear(s, h->st);
+    h->launches += 1;
   }
   h->launches += 1;
   if (timed) h->force_launches += 1;
@@ -958,7 +971,7 @@ static int tune(pe_engine *h, int samples) {
   const int rebuilds = (int)h->rebuilds;
   for (int C : Cs)
     for (int T : Ts) {
-      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : 1;
+      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 2) : 1;
       for (int v = 0; v < nv; ++v) {
         PE_TRY(apply_config(h, C, T, v));
         std::vector<float> t;
@@ -1205,8 +1218,7 @@ int pe_compute_forces(pe_engine *h, pe_globals *globals) {
   if (pruning(h)) {
     DeviceState s = h->state();
     launch_displacement(s, h->st);  // positions may have been set from the host since the last prune
-    launch_prune(s, h->st);
-    h->launches += 3;
+    h->launches += 1;
   }
   PE_TRY(force_eval(h, false, 0.0, true));
   return read_globals(h, globals);
@@ -1249,11 +1261,7 @@ int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, doub
 // The launches of one step after the position update: forces (+ three-body forces and the velocity half when
 // ATM is on, else the velocity half is fused into the force kernel) and the globals reduction.
 static int step_forces(pe_engine *h, double dt, const VVFactors &vv, bool timed) {
-  if (pruning(h)) {
-    DeviceState s = h->state();
-    launch_prune(s, h->st);  // positions were tracked by k_positions
-    h->launches += 2;
-  }
+  // with pruning on, the displacement since the last prune was tracked by k_positions
   if (h->cfg.atm_nu > 0) {
     // the velocity update needs the total force: pair forces, then three-body forces, then velocities
     PE_TRY(force_eval(h, false, dt, timed));
@@ -1416,7 +1424,12 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out) {
   out->kernel_launches = h->launches;
   out->pairs_total = pairs;
   out->rebuilds = h->rebuilds;
+  unsigned int prunes = 0;
+  if (h->disp_bits.p)
+    PE_CUDA(h, cudaMemcpy(&prunes, h->disp_bits.p + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+  out->prunes = prunes;
   if (reset) {
+    if (h->disp_bits.p) PE_CUDA(h, cudaMemset(h->disp_bits.p + 2, 0, sizeof(unsigned int)));
     h->force_ev.clear();
     h->ev_used = 0;
     h->force_launches = 0;

@@ -340,7 +340,8 @@ struct MixedAcc {
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
   int hits = 0, hhalo = 0;
 
-  __device__ __forceinline__ void pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+  // returns the pair's FP32 squared distance (the re-prune test uses it)
+  __device__ __forceinline__ float pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                        const float4 &hi_i, const float4 &lo_i, int ti, uint32_t ent,
                                        const float4 &hj, const float4 &lj, float eps24, float sig2, float sh6,
                                        const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
@@ -386,6 +387,7 @@ struct MixedAcc {
       hits += mask ? 1 : 0;
       if (!S.periodic) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
     }
+    return r2;
   }
 
   __device__ __forceinline__ void flush() {
@@ -402,46 +404,19 @@ struct MixedAcc {
   }
 };
 
-// MINB: minimum resident blocks per SM requested from the compiler (caps registers for more warps in flight)
-template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
-  __shared__ float tab[3][kMaxTypes * kMaxTypes];
-  const int T = s.ntypes;
-  if (!ONE_TYPE) {
-    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
-      tab[0][q] = (float)s.types->eps24[q];
-      tab[1][q] = (float)s.types->sig2[q];
-      tab[2][q] = (float)s.types->shift6[q];
-    }
-    __syncthreads();
-  }
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool inrange = i < s.nslots;
-  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
-  int n = 0, ti = 0, oi = 0;
-  if (inrange) {
-    hi_i = s.pk[2 * (i)];
-    lo_i = s.pk[2 * (i) + 1];
-    const int wi = __float_as_int(hi_i.w);
-    ti = wi & 0xffff;
-    oi = wi >> 16;
-    if (oi == 1) n = s.fl_count[i];
-  }
-  const int sy = inrange ? s.sys[i] : 0;
-  const SysDev &S = s.sysd[sy];
-  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
-  if (ONE_TYPE) {
-    eps24 = (float)s.types->eps24[0];
-    sig2 = (float)s.types->sig2[0];
-    sh6 = (float)s.types->shift6[0];
-  }
-  const float band = fa.rc2f * 2e-6f;
-  MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
-  const uint32_t *__restrict__ lp = s.fl_list + i;
+// One thread's walk over its list (UNROLL entries per batch; the list entries of the next batch are loaded while
+// the current batch's positions are gathered and evaluated, so the dependent list -> position chain overlaps
+// arithmetic).  With REPRUNE the walk reads the outer list (rc + skin) and also writes the entries within
+// lim to the inner list out; it returns their number.
+template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool REPRUNE>
+__device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                          const float4 &hi_i, const float4 &lo_i, int ti,
+                                          const uint32_t *__restrict__ lp, int n, float eps24, float sig2, float sh6,
+                                          const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
+                                          MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc, uint32_t *__restrict__ out,
+                                          float lim) {
   const int64_t stride = s.pl_stride;
-  int k = 0;
-  // batches of UNROLL entries: the list entries of the next batch are loaded while the current batch's
-  // positions are gathered and evaluated, so the dependent list -> position load chain overlaps arithmetic
+  int k = 0, m = 0;
   uint32_t ent[UNROLL];
   if (UNROLL <= n) {
 #pragma unroll
@@ -460,17 +435,80 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) nxt[u] = more ? __ldg(lp + (int64_t)(k + UNROLL + u) * stride) : 0u;
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u)
-      acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
+    for (int u = 0; u < UNROLL; ++u) {
+      const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
+      if (REPRUNE && r2 <= lim) out[(int64_t)(m++) * stride] = ent[u];
+    }
     acc.flush();
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) ent[u] = nxt[u];
   }
   for (; k < n; ++k) {
-    const uint32_t ent = __ldg(lp + (int64_t)k * stride);
-    const float4 hj = __ldg(&s.pk[2 * (ent >> 5)]);
-    const float4 lj = __ldg(&s.pk[2 * (ent >> 5) + 1]);
-    acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent, hj, lj, eps24, sig2, sh6, tab, T, band);
+    const uint32_t e = __ldg(lp + (int64_t)k * stride);
+    const float4 *q = s.pk + 2 * (int64_t)(e >> 5);
+    const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, e, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
+    if (REPRUNE && r2 <= lim) out[(int64_t)(m++) * stride] = e;
+  }
+  return m;
+}
+
+// MINB: minimum resident blocks per SM requested from the compiler (caps registers for more warps in flight).
+// With rolling pruning on, the kernel itself refreshes the inner lists when the displacement since the last
+// prune (tracked by the position update) reaches half the buffer: it then walks the outer lists, writes the
+// entries within rc + buffer (or the whole outer list once the particles have used up the skin beyond the
+// buffer since the rebuild) to the inner lists and records the positions of the prune.  The flag is read
+// by every thread and cleared by a later launch, so all threads take the same branch.
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  const int T = s.ntypes;
+  if (!ONE_TYPE) {
+    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
+      tab[0][q] = (float)s.types->eps24[q];
+      tab[1][q] = (float)s.types->sig2[q];
+      tab[2][q] = (float)s.types->shift6[q];
+    }
+    __syncthreads();
+  }
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool inrange = i < s.nslots;
+  const bool reprune = s.prune && s.disp_bits[0] >= f2bits(s.prune_half2);
+  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+  int n = 0, ti = 0, oi = 0;
+  if (inrange) {
+    hi_i = s.pk[2 * (i)];
+    lo_i = s.pk[2 * (i) + 1];
+    const int wi = __float_as_int(hi_i.w);
+    ti = wi & 0xffff;
+    oi = wi >> 16;
+    if (oi == 1) n = reprune ? min(s.pl_count[i], s.pl_cap) : s.fl_count[i];
+  }
+  const int sy = inrange ? s.sys[i] : 0;
+  const SysDev &S = s.sysd[sy];
+  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
+  if (ONE_TYPE) {
+    eps24 = (float)s.types->eps24[0];
+    sig2 = (float)s.types->sig2[0];
+    sh6 = (float)s.types->shift6[0];
+  }
+  const float band = fa.rc2f * 2e-6f;
+  MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
+  if (reprune) {
+    const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
+    // single-entry batches: this branch runs once per prune, and fewer live registers keep the other one spill-free
+    const int m = plist_walk<GLOB, ONE_TYPE, KAHAN, 1, true>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list + i, n, eps24,
+                                                                  sig2, sh6, tab, T, band, acc, s.pi_list + i, lim);
+    if (inrange) {
+      s.pi_count[i] = m;
+      if (oi != 0) {
+        s.x_prune[3 * i] = s.x[i];
+        s.x_prune[3 * i + 1] = s.y[i];
+        s.x_prune[3 * i + 2] = s.z[i];
+      }
+    }
+  } else {
+    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, false>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list + i, n, eps24, sig2, sh6,
+                                                     tab, T, band, acc, nullptr, 0.f);
   }
   acc.flush();
   const double Fx = (double)acc.fxs - (double)acc.fxc, Fy = (double)acc.fys - (double)acc.fyc,
@@ -614,23 +652,14 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
       k_lj_fp64_plist<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     return;
   }
-  // kernel variants, chosen by the engine's tuner: list loads batched per 1, 2 or 4 entries under register
-  // caps of 64 (8 blocks of 128 threads per SM), 85 (6 blocks), 40 (12 blocks) or 51 (10 blocks)
+  // kernel variants, chosen by the engine's tuner: list entries batched by 2 under a cap of 64 registers
+  // (8 blocks of 128 threads per SM) or by 4 under a cap of 80 (6 blocks); tighter caps spill
 #define PE_PLIST(G, O)                                                                   \
   do {                                                                                   \
-    switch (s.variant) {                                                                 \
-      case 1:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 4, 6><<<(unsigned)nb, 128, 0, st>>>(s, fa);      \
-        break;                                                                           \
-      case 2:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 2, 12><<<(unsigned)nb, 128, 0, st>>>(s, fa);     \
-        break;                                                                           \
-      case 3:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 1, 10><<<(unsigned)nb, 128, 0, st>>>(s, fa);     \
-        break;                                                                           \
-      default:                                                                           \
-        k_lj_mixed_plist<C, G, O, true, 2, 8><<<(unsigned)nb, 128, 0, st>>>(s, fa);      \
-    }                                                                                    \
+    if (s.variant == 1)                                                                  \
+      k_lj_mixed_plist<C, G, O, true, 4, 6><<<(unsigned)nb, 128, 0, st>>>(s, fa);        \
+    else                                                                                 \
+      k_lj_mixed_plist<C, G, O, true, 2, 8><<<(unsigned)nb, 128, 0, st>>>(s, fa);        \
   } while (0)
   if (s.ntypes == 1) {
     if (fa.calc_globals)

@@ -61,7 +61,8 @@ struct DeviceState {
   int32_t *pi_count = nullptr;
   double *x_prune = nullptr;       // [3 * slots] positions at the last prune
   double *x_reb = nullptr;         // [3 * slots] positions at the last rebuild
-  unsigned int *disp_bits = nullptr;  // [2] max squared displacement (float bits) since prune / since rebuild
+  unsigned int *disp_bits = nullptr;  // [3] max squared displacement (float bits) since prune / since rebuild,
+                                      // prunes done
   float prune_half2 = 0;           // (buffer/2)^2: a larger displacement since the last prune forces a prune
   float reb_limit2 = 0;            // ((skin - buffer)/2)^2: beyond it a prune keeps the whole outer list
   float r_in2f = 0;                // (rc + buffer)^2 with a relative margin of 1e-5
@@ -91,7 +92,8 @@ __device__ __forceinline__ unsigned int f2bits(float v) { return __float_as_uint
 __device__ __forceinline__ void warp_max_atomic(unsigned int *addr, float v) {
   unsigned int b = f2bits(v);
   for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(addr, b);
+  // values only grow while a kernel runs, so a warp whose maximum is not above the stored one has nothing to add
+  if ((threadIdx.x & 31) == 0 && b > __ldcg(addr)) atomicMax(addr, b);
 }
 
 // squared displacement of slot i since the last prune and since the last rebuild, rounded up, into
@@ -125,6 +127,7 @@ void launch_plist_build(DeviceState &s, cudaStream_t st);
 void launch_prune_reset_refs(DeviceState &s, cudaStream_t st);   // x_prune = x_reb = x, force the next prune
 void launch_displacement(DeviceState &s, cudaStream_t st);       // update disp_bits from the current positions
 void launch_prune(DeviceState &s, cudaStream_t st);              // prune if needed, then clear the flag
+void launch_prune_clear(DeviceState &s, cudaStream_t st);        // clear the flag after a kernel that pruned
 void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
                       unsigned long long *count, cudaStream_t st);
 

@@ -37,7 +37,7 @@ FLOP_PER_PAIR = 38  # 8 distance + 18 newton3 kernel + 12 globals (unshifted), L
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=2_000_000, help="particles of the slab workload")
@@ -216,10 +216,10 @@ def run_ours(args):
     pos, vel, bmin, bmax = make_slab(args.n, seed=7 + rank)
     n = len(pos)
 
-    def new_engine(prec):
+    def new_engine(prec, use_graphs=True):
         e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
                          newton3=0, rebuild_frequency=REBUILD, calc_globals=True, traversal=args.traversal,
-                         prune_buffer=args.prune)
+                         prune_buffer=args.prune, use_graphs=use_graphs)
         e.set_particles(pos, vel)
         return e
 
@@ -267,17 +267,19 @@ def run_ours(args):
     pairs_all = sum_over_ranks(pg, pairs_total)
     value = pairs_all / (ms_max * 1e-3)
     steps_per_s = args.steps / (ms_max * 1e-3)
-    # force kernels outside graph replays (the rebuild steps) are timed with events on the engine's stream;
-    # every step evaluates the forces once
-    pairs_per_launch = pairs_total / max(args.steps, 1)
-    if st["force_launches"] == 0:
-        # no rebuild step fell into the timed region: time eager force evaluations of the same state instead
-        for _ in range(5):
-            e.compute_forces()
-        st_f = e.stats(reset=True)
-        force_ms_per_launch = st_f["force_ms"] / max(st_f["force_launches"], 1)
-    else:
-        force_ms_per_launch = st["force_ms"] / st["force_launches"]
+    e.close()
+    # the force kernel alone: the same steps without graph replay, every force launch timed with CUDA events on
+    # the engine's stream (rebuild steps, prune steps and plain steps in their natural proportion)
+    ek = new_engine(E.PRECISION_MIXED, use_graphs=False)
+    ek.compute_forces()
+    ek.step(DT, args.warmup, want_globals=False)
+    ek.stats(reset=True)
+    nk = min(args.steps, 2 * REBUILD * 5)
+    ek.step(DT, nk, want_globals=True)
+    st_k = ek.stats(reset=True)
+    ek.close()
+    force_ms_per_launch = st_k["force_ms"] / max(st_k["force_launches"], 1)
+    pairs_per_launch = st_k["pairs_total"] / max(st_k["force_launches"], 1)
 
     # ---- FP64 form on the same workload
     fp64 = None
@@ -337,7 +339,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.profile:
         nthreads = os.cpu_count() or 1
-        rate, pairs_s, evals, tt = cpu_reference_rate(250_000, nthreads, budget_s=15.0, max_evals=20)
+        rate, pairs_s, evals, tt = cpu_reference_rate(250_000, nthreads, budget_s=10.0)
         cpu = {"value": rate, "unit": "pair interactions/s", "cores": nthreads, "kind": "port",
                "sample": f"{evals} force evaluations (lc_c08 + SoA LJ, newton3, FP64, OpenMP) of a 250,000-particle "
                          f"slab with the workload's densities and shape ({pairs_s} interacting pairs), {tt:.1f} s"}
@@ -364,11 +366,13 @@ def run_ours(args):
         "config": config_dict(args),
         "md_steps_per_s": steps_per_s,
         "force_kernel": {"ms_per_launch": force_ms_per_launch, "pairs_per_launch": pairs_per_launch,
-                         "pair_interactions_per_s": pairs_per_launch / (force_ms_per_launch * 1e-3)},
+                         "pair_interactions_per_s": pairs_per_launch / (force_ms_per_launch * 1e-3),
+                         "launches_timed": st_k["force_launches"], "prunes": st_k["prunes"]},
         "fp64_gpu": fp64,
         "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
         "force_error": err,
         "upot_last_step": g_last["upot"], "rebuilds_in_timed_region": st["rebuilds"],
+        "prunes_in_timed_region": st["prunes"],
         "engine": {k: info[k] for k in ("cluster_size", "traversal", "num_clusters", "num_cluster_pairs",
                                         "max_tower_size", "num_towers", "list_capacity")},
         "tuning": tuning,
@@ -466,7 +470,7 @@ def run_drift(args):
     __graft_entry__.build()
     from autopas_gb300 import engine as E, workloads
     pos, vel, bmin, bmax = workloads.fcc_lj(20, 0.8442, 0.72, seed=1)
-    nsteps = args.steps if args.steps >= 1000 else 10000
+    nsteps = max(args.steps, 10000)
     out = {}
     for name, prec in (("fp64", E.PRECISION_FP64), ("mixed", E.PRECISION_MIXED)):
         e = E.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10)

@@ -186,13 +186,15 @@ int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, in
 /* Counters of the engine since the last reset: CUDA-event time of the force kernels launched outside CUDA
  * graphs (force_ms) and the number of launches it covers (force_launches), launches of the engine's own
  * kernels including those inside graph replays (kernel_launches), interacting pairs summed over all force
- * evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds. */
+ * evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds, and
+ * refreshes of the pruned inner lists (prunes; 0 unless prune_buffer > 0). */
 typedef struct {
   double force_ms;
   int64_t force_launches;
   int64_t kernel_launches;
   int64_t pairs_total;
   int64_t rebuilds;
+  int64_t prunes;
 } pe_stats;
 int pe_get_stats(pe_engine *h, int reset, pe_stats *out);
 

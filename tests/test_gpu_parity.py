@@ -408,7 +408,9 @@ def test_pruned_lists_keep_the_interacting_set(eng_mod, orc, prec):
             g = e.step(0.002, 5)[0]
             pairs.append(g["num_pairs"])
         P, V = e.state()
-        runs.append((pairs, P, e.forces(), g))
+        runs.append((pairs, P, e.forces(), g, e.stats()["prunes"]))
+    assert runs[0][4] == 0
+    assert runs[1][4] >= 3  # at least one after each rebuild
     assert runs[0][0] == runs[1][0]
     tol = 1e-9 if prec == 0 else 1e-5
     np.testing.assert_allclose(runs[1][1], runs[0][1], rtol=0, atol=tol)
