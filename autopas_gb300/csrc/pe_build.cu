@@ -99,7 +99,7 @@ __global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, c
   uint64_t *k = reinterpret_cast<uint64_t *>(smem);
   int32_t *tie = reinterpret_cast<int32_t *>(k + p2);
   int32_t *val = tie + p2;
-  __shared__ double red[4][32];
+  __shared__ uint64_t red[4][32];
 
   const int t = blockIdx.x;
   const int n = s.tw_count[t];
@@ -110,30 +110,32 @@ __global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, c
     if (threadIdx.x == 0) atomicOr(s.err, kErrTowerOverflow);
     return;
   }
-  double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  // tower xy bbox on the monotone integer keys of the coordinates (min/max on the integer pipes; the FP64
+  // pipe of this GPU is 1/64 of FP32), decoded once per tower
+  uint64_t mnx = ~0ull, mny = ~0ull, mxx = 0ull, mxy = 0ull;
   for (int q = threadIdx.x; q < p2; q += blockDim.x) {
     if (q < n) {
       const int32_t v = sval[base + q];
       k[q] = skey[base + q];
       tie[q] = s.orig[v];
       val[q] = v;
-      const double px = s.x[v], py = s.y[v];
-      mnx = fmin(mnx, px);
-      mxx = fmax(mxx, px);
-      mny = fmin(mny, py);
-      mxy = fmax(mxy, py);
+      const uint64_t kx = dbl_key(s.x[v]), ky = dbl_key(s.y[v]);
+      mnx = min(mnx, kx);
+      mxx = max(mxx, kx);
+      mny = min(mny, ky);
+      mxy = max(mxy, ky);
     } else {
       k[q] = ~0ull;
       tie[q] = 0x7fffffff;
       val[q] = -1;
     }
   }
-  // tower bbox: warp then block reduction
+  // warp then block reduction
   for (int o = 16; o > 0; o >>= 1) {
-    mnx = fmin(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-    mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-    mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-    mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    mnx = min(mnx, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mnx, o));
+    mny = min(mny, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mny, o));
+    mxx = max(mxx, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mxx, o));
+    mxy = max(mxy, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mxy, o));
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
   if (l == 0) {
@@ -145,15 +147,15 @@ __global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, c
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int q = 1; q < nw; ++q) {
-      mnx = fmin(mnx, red[0][q]);
-      mny = fmin(mny, red[1][q]);
-      mxx = fmax(mxx, red[2][q]);
-      mxy = fmax(mxy, red[3][q]);
+      mnx = min(mnx, red[0][q]);
+      mny = min(mny, red[1][q]);
+      mxx = max(mxx, red[2][q]);
+      mxy = max(mxy, red[3][q]);
     }
-    s.tw_bb[4 * t + 0] = mnx;
-    s.tw_bb[4 * t + 1] = mny;
-    s.tw_bb[4 * t + 2] = mxx;
-    s.tw_bb[4 * t + 3] = mxy;
+    // an empty tower keeps an empty box (min +inf, max -inf)
+    s.tw_bbf[t] = n > 0 ? make_float4(__double2float_rd(key_dbl(mnx)), __double2float_rd(key_dbl(mny)),
+                                      __double2float_ru(key_dbl(mxx)), __double2float_ru(key_dbl(mxy)))
+                        : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
   }
   // bitonic sort, ascending on (k, tie)
   for (int size = 2; size <= p2; size <<= 1) {
@@ -225,7 +227,11 @@ __global__ void k_cluster_bbox(DeviceState s) {
     s.cl_bb[6 * c + d] = lo[d];
     s.cl_bb[6 * c + 3 + d] = hi[d];
   }
-  s.cl_z[c] = make_float2(__double2float_rd(lo[2]), __double2float_ru(hi[2]));
+  const float4 lof = make_float4(__double2float_rd(lo[0]), __double2float_rd(lo[1]), __double2float_rd(lo[2]), 0.f);
+  const float4 hif = make_float4(__double2float_ru(hi[0]), __double2float_ru(hi[1]), __double2float_ru(hi[2]), 0.f);
+  s.cl_bbf[2 * c] = lof;
+  s.cl_bbf[2 * c + 1] = hif;
+  s.cl_z[c] = make_float2(lof.z, hif.z);
   s.cl_flags[c] = flags;
   s.cl_sys[c] = s.sys[c * C];
 }
@@ -244,18 +250,21 @@ __device__ __forceinline__ double gap1(double alo, double ahi, double blo, doubl
   const double g2 = blo - ahi;
   return fmax(0.0, fmax(g1, g2));
 }
+__device__ __forceinline__ float gap1f(float alo, float ahi, float blo, float bhi) {
+  return fmaxf(0.f, fmaxf(alo - bhi, blo - ahi));
+}
 
 constexpr int kListWarps = 4;
 
 // Candidate segments of an i-cluster: for every neighbour tower (xy offset within the tower reach, wrapped
 // with an image shift for periodic systems) and z image shift, the run of the tower's clusters whose z-range
-// can come within L.  Lanes find the runs of 32 segments at once (two binary searches each, since lo.z and
-// hi.z are non-decreasing inside a tower); the runs are then walked in segment order, so the list order is
-// deterministic.
+// can come within L.  Lanes find the runs of 32 segments at once (two interpolated searches each, since lo.z
+// and hi.z are non-decreasing inside a tower); the runs are then walked in segment order, so the list order
+// is deterministic.  Everything here only narrows the candidates, on float boxes rounded outwards and with
+// margins that cover the float rounding; the FP64 box test decides.
 __device__ __forceinline__ void segment_run(const DeviceState &s, const SysDev &S, int tx, int ty, int seg,
-                                            int nseg_z, const double *alo, const double *ahi, double L2, double Lz,
-                                            int &c_first, int &c_end, int &code, double &shx, double &shy,
-                                            double &shz) {
+                                            int nseg_z, const float4 &alo, const float4 &ahi, float L2hi, float Lz,
+                                            int &c_first, int &c_end, int &code) {
   c_first = c_end = 0;
   const int side_x = 2 * S.kx + 1;
   const int sz = (seg % nseg_z) - (nseg_z > 1 ? 1 : 0);
@@ -271,23 +280,21 @@ __device__ __forceinline__ void segment_run(const DeviceState &s, const SysDev &
   } else if (nx < 0 || ny < 0 || nx >= S.nt[0] || ny >= S.nt[1]) {
     return;
   }
-  shx = sx == 0 ? 0.0 : (sx > 0 ? S.len[0] : -S.len[0]);
-  shy = sy == 0 ? 0.0 : (sy > 0 ? S.len[1] : -S.len[1]);
-  shz = sz == 0 ? 0.0 : (sz > 0 ? S.len[2] : -S.len[2]);
+  const float shx = (float)sx * S.lenf[0], shy = (float)sy * S.lenf[1], shz = (float)sz * S.lenf[2];
   // an image shifted in z can only matter for an i-cluster near the opposite face
-  if (sz > 0 && S.bmin[2] + shz > ahi[2] + Lz) return;
-  if (sz < 0 && S.bmax[2] + shz < alo[2] - Lz) return;
+  if (sz > 0 && S.bminf[2] + shz > ahi.z + Lz) return;
+  if (sz < 0 && S.bmaxf[2] + shz < alo.z - Lz) return;
   const int tB = S.tower_base + ny * S.nt[0] + nx;
   const int c0 = s.tw_cl_start[tB], c1 = s.tw_cl_start[tB + 1];
   if (c0 == c1) return;
-  const double gx = gap1(alo[0], ahi[0], s.tw_bb[4 * tB + 0] + shx, s.tw_bb[4 * tB + 2] + shx);
-  const double gy = gap1(alo[1], ahi[1], s.tw_bb[4 * tB + 1] + shy, s.tw_bb[4 * tB + 3] + shy);
-  if (gx * gx + gy * gy > L2) return;
-  // window of clusters with hi.z >= zmin and lo.z <= zmax, on the float z ranges (rounded outwards, so the
-  // window can only be wider than the FP64 one; the FP64 box test decides).  Clusters of a tower are
+  const float4 tb = s.tw_bbf[tB];
+  const float gx = gap1f(alo.x, ahi.x, tb.x + shx, tb.z + shx);
+  const float gy = gap1f(alo.y, ahi.y, tb.y + shy, tb.w + shy);
+  if (fmaf(gy, gy, gx * gx) > L2hi) return;
+  // window of clusters with hi.z >= zmin and lo.z <= zmax on the float z ranges.  Clusters of a tower are
   // z-ordered and nearly uniform in z: an interpolated first guess plus a short walk finds the bounds.
-  const float zmin = __double2float_rd(alo[2] - Lz - shz);
-  const float zmax = __double2float_ru(ahi[2] + Lz - shz);
+  const float zmin = alo.z - Lz - shz;
+  const float zmax = ahi.z + Lz - shz;
   const float z0 = s.cl_z[c0].x, z1 = s.cl_z[c1 - 1].y;
   if (z1 < zmin || z0 > zmax) return;
   const float span = fmaxf(z1 - z0, 1e-30f);
@@ -302,6 +309,22 @@ __device__ __forceinline__ void segment_run(const DeviceState &s, const SysDev &
   c_first = a;
   c_end = b;
   code = shift_code(sx, sy, sz);
+}
+
+// FP64 box distance test of cluster pair (A, B + image shift) -- the decision, taken only near the threshold
+__device__ __forceinline__ bool box_within_fp64(const DeviceState &s, const SysDev &S, int64_t A, int64_t B,
+                                                int code, double L2) {
+  int sx, sy, sz;
+  shift_of(code, sx, sy, sz);
+  const double hx = sx == 0 ? 0.0 : (sx > 0 ? S.len[0] : -S.len[0]);
+  const double hy = sy == 0 ? 0.0 : (sy > 0 ? S.len[1] : -S.len[1]);
+  const double hz = sz == 0 ? 0.0 : (sz > 0 ? S.len[2] : -S.len[2]);
+  const double *a = s.cl_bb + 6 * A;
+  const double *b = s.cl_bb + 6 * B;
+  const double g0 = gap1(a[0], a[3], b[0] + hx, b[3] + hx);
+  const double g1 = gap1(a[1], a[4], b[1] + hy, b[4] + hy);
+  const double g2 = gap1(a[2], a[5], b[2] + hz, b[5] + hz);
+  return (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
 }
 
 __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
@@ -320,14 +343,13 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     return;
   }
   const SysDev &S = s.sysd[s.cl_sys[A]];
-  double alo[3], ahi[3];
-  for (int d = 0; d < 3; ++d) {
-    alo[d] = s.cl_bb[6 * A + d];
-    ahi[d] = s.cl_bb[6 * A + 3 + d];
-  }
+  const float4 alo = s.cl_bbf[2 * A], ahi = s.cl_bbf[2 * A + 1];
   const double L = s.cutoff + s.skin;
   const double L2 = L * L * (1.0 + 1e-12);
-  const double Lz = L * (1.0 + 1e-12);
+  // float thresholds: below L2lo the FP64 test must accept, above L2hi it must reject
+  const float L2f = (float)L2;
+  const float L2lo = L2f - S.bb_tol2, L2hi = L2f + S.bb_tol2;
+  const float Lz = (float)L + S.coord_tol;
   const int tloc = s.cl_tower[A] - S.tower_base;
   const int tx = tloc % S.nt[0], ty = tloc / S.nt[0];
   int cnt = 0;
@@ -337,13 +359,12 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     cnt = 1;
   }
   // z images only matter for an i-cluster within L of a z face
-  const bool zface = S.periodic && (alo[2] - Lz < S.bmin[2] || ahi[2] + Lz > S.bmax[2]);
+  const bool zface = S.periodic && (alo.z - Lz < S.bminf[2] + S.coord_tol || ahi.z + Lz > S.bmaxf[2] - S.coord_tol);
   const int nseg_z = zface ? 3 : 1;
   const int nseg = (2 * S.kx + 1) * (2 * S.ky + 1) * nseg_z;
   for (int sb = 0; sb < nseg && !overflow; sb += 32) {
     int cf = 0, ce = 0, code = kShiftNone;
-    double shx = 0, shy = 0, shz = 0;
-    if (sb + lane < nseg) segment_run(s, S, tx, ty, sb + lane, nseg_z, alo, ahi, L2, Lz, cf, ce, code, shx, shy, shz);
+    if (sb + lane < nseg) segment_run(s, S, tx, ty, sb + lane, nseg_z, alo, ahi, L2hi, Lz, cf, ce, code);
     // flatten the runs of the 32 segments into one candidate index space (exclusive prefix over lanes)
     const int len = ce - cf;
     int incl = len;
@@ -364,12 +385,9 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
         const int om = __shfl_sync(0xffffffffu, excl, mid);
         if (om <= t) lo = mid; else hi = mid - 1;
       }
-      // lanes with empty runs share offsets with the next non-empty one; step forward to a run holding t
       const int src = lo;
       const int f = __shfl_sync(0xffffffffu, cf, src), e0 = __shfl_sync(0xffffffffu, excl, src);
       const int cd = __shfl_sync(0xffffffffu, code, src);
-      const double hx = __shfl_sync(0xffffffffu, shx, src), hy = __shfl_sync(0xffffffffu, shy, src);
-      const double hz = __shfl_sync(0xffffffffu, shz, src);
       bool accept = false;
       int c = 0;
       if (t < total) {
@@ -380,11 +398,16 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
         const int fb = s.cl_flags[c];
         const bool haloHalo = !aOwned && !(fb & 1);
         if (!self && canon && !haloHalo && (fb & 2)) {
-          const double *bb = s.cl_bb + 6 * (int64_t)c;
-          const double g0 = gap1(alo[0], ahi[0], bb[0] + hx, bb[3] + hx);
-          const double g1 = gap1(alo[1], ahi[1], bb[1] + hy, bb[4] + hy);
-          const double g2 = gap1(alo[2], ahi[2], bb[2] + hz, bb[5] + hz);
-          accept = (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
+          int sx, sy, sz;
+          shift_of(cd, sx, sy, sz);
+          const float4 blo = s.cl_bbf[2 * (int64_t)c], bhi = s.cl_bbf[2 * (int64_t)c + 1];
+          const float hx = (float)sx * S.lenf[0], hy = (float)sy * S.lenf[1], hz = (float)sz * S.lenf[2];
+          const float g0 = gap1f(alo.x, ahi.x, blo.x + hx, bhi.x + hx);
+          const float g1 = gap1f(alo.y, ahi.y, blo.y + hy, bhi.y + hy);
+          const float g2 = gap1f(alo.z, ahi.z, blo.z + hz, bhi.z + hz);
+          const float d2 = fmaf(g2, g2, fmaf(g1, g1, g0 * g0));
+          accept = d2 <= L2lo;
+          if (!accept && d2 <= L2hi) accept = box_within_fp64(s, S, A, c, cd, L2);
         }
       }
       const unsigned am = __ballot_sync(0xffffffffu, accept);

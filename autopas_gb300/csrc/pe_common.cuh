@@ -43,17 +43,40 @@ struct SysDev {
   int kx, ky;           // neighbour tower reach per dim (ceil(L/side))
   int periodic;
   int tower_base;       // first global tower index
-  // mixed-precision encoding: x' = (x - enc_o) + B in [B, 2B); len split as hi (multiple of ulp(B)) + lo
-  double enc_o[3];
+  // mixed-precision encoding: x' = x + enc_K in [B, 2B) (enc_K = B - o, o = bmin - margin); len split as hi
+  // (a multiple of ulp(B)) + lo
+  double enc_K[3];
   double enc_B;
   float len_hi[3], len_lo[3];
+  // float box tests of the list build: the box and image lengths in float (box rounded outwards), a bound on
+  // the error of one float box gap (outward rounding of both boxes, the shift and the subtraction), and the
+  // resulting bound on |float - FP64| of a squared box distance near (rc+skin)^2
+  float lenf[3], bminf[3], bmaxf[3];
+  float coord_tol;
+  float bb_tol2;
 };
+
+// v = hi + lo for a double v with 2^-74 <= |v| < 2^127: hi keeps the leading 24 significant bits of v
+// (truncated, so for v in [B, 2B) it is a multiple of B * 2^-23 and hi differences are exact), lo is the
+// remaining 29 bits rounded to float.  Integer operations only: this GPU's FP64 pipe (conversions included)
+// runs at 1/64 of the FP32 rate, and this split runs for every particle of every step.
+__device__ __forceinline__ void split_hi_lo(double v, float &hi, float &lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const unsigned long long a = b & 0x7fffffffffffffffull;
+  // (a >> 29) holds the biased double exponent above the top 23 fraction bits: rebias 1023 -> 127
+  hi = __uint_as_float(sign | (unsigned int)((a >> 29) - (896ull << 23)));
+  const unsigned int e = (unsigned int)(a >> 52);
+  const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1023 - 52): weight of the lowest fraction bit
+  lo = __uint_as_float(__float_as_uint(__uint2float_rn((unsigned int)(a & 0x1fffffffull)) * scale) | sign);
+}
 
 // Velocity-Verlet factors per type, computed on the host with the reference's operation order
 // (TimeDiscretization.cpp:42: dt*dt/(2*m); :160: dt/(2*m)) so that no kernel divides in FP64.
 struct VVFactors {
-  double c[kMaxTypes];  // dt*dt / (2 m)
-  double h[kMaxTypes];  // dt / (2 m)
+  double c[kMaxTypes];        // dt*dt / (2 m)
+  double h[kMaxTypes];        // dt / (2 m)
+  float half_mass[kMaxTypes];  // 0.5 m, for the float kinetic energy of the mixed-precision kernels
 };
 
 struct TypeTable {
@@ -84,10 +107,13 @@ __device__ __forceinline__ double image_coord(double x, int s, double len) {
   return s == 0 ? x : __dadd_rn(x, s > 0 ? len : -len);
 }
 
-// Monotone map of a double onto uint64 (for sorting by z).
+// Monotone map of a double onto uint64 (for sorting by z, and for min/max on the integer pipes).
 __device__ __forceinline__ uint64_t dbl_key(double v) {
   uint64_t b = (uint64_t)__double_as_longlong(v);
   return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_dbl(uint64_t k) {
+  return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
 }
 
 // ---- launch wrappers implemented in the .cu files (all asynchronous on `st`) ----

@@ -109,8 +109,9 @@ struct pe_engine {
   // towers / clusters
   int64_t ntowers = 0, nclusters = 0;
   DBuf<int32_t> tw_count, tw_start, tw_cl_start, tw_ncl, tw_fill;
-  DBuf<double> tw_bb;
+  DBuf<float4> tw_bbf;
   DBuf<double> cl_bb;
+  DBuf<float4> cl_bbf;
   DBuf<float2> cl_z;
   DBuf<int32_t> cl_sys, cl_tower, cl_flags, cp_count;
   DBuf<int64_t> cp_start;
@@ -188,8 +189,9 @@ struct pe_engine {
     s.tw_count = tw_count.p;
     s.tw_start = tw_start.p;
     s.tw_cl_start = tw_cl_start.p;
-    s.tw_bb = tw_bb.p;
+    s.tw_bbf = tw_bbf.p;
     s.cl_bb = cl_bb.p;
+    s.cl_bbf = cl_bbf.p;
     s.cl_z = cl_z.p;
     s.cl_sys = cl_sys.p;
     s.cl_tower = cl_tower.p;
@@ -384,10 +386,12 @@ __device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) {
   const SysDev &S = s.sysd[s.sys[i]];
   const double p[3] = {s.x[i], s.y[i], s.z[i]};
   float h[3], l[3];
-  for (int d = 0; d < 3; ++d) {
-    const double xp = (p[d] - S.enc_o[d]) + S.enc_B;
-    h[d] = (float)xp;
-    l[d] = (float)(xp - (double)h[d]);
+  for (int d = 0; d < 3; ++d) split_hi_lo(p[d] + S.enc_K[d], h[d], l[d]);
+  if (o == 0) {
+    // dummies (parked far outside the box) sit at x' = -B: at least 2B from every real particle
+    const float far = -(float)S.enc_B;
+    h[0] = h[1] = h[2] = far;
+    l[0] = l[1] = l[2] = 0.f;
   }
   const int w = (s.type[i] & 0xffff) | (o << 16);
   s.pk[2 * (i)] = make_float4(h[0], h[1], h[2], __int_as_float(w));
@@ -571,12 +575,27 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
   const double M = L + 2.0;
   double ext = 0;
   for (int q = 0; q < 3; ++q) ext = std::max(ext, d.len[q]);
-  // x' = (x - o) + B must stay in [0, 2B) for x in [bmin - M, bmax + M] and for x' +- len (image shifts)
+  // x' = x + (B - o), o = bmin - M, must stay in [0, 2B) for x in [bmin - M, bmax + M] and for x' +- len
+  // (image shifts); it lies in [B, 2B) for the particles themselves
   const double B = next_pow2(2.0 * ext + 2.0 * M + 4.0);
   d.enc_B = B;
   const double ulp = std::ldexp(B, -23);
+  // float box tests of the list build (k_list_build): coordinates stay below Mc in magnitude, so one float
+  // rounding is at most Mc * 2^-24 and a gap (outward-rounded boxes, a rounded shift, one subtraction) is
+  // within 4 roundings, Mc * 2^-22, of its FP64 value; coord_tol doubles that
+  double Mc = 0;
+  for (int q = 0; q < 3; ++q)
+    Mc = std::max(Mc, std::max(std::fabs(d.bmin[q]), std::fabs(d.bmax[q])) + d.len[q] + 2 * L + 2);
+  const double ct = Mc * std::ldexp(1.0, -21);
+  d.coord_tol = (float)ct;
+  d.bb_tol2 = (float)(2.0 * (3.0 * (2.0 * (L + ct) * ct + ct * ct) + 8.0 * std::ldexp(L * L, -24)) + 1e-30);
   for (int q = 0; q < 3; ++q) {
-    d.enc_o[q] = d.bmin[q] - M;
+    d.lenf[q] = (float)d.len[q];
+    d.bminf[q] = std::nextafter((float)d.bmin[q], -INFINITY);
+    d.bmaxf[q] = std::nextafter((float)d.bmax[q], INFINITY);
+  }
+  for (int q = 0; q < 3; ++q) {
+    d.enc_K[q] = B - (d.bmin[q] - M);
     const double hi = std::nearbyint(d.len[q] / ulp) * ulp;  // a multiple of ulp(B): exact in float
     d.len_hi[q] = (float)hi;
     d.len_lo[q] = (float)(d.len[q] - hi);
@@ -675,7 +694,7 @@ static int setup_grids(pe_engine *h) {
                              cudaMemcpyHostToDevice, h->st));
   const size_t nt = (size_t)h->ntowers;
   if (!h->tw_count.ensure(nt) || !h->tw_start.ensure(nt + 1) || !h->tw_cl_start.ensure(nt + 1) ||
-      !h->tw_ncl.ensure(nt) || !h->tw_fill.ensure(nt) || !h->tw_bb.ensure(4 * nt))
+      !h->tw_ncl.ensure(nt) || !h->tw_fill.ensure(nt) || !h->tw_bbf.ensure(nt))
     return h->fail(PE_ERR_OOM, "tower arrays (%lld towers)", (long long)nt);
   // slot capacity: every tower can add at most C-1 padding dummies
   h->pcap = h->nuser + (int64_t)nt * (h->C - 1) + 64;
@@ -688,7 +707,7 @@ static int ensure_particle_capacity(pe_engine *h) {
       !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
-  if (!h->cl_bb.ensure(6 * ncl) || !h->cl_z.ensure(ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
+  if (!h->cl_bb.ensure(6 * ncl) || !h->cl_bbf.ensure(2 * ncl) || !h->cl_z.ensure(ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
       !h->cp_count.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(kGlob * ncl) ||
       !h->cl_hits.ensure(ncl) || !h->key.ensure(n) || !h->skey.ensure(n) || !h->tower_of.ensure(n) ||
       !h->sval.ensure(n) || !h->perm_src.ensure(n) || !h->cp_total.ensure(1) || !h->derr.ensure(1) ||
@@ -865,6 +884,7 @@ static VVFactors vv_factors(const pe_engine *h, double dt) {
     const double m = h->mass[t];
     v.c[t] = dt * dt / (2 * m);
     v.h[t] = dt / (2 * m);
+    v.half_mass[t] = (float)(0.5 * m);
   }
   return v;
 }
@@ -1093,12 +1113,14 @@ int pe_destroy(pe_engine *h) {
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})
     b->release();
-  for (auto *b : {&h->tw_bb, &h->cl_bb, &h->cl_glob, &h->sys_glob, &h->dmass, &h->tmp3}) b->release();
+  for (auto *b : {&h->cl_bb, &h->cl_glob, &h->sys_glob, &h->dmass, &h->tmp3}) b->release();
   for (auto *b : {&h->cp_start, &h->sys_cl_range, &h->dump_a, &h->dump_b, &h->chunks}) b->release();
   h->sys_chunk0.release();
   h->chunk_part.release();
   h->cp_list.release();
   h->cl_z.release();
+  h->cl_bbf.release();
+  h->tw_bbf.release();
   h->cp_total.release();
   h->cl_hits.release();
   h->dump_n.release();

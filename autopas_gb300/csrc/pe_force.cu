@@ -511,26 +511,36 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
                                                      tab, T, band, acc, nullptr, 0.f);
   }
   acc.flush();
-  const double Fx = (double)acc.fxs - (double)acc.fxc, Fy = (double)acc.fys - (double)acc.fyc,
-               Fz = (double)acc.fzs - (double)acc.fzc;
-  double ek = 0.0;
+  // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
+  // epilogue keeps to the FP64 work the state needs: the force rounded once from its compensated sum, the
+  // velocity half in FP64 with the reference's operation order.  Per-particle globals, the kinetic energy
+  // included, are float values summed over the cluster's lanes in float and widened once per cluster.
+  const double Fx = (double)(acc.fxs - acc.fxc), Fy = (double)(acc.fys - acc.fyc), Fz = (double)(acc.fzs - acc.fzc);
+  float ek = 0.f;
   if (oi == 1) {
     s.fx[i] = Fx;
     s.fy[i] = Fy;
     s.fz[i] = Fz;
+    double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
     if (fa.fuse_velocity) {
       const double h = fa.vv.h[ti];
-      s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
-      s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
-      s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
+      vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
+      vy = __dadd_rn(vy, __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
+      vz = __dadd_rn(vz, __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
+      s.vx[i] = vx;
+      s.vy[i] = vy;
+      s.vz[i] = vz;
     }
-    if (GLOB) ek = kinetic(s, i, ti);
+    if (GLOB) {
+      const float ux = (float)vx, uy = (float)vy, uz = (float)vz;
+      ek = fa.vv.half_mass[ti] * fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+    }
   }
   if (GLOB) {
     const bool owned = oi == 1;
-    double g0 = owned ? (double)acc.pot : 0.0, g1 = owned ? (double)acc.vx : 0.0;
-    double g2 = owned ? (double)acc.vy : 0.0, g3 = owned ? (double)acc.vz : 0.0;
-    long long h = owned ? (long long)(acc.hits + acc.hhalo) : 0;
+    float g0 = owned ? acc.pot : 0.f, g1 = owned ? acc.vx : 0.f, g2 = owned ? acc.vy : 0.f;
+    float g3 = owned ? acc.vz : 0.f;
+    int h = owned ? acc.hits + acc.hhalo : 0;
 #pragma unroll
     for (int o = 1; o < C; o <<= 1) {
       g0 += __shfl_xor_sync(0xffffffffu, g0, o);
@@ -542,11 +552,11 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     }
     if (inrange && (i % C) == 0) {
       const int64_t cl = i / C;
-      s.cl_glob[kGlob * cl + 0] = g0;
-      s.cl_glob[kGlob * cl + 1] = g1;
-      s.cl_glob[kGlob * cl + 2] = g2;
-      s.cl_glob[kGlob * cl + 3] = g3;
-      s.cl_glob[kGlob * cl + 4] = ek;
+      s.cl_glob[kGlob * cl + 0] = (double)g0;
+      s.cl_glob[kGlob * cl + 1] = (double)g1;
+      s.cl_glob[kGlob * cl + 2] = (double)g2;
+      s.cl_glob[kGlob * cl + 3] = (double)g3;
+      s.cl_glob[kGlob * cl + 4] = (double)ek;
       s.cl_hits[cl] = (unsigned long long)h;
     }
   }
@@ -707,7 +717,7 @@ static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, c
 
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
                   const VVFactors *vv) {
-  ForceArgs fa;
+  ForceArgs fa{};
   if (vv) fa.vv = *vv;
   fa.rc2 = s.cutoff * s.cutoff;
   fa.rc2f = (float)fa.rc2;

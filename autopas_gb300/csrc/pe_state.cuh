@@ -29,8 +29,10 @@ struct DeviceState {
   int32_t *tw_count = nullptr;     // [ntowers]
   int32_t *tw_start = nullptr;     // [ntowers+1] exclusive scan of counts (compact order)
   int32_t *tw_cl_start = nullptr;  // [ntowers+1] first cluster of each tower
-  double *tw_bb = nullptr;         // [ntowers*4] xy bbox of the tower's particles (minx,miny,maxx,maxy)
+  float4 *tw_bbf = nullptr;        // [ntowers] xy bbox of the tower's particles (minx,miny,maxx,maxy), rounded
+                                   // outwards to float
   double *cl_bb = nullptr;         // [nclusters*6] lo xyz, hi xyz (real members only)
+  float4 *cl_bbf = nullptr;        // [nclusters*2] the same box rounded outwards to float: lo xyz, hi xyz
   float2 *cl_z = nullptr;          // [nclusters] z range rounded outwards to float (window search only)
   int32_t *cl_sys = nullptr;       // [nclusters]
   int32_t *cl_tower = nullptr;     // [nclusters]
