@@ -991,7 +991,7 @@ static int tune(pe_engine *h, int samples) {
   const int rebuilds = (int)h->rebuilds;
   for (int C : Cs)
     for (int T : Ts) {
-      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 2) : 1;
+      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : 1;
       for (int v = 0; v < nv; ++v) {
         PE_TRY(apply_config(h, C, T, v));
         std::vector<float> t;

@@ -404,11 +404,18 @@ struct MixedAcc {
   }
 };
 
+// List entries are read once per launch: with STREAM they are loaded with the evict-first (streaming) cache
+// hint, so that the gathered positions keep the caches.
+template <bool STREAM>
+__device__ __forceinline__ uint32_t list_entry(const uint32_t *p) {
+  return STREAM ? __ldcs(p) : __ldg(p);
+}
+
 // One thread's walk over its list (UNROLL entries per batch; the list entries of the next batch are loaded while
 // the current batch's positions are gathered and evaluated, so the dependent list -> position chain overlaps
 // arithmetic).  With REPRUNE the walk reads the outer list (rc + skin) and also writes the entries within
 // lim to the inner list out; it returns their number.
-template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool REPRUNE>
+template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool REPRUNE, bool STREAM>
 __device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                           const float4 &hi_i, const float4 &lo_i, int ti,
                                           const uint32_t *__restrict__ lp, int n, float eps24, float sig2, float sh6,
@@ -420,7 +427,7 @@ __device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S,
   uint32_t ent[UNROLL];
   if (UNROLL <= n) {
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) ent[u] = __ldg(lp + (int64_t)u * stride);
+    for (int u = 0; u < UNROLL; ++u) ent[u] = list_entry<STREAM>(lp + (int64_t)u * stride);
   }
   for (; k + UNROLL <= n; k += UNROLL) {
     float4 hj[UNROLL], lj[UNROLL];
@@ -433,7 +440,8 @@ __device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S,
     uint32_t nxt[UNROLL];
     const bool more = k + 2 * UNROLL <= n;
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) nxt[u] = more ? __ldg(lp + (int64_t)(k + UNROLL + u) * stride) : 0u;
+    for (int u = 0; u < UNROLL; ++u)
+      nxt[u] = more ? list_entry<STREAM>(lp + (int64_t)(k + UNROLL + u) * stride) : 0u;
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
@@ -444,12 +452,69 @@ __device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S,
     for (int u = 0; u < UNROLL; ++u) ent[u] = nxt[u];
   }
   for (; k < n; ++k) {
-    const uint32_t e = __ldg(lp + (int64_t)k * stride);
+    const uint32_t e = list_entry<STREAM>(lp + (int64_t)k * stride);
     const float4 *q = s.pk + 2 * (int64_t)(e >> 5);
     const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, e, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
     if (REPRUNE && r2 <= lim) out[(int64_t)(m++) * stride] = e;
   }
   return m;
+}
+
+// A deeper pipeline: while batch k is evaluated, the positions of batch k+1 and the list entries of batch k+2
+// are in flight.  Entries past the end of the list read slot 0 (a valid address) and are never evaluated.
+template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL>
+__device__ __forceinline__ void plist_walk_deep(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                                const float4 &hi_i, const float4 &lo_i, int ti,
+                                                const uint32_t *__restrict__ lp, int n, float eps24, float sig2,
+                                                float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
+                                                float band, MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc) {
+  const int64_t stride = s.pl_stride;
+  int k = 0;
+  uint32_t e0[UNROLL], e1[UNROLL];
+  float4 h0[UNROLL], l0[UNROLL];
+  if (UNROLL <= n) {
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) e0[u] = list_entry<true>(lp + (int64_t)u * stride);
+    const bool more = 2 * UNROLL <= n;
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) e1[u] = more ? list_entry<true>(lp + (int64_t)(UNROLL + u) * stride) : 0u;
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const float4 *q = s.pk + 2 * (int64_t)(e0[u] >> 5);
+      h0[u] = __ldg(q);
+      l0[u] = __ldg(q + 1);
+    }
+  }
+  for (; k + UNROLL <= n; k += UNROLL) {
+    float4 h1[UNROLL], l1[UNROLL];
+    uint32_t e2[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const float4 *q = s.pk + 2 * (int64_t)(e1[u] >> 5);
+      h1[u] = __ldg(q);
+      l1[u] = __ldg(q + 1);
+    }
+    const bool more2 = k + 3 * UNROLL <= n;
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u)
+      e2[u] = more2 ? list_entry<true>(lp + (int64_t)(k + 2 * UNROLL + u) * stride) : 0u;
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u)
+      acc.pair(s, S, fa, i, hi_i, lo_i, ti, e0[u], h0[u], l0[u], eps24, sig2, sh6, tab, T, band);
+    acc.flush();
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      e0[u] = e1[u];
+      h0[u] = h1[u];
+      l0[u] = l1[u];
+      e1[u] = e2[u];
+    }
+  }
+  for (; k < n; ++k) {
+    const uint32_t e = list_entry<true>(lp + (int64_t)k * stride);
+    const float4 *q = s.pk + 2 * (int64_t)(e >> 5);
+    acc.pair(s, S, fa, i, hi_i, lo_i, ti, e, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
+  }
 }
 
 // MINB: minimum resident blocks per SM requested from the compiler (caps registers for more warps in flight).
@@ -458,8 +523,10 @@ __device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S,
 // entries within rc + buffer (or the whole outer list once the particles have used up the skin beyond the
 // buffer since the rebuild) to the inner lists and records the positions of the prune.  The flag is read
 // by every thread and cleared by a later launch, so all threads take the same branch.
-template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB>
+// PIPE: bit 0 streams the list entries past the caches, bit 1 selects the deeper pipeline
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, int PIPE>
 __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
+  constexpr bool STREAM = (PIPE & 1) != 0, DEEP = (PIPE & 2) != 0;
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
   const int T = s.ntypes;
   if (!ONE_TYPE) {
@@ -496,7 +563,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   if (reprune) {
     const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
     // single-entry batches: this branch runs once per prune, and fewer live registers keep the other one spill-free
-    const int m = plist_walk<GLOB, ONE_TYPE, KAHAN, 1, true>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list + i, n, eps24,
+    const int m = plist_walk<GLOB, ONE_TYPE, KAHAN, 1, true, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list + i, n, eps24,
                                                                   sig2, sh6, tab, T, band, acc, s.pi_list + i, lim);
     if (inrange) {
       s.pi_count[i] = m;
@@ -506,9 +573,12 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
         s.x_prune[3 * i + 2] = s.z[i];
       }
     }
+  } else if (DEEP) {
+    plist_walk_deep<GLOB, ONE_TYPE, KAHAN, UNROLL>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list + i, n, eps24, sig2, sh6,
+                                                   tab, T, band, acc);
   } else {
-    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, false>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list + i, n, eps24, sig2, sh6,
-                                                     tab, T, band, acc, nullptr, 0.f);
+    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, false, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list + i, n, eps24,
+                                                             sig2, sh6, tab, T, band, acc, nullptr, 0.f);
   }
   acc.flush();
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
@@ -663,13 +733,23 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
     return;
   }
   // kernel variants, chosen by the engine's tuner: list entries batched by 2 under a cap of 64 registers
-  // (8 blocks of 128 threads per SM) or by 4 under a cap of 80 (6 blocks); tighter caps spill
+  // (8 blocks of 128 threads per SM) or by 4 under a cap of 80 (6 blocks); list entries cached or streamed;
+  // positions gathered one batch ahead (up to 102 registers, 5 blocks).  Tighter register caps spill.
 #define PE_PLIST(G, O)                                                                   \
   do {                                                                                   \
-    if (s.variant == 1)                                                                  \
-      k_lj_mixed_plist<C, G, O, true, 4, 6><<<(unsigned)nb, 128, 0, st>>>(s, fa);        \
-    else                                                                                 \
-      k_lj_mixed_plist<C, G, O, true, 2, 8><<<(unsigned)nb, 128, 0, st>>>(s, fa);        \
+    switch (s.variant) {                                                                 \
+      case 1:                                                                            \
+        k_lj_mixed_plist<C, G, O, true, 4, 6, 0><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        break;                                                                           \
+      case 2:                                                                            \
+        k_lj_mixed_plist<C, G, O, true, 2, 8, 1><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        break;                                                                           \
+      case 3:                                                                            \
+        k_lj_mixed_plist<C, G, O, true, 2, 5, 3><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        break;                                                                           \
+      default:                                                                           \
+        k_lj_mixed_plist<C, G, O, true, 2, 8, 0><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+    }                                                                                    \
   } while (0)
   if (s.ntypes == 1) {
     if (fa.calc_globals)
