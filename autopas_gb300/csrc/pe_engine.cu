@@ -381,10 +381,10 @@ __global__ void k_wrap(DeviceState s, int64_t n) {
   s.z[i] = wrap1(s.z[i], S.bmin[2], S.bmax[2]);
 }
 
-__device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) {
+__device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double px, double py, double pz) {
   const int o = s.own[i];
   const SysDev &S = s.sysd[s.sys[i]];
-  const double p[3] = {s.x[i], s.y[i], s.z[i]};
+  const double p[3] = {px, py, pz};
   float h[3], l[3];
   for (int d = 0; d < 3; ++d) split_hi_lo(p[d] + S.enc_K[d], h[d], l[d]);
   if (o == 0) {
@@ -397,6 +397,8 @@ __device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) {
   s.pk[2 * (i)] = make_float4(h[0], h[1], h[2], __int_as_float(w));
   s.pk[2 * (i) + 1] = make_float4(l[0], l[1], l[2], 0.f);
 }
+
+__device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) { pack_xyz(s, i, s.x[i], s.y[i], s.z[i]); }
 
 __global__ void k_pack(DeviceState s, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -502,6 +504,32 @@ __global__ void k_from_user(double *__restrict__ a, const int32_t *__restrict__ 
                             const double *__restrict__ in) {
   const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (u < n) a[slot_of[u]] = in[u];
+}
+
+// user-order positions read straight from page-locked host memory (device mapping of the host buffers),
+// scattered into slot order and re-encoded in the same pass
+__global__ void k_positions_from_host(DeviceState s, int64_t n, const double *__restrict__ hx,
+                                      const double *__restrict__ hy, const double *__restrict__ hz) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int32_t q = s.slot_of[u];
+  const double x = hx[u], y = hy[u], z = hz[u];
+  s.x[q] = x;
+  s.y[q] = y;
+  s.z[q] = z;
+  pack_xyz(s, q, x, y, z);
+}
+
+// forces of owned particles in user order, written straight into page-locked host memory
+__global__ void k_forces_to_host(DeviceState s, int64_t n, double *__restrict__ hx, double *__restrict__ hy,
+                                 double *__restrict__ hz) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int32_t q = s.slot_of[u];
+  const bool owned = s.own[q] == 1;
+  hx[u] = owned ? s.fx[q] : 0.0;
+  hy[u] = owned ? s.fy[q] : 0.0;
+  hz[u] = owned ? s.fz[q] : 0.0;
 }
 
 }  // namespace pe
@@ -1209,10 +1237,33 @@ int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, 
   return h->cuda_check("set_particles");
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister), or null for any other
+// memory.  Kernels read and write such buffers directly (over NVLink-C2C on a Grace-Blackwell node), which
+// fuses the transfer with the permutation between user and slot order.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
 int pe_update_positions(pe_engine *h, const double *x, const double *y, const double *z) {
   if (!h || !x || !y || !z) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
   const int64_t n = h->nuser;
+  {
+    const double *mx = (const double *)mapped_host(x), *my = (const double *)mapped_host(y),
+                 *mz = (const double *)mapped_host(z);
+    if (mx && my && mz) {
+      DeviceState s = h->state();
+      if (n > 0) k_positions_from_host<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(s, n, mx, my, mz);
+      h->launches += 1;
+      PE_CUDA(h, cudaStreamSynchronize(h->st));
+      return h->cuda_check("update_positions");
+    }
+  }
   if (!h->tmp3.ensure(3 * (size_t)std::max<int64_t>(n, 1))) return h->fail(PE_ERR_OOM, "tmp");
   cudaStream_t st = h->st;
   const double *src[3] = {x, y, z};
@@ -1250,6 +1301,16 @@ int pe_get_forces(pe_engine *h, double *fx, double *fy, double *fz) {
   if (!h) return PE_ERR_ARG;
   if (!h->forces_valid) return h->fail(PE_ERR_STATE, "no forces computed");
   const int64_t n = h->nuser;
+  if (fx && fy && fz) {
+    double *mx = (double *)mapped_host(fx), *my = (double *)mapped_host(fy), *mz = (double *)mapped_host(fz);
+    if (mx && my && mz) {
+      DeviceState s = h->state();
+      if (n > 0) k_forces_to_host<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(s, n, mx, my, mz);
+      h->launches += 1;
+      PE_CUDA(h, cudaStreamSynchronize(h->st));
+      return h->cuda_check("get_forces");
+    }
+  }
   if (!h->tmp3.ensure(3 * (size_t)std::max<int64_t>(n, 1))) return h->fail(PE_ERR_OOM, "tmp");
   double *outs[3] = {fx, fy, fz};
   const double *src[3] = {h->A.fx.p, h->A.fy.p, h->A.fz.p};

@@ -202,6 +202,10 @@ class PairEngine:
         x, y, z = (np.ascontiguousarray(pos[:, d]) for d in range(3))
         self._check(self._L.pe_update_positions(self._h, _ptr(x), _ptr(y), _ptr(z)))
 
+    def update_positions_soa(self, x, y, z):
+        """Zero-copy variant: contiguous float64 arrays; page-locked ones are read by the GPU directly."""
+        self._check(self._L.pe_update_positions(self._h, _ptr(x), _ptr(y), _ptr(z)))
+
     def rebuild(self):
         self._check(self._L.pe_rebuild(self._h))
 
