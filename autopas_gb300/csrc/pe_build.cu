@@ -110,10 +110,13 @@ __global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, c
     if (threadIdx.x == 0) atomicOr(s.err, kErrTowerOverflow);
     return;
   }
+  // the tower's own power of two (p2 sizes the shared arrays for the largest tower)
+  int lp2 = 2;
+  while (lp2 < n) lp2 <<= 1;
   // tower xy bbox on the monotone integer keys of the coordinates (min/max on the integer pipes; the FP64
   // pipe of this GPU is 1/64 of FP32), decoded once per tower
   uint64_t mnx = ~0ull, mny = ~0ull, mxx = 0ull, mxy = 0ull;
-  for (int q = threadIdx.x; q < p2; q += blockDim.x) {
+  for (int q = threadIdx.x; q < lp2; q += blockDim.x) {
     if (q < n) {
       const int32_t v = sval[base + q];
       k[q] = skey[base + q];
@@ -158,10 +161,10 @@ __global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, c
                         : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
   }
   // bitonic sort, ascending on (k, tie)
-  for (int size = 2; size <= p2; size <<= 1) {
+  for (int size = 2; size <= lp2; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
       __syncthreads();
-      for (int q = threadIdx.x; q < (p2 >> 1); q += blockDim.x) {
+      for (int q = threadIdx.x; q < (lp2 >> 1); q += blockDim.x) {
         const int lo = 2 * q - (q & (stride - 1));
         const int hi = lo + stride;
         const bool asc = ((lo & size) == 0);
@@ -462,75 +465,91 @@ void launch_list_build(DeviceState &s, cudaStream_t st) {
 // ---------------------------------------------------------------------------------------------
 // 6. particle neighbour lists from the (full) cluster-pair lists: every j within rc+skin of an owned i,
 //    tested on the hi/lo float positions with a relative margin of 1e-5 on (rc+skin)^2 (the float distance is
-//    within ~1e-7 of the FP64 one, so the list is a superset of the FP64 rc+skin pair set).  Lanes append in
-//    (entry, j-lane) order via ballots, so every list has a deterministic order.
+//    within ~1e-7 of the FP64 one, so the list is a superset of the FP64 rc+skin pair set).  Every list is
+//    appended in (cluster-pair entry, j) order, so it has a deterministic order.
 // ---------------------------------------------------------------------------------------------
+// One warp serves 32/C i-clusters, C lanes each (lane = one i particle).  For each cluster-pair entry the C lanes of
+// a group stage the C particles of the j-cluster in shared memory, then every lane tests its i against all of
+// them and appends the survivors to its own row in (entry, j) order.
 template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
-  constexpr int JL = 32 / C;
-  constexpr int EPI = 64 / (C * C);
-  const int lane = threadIdx.x & 31;
-  const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (A >= s.nclusters) return;
-  const int n = s.cp_count[A];
-  const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
-  const int ii = lane % C, jl = lane / C;
+  constexpr int G = 32 / C;
+  __shared__ float4 sj[4][G][C][2];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / C, ii = lane % C;
+  const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + g;
+  const bool validA = A < s.nclusters;
   const int64_t i = A * C + ii;
-  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
-  const int oi = __float_as_int(hi_i.w) >> 16;
-  const SysDev &S = s.sysd[s.cl_sys[A]];
-  const unsigned same_i = (C == 8 ? 0x01010101u : 0x11111111u) << ii;
-  const unsigned lt = (1u << lane) - 1;
-  const int cap = s.pl_cap;
-  int cnt = 0;
-  for (int e = 0; e < n; e += EPI) {
+  int n = 0, oi = 0;
+  const uint32_t *lst = s.cp_list;
+  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+  int sy = 0;
+  if (validA) {
+    n = s.cp_count[A];
+    lst = s.cp_list + s.cp_start[A];
+    hi_i = s.pk[2 * i];
+    lo_i = s.pk[2 * i + 1];
+    oi = __float_as_int(hi_i.w) >> 16;
+    sy = s.cl_sys[A];
+  }
+  const SysDev &S = s.sysd[sy];
+  int nmax = n;
 #pragma unroll
-    for (int p = 0; p < 2; ++p) {
-      const int f = jl + p * JL;
-      const int ee = e + f / C;
-      const int jj = f % C;
-      bool keep = false;
-      uint32_t ent = 0;
-      if (ee < n && oi == 1) {
-        ent = __ldg(lst + ee);
-        const int64_t j = (int64_t)(ent >> 5) * C + jj;
-        const int code = ent & 31;
-        const float4 hj = __ldg(&s.pk[2 * (j)]);
-        const float4 lj = __ldg(&s.pk[2 * (j) + 1]);
-        float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-        if (code != kShiftNone) {
-          const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
-          xh = fmaf(-sxf, S.len_hi[0], xh);
-          yh = fmaf(-syf, S.len_hi[1], yh);
-          zh = fmaf(-szf, S.len_hi[2], zh);
-          xl = fmaf(-sxf, S.len_lo[0], xl);
-          yl = fmaf(-syf, S.len_lo[1], yl);
-          zl = fmaf(-szf, S.len_lo[2], zl);
-        }
+  for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+  const int cap = s.pl_cap;
+  const int64_t stride = s.pl_stride;
+  int cnt = 0;
+  for (int e = 0; e < nmax; ++e) {
+    const bool act = e < n;
+    uint32_t ent = 0;
+    if (act) {
+      ent = __ldg(lst + e);
+      const int64_t j = (int64_t)(ent >> 5) * C + ii;
+      sj[w][g][ii][0] = __ldg(&s.pk[2 * j]);
+      sj[w][g][ii][1] = __ldg(&s.pk[2 * j + 1]);
+    }
+    __syncwarp();
+    if (act && oi == 1) {
+      const int code = ent & 31;
+      float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+      if (code != kShiftNone) {
+        const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+        xh = fmaf(-sxf, S.len_hi[0], xh);
+        yh = fmaf(-syf, S.len_hi[1], yh);
+        zh = fmaf(-szf, S.len_hi[2], zh);
+        xl = fmaf(-sxf, S.len_lo[0], xl);
+        yl = fmaf(-syf, S.len_lo[1], yl);
+        zl = fmaf(-szf, S.len_lo[2], zl);
+      }
+      const uint32_t jbase = (ent >> 5) * (uint32_t)C;
+#pragma unroll
+      for (int jj = 0; jj < C; ++jj) {
+        const float4 hj = sj[w][g][jj][0], lj = sj[w][g][jj][1];
         const float dx = (xh - hj.x) + (xl - lj.x);
         const float dy = (yh - hj.y) + (yl - lj.y);
         const float dz = (zh - hj.z) + (zl - lj.z);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        keep = (r2 > 0.f) && (r2 <= L2f) && ((__float_as_int(hj.w) >> 16) != 0);
-        ent = ((uint32_t)j << 5) | (uint32_t)code;
+        if ((r2 > 0.f) && (r2 <= L2f) && ((__float_as_int(hj.w) >> 16) != 0)) {
+          if (cnt < cap) s.pl_list[(int64_t)cnt * stride + i] = ((jbase + (uint32_t)jj) << 5) | (uint32_t)code;
+          ++cnt;
+        }
       }
-      const unsigned mine = __ballot_sync(0xffffffffu, keep) & same_i;
-      const int k = cnt + __popc(mine & lt);
-      if (keep && k < cap) s.pl_list[(int64_t)k * s.pl_stride + i] = ent;
-      cnt += __popc(mine);
     }
+    __syncwarp();
   }
-  if (jl == 0) {
-    s.pl_count[i] = cnt;
-    if (cnt > 0) atomicMax(s.pl_max, cnt);
-  }
+  if (validA) s.pl_count[i] = cnt;
+  int mx = cnt;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0 && mx > 0) atomicMax(s.pl_max, mx);
 }
 
 void launch_plist_build(DeviceState &s, cudaStream_t st) {
   const double L = s.cutoff + s.skin;
   const float L2f = (float)(L * L * (1.0 + 1e-5));
   cudaMemsetAsync(s.pl_max, 0, sizeof(int), st);
-  const int64_t nb = (s.nclusters + 3) / 4;
+  const int64_t per_block = 4 * (32 / s.C);  // i-clusters per block of 4 warps
+  const int64_t nb = (s.nclusters + per_block - 1) / per_block;
   if (nb == 0) return;
   if (s.C == 4)
     k_plist_build<4><<<(unsigned)nb, 128, 0, st>>>(s, L2f);

@@ -812,11 +812,40 @@ void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_vel
 
 // ---------------------------------------------------------------------------------------------
 // per-system globals: the clusters of each system are cut into chunks of at most kChunk clusters; one block
-// reduces each chunk (fixed thread assignment and tree), then one thread per system adds its chunks in
-// order, so the result is bitwise reproducible.  LJFunctor::endTraversal post-processing (x0.5, /6;
+// reduces each chunk (fixed thread assignment and tree), then one block per system reduces its chunk sums
+// the same way, so the result is bitwise reproducible.  LJFunctor::endTraversal post-processing (x0.5, /6;
 // LJFunctor.h:661-685) is applied at the end.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, double *__restrict__ cpart) {
+// fixed-order sum of kGlob doubles and a count over a 256-thread block: warp trees, then warp 0 over the
+// eight warp sums.  Thread 0 returns the result.
+__device__ __forceinline__ void block_sum6(double (&g)[kGlob], long long &h) {
+  __shared__ double wred[8][kGlob];
+  __shared__ long long wh[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int q = 0; q < kGlob; ++q) g[q] += __shfl_xor_sync(0xffffffffu, g[q], o);
+    h += __shfl_xor_sync(0xffffffffu, h, o);
+  }
+  if (lane == 0) {
+    for (int q = 0; q < kGlob; ++q) wred[w][q] = g[q];
+    wh[w] = h;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < kGlob; ++q) g[q] = wred[0][q];
+    h = wh[0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      for (int q = 0; q < kGlob; ++q) g[q] += wred[k][q];
+      h += wh[k];
+    }
+  }
+}
+
+// one block of 256 threads per chunk of at most kChunk = 256 clusters: one cluster per thread
+__global__ void __launch_bounds__(256) k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks,
+                                                        double *__restrict__ cpart) {
   const int64_t c0 = chunks[3 * blockIdx.x + 1], c1 = chunks[3 * blockIdx.x + 2];
   double g[kGlob] = {0, 0, 0, 0, 0};
   long long h = 0;
@@ -825,33 +854,25 @@ __global__ void k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunk
     for (int q = 0; q < kGlob; ++q) g[q] += s.cl_glob[kGlob * c + q];
     h += (long long)s.cl_hits[c];
   }
-  __shared__ double red[kGlob][256];
-  __shared__ long long redh[256];
-  for (int q = 0; q < kGlob; ++q) red[q][threadIdx.x] = g[q];
-  redh[threadIdx.x] = h;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      for (int q = 0; q < kGlob; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
-      redh[threadIdx.x] += redh[threadIdx.x + o];
-    }
-    __syncthreads();
-  }
+  block_sum6(g, h);
   if (threadIdx.x == 0) {
-    for (int q = 0; q < kGlob; ++q) cpart[(kGlob + 1) * blockIdx.x + q] = red[q][0];
-    cpart[(kGlob + 1) * blockIdx.x + kGlob] = (double)redh[0];
+    for (int q = 0; q < kGlob; ++q) cpart[(kGlob + 1) * blockIdx.x + q] = g[q];
+    cpart[(kGlob + 1) * blockIdx.x + kGlob] = (double)h;
   }
 }
 
-__global__ void k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0, const double *__restrict__ cpart) {
-  const int sy = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sy >= s.nsys) return;
+// one block per system over its chunk partials (fixed assignment and tree), then the endTraversal scaling
+__global__ void __launch_bounds__(256) k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0,
+                                                         const double *__restrict__ cpart) {
+  const int sy = blockIdx.x;
   double g[kGlob] = {0, 0, 0, 0, 0};
-  double h = 0;
-  for (int k = sys_chunk0[sy]; k < sys_chunk0[sy + 1]; ++k) {
+  long long hh = 0;
+  for (int k = sys_chunk0[sy] + threadIdx.x; k < sys_chunk0[sy + 1]; k += blockDim.x) {
     for (int q = 0; q < kGlob; ++q) g[q] += cpart[(kGlob + 1) * k + q];
-    h += cpart[(kGlob + 1) * k + kGlob];
+    hh += (long long)cpart[(kGlob + 1) * k + kGlob];
   }
+  block_sum6(g, hh);
+  if (threadIdx.x != 0) return;
   const double up = g[0] * 0.5 / 6.;
   const double vx = g[1] * 0.5, vy = g[2] * 0.5, vz = g[3] * 0.5;
   s.sys_glob[kSysGlob * sy + 0] = up;
@@ -860,7 +881,7 @@ __global__ void k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_
   s.sys_glob[kSysGlob * sy + 3] = vy;
   s.sys_glob[kSysGlob * sy + 4] = vz;
   s.sys_glob[kSysGlob * sy + 5] = g[4];
-  const long long pairs = (long long)(h + 0.5) / 2;
+  const long long pairs = hh / 2;
   s.sys_hits[sy] = pairs;
   atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)pairs);
 }
@@ -868,7 +889,7 @@ __global__ void k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
                            double *cpart, cudaStream_t st) {
   if (nchunks > 0) k_reduce_chunks<<<nchunks, 256, 0, st>>>(s, chunks, cpart);
-  if (s.nsys > 0) k_reduce_systems<<<(s.nsys + 127) / 128, 128, 0, st>>>(s, sys_chunk0, cpart);
+  if (s.nsys > 0) k_reduce_systems<<<s.nsys, 256, 0, st>>>(s, sys_chunk0, cpart);
 }
 
 }  // namespace pe
