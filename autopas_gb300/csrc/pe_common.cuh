@@ -47,6 +47,7 @@ struct SysDev {
   // (a multiple of ulp(B)) + lo
   double enc_K[3];
   double enc_B;
+  float enc_far;  // -B: where dummies sit in the encoded frame, at least 2B from every real particle
   float len_hi[3], len_lo[3];
   // float box tests of the list build: the box and image lengths in float (box rounded outwards), a bound on
   // the error of one float box gap (outward rounding of both boxes, the shift and the subtraction), and the

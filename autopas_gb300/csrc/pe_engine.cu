@@ -389,8 +389,7 @@ __device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double
   for (int d = 0; d < 3; ++d) split_hi_lo(p[d] + S.enc_K[d], h[d], l[d]);
   if (o == 0) {
     // dummies (parked far outside the box) sit at x' = -B: at least 2B from every real particle
-    const float far = -(float)S.enc_B;
-    h[0] = h[1] = h[2] = far;
+    h[0] = h[1] = h[2] = S.enc_far;
     l[0] = l[1] = l[2] = 0.f;
   }
   const int w = (s.type[i] & 0xffff) | (o << 16);
@@ -607,6 +606,7 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
   // (image shifts); it lies in [B, 2B) for the particles themselves
   const double B = next_pow2(2.0 * ext + 2.0 * M + 4.0);
   d.enc_B = B;
+  d.enc_far = (float)(-B);
   const double ulp = std::ldexp(B, -23);
   // float box tests of the list build (k_list_build): coordinates stay below Mc in magnitude, so one float
   // rounding is at most Mc * 2^-24 and a gap (outward-rounded boxes, a rounded shift, one subtraction) is

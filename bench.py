@@ -374,7 +374,7 @@ def run_ours(args):
         "upot_last_step": g_last["upot"], "rebuilds_in_timed_region": st["rebuilds"],
         "prunes_in_timed_region": st["prunes"],
         "engine": {k: info[k] for k in ("cluster_size", "traversal", "num_clusters", "num_cluster_pairs",
-                                        "max_tower_size", "num_towers", "list_capacity")},
+                                        "max_tower_size", "num_towers", "list_capacity", "num_list_entries")},
         "tuning": tuning,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
