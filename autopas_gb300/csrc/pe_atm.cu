@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
     float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t ent = 0;
     if (k < n) {
-      ent = s.pl_list[(int64_t)k * s.pl_stride + i];
+      ent = s.pl_list[plist_index(s.pl_stride, i, k)];
       const int64_t j = ent >> 5;
       const int code = ent & 31;
       const float4 hj = s.pk[2 * (j)], lj = s.pk[2 * (j) + 1];

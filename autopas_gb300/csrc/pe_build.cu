@@ -475,6 +475,7 @@ template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   constexpr int G = 32 / C;
   __shared__ float4 sj[4][G][C][2];
+  __shared__ __align__(16) uint32_t stage[4][32][kPlistBlock];  // each lane's current block of entries
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / C, ii = lane % C;
   const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + g;
@@ -498,6 +499,15 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
   const int cap = s.pl_cap;
   const int64_t stride = s.pl_stride;
+  uint32_t *stg = stage[w][lane];
+  // a full block goes out as one 32-byte sector (partial-sector writes cost a read-modify-write in HBM)
+  auto put_block = [&](int b) {
+    if (b * kPlistBlock < cap) {
+      uint4 *dst = reinterpret_cast<uint4 *>(s.pl_list + plist_index(stride, i, b * kPlistBlock));
+      dst[0] = make_uint4(stg[0], stg[1], stg[2], stg[3]);
+      dst[1] = make_uint4(stg[4], stg[5], stg[6], stg[7]);
+    }
+  };
   int cnt = 0;
   for (int e = 0; e < nmax; ++e) {
     const bool act = e < n;
@@ -530,14 +540,18 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
         const float dz = (zh - hj.z) + (zl - lj.z);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         if ((r2 > 0.f) && (r2 <= L2f) && ((__float_as_int(hj.w) >> 16) != 0)) {
-          if (cnt < cap) s.pl_list[(int64_t)cnt * stride + i] = ((jbase + (uint32_t)jj) << 5) | (uint32_t)code;
+          stg[cnt & (kPlistBlock - 1)] = ((jbase + (uint32_t)jj) << 5) | (uint32_t)code;
           ++cnt;
+          if ((cnt & (kPlistBlock - 1)) == 0) put_block((cnt - 1) / kPlistBlock);
         }
       }
     }
     __syncwarp();
   }
-  if (validA) s.pl_count[i] = cnt;
+  if (validA) {
+    if (cnt & (kPlistBlock - 1)) put_block(cnt / kPlistBlock);  // the last block; entries past cnt are never read
+    s.pl_count[i] = cnt;
+  }
   int mx = cnt;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -619,7 +633,7 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
   const int n = min(s.pl_count[i], s.pl_cap);
   int m = 0;
   for (int k = 0; k < n; ++k) {
-    const uint32_t ent = __ldg(s.pl_list + (int64_t)k * s.pl_stride + i);
+    const uint32_t ent = __ldg(s.pl_list + plist_index(s.pl_stride, i, k));
     const int64_t j = ent >> 5;
     const int code = ent & 31;
     const float4 hj = __ldg(&s.pk[2 * (j)]), lj = __ldg(&s.pk[2 * (j) + 1]);
@@ -637,7 +651,7 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
     const float dy = (yh - hj.y) + (yl - lj.y);
     const float dz = (zh - hj.z) + (zl - lj.z);
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    if (r2 <= lim) s.pi_list[(int64_t)(m++) * s.pl_stride + i] = ent;
+    if (r2 <= lim) s.pi_list[plist_index(s.pl_stride, i, m++)] = ent;
   }
   s.pi_count[i] = m;
   s.x_prune[3 * i] = s.x[i];
@@ -765,7 +779,7 @@ __global__ void k_pair_dump_plist(DeviceState s, int which, int64_t cap, int64_t
   const int n = min(s.pl_count[i], s.pl_cap);
   const double pi[3] = {s.x[i], s.y[i], s.z[i]};
   for (int k = 0; k < n; ++k) {
-    const uint32_t ent = s.pl_list[(int64_t)k * s.pl_stride + i];
+    const uint32_t ent = s.pl_list[plist_index(s.pl_stride, i, k)];
     const int64_t j = ent >> 5;
     const int code = ent & 31;
     int sx, sy, sz;

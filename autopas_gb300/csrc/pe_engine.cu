@@ -447,6 +447,14 @@ __global__ void k_max_i32(const int32_t *__restrict__ a, int64_t n, int *__restr
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
+__global__ void k_sum_i32(const int32_t *__restrict__ a, int64_t n, unsigned long long *__restrict__ out) {
+  long long m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m += a[i];
+  for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, (unsigned long long)m);
+}
+
 __global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int32_t *__restrict__ tower_base,
                              int nsys, int64_t *__restrict__ range) {
   const int sy = blockIdx.x * blockDim.x + threadIdx.x;
@@ -759,6 +767,7 @@ static int build_particle_lists(pe_engine *h) {
     const double L = h->cfg.cutoff + h->cfg.skin;
     h->pl_cap = (int)std::min(4096.0, 4.18879 * L * L * L * rho * 1.4 + 32);
   }
+  h->pl_cap = (h->pl_cap + kPlistBlock - 1) / kPlistBlock * kPlistBlock;
   for (int attempt = 0; attempt < 3; ++attempt) {
     const size_t need = (size_t)h->pl_cap * (size_t)h->pcap;
     if (!h->pl_list.ensure(need)) return h->fail(PE_ERR_OOM, "particle lists (%zu entries)", need);
@@ -785,7 +794,7 @@ static int build_particle_lists(pe_engine *h) {
       }
       return PE_OK;
     }
-    h->pl_cap = (int)(mx * 1.2) + 8;
+    h->pl_cap = ((int)(mx * 1.2) + 8 + kPlistBlock - 1) / kPlistBlock * kPlistBlock;
     h->pl_list.release();
   }
   return h->fail(PE_ERR_LIST_OVERFLOW, "particle lists kept overflowing");
@@ -1446,6 +1455,20 @@ int pe_get_info(pe_engine *h, pe_info *info) {
   info->newton3 = h->newton3;
   info->precision = h->precision;
   info->traversal = h->traversal;
+  if (h->traversal == 1 && h->lists_valid && h->pl_entries == 0 && h->nslots > 0 && h->pl_count.p) {
+    // counted once per list build, on request
+    unsigned long long *acc = nullptr;
+    if (cudaMalloc(&acc, sizeof(unsigned long long)) == cudaSuccess) {
+      unsigned long long v = 0;
+      cudaMemsetAsync(acc, 0, sizeof(v), h->st);
+      k_sum_i32<<<304, 256, 0, h->st>>>(h->pl_count.p, h->nslots, acc);
+      cudaMemcpyAsync(&v, acc, sizeof(v), cudaMemcpyDeviceToHost, h->st);
+      cudaStreamSynchronize(h->st);
+      cudaFree(acc);
+      h->pl_entries = (int64_t)v;
+    }
+    PE_TRY(h->cuda_check("list entry count"));
+  }
   info->num_list_entries = h->pl_entries;
   info->list_capacity = h->pl_cap;
   info->num_particles = h->nuser;

@@ -405,116 +405,88 @@ struct MixedAcc {
 };
 
 // List entries are read once per launch: with STREAM they are loaded with the evict-first (streaming) cache
-// hint, so that the gathered positions keep the caches.
-template <bool STREAM>
-__device__ __forceinline__ uint32_t list_entry(const uint32_t *p) {
-  return STREAM ? __ldcs(p) : __ldg(p);
+// hint, so that the gathered positions keep the caches.  U entries (2 or 4, consecutive in one sector) per load.
+template <int U, bool STREAM>
+__device__ __forceinline__ void list_load(const uint32_t *p, uint32_t (&e)[U]) {
+  if (U == 4) {
+    const uint4 v = STREAM ? __ldcs(reinterpret_cast<const uint4 *>(p)) : __ldg(reinterpret_cast<const uint4 *>(p));
+    e[0] = v.x;
+    e[1] = v.y;
+    e[U > 2 ? 2 : 0] = v.z;
+    e[U > 3 ? 3 : 0] = v.w;
+  } else {
+    const uint2 v = STREAM ? __ldcs(reinterpret_cast<const uint2 *>(p)) : __ldg(reinterpret_cast<const uint2 *>(p));
+    e[0] = v.x;
+    e[1] = v.y;
+  }
 }
 
-// One thread's walk over its list (UNROLL entries per batch; the list entries of the next batch are loaded while
-// the current batch's positions are gathered and evaluated, so the dependent list -> position chain overlaps
-// arithmetic).  With REPRUNE the walk reads the outer list (rc + skin) and also writes the entries within
-// lim to the inner list out; it returns their number.
-template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool REPRUNE, bool STREAM>
-__device__ __forceinline__ int plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                          const float4 &hi_i, const float4 &lo_i, int ti,
-                                          const uint32_t *__restrict__ lp, int n, float eps24, float sig2, float sh6,
-                                          const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
-                                          MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc, uint32_t *__restrict__ out,
-                                          float lim) {
+// One thread's walk over its list.  Entries arrive UNROLL (2 or 4) at a time in one vector load, the next
+// UNROLL being loaded while the current ones are evaluated; the position gathers of a batch are all issued
+// before its arithmetic.  Leftover entries (n mod UNROLL) are read one by one.
+template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM>
+__device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                           const float4 &hi_i, const float4 &lo_i, int ti,
+                                           const uint32_t *__restrict__ list, int n, float eps24, float sig2,
+                                           float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
+                                           MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc) {
+  static_assert(UNROLL == 2 || UNROLL == 4, "batches of 2 or 4 entries");
   const int64_t stride = s.pl_stride;
-  int k = 0, m = 0;
-  uint32_t ent[UNROLL];
-  if (UNROLL <= n) {
+  const uint32_t *base = list + i * kPlistBlock;
+  const int64_t bstride = stride * kPlistBlock;
+  int k = 0;
+  uint32_t e[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) ent[u] = list_entry<STREAM>(lp + (int64_t)u * stride);
-  }
+  for (int u = 0; u < UNROLL; ++u) e[u] = 0u;
+  if (UNROLL <= n) list_load<UNROLL, STREAM>(base, e);
   for (; k + UNROLL <= n; k += UNROLL) {
+    const int kn = k + UNROLL;
+    uint32_t nx[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) nx[u] = 0u;
+    if (kn + UNROLL <= n) list_load<UNROLL, STREAM>(base + (int64_t)(kn >> 3) * bstride + (kn & 7), nx);
     float4 hj[UNROLL], lj[UNROLL];
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      const float4 *q = s.pk + 2 * (int64_t)(ent[u] >> 5);
+      const float4 *q = s.pk + 2 * (int64_t)(e[u] >> 5);
       hj[u] = __ldg(q);
       lj[u] = __ldg(q + 1);
     }
-    uint32_t nxt[UNROLL];
-    const bool more = k + 2 * UNROLL <= n;
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u)
-      nxt[u] = more ? list_entry<STREAM>(lp + (int64_t)(k + UNROLL + u) * stride) : 0u;
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, ent[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
-      if (REPRUNE && r2 <= lim) out[(int64_t)(m++) * stride] = ent[u];
-    }
+      acc.pair(s, S, fa, i, hi_i, lo_i, ti, e[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
     acc.flush();
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) ent[u] = nxt[u];
+    for (int u = 0; u < UNROLL; ++u) e[u] = nx[u];
   }
   for (; k < n; ++k) {
-    const uint32_t e = list_entry<STREAM>(lp + (int64_t)k * stride);
-    const float4 *q = s.pk + 2 * (int64_t)(e >> 5);
-    const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, e, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
-    if (REPRUNE && r2 <= lim) out[(int64_t)(m++) * stride] = e;
+    const uint32_t en = __ldg(list + plist_index(stride, i, k));
+    const float4 *q = s.pk + 2 * (int64_t)(en >> 5);
+    acc.pair(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
   }
-  return m;
+  acc.flush();
 }
 
-// A deeper pipeline: while batch k is evaluated, the positions of batch k+1 and the list entries of batch k+2
-// are in flight.  Entries past the end of the list read slot 0 (a valid address) and are never evaluated.
-template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL>
-__device__ __forceinline__ void plist_walk_deep(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                                const float4 &hi_i, const float4 &lo_i, int ti,
-                                                const uint32_t *__restrict__ lp, int n, float eps24, float sig2,
-                                                float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
-                                                float band, MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc) {
+// The re-prune walk: the outer list (rc + skin) entry by entry; entries within lim also go to the inner list
+// out.  Returns their number.
+template <bool GLOB, bool ONE_TYPE, bool KAHAN>
+__device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const SysDev &S, const ForceArgs &fa,
+                                                  int64_t i, const float4 &hi_i, const float4 &lo_i, int ti,
+                                                  const uint32_t *__restrict__ list, int n, float eps24, float sig2,
+                                                  float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
+                                                  float band, MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc,
+                                                  uint32_t *__restrict__ out, float lim) {
   const int64_t stride = s.pl_stride;
-  int k = 0;
-  uint32_t e0[UNROLL], e1[UNROLL];
-  float4 h0[UNROLL], l0[UNROLL];
-  if (UNROLL <= n) {
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) e0[u] = list_entry<true>(lp + (int64_t)u * stride);
-    const bool more = 2 * UNROLL <= n;
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) e1[u] = more ? list_entry<true>(lp + (int64_t)(UNROLL + u) * stride) : 0u;
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const float4 *q = s.pk + 2 * (int64_t)(e0[u] >> 5);
-      h0[u] = __ldg(q);
-      l0[u] = __ldg(q + 1);
-    }
+  int m = 0;
+  for (int k = 0; k < n; ++k) {
+    const uint32_t en = __ldg(list + plist_index(stride, i, k));
+    const float4 *q = s.pk + 2 * (int64_t)(en >> 5);
+    const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
+    if (r2 <= lim) out[plist_index(stride, i, m++)] = en;
+    if ((k & 1) == 1) acc.flush();
   }
-  for (; k + UNROLL <= n; k += UNROLL) {
-    float4 h1[UNROLL], l1[UNROLL];
-    uint32_t e2[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const float4 *q = s.pk + 2 * (int64_t)(e1[u] >> 5);
-      h1[u] = __ldg(q);
-      l1[u] = __ldg(q + 1);
-    }
-    const bool more2 = k + 3 * UNROLL <= n;
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u)
-      e2[u] = more2 ? list_entry<true>(lp + (int64_t)(k + 2 * UNROLL + u) * stride) : 0u;
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u)
-      acc.pair(s, S, fa, i, hi_i, lo_i, ti, e0[u], h0[u], l0[u], eps24, sig2, sh6, tab, T, band);
-    acc.flush();
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      e0[u] = e1[u];
-      h0[u] = h1[u];
-      l0[u] = l1[u];
-      e1[u] = e2[u];
-    }
-  }
-  for (; k < n; ++k) {
-    const uint32_t e = list_entry<true>(lp + (int64_t)k * stride);
-    const float4 *q = s.pk + 2 * (int64_t)(e >> 5);
-    acc.pair(s, S, fa, i, hi_i, lo_i, ti, e, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
-  }
+  acc.flush();
+  return m;
 }
 
 // MINB: minimum resident blocks per SM requested from the compiler (caps registers for more warps in flight).
@@ -523,10 +495,9 @@ __device__ __forceinline__ void plist_walk_deep(const DeviceState &s, const SysD
 // entries within rc + buffer (or the whole outer list once the particles have used up the skin beyond the
 // buffer since the rebuild) to the inner lists and records the positions of the prune.  The flag is read
 // by every thread and cleared by a later launch, so all threads take the same branch.
-// PIPE: bit 0 streams the list entries past the caches, bit 1 selects the deeper pipeline
-template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, int PIPE>
+// STREAM: list entries loaded with the streaming (evict-first) hint
+template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, bool STREAM>
 __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
-  constexpr bool STREAM = (PIPE & 1) != 0, DEEP = (PIPE & 2) != 0;
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
   const int T = s.ntypes;
   if (!ONE_TYPE) {
@@ -562,9 +533,8 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
   if (reprune) {
     const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
-    // single-entry batches: this branch runs once per prune, and fewer live registers keep the other one spill-free
-    const int m = plist_walk<GLOB, ONE_TYPE, KAHAN, 1, true, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list + i, n, eps24,
-                                                                  sig2, sh6, tab, T, band, acc, s.pi_list + i, lim);
+    const int m = plist_walk_reprune<GLOB, ONE_TYPE, KAHAN>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list, n, eps24, sig2,
+                                                           sh6, tab, T, band, acc, s.pi_list, lim);
     if (inrange) {
       s.pi_count[i] = m;
       if (oi != 0) {
@@ -573,14 +543,10 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
         s.x_prune[3 * i + 2] = s.z[i];
       }
     }
-  } else if (DEEP) {
-    plist_walk_deep<GLOB, ONE_TYPE, KAHAN, UNROLL>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list + i, n, eps24, sig2, sh6,
-                                                   tab, T, band, acc);
   } else {
-    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, false, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list + i, n, eps24,
-                                                             sig2, sh6, tab, T, band, acc, nullptr, 0.f);
+    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list, n, eps24, sig2, sh6,
+                                                      tab, T, band, acc);
   }
-  acc.flush();
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
   // epilogue keeps to the FP64 work the state needs: the force rounded once from its compensated sum, the
   // velocity half in FP64 with the reference's operation order.  Per-particle globals, the kinetic energy
@@ -652,7 +618,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
   double fx = 0, fy = 0, fz = 0, pot = 0, vx = 0, vy = 0, vz = 0;
   long long hits2 = 0;
   for (int k = 0; k < n; ++k) {
-    const uint32_t ent = __ldg(s.fl_list + (int64_t)k * s.pl_stride + i);
+    const uint32_t ent = __ldg(s.fl_list + plist_index(s.pl_stride, i, k));
     const int64_t j = ent >> 5;
     const int code = ent & 31;
     int sx, sy, sz;
@@ -732,23 +698,23 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
       k_lj_fp64_plist<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     return;
   }
-  // kernel variants, chosen by the engine's tuner: list entries batched by 2 under a cap of 64 registers
-  // (8 blocks of 128 threads per SM) or by 4 under a cap of 80 (6 blocks); list entries cached or streamed;
-  // positions gathered one batch ahead (up to 102 registers, 5 blocks).  Tighter register caps spill.
+  // kernel variants, chosen by the engine's tuner: positions gathered in batches of 2 under a cap of 64
+  // registers (8 blocks of 128 threads per SM) or of 4 under a cap of 80 (6 blocks); list entries cached or
+  // streamed.  Tighter register caps spill.
 #define PE_PLIST(G, O)                                                                   \
   do {                                                                                   \
     switch (s.variant) {                                                                 \
       case 1:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 4, 6, 0><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        k_lj_mixed_plist<C, G, O, true, 4, 6, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
         break;                                                                           \
       case 2:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 2, 8, 1><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        k_lj_mixed_plist<C, G, O, true, 2, 8, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
         break;                                                                           \
       case 3:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 2, 5, 3><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        k_lj_mixed_plist<C, G, O, true, 4, 6, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
         break;                                                                           \
       default:                                                                           \
-        k_lj_mixed_plist<C, G, O, true, 2, 8, 0><<<(unsigned)nb, 128, 0, st>>>(s, fa);   \
+        k_lj_mixed_plist<C, G, O, true, 2, 8, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
     }                                                                                    \
   } while (0)
   if (s.ntypes == 1) {

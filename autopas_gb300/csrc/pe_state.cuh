@@ -6,6 +6,14 @@
 namespace pe {
 
 // Plain pointer bundle; owned and sized by the engine (pe_engine.cu).
+// Particle-list layout: the entries of a slot come in blocks of kPlistBlock = 8 (one 32-byte sector); block b
+// of consecutive slots is contiguous.  A thread appends whole sectors, and a warp of consecutive slots reads
+// 32 consecutive sectors with one 16-byte load per lane per 4 entries.
+constexpr int kPlistBlock = 8;
+__host__ __device__ __forceinline__ int64_t plist_index(int64_t stride, int64_t i, int k) {
+  return (((int64_t)(k >> 3) * stride + i) << 3) + (k & 7);
+}
+
 struct DeviceState {
   // ---- particles, slot order ----
   int64_t nslots = 0;      // slots in use (real + padding dummies)
@@ -44,8 +52,9 @@ struct DeviceState {
   unsigned long long *cp_total = nullptr;  // device counter
   int newton3 = 0;
 
-  // particle neighbour lists (traversal 1): entry k of slot i at pl_list[k * pl_stride + i],
-  // (j slot << 5 | image-shift code), every j within rc+skin of i (FP32 test with a safety margin)
+  // particle neighbour lists (traversal 1): entry k of slot i at pl_list[plist_index(pl_stride, i, k)],
+  // (j slot << 5 | image-shift code), every j within rc+skin of i (FP32 test with a safety margin).  pl_cap is
+  // a multiple of kPlistBlock.
   int traversal = 0;               // 0: cluster-pair lists, 1: particle lists
   int variant = 0;                 // kernel variant inside a traversal (tuner dimension)
   uint32_t *pl_list = nullptr;
