@@ -508,15 +508,36 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
       dst[1] = make_uint4(stg[4], stg[5], stg[6], stg[7]);
     }
   };
+  // software pipeline: the group's list entries arrive C at a time (lane ii holds entry c*C + ii, one chunk
+  // ahead), and the j particles of entry e+1 are loaded while entry e is tested
+  const unsigned full = 0xffffffffu;
+  uint32_t ech = ii < n ? __ldg(lst + ii) : 0u;
+  uint32_t ech_next = C + ii < n ? __ldg(lst + C + ii) : 0u;
+  uint32_t ent_next = __shfl_sync(full, ech, g * C);
+  float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
+  if (0 < n) {
+    const int64_t j = (int64_t)(ent_next >> 5) * C + ii;
+    ph = __ldg(&s.pk[2 * j]);
+    pl = __ldg(&s.pk[2 * j + 1]);
+  }
   int cnt = 0;
   for (int e = 0; e < nmax; ++e) {
     const bool act = e < n;
-    uint32_t ent = 0;
+    const uint32_t ent = ent_next;
     if (act) {
-      ent = __ldg(lst + e);
-      const int64_t j = (int64_t)(ent >> 5) * C + ii;
-      sj[w][g][ii][0] = __ldg(&s.pk[2 * j]);
-      sj[w][g][ii][1] = __ldg(&s.pk[2 * j + 1]);
+      sj[w][g][ii][0] = ph;
+      sj[w][g][ii][1] = pl;
+    }
+    const int e1 = e + 1;
+    if ((e1 & (C - 1)) == 0) {
+      ech = ech_next;
+      ech_next = e1 + C + ii < n ? __ldg(lst + e1 + C + ii) : 0u;
+    }
+    ent_next = __shfl_sync(full, ech, g * C + (e1 & (C - 1)));
+    if (e1 < n) {
+      const int64_t j = (int64_t)(ent_next >> 5) * C + ii;
+      ph = __ldg(&s.pk[2 * j]);
+      pl = __ldg(&s.pk[2 * j + 1]);
     }
     __syncwarp();
     if (act && oi == 1) {
@@ -532,6 +553,8 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
         zl = fmaf(-szf, S.len_lo[2], zl);
       }
       const uint32_t jbase = (ent >> 5) * (uint32_t)C;
+      // dummies sit at x' = -B, at least 2B from everything, so the distance test excludes them; r2 > 0
+      // excludes i itself
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
         const float4 hj = sj[w][g][jj][0], lj = sj[w][g][jj][1];
@@ -539,7 +562,7 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
         const float dy = (yh - hj.y) + (yl - lj.y);
         const float dz = (zh - hj.z) + (zl - lj.z);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        if ((r2 > 0.f) && (r2 <= L2f) && ((__float_as_int(hj.w) >> 16) != 0)) {
+        if ((r2 > 0.f) && (r2 <= L2f)) {
           stg[cnt & (kPlistBlock - 1)] = ((jbase + (uint32_t)jj) << 5) | (uint32_t)code;
           ++cnt;
           if ((cnt & (kPlistBlock - 1)) == 0) put_block((cnt - 1) / kPlistBlock);

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -1026,11 +1027,21 @@ static int tune(pe_engine *h, int samples) {
   std::vector<int> Ts = h->cfg.traversal == -1 ? std::vector<int>{0, 1} : std::vector<int>{h->traversal};
   h->tune_log.clear();
   const int rebuilds = (int)h->rebuilds;
+  const double per_step = 1.0 / std::max(1, h->cfg.rebuild_frequency);
   for (int C : Cs)
     for (int T : Ts) {
       const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : 1;
+      double reb_ms = 0;
       for (int v = 0; v < nv; ++v) {
         PE_TRY(apply_config(h, C, T, v));
+        if (v == 0) {
+          // the rebuild of this cluster size and traversal, with its host synchronisations, by the host clock
+          PE_CUDA(h, cudaStreamSynchronize(h->st));
+          const auto t0 = std::chrono::steady_clock::now();
+          PE_TRY(do_rebuild(h));
+          PE_CUDA(h, cudaStreamSynchronize(h->st));
+          reb_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
         std::vector<float> t;
         for (int k = 0; k < samples + 1; ++k) {
           cudaEvent_t a = h->ev(), b = h->ev();
@@ -1045,12 +1056,13 @@ static int tune(pe_engine *h, int samples) {
         }
         h->ev_used -= 2 * (samples + 1);
         std::sort(t.begin(), t.end());
-        h->tune_log.push_back({C, T, v, (double)t[t.size() / 2]});
+        const double ms = t[t.size() / 2];
+        h->tune_log.push_back({C, T, v, ms, reb_ms, ms + reb_ms * per_step});
       }
     }
   int best = 0;
   for (int k = 1; k < (int)h->tune_log.size(); ++k)
-    if (h->tune_log[k].ms < h->tune_log[best].ms) best = k;
+    if (h->tune_log[k].score < h->tune_log[best].score) best = k;
   h->tune_chosen = best;
   const auto &b = h->tune_log[best];
   PE_TRY(apply_config(h, b.cluster_size, b.traversal, b.variant));
@@ -1079,6 +1091,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->traversal < -1 || cfg->traversal > 1) return PE_ERR_ARG;
   if (cfg->atm_nu > 0 && !(cfg->atm_cutoff > 0 && cfg->atm_cutoff <= cfg->cutoff + cfg->skin)) return PE_ERR_ARG;
   if (cfg->prune_buffer < 0 || cfg->prune_buffer > cfg->skin) return PE_ERR_ARG;
+  if (cfg->kernel_variant < 0 || cfg->kernel_variant > 3) return PE_ERR_ARG;
   // every force kernel evaluates each pair from both sides (full lists); half lists are not offered
   if (cfg->newton3 == 1) return PE_ERR_ARG;
   int ndev = 0;
@@ -1096,6 +1109,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   h->need_plist = cfg->atm_nu > 0;
   h->newton3 = (cfg->newton3 == 1 && h->traversal == 0) ? 1 : 0;
   h->precision = cfg->precision;
+  h->variant = cfg->kernel_variant;
   cudaGetDevice(&h->device);
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;

@@ -39,7 +39,7 @@ class PeConfig(C.Structure):
         ("apply_shift", C.c_int), ("precision", C.c_int), ("cluster_size", C.c_int), ("newton3", C.c_int),
         ("dist_mode", C.c_int), ("rebuild_frequency", C.c_int), ("calc_globals", C.c_int),
         ("tower_sizing", C.c_int), ("traversal", C.c_int), ("atm_nu", C.c_double), ("atm_cutoff", C.c_double),
-        ("use_graphs", C.c_int), ("prune_buffer", C.c_double),
+        ("use_graphs", C.c_int), ("prune_buffer", C.c_double), ("kernel_variant", C.c_int),
     ]
 
 
@@ -58,7 +58,8 @@ class PeStats(C.Structure):
 
 
 class PeTuningEntry(C.Structure):
-    _fields_ = [("cluster_size", C.c_int), ("traversal", C.c_int), ("variant", C.c_int), ("ms", C.c_double)]
+    _fields_ = [("cluster_size", C.c_int), ("traversal", C.c_int), ("variant", C.c_int), ("ms", C.c_double),
+                ("rebuild_ms", C.c_double), ("score", C.c_double)]
 
 
 class PeInfo(C.Structure):
@@ -129,7 +130,7 @@ class PairEngine:
     def __init__(self, cutoff, skin, boxes, periodic=True, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,),
                  shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_STRICT,
                  rebuild_frequency=10, calc_globals=True, tower_sizing=1, traversal=1, atm_nu=0.0, atm_cutoff=0.0,
-                 use_graphs=True, prune_buffer=0.0):
+                 use_graphs=True, prune_buffer=0.0, kernel_variant=0):
         L = load()
         self._L = L
         self._eps = np.ascontiguousarray(epsilon, np.float64)
@@ -140,7 +141,8 @@ class PairEngine:
         cfg = PeConfig(cutoff, skin, T, self._eps.ctypes.data_as(dp), self._sig.ctypes.data_as(dp),
                        self._mass.ctypes.data_as(dp), int(shift), int(precision), int(cluster_size), int(newton3),
                        int(dist_mode), int(rebuild_frequency), int(calc_globals), int(tower_sizing),
-                       int(traversal), float(atm_nu), float(atm_cutoff), int(use_graphs), float(prune_buffer))
+                       int(traversal), float(atm_nu), float(atm_cutoff), int(use_graphs), float(prune_buffer),
+                       int(kernel_variant))
         boxes = list(boxes)
         if np.ndim(boxes[0]) == 1:  # single (bmin, bmax)
             boxes = [boxes]
@@ -280,7 +282,8 @@ class PairEngine:
         chosen = C.c_int()
         self._check(self._L.pe_get_tuning(self._h, 64, arr, C.byref(cnt), C.byref(chosen)))
         return {"candidates": [{"cluster_size": a.cluster_size, "traversal": a.traversal, "variant": a.variant,
-                                "ms": a.ms} for a in arr[:cnt.value]], "chosen": chosen.value}
+                                "ms": a.ms, "rebuild_ms": a.rebuild_ms, "score": a.score}
+                               for a in arr[:cnt.value]], "chosen": chosen.value}
 
     def timer_start(self):
         self._check(self._L.pe_device_timer(self._h, 0, None))
@@ -298,7 +301,7 @@ def make_config(cutoff, skin=0.0, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,), shi
     ms = np.ascontiguousarray(mass, np.float64)
     dp = C.POINTER(C.c_double)
     cfg = PeConfig(cutoff, skin, len(eps), eps.ctypes.data_as(dp), sig.ctypes.data_as(dp), ms.ctypes.data_as(dp),
-                   int(shift), PRECISION_FP64, 8, 0, int(dist_mode), 1, 1, 1, 1, 0.0, 0.0, 0, 0.0)
+                   int(shift), PRECISION_FP64, 8, 0, int(dist_mode), 1, 1, 1, 1, 0.0, 0.0, 0, 0.0, 0)
     return cfg, (eps, sig, ms)
 
 

@@ -45,6 +45,7 @@ def parse():
     p.add_argument("--cluster-size", type=int, default=0, help="0: the engine's tuner picks 4 or 8")
     p.add_argument("--traversal", type=int, default=-1, help="-1: tuner; 0 cluster pairs; 1 particle lists")
     p.add_argument("--prune", type=float, default=0.0, help="rolling-prune buffer of the particle lists (0: off)")
+    p.add_argument("--variant", type=int, default=0, help="particle-list kernel variant when the tuner is off")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
@@ -219,7 +220,7 @@ def run_ours(args):
     def new_engine(prec, use_graphs=True):
         e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
                          newton3=0, rebuild_frequency=REBUILD, calc_globals=True, traversal=args.traversal,
-                         prune_buffer=args.prune, use_graphs=use_graphs)
+                         prune_buffer=args.prune, use_graphs=use_graphs, kernel_variant=args.variant)
         e.set_particles(pos, vel)
         return e
 

@@ -91,6 +91,8 @@ typedef struct {
   double prune_buffer;     /* > 0 (particle lists only): the force kernels read inner lists holding the pairs within
                               cutoff + prune_buffer, refreshed on the device from the rc+skin lists whenever a
                               particle has moved prune_buffer/2 since the last refresh; 0: off */
+  int kernel_variant;      /* particle-list force kernel variant (0-3: entry batches of 2 or 4, list entries
+                              cached or streamed) used when the tuner does not run; the tuner picks its own */
 } pe_config;
 
 /* One particle system of the ensemble. */
@@ -200,16 +202,19 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out);
 
 /* The engine's tuner (the counterpart of AutoPas's AutoTuner full search, tuning/AutoTuner.cpp:85-175, over
  * the engine-internal dimensions that AutoPas does not tune): every candidate (cluster size 4/8 when
- * cluster_size == 0, traversal 0/1 when traversal == -1, kernel variant) is applied, the lists rebuilt, and
- * `samples` force evaluations timed with CUDA events; the fastest candidate (median time) is kept.  It runs
- * by itself at the first pe_compute_forces when cluster_size == 0 or traversal == -1.  The evidence of the
- * last tuning is returned by pe_get_tuning: up to cap entries of {cluster_size, traversal, variant, ms};
- * *count receives the number of candidates and *chosen the index of the kept one. */
+ * cluster_size == 0, traversal 0/1 when traversal == -1, kernel variant) is applied, the lists rebuilt, one
+ * more rebuild timed (rebuild_ms, once per cluster size and traversal), and `samples` force evaluations timed
+ * with CUDA events (ms, the median).  The candidate with the lowest cost per step, score = ms + rebuild_ms /
+ * rebuild_frequency, is kept.  It runs by itself at the first pe_compute_forces when cluster_size == 0 or
+ * traversal == -1.  The evidence of the last tuning is returned by pe_get_tuning: up to cap entries; *count
+ * receives the number of candidates and *chosen the index of the kept one. */
 typedef struct {
   int cluster_size;
   int traversal;
   int variant;
   double ms;
+  double rebuild_ms;
+  double score;
 } pe_tuning_entry;
 int pe_tune(pe_engine *h, int samples);
 int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, int *chosen);

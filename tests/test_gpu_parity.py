@@ -265,8 +265,9 @@ def test_local_density_towers_keep_pair_set(eng_mod, orc):
 
 
 def test_tuner_full_search_keeps_results(eng_mod, orc):
-    """The engine tuner times every (cluster size, traversal, variant) candidate and keeps the fastest;
-    whatever it picks, the forces stay those of the oracle."""
+    """The engine tuner times every (cluster size, traversal, variant) candidate -- force evaluation and the
+    rebuild amortised over the rebuild frequency -- and keeps the cheapest per step; whatever it picks, the
+    forces stay those of the oracle."""
     pos, vel, bmin, bmax = liquid(7, seed=17)
     rc, skin = 2.5, 0.3
     e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_MIXED, cluster_size=0,
@@ -281,7 +282,10 @@ def test_tuner_full_search_keeps_results(eng_mod, orc):
     assert len(cands) == 2 * (1 + len({c["variant"] for c in cands if c["traversal"] == 1}))
     assert 0 <= tun["chosen"] < len(cands)
     best = tun["candidates"][tun["chosen"]]
-    assert best["ms"] == min(c["ms"] for c in tun["candidates"])
+    for c in cands:
+        assert c["rebuild_ms"] > 0
+        assert c["score"] == pytest.approx(c["ms"] + c["rebuild_ms"] / 10)  # rebuild_frequency 10
+    assert best["score"] == min(c["score"] for c in cands)
     info = e.info()
     assert (info["cluster_size"], info["traversal"]) == (best["cluster_size"], best["traversal"])
     F = e.forces()
