@@ -493,7 +493,9 @@ template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   constexpr int G = 32 / C;
   __shared__ float4 sj[4][G][C][2];
-  __shared__ __align__(16) uint32_t stage[4][32][kPlistBlock];  // each lane's current block of entries
+  // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
+  // most one block)
+  __shared__ __align__(16) uint32_t stage[4][32][2 * kPlistBlock];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / C, ii = lane % C;
   const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + g;
@@ -522,9 +524,10 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   // a full block goes out as one 32-byte sector (partial-sector writes cost a read-modify-write in HBM)
   auto put_block = [&](int b) {
     if (b * kPlistBlock < cap) {
+      const uint32_t *src = stg + (b & 1) * kPlistBlock;
       uint4 *dst = reinterpret_cast<uint4 *>(s.pl_list + plist_index(stride, i, b * kPlistBlock));
-      dst[0] = make_uint4(stg[0], stg[1], stg[2], stg[3]);
-      dst[1] = make_uint4(stg[4], stg[5], stg[6], stg[7]);
+      dst[0] = make_uint4(src[0], src[1], src[2], src[3]);
+      dst[1] = make_uint4(src[4], src[5], src[6], src[7]);
     }
   };
   // software pipeline: the group's list entries arrive C at a time (lane ii holds entry c*C + ii, one chunk
@@ -572,9 +575,11 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
         yl = fmaf(-syf, S.len_lo[1], yl);
         zl = fmaf(-szf, S.len_lo[2], zl);
       }
-      const uint32_t jbase = (ent >> 5) * (uint32_t)C;
+      const uint32_t ebase = (((ent >> 5) * (uint32_t)C) << 5) | (uint32_t)code;
+      const int before = cnt;
       // dummies sit at x' = -B, at least 2B from everything, so the distance test excludes them; r2 > 0
-      // excludes i itself
+      // excludes i itself.  Branch-free append: the entry is always written at the ring position, which only
+      // advances when it is kept.
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
         const float4 hj = sj[w][g][jj][0], lj = sj[w][g][jj][1];
@@ -582,12 +587,10 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
         const float dy = (yh - hj.y) + (yl - lj.y);
         const float dz = (zh - hj.z) + (zl - lj.z);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        if ((r2 > 0.f) && (r2 <= L2f)) {
-          stg[cnt & (kPlistBlock - 1)] = ((jbase + (uint32_t)jj) << 5) | (uint32_t)code;
-          ++cnt;
-          if ((cnt & (kPlistBlock - 1)) == 0) put_block((cnt - 1) / kPlistBlock);
-        }
+        stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
+        cnt += ((r2 > 0.f) && (r2 <= L2f)) ? 1 : 0;
       }
+      if ((before ^ cnt) & ~(kPlistBlock - 1)) put_block(before / kPlistBlock);
     }
     __syncwarp();
   }
