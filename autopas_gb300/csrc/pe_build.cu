@@ -341,7 +341,6 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
   if (!aOwned && !s.newton3) {
     if (lane == 0) {
       s.cp_count[A] = 0;
-      s.cp_count0[A] = 0;
       s.cp_start[A] = 0;
     }
     return;
@@ -429,7 +428,6 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     if (lane == 0) {
       atomicOr(s.err, kErrListOverflow);
       s.cp_count[A] = 0;
-      s.cp_count0[A] = 0;
       s.cp_start[A] = 0;
     }
     return;
@@ -441,30 +439,14 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
     if (lane == 0) {
       atomicOr(s.err, kErrListCapacity);
       s.cp_count[A] = 0;
-      s.cp_count0[A] = 0;
       s.cp_start[A] = 0;
     }
     return;
   }
-  // entries without image shift first, then the shifted ones, each in candidate order
-  int n0 = 0;
-  for (int pass = 0; pass < 2; ++pass) {
-    const int off = pass == 0 ? 0 : n0;
-    int w = 0;
-    for (int q0 = 0; q0 < cnt; q0 += 32) {
-      const int q = q0 + lane;
-      const uint32_t v = q < cnt ? buf[q] : 0u;
-      const bool take = q < cnt && (((v & 31u) == (uint32_t)kShiftNone) == (pass == 0));
-      const unsigned tb = __ballot_sync(0xffffffffu, take);
-      if (take) s.cp_list[base + off + w + __popc(tb & ((1u << lane) - 1))] = v;
-      w += __popc(tb);
-    }
-    if (pass == 0) n0 = w;
-  }
+  for (int q = lane; q < cnt; q += 32) s.cp_list[base + q] = buf[q];
   if (lane == 0) {
     s.cp_start[A] = (int64_t)base;
     s.cp_count[A] = cnt;
-    s.cp_count0[A] = n0;
   }
 }
 
@@ -501,13 +483,12 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + g;
   const bool validA = A < s.nclusters;
   const int64_t i = A * C + ii;
-  int n = 0, n0 = 0, oi = 0;
+  int n = 0, oi = 0;
   const uint32_t *lst = s.cp_list;
   float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
   int sy = 0;
   if (validA) {
     n = s.cp_count[A];
-    n0 = s.cp_count0[A];
     lst = s.cp_list + s.cp_start[A];
     hi_i = s.pk[2 * i];
     lo_i = s.pk[2 * i + 1];
@@ -542,11 +523,10 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
     ph = __ldg(&s.pk[2 * j]);
     pl = __ldg(&s.pk[2 * j + 1]);
   }
-  int cnt = 0, cnt0 = 0;
+  int cnt = 0;
   for (int e = 0; e < nmax; ++e) {
     const bool act = e < n;
     const uint32_t ent = ent_next;
-    if (e == n0) cnt0 = cnt;  // the entries of unshifted cluster pairs end here
     if (act) {
       sj[w][g][ii][0] = ph;
       sj[w][g][ii][1] = pl;
@@ -597,7 +577,6 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   if (validA) {
     if (cnt & (kPlistBlock - 1)) put_block(cnt / kPlistBlock);  // the last block; entries past cnt are never read
     s.pl_count[i] = cnt;
-    s.pl_count0[i] = n0 >= n ? cnt : cnt0;
   }
   int mx = cnt;
 #pragma unroll

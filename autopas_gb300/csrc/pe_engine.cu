@@ -114,7 +114,7 @@ struct pe_engine {
   DBuf<double> cl_bb;
   DBuf<float4> cl_bbf;
   DBuf<float2> cl_z;
-  DBuf<int32_t> cl_sys, cl_tower, cl_flags, cp_count, cp_count0;
+  DBuf<int32_t> cl_sys, cl_tower, cl_flags, cp_count;
   DBuf<int64_t> cp_start;
   DBuf<uint32_t> cp_list;
   DBuf<unsigned long long> cp_total;
@@ -132,7 +132,7 @@ struct pe_engine {
   int64_t num_cluster_pairs = 0;
   // particle lists
   DBuf<uint32_t> pl_list;
-  DBuf<int32_t> pl_count, pl_count0;
+  DBuf<int32_t> pl_count;
   DBuf<int> pl_max;
   int pl_cap = 0;
   int64_t pl_entries = 0;
@@ -199,7 +199,6 @@ struct pe_engine {
     s.cl_flags = cl_flags.p;
     s.cp_start = cp_start.p;
     s.cp_count = cp_count.p;
-    s.cp_count0 = cp_count0.p;
     s.cp_list = cp_list.p;
     s.cp_cap = (int64_t)cp_list.cap;
     s.cp_total = cp_total.p;
@@ -208,7 +207,6 @@ struct pe_engine {
     s.variant = variant;
     s.pl_list = pl_list.p;
     s.pl_count = pl_count.p;
-    s.pl_count0 = pl_count0.p;
     s.pl_cap = pl_cap;
     s.pl_stride = pcap;
     s.pl_max = pl_max.p;
@@ -747,7 +745,7 @@ static int ensure_particle_capacity(pe_engine *h) {
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
   if (!h->cl_bb.ensure(6 * ncl) || !h->cl_bbf.ensure(2 * ncl) || !h->cl_z.ensure(ncl) || !h->cl_sys.ensure(ncl) || !h->cl_tower.ensure(ncl) || !h->cl_flags.ensure(ncl) ||
-      !h->cp_count.ensure(ncl) || !h->cp_count0.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(kGlob * ncl) ||
+      !h->cp_count.ensure(ncl) || !h->cp_start.ensure(ncl) || !h->cl_glob.ensure(kGlob * ncl) ||
       !h->cl_hits.ensure(ncl) || !h->key.ensure(n) || !h->skey.ensure(n) || !h->tower_of.ensure(n) ||
       !h->sval.ensure(n) || !h->perm_src.ensure(n) || !h->cp_total.ensure(1) || !h->derr.ensure(1) ||
       !h->dmax.ensure(1) || !h->sys_glob.ensure(kSysGlob * h->sys.size()) || !h->sys_hits.ensure(h->sys.size()) ||
@@ -759,8 +757,7 @@ static int ensure_particle_capacity(pe_engine *h) {
 // particle lists filtered from the full cluster-pair lists; the per-particle capacity grows when exceeded
 static int build_particle_lists(pe_engine *h) {
   cudaStream_t st = h->st;
-  if (!h->pl_count.ensure((size_t)h->pcap) || !h->pl_count0.ensure((size_t)h->pcap) || !h->pl_max.ensure(1))
-    return h->fail(PE_ERR_OOM, "particle lists");
+  if (!h->pl_count.ensure((size_t)h->pcap) || !h->pl_max.ensure(1)) return h->fail(PE_ERR_OOM, "particle lists");
   if (h->pl_cap == 0) {
     double rho = 0;
     for (auto &S : h->sys) {
@@ -1164,7 +1161,7 @@ int pe_destroy(pe_engine *h) {
   h->Bk.release();
   h->pk.release();
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
-                  &h->cl_tower, &h->cl_flags, &h->cp_count, &h->cp_count0, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
+                  &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})
     b->release();
   for (auto *b : {&h->cl_bb, &h->cl_glob, &h->sys_glob, &h->dmass, &h->tmp3}) b->release();
@@ -1192,7 +1189,6 @@ int pe_destroy(pe_engine *h) {
   h->pairs_acc.release();
   h->pl_list.release();
   h->pl_count.release();
-  h->pl_count0.release();
   h->pl_max.release();
   h->atm_slot.release();
   h->pi_list.release();

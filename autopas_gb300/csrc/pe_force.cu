@@ -340,16 +340,14 @@ struct MixedAcc {
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
   int hits = 0, hhalo = 0;
 
-  // returns the pair's FP32 squared distance (the re-prune test uses it).  SH: the entry's image shift is
-  // kShiftNone (0), is not (1), or is read from the entry (2).
-  template <int SH = 2>
+  // returns the pair's FP32 squared distance (the re-prune test uses it)
   __device__ __forceinline__ float pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                        const float4 &hi_i, const float4 &lo_i, int ti, uint32_t ent,
                                        const float4 &hj, const float4 &lj, float eps24, float sig2, float sh6,
                                        const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
-    const int code = SH == 0 ? kShiftNone : (int)(ent & 31);
+    const int code = ent & 31;
     float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-    if (SH == 1 || (SH == 2 && code != kShiftNone)) {
+    if (code != kShiftNone) {
       const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
       xh = fmaf(-sxf, S.len_hi[0], xh);
       yh = fmaf(-syf, S.len_hi[1], yh);
@@ -426,7 +424,7 @@ __device__ __forceinline__ void list_load(const uint32_t *p, uint32_t (&e)[U]) {
 // One thread's walk over its list.  Entries arrive UNROLL (2 or 4) at a time in one vector load, the next
 // UNROLL being loaded while the current ones are evaluated; the position gathers of a batch are all issued
 // before its arithmetic.  Leftover entries (n mod UNROLL) are read one by one.
-template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM, int SH>
+template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM>
 __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                            const float4 &hi_i, const float4 &lo_i, int ti,
                                            const uint32_t *__restrict__ list, int n, float eps24, float sig2,
@@ -456,7 +454,7 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
     }
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u)
-      acc.template pair<SH>(s, S, fa, i, hi_i, lo_i, ti, e[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
+      acc.pair(s, S, fa, i, hi_i, lo_i, ti, e[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
     acc.flush();
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) e[u] = nx[u];
@@ -464,24 +462,7 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
   for (; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
     const float4 *q = s.pk + 2 * (int64_t)(en >> 5);
-    acc.template pair<SH>(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
-  }
-  acc.flush();
-}
-
-// entries [k0, n) of a list, one by one, all with an image shift (the shifted tail of a two-region list)
-template <bool GLOB, bool ONE_TYPE, bool KAHAN>
-__device__ __forceinline__ void plist_walk_shifted(const DeviceState &s, const SysDev &S, const ForceArgs &fa,
-                                                   int64_t i, const float4 &hi_i, const float4 &lo_i, int ti,
-                                                   const uint32_t *__restrict__ list, int k0, int n, float eps24,
-                                                   float sig2, float sh6, const float (*tab)[kMaxTypes * kMaxTypes],
-                                                   int T, float band, MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc) {
-  const int64_t stride = s.pl_stride;
-  for (int k = k0; k < n; ++k) {
-    const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    const float4 *q = s.pk + 2 * (int64_t)(en >> 5);
-    acc.template pair<1>(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
-    if (((k - k0) & 1) == 1) acc.flush();
+    acc.pair(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
   }
   acc.flush();
 }
@@ -562,16 +543,9 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
         s.x_prune[3 * i + 2] = s.z[i];
       }
     }
-  } else if (!s.prune) {
-    // two-region lists: the entries without image shift first (no shift arithmetic), then the shifted ones
-    const int n0 = oi == 1 ? s.pl_count0[i] : 0;
-    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM, 0>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list, n0, eps24, sig2,
-                                                         sh6, tab, T, band, acc);
-    plist_walk_shifted<GLOB, ONE_TYPE, KAHAN>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list, n0, n, eps24, sig2, sh6, tab,
-                                             T, band, acc);
   } else {
-    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM, 2>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list, n, eps24, sig2,
-                                                         sh6, tab, T, band, acc);
+    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list, n, eps24, sig2, sh6,
+                                                      tab, T, band, acc);
   }
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
   // epilogue keeps to the FP64 work the state needs: the force rounded once from its compensated sum, the

@@ -47,7 +47,6 @@ struct DeviceState {
   int32_t *cl_flags = nullptr;     // bit0: has owned member, bit1: has any real member
   int64_t *cp_start = nullptr;     // [nclusters]
   int32_t *cp_count = nullptr;     // [nclusters]
-  int32_t *cp_count0 = nullptr;    // [nclusters] leading entries without image shift (they come first)
   uint32_t *cp_list = nullptr;     // [cp_cap]
   int64_t cp_cap = 0;
   unsigned long long *cp_total = nullptr;  // device counter
@@ -60,7 +59,6 @@ struct DeviceState {
   int variant = 0;                 // kernel variant inside a traversal (tuner dimension)
   uint32_t *pl_list = nullptr;
   int32_t *pl_count = nullptr;     // [nslots]
-  int32_t *pl_count0 = nullptr;    // [nslots] leading entries without image shift (they come first)
   int pl_cap = 0;
   int64_t pl_stride = 0;
   int *pl_max = nullptr;           // device max of pl_count
