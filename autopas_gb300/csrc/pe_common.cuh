@@ -27,6 +27,7 @@ enum DeviceError : int {
   kErrListOverflow = 1,   // a cluster list exceeded kListBufPerWarp entries
   kErrListCapacity = 2,   // the global list buffer is too small (host regrows and retries)
   kErrTowerOverflow = 4,  // a tower holds more than kTowerSortMax particles
+  kErrEncode = 8,         // a particle left the range of the position encoding ([B, 2B) in every dimension)
 };
 
 // Per-system constants (device copy).
@@ -49,6 +50,11 @@ struct SysDev {
   double enc_B;
   float enc_far;  // -B: where dummies sit in the encoded frame, at least 2B from every real particle
   float len_hi[3], len_lo[3];
+  // compact record (pq): the exponent bits of B, the weight of one unit of the 16-bit low part (B * 2^-39),
+  // and len - len_hi in those units (an integer-valued float)
+  unsigned int pq_expb;
+  float pq_unit;
+  float len_lo_u[3];
   // float box tests of the list build: the box and image lengths in float (box rounded outwards), a bound on
   // the error of one float box gap (outward rounding of both boxes, the shift and the subtraction), and the
   // resulting bound on |float - FP64| of a squared box distance near (rc+skin)^2
@@ -71,6 +77,38 @@ __device__ __forceinline__ void split_hi_lo(double v, float &hi, float &lo) {
   const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1023 - 52): weight of the lowest fraction bit
   lo = __uint_as_float(__float_as_uint(__uint2float_rn((unsigned int)(a & 0x1fffffffull)) * scale) | sign);
 }
+
+// Compact position record of the particle-list force kernel (16 B: one sector-aligned load per gathered
+// particle).  For x' in [B, 2B) (exponent implicit) hi keeps the 23 fraction bits below the leading one and
+// lo the next 16 bits (units of B * 2^-39, truncated):
+//   w0 = [type:4 | own:2 | 0:3][hi x:23]   w1 = [lo z bits 0-8:9][hi y:23]
+//   w2 = [lo z bits 9-15:7 | 0:2][hi z:23] w3 = [lo y:16][lo x:16]
+// A dummy encodes x' = B (hi = lo = 0); the encoding places real particles at least 2(rc+skin) + 4 above B.
+__device__ __forceinline__ void pq_fields(double v, unsigned int &hi, unsigned int &lo) {
+  const unsigned long long f = (unsigned long long)__double_as_longlong(v) & 0xFFFFFFFFFFFFFull;  // 52 fraction bits
+  hi = (unsigned int)(f >> 29);
+  lo = (unsigned int)(f >> 13) & 0xFFFFu;
+}
+__device__ __forceinline__ uint4 pq_encode(const double (&xp)[3], int type, int own) {
+  unsigned int h[3], l[3];
+  for (int d = 0; d < 3; ++d) pq_fields(xp[d], h[d], l[d]);
+  uint4 r;
+  r.x = h[0] | ((unsigned int)(type & 15) << 23) | ((unsigned int)(own & 3) << 27);
+  r.y = h[1] | ((l[2] & 0x1FFu) << 23);
+  r.z = h[2] | ((l[2] >> 9) << 23);
+  r.w = l[0] | (l[1] << 16);
+  return r;
+}
+// hi as the float it stands for, given the exponent bits of B
+__device__ __forceinline__ float pq_hi(unsigned int w, unsigned int expb) { return __uint_as_float((w & 0x7FFFFFu) | expb); }
+// the low parts as integer-valued floats biased by 2^23 (exact; differences of two are the integer difference)
+__device__ __forceinline__ float pq_lox(const uint4 &q) { return __uint_as_float((q.w & 0xFFFFu) | 0x4B000000u); }
+__device__ __forceinline__ float pq_loy(const uint4 &q) { return __uint_as_float((q.w >> 16) | 0x4B000000u); }
+__device__ __forceinline__ float pq_loz(const uint4 &q) {
+  return __uint_as_float(((q.y >> 23) | ((q.z >> 23) << 9)) | 0x4B000000u);
+}
+__device__ __forceinline__ int pq_type(const uint4 &q) { return (int)((q.x >> 23) & 15u); }
+__device__ __forceinline__ int pq_own(const uint4 &q) { return (int)((q.x >> 27) & 3u); }
 
 // Velocity-Verlet factors per type, computed on the host with the reference's operation order
 // (TimeDiscretization.cpp:42: dt*dt/(2*m); :160: dt/(2*m)) so that no kernel divides in FP64.

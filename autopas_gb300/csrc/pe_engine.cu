@@ -98,6 +98,7 @@ struct pe_engine {
 
   ParticleArrays A, Bk;  // current and gather target
   DBuf<float4> pk;
+  DBuf<uint4> pq;
   DBuf<int32_t> slot_of;
   int64_t nuser = 0;     // particles of the last set_particles
   int64_t nslots = 0;
@@ -182,6 +183,7 @@ struct pe_engine {
     s.nreal = nuser;
     A.bind(s);
     s.pk = pk.p;
+    s.pq = pq.p;
     s.slot_of = slot_of.p;
     s.nsys = (int)sys.size();
     s.ntowers = ntowers;
@@ -386,14 +388,25 @@ __device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double
   const int o = s.own[i];
   const SysDev &S = s.sysd[s.sys[i]];
   const double p[3] = {px, py, pz};
+  double xp[3];
   float h[3], l[3];
-  for (int d = 0; d < 3; ++d) split_hi_lo(p[d] + S.enc_K[d], h[d], l[d]);
+  for (int d = 0; d < 3; ++d) {
+    xp[d] = p[d] + S.enc_K[d];
+    split_hi_lo(xp[d], h[d], l[d]);
+  }
+  const int ty = s.type[i];
   if (o == 0) {
     // dummies (parked far outside the box) sit at x' = -B: at least 2B from every real particle
     h[0] = h[1] = h[2] = S.enc_far;
     l[0] = l[1] = l[2] = 0.f;
+    xp[0] = xp[1] = xp[2] = S.enc_B;  // compact record: x' = B, far below every real particle
+  } else {
+    const double B2 = 2.0 * S.enc_B;
+    if (!(xp[0] >= S.enc_B && xp[0] < B2 && xp[1] >= S.enc_B && xp[1] < B2 && xp[2] >= S.enc_B && xp[2] < B2))
+      atomicOr(s.err, kErrEncode);
   }
-  const int w = (s.type[i] & 0xffff) | (o << 16);
+  s.pq[i] = pq_encode(xp, ty, o);
+  const int w = (ty & 0xffff) | (o << 16);
   s.pk[2 * (i)] = make_float4(h[0], h[1], h[2], __int_as_float(w));
   s.pk[2 * (i) + 1] = make_float4(l[0], l[1], l[2], 0.f);
 }
@@ -608,7 +621,9 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
     d.img_left[q] = d.bmin[q] + cutoff + skin;
     d.img_right[q] = d.bmax[q] - cutoff - skin;
   }
-  const double M = L + 2.0;
+  // the margin keeps real particles (halos reach L below bmin) at least 2L + 4 above x' = B, where dummies of
+  // the compact record sit
+  const double M = 3.0 * L + 4.0;
   double ext = 0;
   for (int q = 0; q < 3; ++q) ext = std::max(ext, d.len[q]);
   // x' = x + (B - o), o = bmin - M, must stay in [0, 2B) for x in [bmin - M, bmax + M] and for x' +- len
@@ -617,6 +632,13 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
   d.enc_B = B;
   d.enc_far = (float)(-B);
   const double ulp = std::ldexp(B, -23);
+  {
+    float bf = (float)B;
+    unsigned int bb;
+    std::memcpy(&bb, &bf, sizeof bb);
+    d.pq_expb = bb & 0x7F800000u;
+    d.pq_unit = (float)std::ldexp(B, -39);
+  }
   // float box tests of the list build (k_list_build): coordinates stay below Mc in magnitude, so one float
   // rounding is at most Mc * 2^-24 and a gap (outward-rounded boxes, a rounded shift, one subtraction) is
   // within 4 roundings, Mc * 2^-22, of its FP64 value; coord_tol doubles that
@@ -636,6 +658,7 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
     const double hi = std::nearbyint(d.len[q] / ulp) * ulp;  // a multiple of ulp(B): exact in float
     d.len_hi[q] = (float)hi;
     d.len_lo[q] = (float)(d.len[q] - hi);
+    d.len_lo_u[q] = (float)std::nearbyint((d.len[q] - hi) / std::ldexp(B, -39));
   }
 }
 
@@ -740,7 +763,7 @@ static int setup_grids(pe_engine *h) {
 
 static int ensure_particle_capacity(pe_engine *h) {
   const size_t n = (size_t)h->pcap;
-  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pk.ensure(2 * n) ||
+  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pk.ensure(2 * n) || !h->pq.ensure(n) ||
       !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
@@ -807,6 +830,8 @@ static int do_rebuild(pe_engine *h) {
   DeviceState s = h->state();
   const int64_t nold = h->nslots;
   h->launches += 1;
+  int e_steps = 0;  // errors flagged by the position updates since the last rebuild
+  PE_CUDA(h, cudaMemcpyAsync(&e_steps, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (nold > 0) k_wrap<<<(unsigned)((nold + 255) / 256), 256, 0, st>>>(s, nold);
   PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
   launch_bin(s, nold, h->key.p, h->tower_of.p, st);
@@ -822,6 +847,8 @@ static int do_rebuild(pe_engine *h) {
   PE_CUDA(h, cudaMemcpyAsync(&maxt, h->dmax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   PE_CUDA(h, cudaStreamSynchronize(st));
   PE_TRY(h->cuda_check("binning"));
+  if (e_steps & kErrEncode)
+    return h->fail(PE_ERR_DOMAIN, "a particle moved beyond the encodable range of its system between rebuilds");
   if (maxt > kTowerSortMax)
     return h->fail(PE_ERR_TOWER_OVERFLOW, "a tower holds %d particles; the on-chip tower sort supports %d", maxt,
                    kTowerSortMax);
@@ -852,7 +879,8 @@ static int do_rebuild(pe_engine *h) {
       if (!h->cp_list.ensure((size_t)est)) return h->fail(PE_ERR_OOM, "cluster-pair list (%lld)", (long long)est);
     }
     s = h->state();
-    PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
+    // the first attempt keeps what k_pack flagged; a retry starts from a clean flag word
+    if (attempt > 0) PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
     launch_list_build(s, st);
     h->launches += 1;
     int e = 0;
@@ -862,6 +890,9 @@ static int do_rebuild(pe_engine *h) {
     PE_CUDA(h, cudaStreamSynchronize(st));
     PE_TRY(h->cuda_check("list build"));
     if (e & kErrTowerOverflow) return h->fail(PE_ERR_TOWER_OVERFLOW, "tower overflow in sort");
+    if (e & kErrEncode)
+      return h->fail(PE_ERR_DOMAIN, "a particle lies beyond the encodable range of its system (more than "
+                                    "2(rc+skin)+4 outside the box)");
     if (e & kErrListOverflow)
       return h->fail(PE_ERR_LIST_OVERFLOW, "a cluster list exceeded %d entries", kListBufPerWarp);
     if (e & kErrListCapacity) {
@@ -1160,6 +1191,7 @@ int pe_destroy(pe_engine *h) {
   h->A.release();
   h->Bk.release();
   h->pk.release();
+  h->pq.release();
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})

@@ -340,30 +340,17 @@ struct MixedAcc {
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
   int hits = 0, hhalo = 0;
 
-  // returns the pair's FP32 squared distance (the re-prune test uses it)
-  __device__ __forceinline__ float pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                       const float4 &hi_i, const float4 &lo_i, int ti, uint32_t ent,
-                                       const float4 &hj, const float4 &lj, float eps24, float sig2, float sh6,
-                                       const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
-    const int code = ent & 31;
-    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-    if (code != kShiftNone) {
-      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
-      xh = fmaf(-sxf, S.len_hi[0], xh);
-      yh = fmaf(-syf, S.len_hi[1], yh);
-      zh = fmaf(-szf, S.len_hi[2], zh);
-      xl = fmaf(-sxf, S.len_lo[0], xl);
-      yl = fmaf(-syf, S.len_lo[1], yl);
-      zl = fmaf(-szf, S.len_lo[2], zl);
-    }
-    const float dx = (xh - hj.x) + (xl - lj.x);
-    const float dy = (yh - hj.y) + (yl - lj.y);
-    const float dz = (zh - hj.z) + (zl - lj.z);
+  // One pair, given its displacement rounded once to FP32: cutoff mask (FP64 re-test near rc), LJ in FP32,
+  // batch sums and globals.  Returns the squared distance (the re-prune test uses it).
+  __device__ __forceinline__ float accum(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                        uint32_t ent, int code, float dx, float dy, float dz, int tj, int oj,
+                                        int ti, float eps24, float sig2, float sh6,
+                                        const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     bool mask = (r2 <= fa.rc2f);
     if (fabsf(r2 - fa.rc2f) <= band) mask = exact_within(s, S, i, (int64_t)(ent >> 5), code, fa.rc2);
     if (!ONE_TYPE) {
-      const int kk = ti * T + (__float_as_int(hj.w) & 0xffff);
+      const int kk = ti * T + tj;
       eps24 = tab[0][kk];
       sig2 = tab[1][kk];
       sh6 = tab[2][kk];
@@ -385,9 +372,58 @@ struct MixedAcc {
       vy = fmaf(py, dy, vy);
       vz = fmaf(pz, dz, vz);
       hits += mask ? 1 : 0;
-      if (!S.periodic) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
+      if (!S.periodic) hhalo += (mask && oj == 2) ? 1 : 0;
     }
     return r2;
+  }
+
+  // a pair from the hi/lo float4 records (pk)
+  __device__ __forceinline__ float pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                       const float4 &hi_i, const float4 &lo_i, int ti, uint32_t ent,
+                                       const float4 &hj, const float4 &lj, float eps24, float sig2, float sh6,
+                                       const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
+    const int code = ent & 31;
+    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
+    if (code != kShiftNone) {
+      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      xh = fmaf(-sxf, S.len_hi[0], xh);
+      yh = fmaf(-syf, S.len_hi[1], yh);
+      zh = fmaf(-szf, S.len_hi[2], zh);
+      xl = fmaf(-sxf, S.len_lo[0], xl);
+      yl = fmaf(-syf, S.len_lo[1], yl);
+      zl = fmaf(-szf, S.len_lo[2], zl);
+    }
+    const float dx = (xh - hj.x) + (xl - lj.x);
+    const float dy = (yh - hj.y) + (yl - lj.y);
+    const float dz = (zh - hj.z) + (zl - lj.z);
+    const int w = __float_as_int(hj.w);
+    return accum(s, S, fa, i, ent, code, dx, dy, dz, w & 0xffff, w >> 16, ti, eps24, sig2, sh6, tab, T, band);
+  }
+
+  // a pair from the compact record (pq) of j; iq holds i's hi parts and biased low parts as floats.  The
+  // displacement is formed exactly (hi differences are multiples of ulp(B); low-part differences are integers
+  // times a power of two) and rounded once, by the final fma.
+  __device__ __forceinline__ float pair_q(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                         const float (&iq)[6], int ti, uint32_t ent, const uint4 &q, float eps24,
+                                         float sig2, float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
+                                         float band) {
+    const int code = ent & 31;
+    float xh = iq[0], yh = iq[1], zh = iq[2], xl = iq[3], yl = iq[4], zl = iq[5];
+    if (code != kShiftNone) {
+      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      xh = fmaf(-sxf, S.len_hi[0], xh);
+      yh = fmaf(-syf, S.len_hi[1], yh);
+      zh = fmaf(-szf, S.len_hi[2], zh);
+      xl = fmaf(-sxf, S.len_lo_u[0], xl);
+      yl = fmaf(-syf, S.len_lo_u[1], yl);
+      zl = fmaf(-szf, S.len_lo_u[2], zl);
+    }
+    const unsigned int eb = S.pq_expb;
+    const float u = S.pq_unit;
+    const float dx = fmaf(xl - pq_lox(q), u, xh - pq_hi(q.x, eb));
+    const float dy = fmaf(yl - pq_loy(q), u, yh - pq_hi(q.y, eb));
+    const float dz = fmaf(zl - pq_loz(q), u, zh - pq_hi(q.z, eb));
+    return accum(s, S, fa, i, ent, code, dx, dy, dz, pq_type(q), pq_own(q), ti, eps24, sig2, sh6, tab, T, band);
   }
 
   __device__ __forceinline__ void flush() {
@@ -426,9 +462,9 @@ __device__ __forceinline__ void list_load(const uint32_t *p, uint32_t (&e)[U]) {
 // before its arithmetic.  Leftover entries (n mod UNROLL) are read one by one.
 template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM>
 __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                           const float4 &hi_i, const float4 &lo_i, int ti,
-                                           const uint32_t *__restrict__ list, int n, float eps24, float sig2,
-                                           float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
+                                           const float (&iq)[6], int ti, const uint32_t *__restrict__ list, int n,
+                                           float eps24, float sig2, float sh6,
+                                           const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
                                            MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc) {
   static_assert(UNROLL == 2 || UNROLL == 4, "batches of 2 or 4 entries");
   const int64_t stride = s.pl_stride;
@@ -445,24 +481,18 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) nx[u] = 0u;
     if (kn + UNROLL <= n) list_load<UNROLL, STREAM>(base + (int64_t)(kn >> 3) * bstride + (kn & 7), nx);
-    float4 hj[UNROLL], lj[UNROLL];
+    uint4 qj[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const float4 *q = s.pk + 2 * (int64_t)(e[u] >> 5);
-      hj[u] = __ldg(q);
-      lj[u] = __ldg(q + 1);
-    }
+    for (int u = 0; u < UNROLL; ++u) qj[u] = __ldg(s.pq + (e[u] >> 5));
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u)
-      acc.pair(s, S, fa, i, hi_i, lo_i, ti, e[u], hj[u], lj[u], eps24, sig2, sh6, tab, T, band);
+    for (int u = 0; u < UNROLL; ++u) acc.pair_q(s, S, fa, i, iq, ti, e[u], qj[u], eps24, sig2, sh6, tab, T, band);
     acc.flush();
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) e[u] = nx[u];
   }
   for (; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    const float4 *q = s.pk + 2 * (int64_t)(en >> 5);
-    acc.pair(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
+    acc.pair_q(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
   }
   acc.flush();
 }
@@ -471,7 +501,7 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
 // out.  Returns their number.
 template <bool GLOB, bool ONE_TYPE, bool KAHAN>
 __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const SysDev &S, const ForceArgs &fa,
-                                                  int64_t i, const float4 &hi_i, const float4 &lo_i, int ti,
+                                                  int64_t i, const float (&iq)[6], int ti,
                                                   const uint32_t *__restrict__ list, int n, float eps24, float sig2,
                                                   float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
                                                   float band, MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc,
@@ -480,8 +510,7 @@ __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const Sy
   int m = 0;
   for (int k = 0; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    const float4 *q = s.pk + 2 * (int64_t)(en >> 5);
-    const float r2 = acc.pair(s, S, fa, i, hi_i, lo_i, ti, en, __ldg(q), __ldg(q + 1), eps24, sig2, sh6, tab, T, band);
+    const float r2 = acc.pair_q(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
     if (r2 <= lim) out[plist_index(stride, i, m++)] = en;
     if ((k & 1) == 1) acc.flush();
   }
@@ -511,18 +540,18 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool inrange = i < s.nslots;
   const bool reprune = s.prune && s.disp_bits[0] >= f2bits(s.prune_half2);
-  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+  uint4 qi = make_uint4(0u, 0u, 0u, 0u);
   int n = 0, ti = 0, oi = 0;
   if (inrange) {
-    hi_i = s.pk[2 * (i)];
-    lo_i = s.pk[2 * (i) + 1];
-    const int wi = __float_as_int(hi_i.w);
-    ti = wi & 0xffff;
-    oi = wi >> 16;
+    qi = s.pq[i];
+    ti = pq_type(qi);
+    oi = pq_own(qi);
     if (oi == 1) n = reprune ? min(s.pl_count[i], s.pl_cap) : s.fl_count[i];
   }
   const int sy = inrange ? s.sys[i] : 0;
   const SysDev &S = s.sysd[sy];
+  const float iq[6] = {pq_hi(qi.x, S.pq_expb), pq_hi(qi.y, S.pq_expb), pq_hi(qi.z, S.pq_expb),
+                       pq_lox(qi), pq_loy(qi), pq_loz(qi)};
   float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
   if (ONE_TYPE) {
     eps24 = (float)s.types->eps24[0];
@@ -533,8 +562,8 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
   if (reprune) {
     const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
-    const int m = plist_walk_reprune<GLOB, ONE_TYPE, KAHAN>(s, S, fa, i, hi_i, lo_i, ti, s.pl_list, n, eps24, sig2,
-                                                           sh6, tab, T, band, acc, s.pi_list, lim);
+    const int m = plist_walk_reprune<GLOB, ONE_TYPE, KAHAN>(s, S, fa, i, iq, ti, s.pl_list, n, eps24, sig2, sh6, tab,
+                                                           T, band, acc, s.pi_list, lim);
     if (inrange) {
       s.pi_count[i] = m;
       if (oi != 0) {
@@ -544,8 +573,8 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       }
     }
   } else {
-    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, hi_i, lo_i, ti, s.fl_list, n, eps24, sig2, sh6,
-                                                      tab, T, band, acc);
+    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, sh6, tab, T,
+                                                      band, acc);
   }
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
   // epilogue keeps to the FP64 work the state needs: the force rounded once from its compensated sum, the
