@@ -547,7 +547,8 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
       const int code = ent & 31;
       float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
       if (code != kShiftNone) {
-        const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+        const float4 us = c_unit_shift[code];
+        const float sxf = us.x, syf = us.y, szf = us.z;
         xh = fmaf(-sxf, S.len_hi[0], xh);
         yh = fmaf(-syf, S.len_hi[1], yh);
         zh = fmaf(-szf, S.len_hi[2], zh);
@@ -665,7 +666,8 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
     const float4 hj = __ldg(&s.pk[2 * (j)]), lj = __ldg(&s.pk[2 * (j) + 1]);
     float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
     if (code != kShiftNone) {
-      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      const float4 us = c_unit_shift[code];
+      const float sxf = us.x, syf = us.y, szf = us.z;
       xh = fmaf(-sxf, S.len_hi[0], xh);
       yh = fmaf(-syf, S.len_hi[1], yh);
       zh = fmaf(-szf, S.len_hi[2], zh);

@@ -78,6 +78,20 @@ __device__ __forceinline__ void split_hi_lo(double v, float &hi, float &lo) {
   lo = __uint_as_float(__float_as_uint(__uint2float_rn((unsigned int)(a & 0x1fffffffull)) * scale) | sign);
 }
 
+// Unit image shift (sx, sy, sz) of each shift code, for the float kernels: one constant-cache load instead
+// of integer divisions and conversions.
+static __constant__ float4 c_unit_shift[27] = {
+    {-1.f, -1.f, -1.f, 0.f}, {0.f, -1.f, -1.f, 0.f}, {1.f, -1.f, -1.f, 0.f},
+    {-1.f, 0.f, -1.f, 0.f}, {0.f, 0.f, -1.f, 0.f}, {1.f, 0.f, -1.f, 0.f},
+    {-1.f, 1.f, -1.f, 0.f}, {0.f, 1.f, -1.f, 0.f}, {1.f, 1.f, -1.f, 0.f},
+    {-1.f, -1.f, 0.f, 0.f}, {0.f, -1.f, 0.f, 0.f}, {1.f, -1.f, 0.f, 0.f},
+    {-1.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {1.f, 0.f, 0.f, 0.f},
+    {-1.f, 1.f, 0.f, 0.f}, {0.f, 1.f, 0.f, 0.f}, {1.f, 1.f, 0.f, 0.f},
+    {-1.f, -1.f, 1.f, 0.f}, {0.f, -1.f, 1.f, 0.f}, {1.f, -1.f, 1.f, 0.f},
+    {-1.f, 0.f, 1.f, 0.f}, {0.f, 0.f, 1.f, 0.f}, {1.f, 0.f, 1.f, 0.f},
+    {-1.f, 1.f, 1.f, 0.f}, {0.f, 1.f, 1.f, 0.f}, {1.f, 1.f, 1.f, 0.f},
+};
+
 // Compact position record of the particle-list force kernel (16 B: one sector-aligned load per gathered
 // particle).  For x' in [B, 2B) (exponent implicit) hi keeps the 23 fraction bits below the leading one and
 // lo the next 16 bits (units of B * 2^-39, truncated):

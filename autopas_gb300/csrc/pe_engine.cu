@@ -1284,6 +1284,8 @@ int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, 
                                                                id != nullptr, system != nullptr);
     k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, n);
   }
+  // the first rebuild wraps and re-encodes every particle and checks the encoding range itself
+  PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
   h->nslots = n;
   h->have_particles = true;
   h->lists_valid = false;

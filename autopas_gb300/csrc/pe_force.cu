@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
       float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
       if (code != kShiftNone) {
         // the j image sits at x_j + s*len; moving i by -s*len instead keeps the hi difference exact
-        const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+        const float4 us = c_unit_shift[code];
+        const float sxf = us.x, syf = us.y, szf = us.z;
         xh = fmaf(-sxf, S.len_hi[0], xh);
         yh = fmaf(-syf, S.len_hi[1], yh);
         zh = fmaf(-szf, S.len_hi[2], zh);
@@ -385,7 +386,8 @@ struct MixedAcc {
     const int code = ent & 31;
     float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
     if (code != kShiftNone) {
-      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      const float4 us = c_unit_shift[code];
+      const float sxf = us.x, syf = us.y, szf = us.z;
       xh = fmaf(-sxf, S.len_hi[0], xh);
       yh = fmaf(-syf, S.len_hi[1], yh);
       zh = fmaf(-szf, S.len_hi[2], zh);
@@ -410,7 +412,8 @@ struct MixedAcc {
     const int code = ent & 31;
     float xh = iq[0], yh = iq[1], zh = iq[2], xl = iq[3], yl = iq[4], zl = iq[5];
     if (code != kShiftNone) {
-      const float sxf = (float)(code % 3 - 1), syf = (float)((code / 3) % 3 - 1), szf = (float)(code / 9 - 1);
+      const float4 us = c_unit_shift[code];
+      const float sxf = us.x, syf = us.y, szf = us.z;
       xh = fmaf(-sxf, S.len_hi[0], xh);
       yh = fmaf(-syf, S.len_hi[1], yh);
       zh = fmaf(-szf, S.len_hi[2], zh);
