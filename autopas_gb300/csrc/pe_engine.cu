@@ -213,6 +213,8 @@ struct pe_engine {
     s.pl_stride = pcap;
     s.pl_max = pl_max.p;
     s.prune = (cfg.prune_buffer > 0 && traversal == 1) ? 1 : 0;
+    s.any_halo_sys = 0;
+    for (const auto &S : sys) s.any_halo_sys |= S.desc.periodic ? 0 : 1;
     s.pi_list = pi_list.p;
     s.pi_count = pi_count.p;
     s.x_prune = x_prune.p;

@@ -333,9 +333,11 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
 // entries read column-major so that a warp's list reads are coalesced.  Globals are reduced per cluster
 // (C consecutive lanes) to match the chunked system reduction.
 // ---------------------------------------------------------------------------------------------
-// one pair of the mixed kernels: displacement from the hi/lo positions, LJ in FP32, compensated sums
-template <bool GLOB, bool ONE_TYPE, bool KAHAN>
+// one pair of the mixed kernels: displacement from the hi/lo positions, LJ in FP32, compensated sums.
+// GM: 0 no globals, 1 globals, 2 globals and the owned-halo pair count of systems with explicit halos.
+template <int GM, bool ONE_TYPE, bool KAHAN>
 struct MixedAcc {
+  static constexpr bool GLOB = GM > 0;
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
   float bx = 0.f, by = 0.f, bz = 0.f;  // plain sum of the current batch, Kahan-added by flush()
   float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
@@ -373,7 +375,7 @@ struct MixedAcc {
       vy = fmaf(py, dy, vy);
       vz = fmaf(pz, dz, vz);
       hits += mask ? 1 : 0;
-      if (!S.periodic) hhalo += (mask && oj == 2) ? 1 : 0;
+      if (GM == 2 && !S.periodic) hhalo += (mask && oj == 2) ? 1 : 0;
     }
     return r2;
   }
@@ -405,13 +407,16 @@ struct MixedAcc {
   // a pair from the compact record (pq) of j; iq holds i's hi parts and biased low parts as floats.  The
   // displacement is formed exactly (hi differences are multiples of ulp(B); low-part differences are integers
   // times a power of two) and rounded once, by the final fma.
+  // SHIFT: false when no lane of the warp holds a shifted entry in this batch (no shift arithmetic), true
+  // otherwise (the shift of code kShiftNone is zero, so every lane applies its entry's shift unconditionally).
+  template <bool SHIFT>
   __device__ __forceinline__ float pair_q(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                          const float (&iq)[6], int ti, uint32_t ent, const uint4 &q, float eps24,
                                          float sig2, float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
                                          float band) {
     const int code = ent & 31;
     float xh = iq[0], yh = iq[1], zh = iq[2], xl = iq[3], yl = iq[4], zl = iq[5];
-    if (code != kShiftNone) {
+    if (SHIFT) {
       const float4 us = c_unit_shift[code];
       const float sxf = us.x, syf = us.y, szf = us.z;
       xh = fmaf(-sxf, S.len_hi[0], xh);
@@ -463,12 +468,12 @@ __device__ __forceinline__ void list_load(const uint32_t *p, uint32_t (&e)[U]) {
 // One thread's walk over its list.  Entries arrive UNROLL (2 or 4) at a time in one vector load, the next
 // UNROLL being loaded while the current ones are evaluated; the position gathers of a batch are all issued
 // before its arithmetic.  Leftover entries (n mod UNROLL) are read one by one.
-template <bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM>
+template <int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM>
 __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                            const float (&iq)[6], int ti, const uint32_t *__restrict__ list, int n,
                                            float eps24, float sig2, float sh6,
                                            const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
-                                           MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc) {
+                                           MixedAcc<GM, ONE_TYPE, KAHAN> &acc) {
   static_assert(UNROLL == 2 || UNROLL == 4, "batches of 2 or 4 entries");
   const int64_t stride = s.pl_stride;
   const uint32_t *base = list + i * kPlistBlock;
@@ -487,33 +492,45 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
     uint4 qj[UNROLL];
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) qj[u] = __ldg(s.pq + (e[u] >> 5));
+    bool shifted = false;
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) acc.pair_q(s, S, fa, i, iq, ti, e[u], qj[u], eps24, sig2, sh6, tab, T, band);
+    for (int u = 0; u < UNROLL; ++u) shifted |= (e[u] & 31u) != (uint32_t)kShiftNone;
+    // a warp-uniform choice: most batches of most warps hold no image-shifted entry
+    if (__any_sync(__activemask(), shifted)) {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u)
+        acc.template pair_q<true>(s, S, fa, i, iq, ti, e[u], qj[u], eps24, sig2, sh6, tab, T, band);
+    } else {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u)
+        acc.template pair_q<false>(s, S, fa, i, iq, ti, e[u], qj[u], eps24, sig2, sh6, tab, T, band);
+    }
     acc.flush();
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) e[u] = nx[u];
   }
   for (; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    acc.pair_q(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
+    acc.template pair_q<true>(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
   }
   acc.flush();
 }
 
 // The re-prune walk: the outer list (rc + skin) entry by entry; entries within lim also go to the inner list
 // out.  Returns their number.
-template <bool GLOB, bool ONE_TYPE, bool KAHAN>
+template <int GM, bool ONE_TYPE, bool KAHAN>
 __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const SysDev &S, const ForceArgs &fa,
                                                   int64_t i, const float (&iq)[6], int ti,
                                                   const uint32_t *__restrict__ list, int n, float eps24, float sig2,
                                                   float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
-                                                  float band, MixedAcc<GLOB, ONE_TYPE, KAHAN> &acc,
+                                                  float band, MixedAcc<GM, ONE_TYPE, KAHAN> &acc,
                                                   uint32_t *__restrict__ out, float lim) {
   const int64_t stride = s.pl_stride;
   int m = 0;
   for (int k = 0; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    const float r2 = acc.pair_q(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
+    const float r2 =
+        acc.template pair_q<true>(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
     if (r2 <= lim) out[plist_index(stride, i, m++)] = en;
     if ((k & 1) == 1) acc.flush();
   }
@@ -528,8 +545,9 @@ __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const Sy
 // buffer since the rebuild) to the inner lists and records the positions of the prune.  The flag is read
 // by every thread and cleared by a later launch, so all threads take the same branch.
 // STREAM: list entries loaded with the streaming (evict-first) hint
-template <int C, bool GLOB, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, bool STREAM>
+template <int C, int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, bool STREAM>
 __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
+  constexpr bool GLOB = GM > 0;
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
   const int T = s.ntypes;
   if (!ONE_TYPE) {
@@ -562,10 +580,10 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     sh6 = (float)s.types->shift6[0];
   }
   const float band = fa.rc2f * 2e-6f;
-  MixedAcc<GLOB, ONE_TYPE, KAHAN> acc;
+  MixedAcc<GM, ONE_TYPE, KAHAN> acc;
   if (reprune) {
     const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
-    const int m = plist_walk_reprune<GLOB, ONE_TYPE, KAHAN>(s, S, fa, i, iq, ti, s.pl_list, n, eps24, sig2, sh6, tab,
+    const int m = plist_walk_reprune<GM, ONE_TYPE, KAHAN>(s, S, fa, i, iq, ti, s.pl_list, n, eps24, sig2, sh6, tab,
                                                            T, band, acc, s.pi_list, lim);
     if (inrange) {
       s.pi_count[i] = m;
@@ -576,7 +594,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       }
     }
   } else {
-    plist_walk<GLOB, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, sh6, tab, T,
+    plist_walk<GM, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, sh6, tab, T,
                                                       band, acc);
   }
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
@@ -749,16 +767,23 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
         k_lj_mixed_plist<C, G, O, true, 2, 8, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
     }                                                                                    \
   } while (0)
+  // globals mode: none, globals, or globals with the owned-halo pair count (engines holding a system with
+  // explicit halos)
+  const int gm = fa.calc_globals ? (s.any_halo_sys ? 2 : 1) : 0;
   if (s.ntypes == 1) {
-    if (fa.calc_globals)
-      PE_PLIST(true, true);
+    if (gm == 2)
+      PE_PLIST(2, true);
+    else if (gm == 1)
+      PE_PLIST(1, true);
     else
-      PE_PLIST(false, true);
+      PE_PLIST(0, true);
   } else {
-    if (fa.calc_globals)
-      PE_PLIST(true, false);
+    if (gm == 2)
+      PE_PLIST(2, false);
+    else if (gm == 1)
+      PE_PLIST(1, false);
     else
-      PE_PLIST(false, false);
+      PE_PLIST(0, false);
   }
 #undef PE_PLIST
 }

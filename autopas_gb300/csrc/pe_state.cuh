@@ -69,6 +69,7 @@ struct DeviceState {
   // rolling pruning: inner lists within rc + prune buffer, refreshed from the outer lists on the device when
   // a particle has moved half the buffer since the last prune (see launch_prune)
   int prune = 0;
+  int any_halo_sys = 0;            // 1 when some system of the engine is non-periodic (explicit halos)
   uint32_t *pi_list = nullptr;
   int32_t *pi_count = nullptr;
   double *x_prune = nullptr;       // [3 * slots] positions at the last prune
