@@ -4,7 +4,7 @@
 // (applicationLibrary/molecularDynamics/molecularDynamicsLibrary/AxilrodTellerMutoFunctor.h:186-293, 360-385).
 //
 // One warp per owned particle i.  The warp first gathers the neighbours of i within the triplet cutoff from i's
-// particle list (displacements d = r_i - r_j from the hi/lo positions, so each is rounded once to FP32) into
+// particle list (displacements d = r_i - r_j from the compact position records, each rounded once to FP32) into
 // shared memory, then the lanes walk the pairs (j, k) of that set; every triplet with all three distances within
 // the cutoff contributes the reference's force on i (forceI, :231-240) and 3*Upot (:268).  Each triplet is thus
 // evaluated once from each of its vertices and no atomics are needed.  Near-cutoff distances repeat the test in
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
     return;
   }
   const SysDev &S = s.sysd[s.sys[i]];
-  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
+  const PQPos pi = pq_decode(s.pq[i], S.pq_expb);
   const int n = min(s.pl_count[i], s.pl_cap);
   const float band = aa.rc2f * 2e-6f;
   // phase 1: neighbours within the triplet cutoff, in list order
@@ -75,21 +75,7 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
       ent = s.pl_list[plist_index(s.pl_stride, i, k)];
       const int64_t j = ent >> 5;
       const int code = ent & 31;
-      const float4 hj = s.pk[2 * (j)], lj = s.pk[2 * (j) + 1];
-      float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-      if (code != kShiftNone) {
-        const float4 us = c_unit_shift[code];
-        const float sxf = us.x, syf = us.y, szf = us.z;
-        xh = fmaf(-sxf, S.len_hi[0], xh);
-        yh = fmaf(-syf, S.len_hi[1], yh);
-        zh = fmaf(-szf, S.len_hi[2], zh);
-        xl = fmaf(-sxf, S.len_lo[0], xl);
-        yl = fmaf(-syf, S.len_lo[1], yl);
-        zl = fmaf(-szf, S.len_lo[2], zl);
-      }
-      d.x = (xh - hj.x) + (xl - lj.x);
-      d.y = (yh - hj.y) + (yl - lj.y);
-      d.z = (zh - hj.z) + (zl - lj.z);
+      pq_disp(pi, S, code, s.pq[j], d.x, d.y, d.z);
       d.w = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
       keep = d.w <= aa.rc2f;
       if (fabsf(d.w - aa.rc2f) <= band) keep = img_dist2(s, S, i, kShiftNone, j, code) <= aa.rc2;

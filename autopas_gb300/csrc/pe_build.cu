@@ -464,7 +464,7 @@ void launch_list_build(DeviceState &s, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------------------------
 // 6. particle neighbour lists from the (full) cluster-pair lists: every j within rc+skin of an owned i,
-//    tested on the hi/lo float positions with a relative margin of 1e-5 on (rc+skin)^2 (the float distance is
+//    tested on the compact position records with a relative margin of 1e-5 on (rc+skin)^2 (the float distance is
 //    within ~1e-7 of the FP64 one, so the list is a superset of the FP64 rc+skin pair set).  Every list is
 //    appended in (cluster-pair entry, j) order, so it has a deterministic order.
 // ---------------------------------------------------------------------------------------------
@@ -474,7 +474,7 @@ void launch_list_build(DeviceState &s, cudaStream_t st) {
 template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   constexpr int G = 32 / C;
-  __shared__ float4 sj[4][G][C][2];
+  __shared__ uint4 sj[4][G][C];  // the compact records of the group's current j-cluster
   // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
   // most one block)
   __shared__ __align__(16) uint32_t stage[4][32][2 * kPlistBlock];
@@ -485,17 +485,20 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   const int64_t i = A * C + ii;
   int n = 0, oi = 0;
   const uint32_t *lst = s.cp_list;
-  float4 hi_i = make_float4(0.f, 0.f, 0.f, 0.f), lo_i = hi_i;
+  uint4 qi = make_uint4(0u, 0u, 0u, 0u);
   int sy = 0;
   if (validA) {
     n = s.cp_count[A];
     lst = s.cp_list + s.cp_start[A];
-    hi_i = s.pk[2 * i];
-    lo_i = s.pk[2 * i + 1];
-    oi = __float_as_int(hi_i.w) >> 16;
+    qi = s.pq[i];
+    oi = pq_own(qi);
     sy = s.cl_sys[A];
   }
   const SysDev &S = s.sysd[sy];
+  const unsigned int eb = S.pq_expb;
+  const float unit = S.pq_unit;
+  const float hxi = pq_hi(qi.x, eb), hyi = pq_hi(qi.y, eb), hzi = pq_hi(qi.z, eb);
+  const float lxi = pq_lox(qi), lyi = pq_loy(qi), lzi = pq_loz(qi);
   int nmax = n;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
@@ -517,56 +520,40 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   uint32_t ech = ii < n ? __ldg(lst + ii) : 0u;
   uint32_t ech_next = C + ii < n ? __ldg(lst + C + ii) : 0u;
   uint32_t ent_next = __shfl_sync(full, ech, g * C);
-  float4 ph = make_float4(0.f, 0.f, 0.f, 0.f), pl = ph;
-  if (0 < n) {
-    const int64_t j = (int64_t)(ent_next >> 5) * C + ii;
-    ph = __ldg(&s.pk[2 * j]);
-    pl = __ldg(&s.pk[2 * j + 1]);
-  }
+  uint4 pj = make_uint4(0u, 0u, 0u, 0u);
+  if (0 < n) pj = __ldg(&s.pq[(int64_t)(ent_next >> 5) * C + ii]);
   int cnt = 0;
   for (int e = 0; e < nmax; ++e) {
     const bool act = e < n;
     const uint32_t ent = ent_next;
-    if (act) {
-      sj[w][g][ii][0] = ph;
-      sj[w][g][ii][1] = pl;
-    }
+    if (act) sj[w][g][ii] = pj;
     const int e1 = e + 1;
     if ((e1 & (C - 1)) == 0) {
       ech = ech_next;
       ech_next = e1 + C + ii < n ? __ldg(lst + e1 + C + ii) : 0u;
     }
     ent_next = __shfl_sync(full, ech, g * C + (e1 & (C - 1)));
-    if (e1 < n) {
-      const int64_t j = (int64_t)(ent_next >> 5) * C + ii;
-      ph = __ldg(&s.pk[2 * j]);
-      pl = __ldg(&s.pk[2 * j + 1]);
-    }
+    if (e1 < n) pj = __ldg(&s.pq[(int64_t)(ent_next >> 5) * C + ii]);
     __syncwarp();
     if (act && oi == 1) {
       const int code = ent & 31;
-      float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-      if (code != kShiftNone) {
-        const float4 us = c_unit_shift[code];
-        const float sxf = us.x, syf = us.y, szf = us.z;
-        xh = fmaf(-sxf, S.len_hi[0], xh);
-        yh = fmaf(-syf, S.len_hi[1], yh);
-        zh = fmaf(-szf, S.len_hi[2], zh);
-        xl = fmaf(-sxf, S.len_lo[0], xl);
-        yl = fmaf(-syf, S.len_lo[1], yl);
-        zl = fmaf(-szf, S.len_lo[2], zl);
-      }
+      // i's position moved by minus the image shift (exact: hi on the ulp(B) grid, low parts integers)
+      const float4 us = c_unit_shift[code];
+      const float xh = fmaf(-us.x, S.len_hi[0], hxi), yh = fmaf(-us.y, S.len_hi[1], hyi);
+      const float zh = fmaf(-us.z, S.len_hi[2], hzi);
+      const float xl = fmaf(-us.x, S.len_lo_u[0], lxi), yl = fmaf(-us.y, S.len_lo_u[1], lyi);
+      const float zl = fmaf(-us.z, S.len_lo_u[2], lzi);
       const uint32_t ebase = (((ent >> 5) * (uint32_t)C) << 5) | (uint32_t)code;
       const int before = cnt;
-      // dummies sit at x' = -B, at least 2B from everything, so the distance test excludes them; r2 > 0
-      // excludes i itself.  Branch-free append: the entry is always written at the ring position, which only
-      // advances when it is kept.
+      // dummies sit at x' = B, at least 2(rc+skin) + 4 from every real particle, so the distance test
+      // excludes them; r2 > 0 excludes i itself.  Branch-free append: the entry is always written at the ring
+      // position, which only advances when it is kept.
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
-        const float4 hj = sj[w][g][jj][0], lj = sj[w][g][jj][1];
-        const float dx = (xh - hj.x) + (xl - lj.x);
-        const float dy = (yh - hj.y) + (yl - lj.y);
-        const float dz = (zh - hj.z) + (zl - lj.z);
+        const uint4 q = sj[w][g][jj];
+        const float dx = fmaf(xl - pq_lox(q), unit, xh - pq_hi(q.x, eb));
+        const float dy = fmaf(yl - pq_loy(q), unit, yh - pq_hi(q.y, eb));
+        const float dz = fmaf(zl - pq_loz(q), unit, zh - pq_hi(q.z, eb));
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
         cnt += ((r2 > 0.f) && (r2 <= L2f)) ? 1 : 0;
@@ -656,28 +643,13 @@ __global__ void __launch_bounds__(128) k_prune(DeviceState s) {
   // whole outer list when particles have used up the skin beyond the buffer since the rebuild
   const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
   const SysDev &S = s.sysd[s.sys[i]];
-  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
+  const PQPos pi = pq_decode(s.pq[i], S.pq_expb);
   const int n = min(s.pl_count[i], s.pl_cap);
   int m = 0;
   for (int k = 0; k < n; ++k) {
     const uint32_t ent = __ldg(s.pl_list + plist_index(s.pl_stride, i, k));
-    const int64_t j = ent >> 5;
-    const int code = ent & 31;
-    const float4 hj = __ldg(&s.pk[2 * (j)]), lj = __ldg(&s.pk[2 * (j) + 1]);
-    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-    if (code != kShiftNone) {
-      const float4 us = c_unit_shift[code];
-      const float sxf = us.x, syf = us.y, szf = us.z;
-      xh = fmaf(-sxf, S.len_hi[0], xh);
-      yh = fmaf(-syf, S.len_hi[1], yh);
-      zh = fmaf(-szf, S.len_hi[2], zh);
-      xl = fmaf(-sxf, S.len_lo[0], xl);
-      yl = fmaf(-syf, S.len_lo[1], yl);
-      zl = fmaf(-szf, S.len_lo[2], zl);
-    }
-    const float dx = (xh - hj.x) + (xl - lj.x);
-    const float dy = (yh - hj.y) + (yl - lj.y);
-    const float dz = (zh - hj.z) + (zl - lj.z);
+    float dx, dy, dz;
+    pq_disp(pi, S, ent & 31, __ldg(&s.pq[ent >> 5]), dx, dy, dz);
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     if (r2 <= lim) s.pi_list[plist_index(s.pl_stride, i, m++)] = ent;
   }

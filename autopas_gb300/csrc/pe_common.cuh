@@ -5,9 +5,9 @@
 //   dummy slots to a multiple of the cluster size C, so cluster c owns slots [c*C, c*C+C).
 //   FP64 SoA:   x y z  vx vy vz  fx fy fz  ofx ofy ofz         (master state, 96 B/particle)
 //   int SoA:    type(int32) own(int8) sys(int32) orig(int32) id(int64)
-//   packed:     pk (2 float4 per slot, hi then lo): the position as an unevaluated sum hi+lo of two floats in a
-//               fixed binade [B, 2B) per system (w of hi carries type | ownership<<16), 32 B/particle in one
-//               sector, read by the mixed-precision kernels.
+//   packed:     pq (16 B per slot): the position mapped into a fixed binade [B, 2B) per system, kept as the
+//               fraction bits below the leading one (23 hi + 16 lo bits per coordinate) with type and
+//               ownership; read by every mixed-precision kernel (pq_encode / pq_disp below).
 //   clusters:   bbox (6 doubles), system, tower, flags; cluster-pair list entries are uint32
 //               (jcluster << 5 | image-shift code), one contiguous run per i-cluster.
 #pragma once
@@ -44,12 +44,11 @@ struct SysDev {
   int kx, ky;           // neighbour tower reach per dim (ceil(L/side))
   int periodic;
   int tower_base;       // first global tower index
-  // mixed-precision encoding: x' = x + enc_K in [B, 2B) (enc_K = B - o, o = bmin - margin); len split as hi
-  // (a multiple of ulp(B)) + lo
+  // mixed-precision encoding: x' = x + enc_K in [B, 2B) (enc_K = B - o, o = bmin - margin); len_hi is len
+  // rounded to a multiple of ulp(B)
   double enc_K[3];
   double enc_B;
-  float enc_far;  // -B: where dummies sit in the encoded frame, at least 2B from every real particle
-  float len_hi[3], len_lo[3];
+  float len_hi[3];
   // compact record (pq): the exponent bits of B, the weight of one unit of the 16-bit low part (B * 2^-39),
   // and len - len_hi in those units (an integer-valued float)
   unsigned int pq_expb;
@@ -62,21 +61,6 @@ struct SysDev {
   float coord_tol;
   float bb_tol2;
 };
-
-// v = hi + lo for a double v with 2^-74 <= |v| < 2^127: hi keeps the leading 24 significant bits of v
-// (truncated, so for v in [B, 2B) it is a multiple of B * 2^-23 and hi differences are exact), lo is the
-// remaining 29 bits rounded to float.  Integer operations only: this GPU's FP64 pipe (conversions included)
-// runs at 1/64 of the FP32 rate, and this split runs for every particle of every step.
-__device__ __forceinline__ void split_hi_lo(double v, float &hi, float &lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-  const unsigned long long a = b & 0x7fffffffffffffffull;
-  // (a >> 29) holds the biased double exponent above the top 23 fraction bits: rebias 1023 -> 127
-  hi = __uint_as_float(sign | (unsigned int)((a >> 29) - (896ull << 23)));
-  const unsigned int e = (unsigned int)(a >> 52);
-  const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1023 - 52): weight of the lowest fraction bit
-  lo = __uint_as_float(__float_as_uint(__uint2float_rn((unsigned int)(a & 0x1fffffffull)) * scale) | sign);
-}
 
 // Unit image shift (sx, sy, sz) of each shift code, for the float kernels: one constant-cache load instead
 // of integer divisions and conversions.
@@ -123,6 +107,25 @@ __device__ __forceinline__ float pq_loz(const uint4 &q) {
 }
 __device__ __forceinline__ int pq_type(const uint4 &q) { return (int)((q.x >> 23) & 15u); }
 __device__ __forceinline__ int pq_own(const uint4 &q) { return (int)((q.x >> 27) & 3u); }
+
+// a decoded record: hi parts as floats, low parts as integer-valued floats biased by 2^23
+struct PQPos {
+  float hx, hy, hz, lx, ly, lz;
+};
+__device__ __forceinline__ PQPos pq_decode(const uint4 &q, unsigned int expb) {
+  return {pq_hi(q.x, expb), pq_hi(q.y, expb), pq_hi(q.z, expb), pq_lox(q), pq_loy(q), pq_loz(q)};
+}
+// r_i - (r_j + s len) for the image shift s of code, each component formed exactly and rounded once: i is
+// moved by -s len instead (its hi part stays on the ulp(B) grid, its low part an integer)
+__device__ __forceinline__ void pq_disp(const PQPos &pi, const SysDev &S, int code, const uint4 &qj, float &dx,
+                                        float &dy, float &dz) {
+  const float4 us = c_unit_shift[code];
+  const unsigned int eb = S.pq_expb;
+  const float u = S.pq_unit;
+  dx = fmaf(fmaf(-us.x, S.len_lo_u[0], pi.lx) - pq_lox(qj), u, fmaf(-us.x, S.len_hi[0], pi.hx) - pq_hi(qj.x, eb));
+  dy = fmaf(fmaf(-us.y, S.len_lo_u[1], pi.ly) - pq_loy(qj), u, fmaf(-us.y, S.len_hi[1], pi.hy) - pq_hi(qj.y, eb));
+  dz = fmaf(fmaf(-us.z, S.len_lo_u[2], pi.lz) - pq_loz(qj), u, fmaf(-us.z, S.len_hi[2], pi.hz) - pq_hi(qj.z, eb));
+}
 
 // Velocity-Verlet factors per type, computed on the host with the reference's operation order
 // (TimeDiscretization.cpp:42: dt*dt/(2*m); :160: dt/(2*m)) so that no kernel divides in FP64.

@@ -97,7 +97,6 @@ struct pe_engine {
   std::string err;
 
   ParticleArrays A, Bk;  // current and gather target
-  DBuf<float4> pk;
   DBuf<uint4> pq;
   DBuf<int32_t> slot_of;
   int64_t nuser = 0;     // particles of the last set_particles
@@ -182,7 +181,6 @@ struct pe_engine {
     s.nslots = nslots;
     s.nreal = nuser;
     A.bind(s);
-    s.pk = pk.p;
     s.pq = pq.p;
     s.slot_of = slot_of.p;
     s.nsys = (int)sys.size();
@@ -389,28 +387,16 @@ __global__ void k_wrap(DeviceState s, int64_t n) {
 __device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double px, double py, double pz) {
   const int o = s.own[i];
   const SysDev &S = s.sysd[s.sys[i]];
-  const double p[3] = {px, py, pz};
-  double xp[3];
-  float h[3], l[3];
-  for (int d = 0; d < 3; ++d) {
-    xp[d] = p[d] + S.enc_K[d];
-    split_hi_lo(xp[d], h[d], l[d]);
-  }
-  const int ty = s.type[i];
+  double xp[3] = {px + S.enc_K[0], py + S.enc_K[1], pz + S.enc_K[2]};
   if (o == 0) {
-    // dummies (parked far outside the box) sit at x' = -B: at least 2B from every real particle
-    h[0] = h[1] = h[2] = S.enc_far;
-    l[0] = l[1] = l[2] = 0.f;
-    xp[0] = xp[1] = xp[2] = S.enc_B;  // compact record: x' = B, far below every real particle
+    // dummies (parked far outside the box) sit at x' = B, at least 2(rc+skin) + 4 from every real particle
+    xp[0] = xp[1] = xp[2] = S.enc_B;
   } else {
     const double B2 = 2.0 * S.enc_B;
     if (!(xp[0] >= S.enc_B && xp[0] < B2 && xp[1] >= S.enc_B && xp[1] < B2 && xp[2] >= S.enc_B && xp[2] < B2))
       atomicOr(s.err, kErrEncode);
   }
-  s.pq[i] = pq_encode(xp, ty, o);
-  const int w = (ty & 0xffff) | (o << 16);
-  s.pk[2 * (i)] = make_float4(h[0], h[1], h[2], __int_as_float(w));
-  s.pk[2 * (i) + 1] = make_float4(l[0], l[1], l[2], 0.f);
+  s.pq[i] = pq_encode(xp, s.type[i], o);
 }
 
 __device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) { pack_xyz(s, i, s.x[i], s.y[i], s.z[i]); }
@@ -632,7 +618,6 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
   // (image shifts); it lies in [B, 2B) for the particles themselves
   const double B = next_pow2(2.0 * ext + 2.0 * M + 4.0);
   d.enc_B = B;
-  d.enc_far = (float)(-B);
   const double ulp = std::ldexp(B, -23);
   {
     float bf = (float)B;
@@ -659,7 +644,6 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
     d.enc_K[q] = B - (d.bmin[q] - M);
     const double hi = std::nearbyint(d.len[q] / ulp) * ulp;  // a multiple of ulp(B): exact in float
     d.len_hi[q] = (float)hi;
-    d.len_lo[q] = (float)(d.len[q] - hi);
     d.len_lo_u[q] = (float)std::nearbyint((d.len[q] - hi) / std::ldexp(B, -39));
   }
 }
@@ -765,7 +749,7 @@ static int setup_grids(pe_engine *h) {
 
 static int ensure_particle_capacity(pe_engine *h) {
   const size_t n = (size_t)h->pcap;
-  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pk.ensure(2 * n) || !h->pq.ensure(n) ||
+  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pq.ensure(n) ||
       !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
@@ -1192,7 +1176,6 @@ int pe_destroy(pe_engine *h) {
   if (h->st) cudaStreamSynchronize(h->st);
   h->A.release();
   h->Bk.release();
-  h->pk.release();
   h->pq.release();
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,

@@ -95,10 +95,10 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
   const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
   const int ii = lane % C, jl = lane / C;
   const int64_t i = A * C + ii;
-  const float4 hi_i = s.pk[2 * (i)], lo_i = s.pk[2 * (i) + 1];
-  const int wi = __float_as_int(hi_i.w);
-  const int ti = wi & 0xffff, oi = wi >> 16;
+  const uint4 qi = s.pq[i];
+  const int ti = pq_type(qi), oi = pq_own(qi);
   const SysDev &S = s.sysd[s.cl_sys[A]];
+  const PQPos pi = pq_decode(qi, S.pq_expb);
   const bool halos = !S.periodic;
   float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
   if (ONE_TYPE) {
@@ -123,28 +123,14 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
       const uint32_t ent = __ldg(lst + ee);
       const int64_t j = (int64_t)(ent >> 5) * C + jj;
       const int code = ent & 31;
-      const float4 hj = __ldg(&s.pk[2 * (j)]);
-      const float4 lj = __ldg(&s.pk[2 * (j) + 1]);
-      float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-      if (code != kShiftNone) {
-        // the j image sits at x_j + s*len; moving i by -s*len instead keeps the hi difference exact
-        const float4 us = c_unit_shift[code];
-        const float sxf = us.x, syf = us.y, szf = us.z;
-        xh = fmaf(-sxf, S.len_hi[0], xh);
-        yh = fmaf(-syf, S.len_hi[1], yh);
-        zh = fmaf(-szf, S.len_hi[2], zh);
-        xl = fmaf(-sxf, S.len_lo[0], xl);
-        yl = fmaf(-syf, S.len_lo[1], yl);
-        zl = fmaf(-szf, S.len_lo[2], zl);
-      }
-      const float dx = (xh - hj.x) + (xl - lj.x);
-      const float dy = (yh - hj.y) + (yl - lj.y);
-      const float dz = (zh - hj.z) + (zl - lj.z);
+      const uint4 qj = __ldg(&s.pq[j]);
+      float dx, dy, dz;
+      pq_disp(pi, S, code, qj, dx, dy, dz);
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
       bool mask = (r2 <= rc2f) && (r2 > 0.f);
       if (fabsf(r2 - rc2f) <= band) mask = (r2 > 0.f) && exact_within(s, S, i, j, code, fa.rc2);
       if (!ONE_TYPE) {
-        const int k = ti * T + (__float_as_int(hj.w) & 0xffff);
+        const int k = ti * T + pq_type(qj);
         eps24 = tab[0][k];
         sig2 = tab[1][k];
         sh6 = tab[2][k];
@@ -172,7 +158,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
         vy = fmaf(py, dy, vy);
         vz = fmaf(pz, dz, vz);
         hits += mask ? 1 : 0;
-        if (halos) hhalo += (mask && (__float_as_int(hj.w) >> 16) == 2) ? 1 : 0;
+        if (halos) hhalo += (mask && pq_own(qj) == 2) ? 1 : 0;
       }
     }
   }
@@ -333,7 +319,7 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
 // entries read column-major so that a warp's list reads are coalesced.  Globals are reduced per cluster
 // (C consecutive lanes) to match the chunked system reduction.
 // ---------------------------------------------------------------------------------------------
-// one pair of the mixed kernels: displacement from the hi/lo positions, LJ in FP32, compensated sums.
+// one pair of the mixed kernels: displacement from the compact position records, LJ in FP32, compensated sums.
 // GM: 0 no globals, 1 globals, 2 globals and the owned-halo pair count of systems with explicit halos.
 template <int GM, bool ONE_TYPE, bool KAHAN>
 struct MixedAcc {
@@ -378,30 +364,6 @@ struct MixedAcc {
       if (GM == 2 && !S.periodic) hhalo += (mask && oj == 2) ? 1 : 0;
     }
     return r2;
-  }
-
-  // a pair from the hi/lo float4 records (pk)
-  __device__ __forceinline__ float pair(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                       const float4 &hi_i, const float4 &lo_i, int ti, uint32_t ent,
-                                       const float4 &hj, const float4 &lj, float eps24, float sig2, float sh6,
-                                       const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
-    const int code = ent & 31;
-    float xh = hi_i.x, yh = hi_i.y, zh = hi_i.z, xl = lo_i.x, yl = lo_i.y, zl = lo_i.z;
-    if (code != kShiftNone) {
-      const float4 us = c_unit_shift[code];
-      const float sxf = us.x, syf = us.y, szf = us.z;
-      xh = fmaf(-sxf, S.len_hi[0], xh);
-      yh = fmaf(-syf, S.len_hi[1], yh);
-      zh = fmaf(-szf, S.len_hi[2], zh);
-      xl = fmaf(-sxf, S.len_lo[0], xl);
-      yl = fmaf(-syf, S.len_lo[1], yl);
-      zl = fmaf(-szf, S.len_lo[2], zl);
-    }
-    const float dx = (xh - hj.x) + (xl - lj.x);
-    const float dy = (yh - hj.y) + (yl - lj.y);
-    const float dz = (zh - hj.z) + (zl - lj.z);
-    const int w = __float_as_int(hj.w);
-    return accum(s, S, fa, i, ent, code, dx, dy, dz, w & 0xffff, w >> 16, ti, eps24, sig2, sh6, tab, T, band);
   }
 
   // a pair from the compact record (pq) of j; iq holds i's hi parts and biased low parts as floats.  The

@@ -25,7 +25,6 @@ struct DeviceState {
   int32_t *type = nullptr, *sys = nullptr, *orig = nullptr;
   int8_t *own = nullptr;
   int64_t *id = nullptr;
-  float4 *pk = nullptr;  // [2 * slots]: hi at 2i, lo at 2i+1 (one 32-byte sector per particle)
   uint4 *pq = nullptr;   // [slots] compact 16-byte position records (pq_encode) for the particle-list force kernel
   // inverse map: user index -> slot
   int32_t *slot_of = nullptr;
