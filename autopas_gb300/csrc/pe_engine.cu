@@ -392,9 +392,12 @@ __device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double
     // dummies (parked far outside the box) sit at x' = B, at least 2(rc+skin) + 4 from every real particle
     xp[0] = xp[1] = xp[2] = S.enc_B;
   } else {
-    const double B2 = 2.0 * S.enc_B;
-    if (!(xp[0] >= S.enc_B && xp[0] < B2 && xp[1] >= S.enc_B && xp[1] < B2 && xp[2] >= S.enc_B && xp[2] < B2))
-      atomicOr(s.err, kErrEncode);
+    // x' in [B, 2B) <=> its exponent field is B's (integer test: FP64 compares run on the slow FP64 pipe)
+    const unsigned long long eB = (unsigned long long)__double_as_longlong(S.enc_B) >> 52;
+    const bool ok = ((unsigned long long)__double_as_longlong(xp[0]) >> 52) == eB &&
+                    ((unsigned long long)__double_as_longlong(xp[1]) >> 52) == eB &&
+                    ((unsigned long long)__double_as_longlong(xp[2]) >> 52) == eB;
+    if (!ok) atomicOr(s.err, kErrEncode);
   }
   s.pq[i] = pq_encode(xp, s.type[i], o);
 }
