@@ -330,12 +330,12 @@ __device__ __forceinline__ bool box_within_fp64(const DeviceState &s, const SysD
   return (g0 * g0 + g1 * g1 + g2 * g2) <= L2;
 }
 
-__global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
+__global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s, int buf_per_warp) {
   extern __shared__ uint32_t lbuf[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t A = blockIdx.x * (int64_t)kListWarps + warp;
   if (A >= s.nclusters) return;
-  uint32_t *buf = lbuf + warp * kListBufPerWarp;
+  uint32_t *buf = lbuf + warp * buf_per_warp;
   const int flagsA = s.cl_flags[A];
   const bool aOwned = flagsA & 1;
   if (!aOwned && !s.newton3) {
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
       }
       const unsigned am = __ballot_sync(0xffffffffu, accept);
       const int na = __popc(am);
-      if (cnt + na > kListBufPerWarp) {
+      if (cnt + na > buf_per_warp) {
         overflow = true;
         break;
       }
@@ -450,16 +450,19 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s) {
   }
 }
 
-void launch_list_build(DeviceState &s, cudaStream_t st) {
+// buf_per_warp: shared-memory entries per warp (the host starts small, for occupancy, and doubles it when a
+// cluster's list overflows)
+void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st) {
   static bool attr_set = false;
-  const size_t sm = (size_t)kListWarps * kListBufPerWarp * sizeof(uint32_t);
   if (!attr_set) {
-    cudaFuncSetAttribute(k_list_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_list_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kListWarps * kListBufMax * sizeof(uint32_t)));
     attr_set = true;
   }
+  const size_t sm = (size_t)kListWarps * buf_per_warp * sizeof(uint32_t);
   cudaMemsetAsync(s.cp_total, 0, sizeof(unsigned long long), st);
   const int64_t nb = (s.nclusters + kListWarps - 1) / kListWarps;
-  if (nb > 0) k_list_build<<<(unsigned)nb, kListWarps * 32, sm, st>>>(s);
+  if (nb > 0) k_list_build<<<(unsigned)nb, kListWarps * 32, sm, st>>>(s, buf_per_warp);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -474,7 +477,7 @@ void launch_list_build(DeviceState &s, cudaStream_t st) {
 template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   constexpr int G = 32 / C;
-  __shared__ uint4 sj[4][G][C];  // the compact records of the group's current j-cluster
+  __shared__ float4 sj[4][G][C][2];  // the group's current j-cluster, decoded: hi parts, biased low parts
   // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
   // most one block)
   __shared__ __align__(16) uint32_t stage[4][32][2 * kPlistBlock];
@@ -522,11 +525,15 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   uint32_t ent_next = __shfl_sync(full, ech, g * C);
   uint4 pj = make_uint4(0u, 0u, 0u, 0u);
   if (0 < n) pj = __ldg(&s.pq[(int64_t)(ent_next >> 5) * C + ii]);
+  // each lane decodes the j particle it staged, once, for the C lanes that test against it
   int cnt = 0;
   for (int e = 0; e < nmax; ++e) {
     const bool act = e < n;
     const uint32_t ent = ent_next;
-    if (act) sj[w][g][ii] = pj;
+    if (act) {
+      sj[w][g][ii][0] = make_float4(pq_hi(pj.x, eb), pq_hi(pj.y, eb), pq_hi(pj.z, eb), 0.f);
+      sj[w][g][ii][1] = make_float4(pq_lox(pj), pq_loy(pj), pq_loz(pj), 0.f);
+    }
     const int e1 = e + 1;
     if ((e1 & (C - 1)) == 0) {
       ech = ech_next;
@@ -550,10 +557,10 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
       // position, which only advances when it is kept.
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
-        const uint4 q = sj[w][g][jj];
-        const float dx = fmaf(xl - pq_lox(q), unit, xh - pq_hi(q.x, eb));
-        const float dy = fmaf(yl - pq_loy(q), unit, yh - pq_hi(q.y, eb));
-        const float dz = fmaf(zl - pq_loz(q), unit, zh - pq_hi(q.z, eb));
+        const float4 hj = sj[w][g][jj][0], lj = sj[w][g][jj][1];
+        const float dx = fmaf(xl - lj.x, unit, xh - hj.x);
+        const float dy = fmaf(yl - lj.y, unit, yh - hj.y);
+        const float dz = fmaf(zl - lj.z, unit, zh - hj.z);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
         cnt += ((r2 > 0.f) && (r2 <= L2f)) ? 1 : 0;

@@ -20,11 +20,12 @@ namespace pe {
 constexpr int kShiftNone = 13;      // code of the zero image shift ((0+1) + 3*(0+1) + 9*(0+1))
 constexpr int kMaxTypes = 16;       // type-table bound held in shared memory by the kernels
 constexpr int kTowerSortMax = 4096; // particles per tower sorted on chip
-constexpr int kListBufPerWarp = 2048;
+constexpr int kListBufStart = 512;  // cluster-pair entries per warp buffered on chip at first
+constexpr int kListBufMax = 8192;   // largest buffer the list build grows to
 
 enum DeviceError : int {
   kErrNone = 0,
-  kErrListOverflow = 1,   // a cluster list exceeded kListBufPerWarp entries
+  kErrListOverflow = 1,   // a cluster list exceeded the on-chip buffer (the host grows it and retries)
   kErrListCapacity = 2,   // the global list buffer is too small (host regrows and retries)
   kErrTowerOverflow = 4,  // a tower holds more than kTowerSortMax particles
   kErrEncode = 8,         // a particle left the range of the position encoding ([B, 2B) in every dimension)

@@ -91,6 +91,7 @@ struct pe_engine {
   int precision = PE_PRECISION_MIXED;
   int traversal = 1;
   int variant = 0;
+  int list_buf = kListBufStart;  // cluster-pair entries per warp buffered on chip by the list build
   bool tuned = false;
   std::vector<pe_tuning_entry> tune_log;
   int tune_chosen = -1;
@@ -862,7 +863,7 @@ static int do_rebuild(pe_engine *h) {
   launch_cluster_bbox(s, st);
   h->launches += 5;
   // cluster-pair lists (grow the buffer and retry when it is too small)
-  for (int attempt = 0; attempt < 4; ++attempt) {
+  for (int attempt = 0; attempt < 8; ++attempt) {
     if (h->cp_list.cap == 0) {
       const int64_t est = std::max<int64_t>(h->nclusters * (h->newton3 ? 48 : 96), 1024);
       if (!h->cp_list.ensure((size_t)est)) return h->fail(PE_ERR_OOM, "cluster-pair list (%lld)", (long long)est);
@@ -870,7 +871,7 @@ static int do_rebuild(pe_engine *h) {
     s = h->state();
     // the first attempt keeps what k_pack flagged; a retry starts from a clean flag word
     if (attempt > 0) PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
-    launch_list_build(s, st);
+    launch_list_build(s, h->list_buf, st);
     h->launches += 1;
     int e = 0;
     unsigned long long tot = 0;
@@ -882,8 +883,13 @@ static int do_rebuild(pe_engine *h) {
     if (e & kErrEncode)
       return h->fail(PE_ERR_DOMAIN, "a particle lies beyond the encodable range of its system (more than "
                                     "2(rc+skin)+4 outside the box)");
-    if (e & kErrListOverflow)
-      return h->fail(PE_ERR_LIST_OVERFLOW, "a cluster list exceeded %d entries", kListBufPerWarp);
+    if (e & kErrListOverflow) {
+      // a cluster's candidate list outgrew the on-chip buffer: double it (it stays doubled for this engine)
+      if (h->list_buf >= kListBufMax)
+        return h->fail(PE_ERR_LIST_OVERFLOW, "a cluster list exceeded %d entries", kListBufMax);
+      h->list_buf *= 2;
+      continue;
+    }
     if (e & kErrListCapacity) {
       const size_t want = (size_t)(tot * 1.25) + 1024;
       h->cp_list.release();

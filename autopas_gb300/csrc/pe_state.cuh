@@ -134,7 +134,7 @@ void launch_scatter(DeviceState &s, int64_t nslots_old, const int32_t *tower_of,
 int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *perm_src, int max_tower,
                       cudaStream_t st);
 void launch_cluster_bbox(DeviceState &s, cudaStream_t st);
-void launch_list_build(DeviceState &s, cudaStream_t st);
+void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st);
 void launch_plist_build(DeviceState &s, cudaStream_t st);
 void launch_prune_reset_refs(DeviceState &s, cudaStream_t st);   // x_prune = x_reb = x, force the next prune
 void launch_displacement(DeviceState &s, cudaStream_t st);       // update disp_bits from the current positions

@@ -220,6 +220,26 @@ def test_ensemble_systems_are_independent(eng_mod, orc, traversal):
                 assert gs[k]["upot"] == pytest.approx(glob[0], rel=1e-6)
 
 
+def test_long_cutoff_grows_the_list_buffer(eng_mod, orc):
+    """rc 6, skin 1, C = 4 at density 0.9: a cluster has more candidate cluster pairs than the list build's
+    first on-chip buffer holds; the build grows the buffer and the forces stay the oracle's."""
+    from autopas_gb300 import workloads
+    bmin, bmax = np.zeros(3), np.full(3, 16.0)
+    pos = workloads.rsa(3600, bmin, bmax, bmin, bmax, 0.85, seed=9)
+    rc, skin = 6.0, 1.0
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+    R = R[: len(pos)]
+    for prec, tol in ((eng_mod.PRECISION_FP64, 1e-12), (eng_mod.PRECISION_MIXED, 1e-6)):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=prec, cluster_size=4, traversal=1)
+        e.set_particles(pos)
+        g = e.compute_forces()[0]
+        assert rel_rms(e.forces(), R) <= tol
+        assert g["upot"] == pytest.approx(glob[0], rel=tol)
+        info = e.info()
+        assert info["num_cluster_pairs"] > 512 * info["num_clusters"]  # more than the first buffer, on average
+
+
 def test_errors_are_reported_not_hidden(eng_mod):
     with pytest.raises(eng_mod.EngineError) as ei:
         eng_mod.PairEngine(2.5, 0.3, ([0, 0, 0], [4.0, 20, 20]), periodic=True).set_particles(
