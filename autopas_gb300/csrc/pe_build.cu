@@ -477,7 +477,9 @@ void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st) {
 template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   constexpr int G = 32 / C;
-  __shared__ float4 sj[4][G][C][2];  // the group's current j-cluster, decoded: hi parts, biased low parts
+  // the group's current j-cluster, decoded (hi parts, biased low parts); one float4 of padding per group keeps
+  // the four groups of a warp in different shared-memory banks
+  __shared__ float4 sj[4][G][2 * C + 1];
   // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
   // most one block)
   __shared__ __align__(16) uint32_t stage[4][32][2 * kPlistBlock];
@@ -531,8 +533,8 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
     const bool act = e < n;
     const uint32_t ent = ent_next;
     if (act) {
-      sj[w][g][ii][0] = make_float4(pq_hi(pj.x, eb), pq_hi(pj.y, eb), pq_hi(pj.z, eb), 0.f);
-      sj[w][g][ii][1] = make_float4(pq_lox(pj), pq_loy(pj), pq_loz(pj), 0.f);
+      sj[w][g][2 * ii] = make_float4(pq_hi(pj.x, eb), pq_hi(pj.y, eb), pq_hi(pj.z, eb), 0.f);
+      sj[w][g][2 * ii + 1] = make_float4(pq_lox(pj), pq_loy(pj), pq_loz(pj), 0.f);
     }
     const int e1 = e + 1;
     if ((e1 & (C - 1)) == 0) {
@@ -557,7 +559,7 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
       // position, which only advances when it is kept.
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
-        const float4 hj = sj[w][g][jj][0], lj = sj[w][g][jj][1];
+        const float4 hj = sj[w][g][2 * jj], lj = sj[w][g][2 * jj + 1];
         const float dx = fmaf(xl - lj.x, unit, xh - hj.x);
         const float dy = fmaf(yl - lj.y, unit, yh - hj.y);
         const float dz = fmaf(zl - lj.z, unit, zh - hj.z);

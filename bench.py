@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
-    p.add_argument("--workload", default="slab", choices=["slab", "ensemble", "drift"],
+    p.add_argument("--workload", default="slab", choices=["slab", "ensemble", "drift", "mixture", "atm"],
                    help="slab: the headline 2M-particle system; ensemble: 512 independent systems in one engine")
     p.add_argument("--systems", type=int, default=512)
     return p.parse_args()
@@ -462,6 +462,139 @@ def run_ensemble(args):
     return 0
 
 
+# ---------------------------------------------------------------------------------------------- mixture
+def run_mixture(args):
+    """4,000,000 particles of 4 types (fractions 0.4/0.3/0.2/0.1, sigma 1.0/1.1/0.9/1.2, epsilon
+    1.0/0.8/1.2/0.6), Lorentz-Berthelot mixing, shifted potential, rc = 2.5 x max sigma = 3.0, skin 0.3, density
+    0.7 in a periodic cube, rebuild every 10; cluster size, traversal and kernel variant tuned.  Positions are
+    random sequential addition with a minimum distance of 0.8 (they stand in for the capped-force soft start);
+    FP32-mixed against the engine's FP64 form on the same configuration."""
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    from autopas_gb300 import engine as E, workloads
+    world, rank, local, pg = dist_setup(args)
+    n = args.n if args.n != 2_000_000 else 4_000_000
+    rho, rc, skin, reb = 0.7, 3.0, 0.3, 10
+    side = (n / rho) ** (1.0 / 3.0)
+    bmin, bmax = np.zeros(3), np.full(3, side)
+    pos = workloads.rsa(n, bmin, bmax, bmin, bmax, 0.8, seed=23)
+    rng = np.random.default_rng(23)
+    types = rng.choice(4, size=len(pos), p=[0.4, 0.3, 0.2, 0.1]).astype(np.int32)
+    vel = workloads.mb_velocities(len(pos), 1.0, seed=23)
+    eps, sig = [1.0, 0.8, 1.2, 0.6], [1.0, 1.1, 0.9, 1.2]
+
+    def engine(prec, **kw):
+        e = E.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=eps, sigma=sig, mass=[1, 1, 1, 1],
+                         shift=True, precision=prec, rebuild_frequency=reb, **kw)
+        e.set_particles(pos, vel, types=types)
+        return e
+
+    e = engine(E.PRECISION_MIXED, cluster_size=0, traversal=-1)
+    g0 = e.compute_forces()[0]
+    F = e.forces()
+    tuning = e.tuning()
+    e.step(DT, args.warmup, want_globals=False)
+    e.stats(reset=True)
+    barrier(pg)
+    e.timer_start()
+    e.step(DT, args.steps, want_globals=True)
+    ms = max_over_ranks(pg, e.timer_stop())
+    st = e.stats(reset=True)
+    info = e.info()
+    e.close()
+    value = sum_over_ranks(pg, st["pairs_total"]) / (ms * 1e-3)
+    if rank != 0:
+        return 0
+    e2 = engine(E.PRECISION_FP64, cluster_size=8, traversal=1)
+    g2 = e2.compute_forces()[0]
+    F64 = e2.forces()
+    e2.stats(reset=True)
+    e2.timer_start()
+    e2.step(DT, 5, want_globals=True)
+    ms2 = e2.timer_stop()
+    st2 = e2.stats(reset=True)
+    e2.close()
+    dF = F - F64
+    err = {"rms_rel": float(np.sqrt((dF ** 2).sum(1).mean() / (F64 ** 2).sum(1).mean())),
+           "upot_rel": abs(g0["upot"] - g2["upot"]) / abs(g2["upot"]),
+           "virial_rel": abs(g0["virial"] - g2["virial"]) / abs(g2["virial"]),
+           "pairs_equal": g0["num_pairs"] == g2["num_pairs"]}
+    line = {"metric": "pair interactions/s, 4-type LJ mixture (FP32-mixed vs FP64 GPU)", "value": value,
+            "unit": "pair interactions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 LJ arithmetic on f64 state", "data": "synthetic",
+            "config": {"workload": f"4-type LJ mixture: {len(pos)} particles, density {rho}, Lorentz-Berthelot, "
+                                   f"shifted, rc {rc}, skin {skin}, rebuild every {reb}, RSA positions dmin 0.8",
+                       "particles": int(len(pos))},
+            "fp64_gpu": {"value": st2["pairs_total"] / (ms2 * 1e-3), "unit": "pair interactions/s",
+                         "ms_per_step": ms2 / 5},
+            "force_error": err, "engine": {k: info[k] for k in ("cluster_size", "traversal", "num_list_entries")},
+            "tuning": tuning, "gpu_launches": st["kernel_launches"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------------------------- three-body
+def run_atm(args):
+    """LJ plus Axilrod-Teller-Muto: 200,000 particles (FCC melted: jittered lattice with MB velocities) at
+    density 0.8, T* 1.0, nu 0.073, pair rc 2.5 with skin 0.3, triplet cutoff 2.5; whole MD steps with both
+    force kernels.  The three-body error is stated against the oracle's FP64 AxilrodTellerMuto restatement on a
+    4,000-particle system of the same density (the oracle's neighbour search is quadratic)."""
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    from autopas_gb300 import engine as E, workloads
+    world, rank, local, pg = dist_setup(args)
+    nu, rc, skin, rho = 0.073, 2.5, 0.3, 0.8
+    nc = 37  # 4 * 37^3 = 202,612 particles
+    pos, vel, bmin, bmax = workloads.fcc_lj(nc, rho, 1.0, seed=29)
+    pos = np.mod(pos + np.random.default_rng(29).normal(0, 0.1, pos.shape), bmax)
+    e = E.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=E.PRECISION_MIXED, rebuild_frequency=10,
+                     atm_nu=nu, atm_cutoff=rc)
+    e.set_particles(pos, vel)
+    e.compute_forces()
+    e.step(DT, args.warmup, want_globals=False)
+    e.stats(reset=True)
+    barrier(pg)
+    e.timer_start()
+    nst = min(args.steps, 100)
+    e.step(DT, nst, want_globals=True)
+    ms = max_over_ranks(pg, e.timer_stop())
+    st = e.stats(reset=True)
+    e.close()
+    if rank != 0:
+        return 0
+    # three-body error against the oracle on a small system of the same kind
+    from oracle import oracle as orc
+    orc.build()
+    p2, v2, b0, b1 = workloads.fcc_lj(10, rho, 1.0, seed=31)
+    p2 = np.mod(p2 + np.random.default_rng(31).normal(0, 0.1, p2.shape), b1)
+    e2 = E.PairEngine(rc, skin, (b0, b1), periodic=True, precision=E.PRECISION_MIXED, atm_nu=nu, atm_cutoff=rc)
+    e2.set_particles(p2, v2)
+    e2.compute_forces()
+    f_pair = e2.forces()
+    g3 = e2.compute_atm(nu, rc)[0]
+    f_tot = e2.forces()
+    e2.close()
+    allpos, own, _, _, _ = orc.periodic_system(p2, b0, b1, rc, skin)
+    R3, glob3, _ = orc.atm_forces(allpos, nu, rc, own=own)
+    R3 = R3[: len(p2)]
+    d3 = (f_tot - f_pair) - R3
+    err = {"force_rms_rel": float(np.sqrt((d3 ** 2).sum(1).mean() / (R3 ** 2).sum(1).mean())),
+           "upot3_rel": abs(g3["upot"] - glob3[0]) / abs(glob3[0]), "sample": f"{len(p2)} particles, same density"}
+    line = {"metric": "MD steps/s, LJ + Axilrod-Teller-Muto (FP32 triplets, FP64 accumulation)",
+            "value": nst / (ms * 1e-3), "unit": "steps/s", "n_gpus": world, "steps": nst, "warmup": args.warmup,
+            "ms_per_step": ms / nst, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 triplet arithmetic, f64 sums", "data": "synthetic",
+            "config": {"workload": f"{len(pos)} particles, FCC melted (jitter 0.1), density {rho}, T* 1.0, nu {nu}, "
+                                   f"pair rc {rc} skin {skin}, triplet cutoff {rc}", "particles": int(len(pos))},
+            "pair_interactions_per_s": st["pairs_total"] / (ms * 1e-3), "atm_error": err,
+            "gpu_launches": st["kernel_launches"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 # ---------------------------------------------------------------------------------------------- energy drift
 def run_drift(args):
     """Energy drift of the FP32-mixed and FP64 forms over --steps steps (default 10^4) on the FCC case:
@@ -509,6 +642,10 @@ def main():
         return run_reference(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "mixture":
+        return run_mixture(args)
+    if args.workload == "atm":
+        return run_atm(args)
     return run_ours(args)
 
 
