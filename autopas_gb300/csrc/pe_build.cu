@@ -482,7 +482,8 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   __shared__ float4 sj[4][G][2 * C + 1];
   // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
   // most one block)
-  __shared__ __align__(16) uint32_t stage[4][32][2 * kPlistBlock];
+  // (17 words per lane: lanes appending at the same ring position hit different banks)
+  __shared__ uint32_t stage[4][32][2 * kPlistBlock + 1];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / C, ii = lane % C;
   const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + g;
