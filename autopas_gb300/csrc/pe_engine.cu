@@ -992,11 +992,17 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
   return h->cuda_check("force kernel");
 }
 
-static int atm_eval(pe_engine *h, double nu, double cutoff3) {
+// three-body buffers; allocated outside any stream capture (a graph capture may not allocate)
+static int ensure_atm(pe_engine *h) {
   const int ns = (int)h->sys.size();
   if (!h->atm_slot.ensure(3 * (size_t)std::max<int64_t>(h->pcap, 1)) || !h->atm_out.ensure(3 * (size_t)ns) ||
       !h->atm_err.ensure(1))
     return h->fail(PE_ERR_OOM, "three-body buffers");
+  return PE_OK;
+}
+
+static int atm_eval(pe_engine *h, double nu, double cutoff3) {
+  PE_TRY(ensure_atm(h));
   DeviceState s = h->state();
   PE_CUDA(h, cudaMemsetAsync(h->atm_err.p, 0, sizeof(int), h->st));
   launch_atm(s, nu, cutoff3, h->atm_slot.p, h->sys_cl_range.p, h->atm_out.p, h->atm_err.p, h->st);
@@ -1414,6 +1420,7 @@ static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
     h->step_graph = nullptr;
   }
   h->step_graph_valid = false;
+  if (h->cfg.atm_nu > 0) PE_TRY(ensure_atm(h));
   const int64_t launches0 = h->launches;
   const int steps0 = h->steps_since_rebuild;
   PE_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));

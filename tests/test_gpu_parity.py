@@ -385,6 +385,23 @@ def test_graph_replay_matches_eager_steps(eng_mod):
     assert out[0][3] == out[1][3]
 
 
+def test_graph_replay_with_three_body_forces(eng_mod):
+    """Steps with pair and three-body forces replayed from the CUDA graph give the same bits as eager steps
+    (the three-body buffers are allocated before the capture)."""
+    pos, vel, bmin, bmax = liquid(5, rho=0.8, seed=27)
+    out = []
+    for graphs in (False, True):
+        e = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, rebuild_frequency=5, use_graphs=graphs,
+                               atm_nu=0.073, atm_cutoff=2.5)
+        e.set_particles(pos, vel)
+        e.compute_forces()
+        g = e.step(0.002, 12)[0]
+        P, V = e.state()
+        out.append((P, V, g["upot"]))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
 def test_fcc_32000_trajectory_matches_oracle(eng_mod, orc):
     """Full-size FCC case: 20^3 unit cells (32,000 particles) at density 0.8442, T* 0.72, rc 2.5, skin 0.3,
     velocity Verlet dt 0.002 for 100 steps with a rebuild every 10.  The FP64 form follows the oracle's
