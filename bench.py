@@ -537,7 +537,9 @@ def run_mixture(args):
 
 # ---------------------------------------------------------------------------------------------- three-body
 def run_atm(args):
-    """LJ plus Axilrod-Teller-Muto: 200,000 particles (FCC melted: jittered lattice with MB velocities) at
+    """LJ plus Axilrod-Teller-Muto: 200,000 particles (an FCC lattice jittered by 0.02 with MB velocities at a
+    liquid state point, where it melts; a jitter of 0.1 already puts some of the 2.4 million nearest-neighbour
+    pairs at overlapping distances) at
     density 0.8, T* 1.0, nu 0.073, pair rc 2.5 with skin 0.3, triplet cutoff 2.5; whole MD steps with both
     force kernels.  The three-body error is stated against the oracle's FP64 AxilrodTellerMuto restatement on a
     4,000-particle system of the same density (the oracle's neighbour search is quadratic)."""
@@ -549,7 +551,7 @@ def run_atm(args):
     nu, rc, skin, rho = 0.073, 2.5, 0.3, 0.8
     nc = 37  # 4 * 37^3 = 202,612 particles
     pos, vel, bmin, bmax = workloads.fcc_lj(nc, rho, 1.0, seed=29)
-    pos = np.mod(pos + np.random.default_rng(29).normal(0, 0.1, pos.shape), bmax)
+    pos = np.mod(pos + np.random.default_rng(29).normal(0, 0.02, pos.shape), bmax)
     e = E.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=E.PRECISION_MIXED, rebuild_frequency=10,
                      atm_nu=nu, atm_cutoff=rc)
     e.set_particles(pos, vel)
@@ -569,7 +571,7 @@ def run_atm(args):
     from oracle import oracle as orc
     orc.build()
     p2, v2, b0, b1 = workloads.fcc_lj(10, rho, 1.0, seed=31)
-    p2 = np.mod(p2 + np.random.default_rng(31).normal(0, 0.1, p2.shape), b1)
+    p2 = np.mod(p2 + np.random.default_rng(31).normal(0, 0.02, p2.shape), b1)
     e2 = E.PairEngine(rc, skin, (b0, b1), periodic=True, precision=E.PRECISION_MIXED, atm_nu=nu, atm_cutoff=rc)
     e2.set_particles(p2, v2)
     e2.compute_forces()
@@ -587,7 +589,7 @@ def run_atm(args):
             "value": nst / (ms * 1e-3), "unit": "steps/s", "n_gpus": world, "steps": nst, "warmup": args.warmup,
             "ms_per_step": ms / nst, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 triplet arithmetic, f64 sums", "data": "synthetic",
-            "config": {"workload": f"{len(pos)} particles, FCC melted (jitter 0.1), density {rho}, T* 1.0, nu {nu}, "
+            "config": {"workload": f"{len(pos)} particles, FCC start (jitter 0.02), density {rho}, T* 1.0, nu {nu}, "
                                    f"pair rc {rc} skin {skin}, triplet cutoff {rc}", "particles": int(len(pos))},
             "pair_interactions_per_s": st["pairs_total"] / (ms * 1e-3), "atm_error": err,
             "gpu_launches": st["kernel_launches"]}
