@@ -722,8 +722,8 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
     return;
   }
   // kernel variants, chosen by the engine's tuner: positions gathered in batches of 2 under a cap of 64
-  // registers (8 blocks of 128 threads per SM) or of 4 under a cap of 80 (6 blocks); list entries cached or
-  // streamed.  Tighter register caps spill.
+  // registers (8 blocks of 128 threads per SM) or of 4 under a cap of 80 (6 blocks) or 72 (7 blocks, a few
+  // spills); list entries cached or streamed.
 #define PE_PLIST(G, O)                                                                   \
   do {                                                                                   \
     switch (s.variant) {                                                                 \
@@ -731,7 +731,7 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
         k_lj_mixed_plist<C, G, O, true, 4, 6, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
         break;                                                                           \
       case 2:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 2, 8, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
+        k_lj_mixed_plist<C, G, O, true, 4, 7, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
         break;                                                                           \
       case 3:                                                                            \
         k_lj_mixed_plist<C, G, O, true, 4, 6, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);\

@@ -91,8 +91,9 @@ typedef struct {
   double prune_buffer;     /* > 0 (particle lists only): the force kernels read inner lists holding the pairs within
                               cutoff + prune_buffer, refreshed on the device from the rc+skin lists whenever a
                               particle has moved prune_buffer/2 since the last refresh; 0: off */
-  int kernel_variant;      /* particle-list force kernel variant (0-3: entry batches of 2 or 4, list entries
-                              cached or streamed) used when the tuner does not run; the tuner picks its own */
+  int kernel_variant;      /* particle-list force kernel variant used when the tuner does not run (0: batches
+                              of 2 entries, 1: of 4, 2: of 4 under a tighter register cap, 3: of 4 with list
+                              entries streamed past the caches); the tuner picks its own */
 } pe_config;
 
 /* One particle system of the ensemble. */
