@@ -588,35 +588,34 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     }
   }
   if (GLOB) {
-    // per-cluster sums: the block's threads hold its 128 slots in a permuted order, so the values go through
-    // shared memory by slot and one thread per cluster adds its C slots in slot order
-    __shared__ float red[5][128];
-    __shared__ int redh[128];
+    // per-warp sums (fixed shuffle tree); the block's clusters carry them: cluster b*(128/C) + w holds warp w's
+    // sum, the block's other clusters zero, so the chunked system reduction adds the same terms in a fixed order
     const bool owned = oi == 1;
-    const int q = (int)(i - blockIdx.x * (int64_t)blockDim.x);  // the slot's place in the block
-    red[0][q] = owned ? acc.pot : 0.f;
-    red[1][q] = owned ? acc.vx : 0.f;
-    red[2][q] = owned ? acc.vy : 0.f;
-    red[3][q] = owned ? acc.vz : 0.f;
-    red[4][q] = ek;
-    redh[q] = owned ? acc.hits + acc.hhalo : 0;
-    __syncthreads();
+    float g0 = owned ? acc.pot : 0.f, g1 = owned ? acc.vx : 0.f, g2 = owned ? acc.vy : 0.f;
+    float g3 = owned ? acc.vz : 0.f;
+    int h = owned ? acc.hits + acc.hhalo : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+      g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+      g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      ek += __shfl_xor_sync(0xffffffffu, ek, o);
+      h += __shfl_xor_sync(0xffffffffu, h, o);
+    }
     constexpr int kClPerBlock = 128 / C;
-    if (threadIdx.x < kClPerBlock) {
-      const int64_t cl = blockIdx.x * (int64_t)kClPerBlock + threadIdx.x;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane < kClPerBlock / 4) {
+      // warp w writes clusters w*(kClPerBlock/4) + lane: its own sum in the first, zeros in the rest
+      const int64_t cl = blockIdx.x * (int64_t)kClPerBlock + w * (kClPerBlock / 4) + lane;
       if (cl < s.nclusters) {
-        float g[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-        int h = 0;
-#pragma unroll
-        for (int k = 0; k < C; ++k) {
-          const int sl = threadIdx.x * C + k;
-#pragma unroll
-          for (int v = 0; v < 5; ++v) g[v] += red[v][sl];
-          h += redh[sl];
-        }
-#pragma unroll
-        for (int v = 0; v < 5; ++v) s.cl_glob[kGlob * cl + v] = (double)g[v];
-        s.cl_hits[cl] = (unsigned long long)h;
+        const bool mine = lane == 0;
+        s.cl_glob[kGlob * cl + 0] = mine ? (double)g0 : 0.0;
+        s.cl_glob[kGlob * cl + 1] = mine ? (double)g1 : 0.0;
+        s.cl_glob[kGlob * cl + 2] = mine ? (double)g2 : 0.0;
+        s.cl_glob[kGlob * cl + 3] = mine ? (double)g3 : 0.0;
+        s.cl_glob[kGlob * cl + 4] = mine ? (double)ek : 0.0;
+        s.cl_hits[cl] = mine ? (unsigned long long)h : 0ull;
       }
     }
   }
