@@ -582,42 +582,6 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   if (lane == 0 && mx > 0) atomicMax(s.pl_max, mx);
 }
 
-// Per block of 128 consecutive slots, the slots in order of decreasing list length (ties by slot): the force
-// kernel's threads take them in this order, so a warp's lanes walk lists of similar length.
-__global__ void __launch_bounds__(128) k_plist_perm(DeviceState s) {
-  __shared__ int key[128];
-  __shared__ int val[128];
-  const int t = threadIdx.x;
-  const int64_t q = blockIdx.x * 128ll + t;
-  const bool in = q < s.nslots;
-  key[t] = in ? s.pl_count[q] : -1;
-  val[t] = in ? (int)q : 0x7fffffff;
-  for (int size = 2; size <= 128; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      __syncthreads();
-      if (t < 64) {
-        const int lo = 2 * t - (t & (stride - 1)), hi = lo + stride;
-        const bool desc = (lo & size) == 0;  // descending runs first: the final order is descending
-        const int ka = key[lo], kb = key[hi], va = val[lo], vb = val[hi];
-        const bool a_first = ka > kb || (ka == kb && va < vb);
-        if (a_first != desc) {
-          key[lo] = kb;
-          key[hi] = ka;
-          val[lo] = vb;
-          val[hi] = va;
-        }
-      }
-    }
-  }
-  __syncthreads();
-  if (in) s.fperm[q] = val[t];
-}
-
-void launch_plist_perm(DeviceState &s, cudaStream_t st) {
-  const int64_t nb = (s.nslots + 127) / 128;
-  if (nb > 0 && s.fperm) k_plist_perm<<<(unsigned)nb, 128, 0, st>>>(s);
-}
-
 void launch_plist_build(DeviceState &s, cudaStream_t st) {
   const double L = s.cutoff + s.skin;
   const float L2f = (float)(L * L * (1.0 + 1e-5));

@@ -133,7 +133,7 @@ struct pe_engine {
   int64_t num_cluster_pairs = 0;
   // particle lists
   DBuf<uint32_t> pl_list;
-  DBuf<int32_t> pl_count, fperm;
+  DBuf<int32_t> pl_count;
   DBuf<int> pl_max;
   int pl_cap = 0;
   int64_t pl_entries = 0;
@@ -208,7 +208,6 @@ struct pe_engine {
     s.variant = variant;
     s.pl_list = pl_list.p;
     s.pl_count = pl_count.p;
-    s.fperm = fperm.p;
     s.pl_cap = pl_cap;
     s.pl_stride = pcap;
     s.pl_max = pl_max.p;
@@ -771,8 +770,7 @@ static int ensure_particle_capacity(pe_engine *h) {
 // particle lists filtered from the full cluster-pair lists; the per-particle capacity grows when exceeded
 static int build_particle_lists(pe_engine *h) {
   cudaStream_t st = h->st;
-  if (!h->pl_count.ensure((size_t)h->pcap) || !h->fperm.ensure((size_t)h->pcap) || !h->pl_max.ensure(1))
-    return h->fail(PE_ERR_OOM, "particle lists");
+  if (!h->pl_count.ensure((size_t)h->pcap) || !h->pl_max.ensure(1)) return h->fail(PE_ERR_OOM, "particle lists");
   if (h->pl_cap == 0) {
     double rho = 0;
     for (auto &S : h->sys) {
@@ -796,9 +794,6 @@ static int build_particle_lists(pe_engine *h) {
     PE_TRY(h->cuda_check("particle list build"));
     if (mx <= h->pl_cap) {
       h->pl_entries = 0;
-      DeviceState s3 = h->state();
-      launch_plist_perm(s3, st);
-      h->launches += 1;
       if (h->cfg.prune_buffer > 0 && h->traversal == 1) {
         const size_t cap = (size_t)h->pl_cap * (size_t)h->pcap;
         const bool fresh = h->disp_bits.p == nullptr;
@@ -1226,7 +1221,6 @@ int pe_destroy(pe_engine *h) {
   h->pairs_acc.release();
   h->pl_list.release();
   h->pl_count.release();
-  h->fperm.release();
   h->pl_max.release();
   h->atm_slot.release();
   h->pi_list.release();

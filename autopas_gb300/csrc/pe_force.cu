@@ -520,11 +520,8 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     }
     __syncthreads();
   }
-  // threads take the slots of their block of 128 in order of decreasing list length (fperm, set at each list
-  // build), so the lanes of a warp walk lists of similar length
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool inrange = t < s.nslots;
-  const int64_t i = (inrange && s.fperm) ? (int64_t)s.fperm[t] : t;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool inrange = i < s.nslots;
   const bool reprune = s.prune && s.disp_bits[0] >= f2bits(s.prune_half2);
   uint4 qi = make_uint4(0u, 0u, 0u, 0u);
   int n = 0, ti = 0, oi = 0;
@@ -588,14 +585,12 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     }
   }
   if (GLOB) {
-    // per-warp sums (fixed shuffle tree); the block's clusters carry them: cluster b*(128/C) + w holds warp w's
-    // sum, the block's other clusters zero, so the chunked system reduction adds the same terms in a fixed order
     const bool owned = oi == 1;
     float g0 = owned ? acc.pot : 0.f, g1 = owned ? acc.vx : 0.f, g2 = owned ? acc.vy : 0.f;
     float g3 = owned ? acc.vz : 0.f;
     int h = owned ? acc.hits + acc.hhalo : 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < C; o <<= 1) {
       g0 += __shfl_xor_sync(0xffffffffu, g0, o);
       g1 += __shfl_xor_sync(0xffffffffu, g1, o);
       g2 += __shfl_xor_sync(0xffffffffu, g2, o);
@@ -603,20 +598,14 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       ek += __shfl_xor_sync(0xffffffffu, ek, o);
       h += __shfl_xor_sync(0xffffffffu, h, o);
     }
-    constexpr int kClPerBlock = 128 / C;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane < kClPerBlock / 4) {
-      // warp w writes clusters w*(kClPerBlock/4) + lane: its own sum in the first, zeros in the rest
-      const int64_t cl = blockIdx.x * (int64_t)kClPerBlock + w * (kClPerBlock / 4) + lane;
-      if (cl < s.nclusters) {
-        const bool mine = lane == 0;
-        s.cl_glob[kGlob * cl + 0] = mine ? (double)g0 : 0.0;
-        s.cl_glob[kGlob * cl + 1] = mine ? (double)g1 : 0.0;
-        s.cl_glob[kGlob * cl + 2] = mine ? (double)g2 : 0.0;
-        s.cl_glob[kGlob * cl + 3] = mine ? (double)g3 : 0.0;
-        s.cl_glob[kGlob * cl + 4] = mine ? (double)ek : 0.0;
-        s.cl_hits[cl] = mine ? (unsigned long long)h : 0ull;
-      }
+    if (inrange && (i % C) == 0) {
+      const int64_t cl = i / C;
+      s.cl_glob[kGlob * cl + 0] = (double)g0;
+      s.cl_glob[kGlob * cl + 1] = (double)g1;
+      s.cl_glob[kGlob * cl + 2] = (double)g2;
+      s.cl_glob[kGlob * cl + 3] = (double)g3;
+      s.cl_glob[kGlob * cl + 4] = (double)ek;
+      s.cl_hits[cl] = (unsigned long long)h;
     }
   }
 }

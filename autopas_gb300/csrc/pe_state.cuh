@@ -59,7 +59,6 @@ struct DeviceState {
   int variant = 0;                 // kernel variant inside a traversal (tuner dimension)
   uint32_t *pl_list = nullptr;
   int32_t *pl_count = nullptr;     // [nslots]
-  int32_t *fperm = nullptr;        // [nslots] force-kernel order: per block of 128 slots, by decreasing list length
   int pl_cap = 0;
   int64_t pl_stride = 0;
   int *pl_max = nullptr;           // device max of pl_count
@@ -137,7 +136,6 @@ int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *pe
 void launch_cluster_bbox(DeviceState &s, cudaStream_t st);
 void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st);
 void launch_plist_build(DeviceState &s, cudaStream_t st);
-void launch_plist_perm(DeviceState &s, cudaStream_t st);         // fperm from pl_count
 void launch_prune_reset_refs(DeviceState &s, cudaStream_t st);   // x_prune = x_reb = x, force the next prune
 void launch_displacement(DeviceState &s, cudaStream_t st);       // update disp_bits from the current positions
 void launch_prune(DeviceState &s, cudaStream_t st);              // prune if needed, then clear the flag
