@@ -98,6 +98,24 @@ __device__ __forceinline__ uint4 pq_encode(const double (&xp)[3], int type, int 
   r.w = l[0] | (l[1] << 16);
   return r;
 }
+// The record of a particle at (x, y, z) of system S: dummies (own 0) at x' = B, at least 2(rc+skin) + 4 from
+// every real particle; a real particle outside [B, 2B) sets kErrEncode in *err (an integer test on the
+// exponent field: FP64 compares run on the slow FP64 pipe).
+__device__ __forceinline__ uint4 pq_pack(const SysDev &S, double x, double y, double z, int type, int own,
+                                         int *err) {
+  double xp[3] = {x + S.enc_K[0], y + S.enc_K[1], z + S.enc_K[2]};
+  if (own == 0) {
+    xp[0] = xp[1] = xp[2] = S.enc_B;
+  } else {
+    const unsigned long long eB = (unsigned long long)__double_as_longlong(S.enc_B) >> 52;
+    const bool ok = ((unsigned long long)__double_as_longlong(xp[0]) >> 52) == eB &&
+                    ((unsigned long long)__double_as_longlong(xp[1]) >> 52) == eB &&
+                    ((unsigned long long)__double_as_longlong(xp[2]) >> 52) == eB;
+    if (!ok) atomicOr(err, kErrEncode);
+  }
+  return pq_encode(xp, type, own);
+}
+
 // hi as the float it stands for, given the exponent bits of B
 __device__ __forceinline__ float pq_hi(unsigned int w, unsigned int expb) { return __uint_as_float((w & 0x7FFFFFu) | expb); }
 // the low parts as integer-valued floats biased by 2^23 (exact; differences of two are the integer difference)

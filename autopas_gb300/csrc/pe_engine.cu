@@ -98,7 +98,14 @@ struct pe_engine {
   std::string err;
 
   ParticleArrays A, Bk;  // current and gather target
-  DBuf<uint4> pq;
+  DBuf<uint4> pq, pq2;
+  // inside pe_step the positions alternate between (A.x/y/z, pq) and (Bk.x/y/z, pq2): a force kernel that also
+  // advances the positions reads one pair and writes the other (pos_parity 1: the current ones are in Bk/pq2)
+  int pos_parity = 0;
+  cudaGraphExec_t fused_graph[2] = {nullptr, nullptr};
+  bool fused_graph_valid[2] = {false, false};
+  double fused_graph_dt = 0;
+  int fused_graph_launches = 0;
   DBuf<int32_t> slot_of;
   int64_t nuser = 0;     // particles of the last set_particles
   int64_t nslots = 0;
@@ -183,6 +190,16 @@ struct pe_engine {
     s.nreal = nuser;
     A.bind(s);
     s.pq = pq.p;
+    s.xn = Bk.x.p;
+    s.yn = Bk.y.p;
+    s.zn = Bk.z.p;
+    s.pqn = pq2.p;
+    if (pos_parity) {
+      std::swap(s.x, s.xn);
+      std::swap(s.y, s.yn);
+      std::swap(s.z, s.zn);
+      std::swap(s.pq, s.pqn);
+    }
     s.slot_of = slot_of.p;
     s.nsys = (int)sys.size();
     s.ntowers = ntowers;
@@ -386,21 +403,7 @@ __global__ void k_wrap(DeviceState s, int64_t n) {
 }
 
 __device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double px, double py, double pz) {
-  const int o = s.own[i];
-  const SysDev &S = s.sysd[s.sys[i]];
-  double xp[3] = {px + S.enc_K[0], py + S.enc_K[1], pz + S.enc_K[2]};
-  if (o == 0) {
-    // dummies (parked far outside the box) sit at x' = B, at least 2(rc+skin) + 4 from every real particle
-    xp[0] = xp[1] = xp[2] = S.enc_B;
-  } else {
-    // x' in [B, 2B) <=> its exponent field is B's (integer test: FP64 compares run on the slow FP64 pipe)
-    const unsigned long long eB = (unsigned long long)__double_as_longlong(S.enc_B) >> 52;
-    const bool ok = ((unsigned long long)__double_as_longlong(xp[0]) >> 52) == eB &&
-                    ((unsigned long long)__double_as_longlong(xp[1]) >> 52) == eB &&
-                    ((unsigned long long)__double_as_longlong(xp[2]) >> 52) == eB;
-    if (!ok) atomicOr(s.err, kErrEncode);
-  }
-  s.pq[i] = pq_encode(xp, s.type[i], o);
+  s.pq[i] = pq_pack(s.sysd[s.sys[i]], px, py, pz, s.type[i], s.own[i], s.err);
 }
 
 __device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) { pack_xyz(s, i, s.x[i], s.y[i], s.z[i]); }
@@ -753,7 +756,7 @@ static int setup_grids(pe_engine *h) {
 
 static int ensure_particle_capacity(pe_engine *h) {
   const size_t n = (size_t)h->pcap;
-  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pq.ensure(n) ||
+  if (!h->A.ensure(n) || !h->Bk.ensure(n) || !h->pq.ensure(n) || !h->pq2.ensure(n) ||
       !h->slot_of.ensure((size_t)std::max<int64_t>(h->nuser, 1)))
     return h->fail(PE_ERR_OOM, "particle arrays (%lld slots)", (long long)n);
   const size_t ncl = n / h->C + 1;
@@ -814,8 +817,11 @@ static int build_particle_lists(pe_engine *h) {
   return h->fail(PE_ERR_LIST_OVERFLOW, "particle lists kept overflowing");
 }
 
+static int normalize_positions(pe_engine *h);
+
 static int do_rebuild(pe_engine *h) {
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "rebuild before pe_set_particles");
+  PE_TRY(normalize_positions(h));
   cudaStream_t st = h->st;
   DeviceState s = h->state();
   const int64_t nold = h->nslots;
@@ -937,10 +943,32 @@ static int do_rebuild(pe_engine *h) {
   h->steps_since_rebuild = 0;
   h->rebuilds += 1;
   h->step_graph_valid = false;  // sizes and buffers may have changed
+  h->fused_graph_valid[0] = h->fused_graph_valid[1] = false;
   return PE_OK;
 }
 
 static bool pruning(const pe_engine *h) { return h->cfg.prune_buffer > 0 && h->traversal == 1; }
+
+// Positions back into A.x/y/z and pq (after pe_step advanced them into the second buffers).
+static int normalize_positions(pe_engine *h) {
+  if (!h->pos_parity) return PE_OK;
+  const size_t n = (size_t)std::max<int64_t>(h->nslots, 0);
+  if (n > 0) {
+    PE_CUDA(h, cudaMemcpyAsync(h->A.x.p, h->Bk.x.p, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    PE_CUDA(h, cudaMemcpyAsync(h->A.y.p, h->Bk.y.p, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    PE_CUDA(h, cudaMemcpyAsync(h->A.z.p, h->Bk.z.p, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    PE_CUDA(h, cudaMemcpyAsync(h->pq.p, h->pq2.p, n * sizeof(uint4), cudaMemcpyDeviceToDevice, h->st));
+  }
+  h->pos_parity = 0;
+  return PE_OK;
+}
+
+// The mixed particle-list kernel can advance the positions of the next step itself (it has the force and the
+// new velocity of its particle); the other kernels, rolling pruning (which tracks displacements in the
+// position update) and three-body forces (which add to the force after the pair kernel) take the plain path.
+static bool fused_positions_ok(const pe_engine *h) {
+  return h->precision != PE_PRECISION_FP64 && h->traversal == 1 && !pruning(h) && !(h->cfg.atm_nu > 0);
+}
 
 static VVFactors vv_factors(const pe_engine *h, double dt) {
   VVFactors v{};
@@ -953,7 +981,7 @@ static VVFactors vv_factors(const pe_engine *h, double dt) {
   return v;
 }
 
-static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
+static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, bool fuse_positions = false) {
   DeviceState s = h->state();
   // rolling pruning: the FP64 form prunes in a kernel of its own before the force kernel; the mixed kernel
   // prunes by itself while it walks the outer lists, and the flag is cleared after it
@@ -972,7 +1000,7 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed) {
     cudaEventRecord(e0, h->st);
   }
   const VVFactors vv = vv_factors(h, dt);
-  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st, &vv);
+  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st, &vv, fuse_positions);
   if (timed) {
     cudaEventRecord(e1, h->st);
     h->force_ev.push_back({i0, i0 + 1});
@@ -1192,6 +1220,9 @@ int pe_destroy(pe_engine *h) {
   h->A.release();
   h->Bk.release();
   h->pq.release();
+  h->pq2.release();
+  for (auto &g : h->fused_graph)
+    if (g) cudaGraphExecDestroy(g);
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})
@@ -1242,6 +1273,7 @@ int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, 
                      const int64_t *id, const int32_t *system) {
   if (!h) return PE_ERR_ARG;
   if (n < 0 || (n > 0 && (!x || !y || !z))) return h->fail(PE_ERR_ARG, "positions required");
+  h->pos_parity = 0;  // every position is set anew
   if (n > (int64_t)0x3fffffff) return h->fail(PE_ERR_ARG, "too many particles (%lld)", (long long)n);
   const int ns = (int)h->sys.size();
   for (auto &S : h->sys) S.count = 0;
@@ -1309,6 +1341,7 @@ static void *mapped_host(const void *p) {
 int pe_update_positions(pe_engine *h, const double *x, const double *y, const double *z) {
   if (!h || !x || !y || !z) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  PE_TRY(normalize_positions(h));
   const int64_t n = h->nuser;
   {
     const double *mx = (const double *)mapped_host(x), *my = (const double *)mapped_host(y),
@@ -1343,6 +1376,7 @@ int pe_rebuild(pe_engine *h) {
 int pe_compute_forces(pe_engine *h, pe_globals *globals) {
   if (!h) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "compute before pe_set_particles");
+  PE_TRY(normalize_positions(h));
   if (!h->tuned && (h->cfg.cluster_size == 0 || h->cfg.traversal == -1)) PE_TRY(tune(h, 3));
   if (!h->lists_valid) PE_TRY(do_rebuild(h));
   if (pruning(h)) {
@@ -1384,6 +1418,7 @@ int pe_get_forces(pe_engine *h, double *fx, double *fy, double *fz) {
 int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, double *vy, double *vz) {
   if (!h) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  PE_TRY(normalize_positions(h));
   const int64_t n = h->nuser;
   if (!h->tmp3.ensure(3 * (size_t)std::max<int64_t>(n, 1))) return h->fail(PE_ERR_OOM, "tmp");
   double *outs[6] = {x, y, z, vx, vy, vz};
@@ -1443,12 +1478,78 @@ static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
   return PE_OK;
 }
 
+// one step of the fused path for the current position parity: force kernel (forces, velocity half, next
+// positions) and the globals reduction
+static int capture_fused_graph(pe_engine *h, double dt, int parity) {
+  cudaGraphExec_t &gx = h->fused_graph[parity];
+  if (gx) {
+    cudaGraphExecDestroy(gx);
+    gx = nullptr;
+  }
+  h->fused_graph_valid[parity] = false;
+  const int64_t launches0 = h->launches;
+  const int steps0 = h->steps_since_rebuild;
+  PE_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  const int rc = force_eval(h, true, dt, false, true);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(h->st, &g);
+  if (rc != PE_OK) return rc;
+  if (ce != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  const cudaError_t ie = cudaGraphInstantiate(&gx, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+  h->fused_graph_launches = (int)(h->launches - launches0);
+  h->launches = launches0;
+  h->steps_since_rebuild = steps0;
+  h->fused_graph_dt = dt;
+  h->fused_graph_valid[parity] = true;
+  return PE_OK;
+}
+
+// Steps whose force kernel also advances the positions of the next step: the first step's position half is a
+// kernel of its own, every later one comes out of the previous step's force kernel, and the last step's force
+// kernel advances nothing.  The operations and their order are those of the plain path (same bits).
+static int steps_fused(pe_engine *h, double dt, int nsteps, const VVFactors &vv) {
+  const int freq = std::max(1, h->cfg.rebuild_frequency);
+  PE_TRY(normalize_positions(h));
+  DeviceState s = h->state();
+  if (h->nslots > 0) k_positions<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, dt, vv);
+  h->launches += 1;
+  for (int k = 0; k < nsteps; ++k) {
+    const bool rebuild_due = !h->lists_valid || h->steps_since_rebuild >= freq;
+    if (rebuild_due) PE_TRY(do_rebuild(h));  // (returns the positions to the first buffers)
+    if (k == nsteps - 1) {
+      PE_TRY(step_forces(h, dt, vv, !h->cfg.use_graphs));
+      break;
+    }
+    const int p = h->pos_parity;
+    if (h->cfg.use_graphs && !rebuild_due) {
+      if (!h->fused_graph_valid[p] || h->fused_graph_dt != dt) PE_TRY(capture_fused_graph(h, dt, p));
+      PE_CUDA(h, cudaGraphLaunch(h->fused_graph[p], h->st));
+      h->launches += h->fused_graph_launches;
+      h->steps_since_rebuild += 1;
+      h->forces_valid = true;
+    } else {
+      PE_TRY(force_eval(h, true, dt, true, true));
+    }
+    h->pos_parity ^= 1;
+  }
+  return normalize_positions(h);
+}
+
 int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals) {
   if (!h || nsteps < 0) return PE_ERR_ARG;
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "step before pe_set_particles");
   if (!h->forces_valid) return h->fail(PE_ERR_STATE, "pe_step needs the forces of the current positions first");
   const int freq = std::max(1, h->cfg.rebuild_frequency);
   const VVFactors vv = vv_factors(h, dt);
+  PE_TRY(normalize_positions(h));
+  if (nsteps >= 2 && fused_positions_ok(h)) {
+    PE_TRY(steps_fused(h, dt, nsteps, vv));
+    PE_TRY(h->cuda_check("step"));
+    if (globals) return read_globals(h, globals);
+    return PE_OK;
+  }
   for (int k = 0; k < nsteps; ++k) {
     const bool rebuild_due = !h->lists_valid || h->steps_since_rebuild >= freq;
     if (!rebuild_due && h->cfg.use_graphs) {
@@ -1474,6 +1575,7 @@ int pe_compute_atm(pe_engine *h, double nu, double cutoff3, pe_globals *globals)
   if (!h) return PE_ERR_ARG;
   if (!(cutoff3 > 0) || cutoff3 > h->cfg.cutoff + h->cfg.skin) return h->fail(PE_ERR_ARG, "ATM cutoff %g", cutoff3);
   if (!h->forces_valid) return h->fail(PE_ERR_STATE, "pe_compute_atm adds to the forces of pe_compute_forces");
+  PE_TRY(normalize_positions(h));
   if (!h->need_plist && h->traversal != 1) {
     h->need_plist = true;
     PE_TRY(build_particle_lists(h));
@@ -1544,6 +1646,7 @@ int pe_get_tower_grid(pe_engine *h, int system, double *side, int64_t *num, int6
 
 int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code, int64_t *count) {
   if (!h || !count || cap < 0 || (cap > 0 && (!a || !b || !code))) return PE_ERR_ARG;
+  PE_TRY(normalize_positions(h));
   if (!h->lists_valid) PE_TRY(do_rebuild(h));
   const size_t c = (size_t)std::max<int64_t>(cap, 1);
   if (!h->dump_a.ensure(c) || !h->dump_b.ensure(c) || !h->dump_c.ensure(c) || !h->dump_n.ensure(1))
@@ -1597,6 +1700,7 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out) {
 
 int pe_tune(pe_engine *h, int samples) {
   if (!h) return PE_ERR_ARG;
+  PE_TRY(normalize_positions(h));
   return tune(h, samples);
 }
 

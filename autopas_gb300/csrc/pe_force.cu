@@ -29,6 +29,7 @@ struct ForceArgs {
   float rc2f;
   double dt;
   int fuse_velocity;
+  int fuse_positions;  // with fuse_velocity: also the next step's position half, into xn/yn/zn/pqn
   int calc_globals;
   VVFactors vv;
 };
@@ -578,11 +579,32 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       s.vx[i] = vx;
       s.vy[i] = vy;
       s.vz[i] = vz;
+      if (fa.fuse_positions) {
+        // the next step's position half (TimeDiscretization.cpp:17-66), the same operations as k_positions:
+        // x += v dt + F dt^2/(2m), old force = F; into the next-step buffers
+        const double c = fa.vv.c[ti], dt = fa.dt;
+        const double x1 = __dadd_rn(s.x[i], __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(Fx, c)));
+        const double y1 = __dadd_rn(s.y[i], __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(Fy, c)));
+        const double z1 = __dadd_rn(s.z[i], __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(Fz, c)));
+        s.xn[i] = x1;
+        s.yn[i] = y1;
+        s.zn[i] = z1;
+        s.ofx[i] = Fx;
+        s.ofy[i] = Fy;
+        s.ofz[i] = Fz;
+        s.pqn[i] = pq_pack(S, x1, y1, z1, ti, oi, s.err);
+      }
     }
     if (GLOB) {
       const float ux = (float)vx, uy = (float)vy, uz = (float)vz;
       ek = fa.vv.half_mass[ti] * fmaf(uz, uz, fmaf(uy, uy, ux * ux));
     }
+  } else if (inrange && fa.fuse_positions) {
+    // halo and dummy slots keep their positions
+    s.xn[i] = s.x[i];
+    s.yn[i] = s.y[i];
+    s.zn[i] = s.z[i];
+    s.pqn[i] = qi;
   }
   if (GLOB) {
     const bool owned = oi == 1;
@@ -781,13 +803,14 @@ static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, c
 }
 
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
-                  const VVFactors *vv) {
+                  const VVFactors *vv, bool fuse_positions) {
   ForceArgs fa{};
   if (vv) fa.vv = *vv;
   fa.rc2 = s.cutoff * s.cutoff;
   fa.rc2f = (float)fa.rc2;
   fa.dt = dt;
   fa.fuse_velocity = fuse_velocity ? 1 : 0;
+  fa.fuse_positions = (fuse_velocity && fuse_positions) ? 1 : 0;
   fa.calc_globals = calc_globals;
   if (s.C == 4)
     launch_force_c<4>(s, precision, fa, st);

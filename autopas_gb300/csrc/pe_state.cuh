@@ -26,6 +26,10 @@ struct DeviceState {
   int8_t *own = nullptr;
   int64_t *id = nullptr;
   uint4 *pq = nullptr;   // [slots] compact 16-byte position records (pq_encode) for the particle-list force kernel
+  // positions of the next step, written by a force kernel that also advances the positions (the current ones
+  // are read by other threads for the neighbour distances, so the update goes to a second buffer)
+  double *xn = nullptr, *yn = nullptr, *zn = nullptr;
+  uint4 *pqn = nullptr;
   // inverse map: user index -> slot
   int32_t *slot_of = nullptr;
 
@@ -148,8 +152,8 @@ void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, con
                 int *err, cudaStream_t st);
 
 // forces (pe_force.cu)
-void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt,
-                  cudaStream_t st, const VVFactors *vv = nullptr);
+void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
+                  const VVFactors *vv = nullptr, bool fuse_positions = false);
 constexpr int kChunk = 256;  // clusters per globals-reduction chunk (one per thread of a reduction block)
 constexpr int kGlob = 5;      // per-cluster partials: 6*Upot, virial x, y, z, kinetic energy
 constexpr int kSysGlob = 6;   // per system: Upot, virial, virial x, y, z, kinetic energy

@@ -385,6 +385,27 @@ def test_graph_replay_matches_eager_steps(eng_mod):
     assert out[0][3] == out[1][3]
 
 
+def test_fused_position_update_gives_the_same_bits(eng_mod):
+    """pe_step over many steps lets the force kernel advance the next step's positions (double-buffered);
+    stepping one step per call takes the plain path.  Both give the same bits, with graphs and without."""
+    pos, vel, bmin, bmax = liquid(5, seed=33)
+    out = []
+    for graphs in (False, True):
+        for chunk in (1, 17):
+            e = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_MIXED,
+                                   rebuild_frequency=6, use_graphs=graphs)
+            e.set_particles(pos, vel)
+            e.compute_forces()
+            for _ in range(34 // chunk):
+                g = e.step(0.002, chunk)[0]
+            P, V = e.state()
+            out.append((P, V, e.forces(), g["upot"], g["ekin"]))
+    for o in out[1:]:
+        for a, b in zip(out[0][:3], o[:3]):
+            assert np.array_equal(a, b)
+        assert out[0][3] == o[3] and out[0][4] == o[4]
+
+
 def test_graph_replay_with_three_body_forces(eng_mod):
     """Steps with pair and three-body forces replayed from the CUDA graph give the same bits as eager steps
     (the three-body buffers are allocated before the capture)."""
