@@ -523,73 +523,29 @@ __global__ void k_from_user(double *__restrict__ a, const int32_t *__restrict__ 
 }
 
 // user-order positions read straight from page-locked host memory (device mapping of the host buffers),
-// scattered into slot order and re-encoded in the same pass.  Each thread moves kHostVec consecutive
-// particles, so every host read is a 32-byte vector: reads across the CPU-GPU link are latency-bound, and
-// fewer, larger requests move more data per round trip.
-constexpr int kHostVec = 4;
+// scattered into slot order and re-encoded in the same pass
 __global__ void k_positions_from_host(DeviceState s, int64_t n, const double *__restrict__ hx,
                                       const double *__restrict__ hy, const double *__restrict__ hz) {
-  const int64_t u0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * kHostVec;
-  if (u0 >= n) return;
-  double x[kHostVec], y[kHostVec], z[kHostVec];
-  if (u0 + kHostVec <= n && ((reinterpret_cast<uintptr_t>(hx + u0) | reinterpret_cast<uintptr_t>(hy + u0) |
-                              reinterpret_cast<uintptr_t>(hz + u0)) & 31) == 0) {
-    const double4 a = *reinterpret_cast<const double4 *>(hx + u0);
-    const double4 b = *reinterpret_cast<const double4 *>(hy + u0);
-    const double4 c = *reinterpret_cast<const double4 *>(hz + u0);
-    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
-    y[0] = b.x; y[1] = b.y; y[2] = b.z; y[3] = b.w;
-    z[0] = c.x; z[1] = c.y; z[2] = c.z; z[3] = c.w;
-  } else {
-    for (int k = 0; k < kHostVec; ++k)
-      if (u0 + k < n) {
-        x[k] = hx[u0 + k];
-        y[k] = hy[u0 + k];
-        z[k] = hz[u0 + k];
-      }
-  }
-#pragma unroll
-  for (int k = 0; k < kHostVec; ++k) {
-    if (u0 + k >= n) break;
-    const int32_t q = s.slot_of[u0 + k];
-    s.x[q] = x[k];
-    s.y[q] = y[k];
-    s.z[q] = z[k];
-    pack_xyz(s, q, x[k], y[k], z[k]);
-  }
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int32_t q = s.slot_of[u];
+  const double x = hx[u], y = hy[u], z = hz[u];
+  s.x[q] = x;
+  s.y[q] = y;
+  s.z[q] = z;
+  pack_xyz(s, q, x, y, z);
 }
 
-// forces of owned particles in user order, written straight into page-locked host memory, 32-byte vectors
+// forces of owned particles in user order, written straight into page-locked host memory
 __global__ void k_forces_to_host(DeviceState s, int64_t n, double *__restrict__ hx, double *__restrict__ hy,
                                  double *__restrict__ hz) {
-  const int64_t u0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * kHostVec;
-  if (u0 >= n) return;
-  double fx[kHostVec], fy[kHostVec], fz[kHostVec];
-#pragma unroll
-  for (int k = 0; k < kHostVec; ++k) {
-    fx[k] = fy[k] = fz[k] = 0.0;
-    if (u0 + k < n) {
-      const int32_t q = s.slot_of[u0 + k];
-      if (s.own[q] == 1) {
-        fx[k] = s.fx[q];
-        fy[k] = s.fy[q];
-        fz[k] = s.fz[q];
-      }
-    }
-  }
-  if (u0 + kHostVec <= n && ((reinterpret_cast<uintptr_t>(hx + u0) | reinterpret_cast<uintptr_t>(hy + u0) |
-                              reinterpret_cast<uintptr_t>(hz + u0)) & 31) == 0) {
-    *reinterpret_cast<double4 *>(hx + u0) = make_double4(fx[0], fx[1], fx[2], fx[3]);
-    *reinterpret_cast<double4 *>(hy + u0) = make_double4(fy[0], fy[1], fy[2], fy[3]);
-    *reinterpret_cast<double4 *>(hz + u0) = make_double4(fz[0], fz[1], fz[2], fz[3]);
-  } else {
-    for (int k = 0; k < kHostVec; ++k)
-      if (u0 + k < n) {
-        hx[u0 + k] = fx[k];
-        hy[u0 + k] = fy[k];
-        hz[u0 + k] = fz[k];
-      }
-  }
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int32_t q = s.slot_of[u];
+  const bool owned = s.own[q] == 1;
+  hx[u] = owned ? s.fx[q] : 0.0;
+  hy[u] = owned ? s.fy[q] : 0.0;
+  hz[u] = owned ? s.fz[q] : 0.0;
 }
 
 }  // namespace pe
@@ -1392,8 +1348,7 @@ int pe_update_positions(pe_engine *h, const double *x, const double *y, const do
                  *mz = (const double *)mapped_host(z);
     if (mx && my && mz) {
       DeviceState s = h->state();
-      const int64_t nt = (n + kHostVec - 1) / kHostVec;
-      if (n > 0) k_positions_from_host<<<(unsigned)((nt + 255) / 256), 256, 0, h->st>>>(s, n, mx, my, mz);
+      if (n > 0) k_positions_from_host<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(s, n, mx, my, mz);
       h->launches += 1;
       PE_CUDA(h, cudaStreamSynchronize(h->st));
       return h->cuda_check("update_positions");
@@ -1441,8 +1396,7 @@ int pe_get_forces(pe_engine *h, double *fx, double *fy, double *fz) {
     double *mx = (double *)mapped_host(fx), *my = (double *)mapped_host(fy), *mz = (double *)mapped_host(fz);
     if (mx && my && mz) {
       DeviceState s = h->state();
-      const int64_t nt = (n + kHostVec - 1) / kHostVec;
-      if (n > 0) k_forces_to_host<<<(unsigned)((nt + 255) / 256), 256, 0, h->st>>>(s, n, mx, my, mz);
+      if (n > 0) k_forces_to_host<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(s, n, mx, my, mz);
       h->launches += 1;
       PE_CUDA(h, cudaStreamSynchronize(h->st));
       return h->cuda_check("get_forces");
