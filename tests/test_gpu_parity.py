@@ -406,6 +406,29 @@ def test_fused_position_update_gives_the_same_bits(eng_mod):
         assert out[0][3] == o[3] and out[0][4] == o[4]
 
 
+def test_fused_position_update_keeps_explicit_halos(eng_mod, orc):
+    """Container mode (owned + static halo particles, no periodic images): many steps per call, with the force
+    kernel advancing the positions, give the bits of one step per call, and the halos do not move."""
+    pos, vel, bmin, bmax = liquid(5, seed=37)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    allvel = np.zeros_like(allpos)
+    allvel[: len(pos)] = vel * 0.1
+    out = []
+    for chunk in (1, 9):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, precision=eng_mod.PRECISION_MIXED,
+                               rebuild_frequency=5)
+        e.set_particles(allpos, allvel, ownership=own)
+        e.compute_forces()
+        for _ in range(18 // chunk):
+            g = e.step(0.002, chunk)[0]
+        P, V = e.state()
+        out.append((P, V, g["upot"]))
+        assert np.array_equal(P[len(pos):], allpos[len(pos):])
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
 def test_graph_replay_with_three_body_forces(eng_mod):
     """Steps with pair and three-body forces replayed from the CUDA graph give the same bits as eager steps
     (the three-body buffers are allocated before the capture)."""
