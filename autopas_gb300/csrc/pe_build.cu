@@ -467,19 +467,20 @@ void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------------------------
 // 6. particle neighbour lists from the (full) cluster-pair lists: every j within rc+skin of an owned i,
-//    tested on the compact position records with a relative margin of 1e-5 on (rc+skin)^2 (the float distance is
-//    within ~1e-7 of the FP64 one, so the list is a superset of the FP64 rc+skin pair set).  Every list is
-//    appended in (cluster-pair entry, j) order, so it has a deterministic order.
+//    tested on the hi parts of the compact position records alone (exact differences on the ulp(B) grid) against
+//    (rc+skin)^2 widened by the hi-part error bound (SysDev::plist_r2max), so the list is a superset of the FP64
+//    rc+skin pair set with a shell of a few ulp(B).  Every list is appended in (cluster-pair entry, j) order, so
+//    it has a deterministic order.
 // ---------------------------------------------------------------------------------------------
 // One warp serves 32/C i-clusters, C lanes each (lane = one i particle).  For each cluster-pair entry the C lanes of
 // a group stage the C particles of the j-cluster in shared memory, then every lane tests its i against all of
 // them and appends the survivors to its own row in (entry, j) order.
 template <int C>
-__global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
+__global__ void __launch_bounds__(128) k_plist_build(DeviceState s) {
   constexpr int G = 32 / C;
-  // the group's current j-cluster, decoded (hi parts, biased low parts); one float4 of padding per group keeps
-  // the four groups of a warp in different shared-memory banks
-  __shared__ float4 sj[4][G][2 * C + 1];
+  // the group's current j-cluster, decoded (hi parts); one float4 of padding per group keeps the four groups of
+  // a warp in different shared-memory banks
+  __shared__ float4 sj[4][G][C + 1];
   // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
   // most one block)
   // (17 words per lane: lanes appending at the same ring position hit different banks)
@@ -502,9 +503,8 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
   }
   const SysDev &S = s.sysd[sy];
   const unsigned int eb = S.pq_expb;
-  const float unit = S.pq_unit;
   const float hxi = pq_hi(qi.x, eb), hyi = pq_hi(qi.y, eb), hzi = pq_hi(qi.z, eb);
-  const float lxi = pq_lox(qi), lyi = pq_loy(qi), lzi = pq_loz(qi);
+  const float r2max = S.plist_r2max;
   int nmax = n;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
@@ -534,8 +534,7 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
     const bool act = e < n;
     const uint32_t ent = ent_next;
     if (act) {
-      sj[w][g][2 * ii] = make_float4(pq_hi(pj.x, eb), pq_hi(pj.y, eb), pq_hi(pj.z, eb), 0.f);
-      sj[w][g][2 * ii + 1] = make_float4(pq_lox(pj), pq_loy(pj), pq_loz(pj), 0.f);
+      sj[w][g][ii] = make_float4(pq_hi(pj.x, eb), pq_hi(pj.y, eb), pq_hi(pj.z, eb), 0.f);
     }
     const int e1 = e + 1;
     if ((e1 & (C - 1)) == 0) {
@@ -547,12 +546,10 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
     __syncwarp();
     if (act && oi == 1) {
       const int code = ent & 31;
-      // i's position moved by minus the image shift (exact: hi on the ulp(B) grid, low parts integers)
+      // i's position moved by minus the image shift (exact: hi parts on the ulp(B) grid)
       const float4 us = c_unit_shift[code];
       const float xh = fmaf(-us.x, S.len_hi[0], hxi), yh = fmaf(-us.y, S.len_hi[1], hyi);
       const float zh = fmaf(-us.z, S.len_hi[2], hzi);
-      const float xl = fmaf(-us.x, S.len_lo_u[0], lxi), yl = fmaf(-us.y, S.len_lo_u[1], lyi);
-      const float zl = fmaf(-us.z, S.len_lo_u[2], lzi);
       const uint32_t ebase = (((ent >> 5) * (uint32_t)C) << 5) | (uint32_t)code;
       const int before = cnt;
       // dummies sit at x' = B, at least 2(rc+skin) + 4 from every real particle, so the distance test
@@ -560,13 +557,11 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
       // position, which only advances when it is kept.
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
-        const float4 hj = sj[w][g][2 * jj], lj = sj[w][g][2 * jj + 1];
-        const float dx = fmaf(xl - lj.x, unit, xh - hj.x);
-        const float dy = fmaf(yl - lj.y, unit, yh - hj.y);
-        const float dz = fmaf(zl - lj.z, unit, zh - hj.z);
+        const float4 hj = sj[w][g][jj];
+        const float dx = xh - hj.x, dy = yh - hj.y, dz = zh - hj.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
-        cnt += ((r2 > 0.f) && (r2 <= L2f)) ? 1 : 0;
+        cnt += ((r2 > 0.f) && (r2 <= r2max)) ? 1 : 0;
       }
       if ((before ^ cnt) & ~(kPlistBlock - 1)) put_block(before / kPlistBlock);
     }
@@ -583,16 +578,14 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s, float L2f) {
 }
 
 void launch_plist_build(DeviceState &s, cudaStream_t st) {
-  const double L = s.cutoff + s.skin;
-  const float L2f = (float)(L * L * (1.0 + 1e-5));
   cudaMemsetAsync(s.pl_max, 0, sizeof(int), st);
   const int64_t per_block = 4 * (32 / s.C);  // i-clusters per block of 4 warps
   const int64_t nb = (s.nclusters + per_block - 1) / per_block;
   if (nb == 0) return;
   if (s.C == 4)
-    k_plist_build<4><<<(unsigned)nb, 128, 0, st>>>(s, L2f);
+    k_plist_build<4><<<(unsigned)nb, 128, 0, st>>>(s);
   else
-    k_plist_build<8><<<(unsigned)nb, 128, 0, st>>>(s, L2f);
+    k_plist_build<8><<<(unsigned)nb, 128, 0, st>>>(s);
 }
 
 // ---------------------------------------------------------------------------------------------

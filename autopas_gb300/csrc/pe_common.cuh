@@ -61,6 +61,10 @@ struct SysDev {
   float lenf[3], bminf[3], bmaxf[3];
   float coord_tol;
   float bb_tol2;
+  // particle-list build: squared-distance threshold for the test on the hi parts alone (a difference of hi parts
+  // is exact and within 2.6 ulp(B) of the displacement, so (rc+skin)^2 (1 + 1e-5) + 6 (rc+skin) ulp(B)
+  // + 8 ulp(B)^2 keeps every pair within rc+skin)
+  float plist_r2max;
 };
 
 // Unit image shift (sx, sy, sz) of each shift code, for the float kernels: one constant-cache load instead

@@ -626,6 +626,9 @@ static void compute_encoding(SysHost &S, double cutoff, double skin) {
   const double B = next_pow2(2.0 * ext + 2.0 * M + 4.0);
   d.enc_B = B;
   const double ulp = std::ldexp(B, -23);
+  // the hi parts of a displacement differ from it by under 1.5 ulp(B) per axis (low parts below ulp(B), the low
+  // part of an image shift at most ulp(B)/2): |error| < 2.6 ulp(B)
+  d.plist_r2max = std::nextafter((float)(L * L * (1.0 + 1e-5) + 6.0 * L * ulp + 8.0 * ulp * ulp), INFINITY);
   {
     float bf = (float)B;
     unsigned int bb;
