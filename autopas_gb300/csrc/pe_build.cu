@@ -553,15 +553,16 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s) {
       const uint32_t ebase = (((ent >> 5) * (uint32_t)C) << 5) | (uint32_t)code;
       const int before = cnt;
       // dummies sit at x' = B, at least 2(rc+skin) + 4 from every real particle, so the distance test
-      // excludes them; r2 > 0 excludes i itself.  Branch-free append: the entry is always written at the ring
-      // position, which only advances when it is kept.
+      // excludes them; r2 > 0 excludes i itself.  Branch-free append: a predicated store at the ring position,
+      // which advances when the entry is kept (lanes that drop it take no shared-memory bandwidth).
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
         const float4 hj = sj[w][g][jj];
         const float dx = xh - hj.x, dy = yh - hj.y, dz = zh - hj.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
-        cnt += ((r2 > 0.f) && (r2 <= r2max)) ? 1 : 0;
+        const bool keep = (r2 > 0.f) && (r2 <= r2max);
+        if (keep) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
+        cnt += keep ? 1 : 0;
       }
       if ((before ^ cnt) & ~(kPlistBlock - 1)) put_block(before / kPlistBlock);
     }

@@ -322,93 +322,146 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
 // ---------------------------------------------------------------------------------------------
 // one pair of the mixed kernels: displacement from the compact position records, LJ in FP32, compensated sums.
 // GM: 0 no globals, 1 globals, 2 globals and the owned-halo pair count of systems with explicit halos.
+// Packed FP32 pairs: the Blackwell f32x2 instructions evaluate two list entries (.x and .y) per instruction,
+// each lane an IEEE round-to-nearest operation, so a packed pair gives the bits of two scalar ones.
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// minus the reciprocal, refined by one Newton-Raphson step: the same magnitude as rcp_nr, sign flipped
+__device__ __forceinline__ float nrcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(-x));
+  return r;
+}
+// the decoded fields of a record with the sign flipped (the sign bit set in the same logic operation)
+__device__ __forceinline__ float pq_nhi(unsigned int w, unsigned int expb) {
+  return __uint_as_float((w & 0x7FFFFFu) | expb | 0x80000000u);
+}
+__device__ __forceinline__ float pq_nlox(const uint4 &q) { return __uint_as_float((q.w & 0xFFFFu) | 0xCB000000u); }
+__device__ __forceinline__ float pq_nloy(const uint4 &q) { return __uint_as_float((q.w >> 16) | 0xCB000000u); }
+__device__ __forceinline__ float pq_nloz(const uint4 &q) {
+  return __uint_as_float(((q.y >> 23) | ((q.z >> 23) << 9)) | 0xCB000000u);
+}
+
 template <int GM, bool ONE_TYPE, bool KAHAN>
 struct MixedAcc {
   static constexpr bool GLOB = GM > 0;
+  // minus the force: compensated running sums and the plain sums of the current batch (two entries wide)
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
-  float bx = 0.f, by = 0.f, bz = 0.f;  // plain sum of the current batch, Kahan-added by flush()
-  float pot = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+  float2 bx = {0.f, 0.f}, by = {0.f, 0.f}, bz = {0.f, 0.f};
+  // globals, two entries wide: the potential without the per-pair shift, minus the virial
+  float2 pot = {0.f, 0.f}, vx = {0.f, 0.f}, vy = {0.f, 0.f}, vz = {0.f, 0.f};
   int hits = 0, hhalo = 0;
 
-  // One pair, given its displacement rounded once to FP32: cutoff mask (FP64 re-test near rc), LJ in FP32,
-  // batch sums and globals.  Returns the squared distance (the re-prune test uses it).
-  __device__ __forceinline__ float accum(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                        uint32_t ent, int code, float dx, float dy, float dz, int tj, int oj,
-                                        int ti, float eps24, float sig2, float sh6,
-                                        const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
-    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    bool mask = (r2 <= fa.rc2f);
-    if (fabsf(r2 - fa.rc2f) <= band) mask = exact_within(s, S, i, (int64_t)(ent >> 5), code, fa.rc2);
-    if (!ONE_TYPE) {
-      const int kk = ti * T + tj;
-      eps24 = tab[0][kk];
-      sig2 = tab[1][kk];
-      sh6 = tab[2][kk];
+  // Two pairs, given their displacements each rounded once to FP32 (.x and .y): cutoff masks (FP64 re-test
+  // near rc), LJ in FP32 with the sign of 1/r^2 flipped (so that no operand needs a negation), batch sums and
+  // globals.  Returns the squared distances (the re-prune test uses them).
+  //   ninv = -1/r2, nlj2 = -(sig2/r2), nlj6 = -(sig2/r2)^3, lj12m6 = lj6^2 - lj6, t = 2 lj6^2 - lj6,
+  //   -fac = eps24 t ninv, so that the pair force on i is fac * d (LJFunctor.h:141-150)
+  __device__ __forceinline__ float2 accum2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                           uint32_t e0, uint32_t e1, float2 dx, float2 dy, float2 dz, int tj0,
+                                           int tj1, int oj0, int oj1, int ti, float eps24, float sig2, float sh6,
+                                           const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
+                                           bool two) {
+    const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+    bool m0 = r2.x <= fa.rc2f, m1 = two && r2.y <= fa.rc2f;
+    const float2 off = add2(r2, dup2(-fa.rc2f));
+    const bool n0 = fabsf(off.x) <= band, n1 = two && fabsf(off.y) <= band;
+    if (n0 || n1) {
+      if (n0) m0 = exact_within(s, S, i, (int64_t)(e0 >> 5), e0 & 31, fa.rc2);
+      if (n1) m1 = exact_within(s, S, i, (int64_t)(e1 >> 5), e1 & 31, fa.rc2);
     }
-    const float inv = rcp_nr(r2);
-    const float lj2 = sig2 * inv;
-    const float lj6 = lj2 * lj2 * lj2;
-    const float lj12 = lj6 * lj6;
-    const float lj12m6 = lj12 - lj6;
-    float fac = eps24 * (lj12 + lj12m6) * inv;
-    fac = mask ? fac : 0.f;
-    const float px = dx * fac, py = dy * fac, pz = dz * fac;
-    bx += px;
-    by += py;
-    bz += pz;
+    float2 ep = dup2(eps24), sg = dup2(sig2), sh = dup2(sh6);
+    if (!ONE_TYPE) {
+      const int k0 = ti * T + tj0, k1 = ti * T + tj1;
+      ep = make_float2(tab[0][k0], tab[0][k1]);
+      sg = make_float2(tab[1][k0], tab[1][k1]);
+      sh = make_float2(tab[2][k0], tab[2][k1]);
+    }
+    const float2 rn = make_float2(nrcp_approx(r2.x), nrcp_approx(r2.y));
+    const float2 ninv = fma2(rn, fma2(r2, rn, dup2(1.0f)), rn);
+    const float2 nlj2 = mul2(sg, ninv);
+    const float2 nlj6 = mul2(mul2(nlj2, nlj2), nlj2);
+    const float2 lj12m6 = fma2(nlj6, nlj6, nlj6);
+    const float2 t = fma2(nlj6, nlj6, lj12m6);
+    const float2 em = make_float2(m0 ? ep.x : 0.f, m1 ? ep.y : 0.f);
+    const float2 nfac = mul2(mul2(em, t), ninv);
+    const float2 px = mul2(dx, nfac), py = mul2(dy, nfac), pz = mul2(dz, nfac);
+    bx = add2(bx, px);
+    by = add2(by, py);
+    bz = add2(bz, pz);
     if (GLOB) {
-      pot += mask ? fmaf(eps24, lj12m6, sh6) : 0.f;
-      vx = fmaf(px, dx, vx);
-      vy = fmaf(py, dy, vy);
-      vz = fmaf(pz, dz, vz);
-      hits += mask ? 1 : 0;
-      if (GM == 2 && !S.periodic) hhalo += (mask && oj == 2) ? 1 : 0;
+      if (!ONE_TYPE) pot = add2(pot, make_float2(m0 ? sh.x : 0.f, m1 ? sh.y : 0.f));
+      pot = fma2(em, lj12m6, pot);
+      vx = fma2(px, dx, vx);
+      vy = fma2(py, dy, vy);
+      vz = fma2(pz, dz, vz);
+      hits += (m0 ? 1 : 0) + (m1 ? 1 : 0);
+      if (GM == 2 && !S.periodic) hhalo += ((m0 && oj0 == 2) ? 1 : 0) + ((m1 && oj1 == 2) ? 1 : 0);
     }
     return r2;
   }
 
-  // a pair from the compact record (pq) of j; iq holds i's hi parts and biased low parts as floats.  The
-  // displacement is formed exactly (hi differences are multiples of ulp(B); low-part differences are integers
-  // times a power of two) and rounded once, by the final fma.
+  // Two pairs from the compact records (pq) of j0 and j1; iq holds i's hi parts and biased low parts as
+  // floats.  Each displacement is formed exactly (hi differences are multiples of ulp(B); low-part differences
+  // are integers times a power of two) and rounded once, by the final fma.  With two == false only .x is a
+  // pair (e1 and q1 must still be valid: they are evaluated and masked).
   // SHIFT: false when no lane of the warp holds a shifted entry in this batch (no shift arithmetic), true
-  // otherwise (the shift of code kShiftNone is zero, so every lane applies its entry's shift unconditionally).
+  // otherwise (the shift of code kShiftNone is zero, so every lane applies its entries' shifts unconditionally).
   template <bool SHIFT>
-  __device__ __forceinline__ float pair_q(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                         const float (&iq)[6], int ti, uint32_t ent, const uint4 &q, float eps24,
-                                         float sig2, float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
-                                         float band) {
-    const int code = ent & 31;
-    float xh = iq[0], yh = iq[1], zh = iq[2], xl = iq[3], yl = iq[4], zl = iq[5];
+  __device__ __forceinline__ float2 pair_q2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
+                                            const float (&iq)[6], int ti, uint32_t e0, uint32_t e1, const uint4 &q0,
+                                            const uint4 &q1, float eps24, float sig2, float sh6,
+                                            const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
+                                            bool two = true) {
+    float2 xh = dup2(iq[0]), yh = dup2(iq[1]), zh = dup2(iq[2]), xl = dup2(iq[3]), yl = dup2(iq[4]),
+           zl = dup2(iq[5]);
     if (SHIFT) {
-      const float4 us = c_unit_shift[code];
-      const float sxf = us.x, syf = us.y, szf = us.z;
-      xh = fmaf(-sxf, S.len_hi[0], xh);
-      yh = fmaf(-syf, S.len_hi[1], yh);
-      zh = fmaf(-szf, S.len_hi[2], zh);
-      xl = fmaf(-sxf, S.len_lo_u[0], xl);
-      yl = fmaf(-syf, S.len_lo_u[1], yl);
-      zl = fmaf(-szf, S.len_lo_u[2], zl);
+      const float4 u0 = c_unit_shift[e0 & 31], u1 = c_unit_shift[e1 & 31];
+      const float2 sx = make_float2(-u0.x, -u1.x), sy = make_float2(-u0.y, -u1.y), sz = make_float2(-u0.z, -u1.z);
+      xh = fma2(sx, dup2(S.len_hi[0]), xh);
+      yh = fma2(sy, dup2(S.len_hi[1]), yh);
+      zh = fma2(sz, dup2(S.len_hi[2]), zh);
+      xl = fma2(sx, dup2(S.len_lo_u[0]), xl);
+      yl = fma2(sy, dup2(S.len_lo_u[1]), yl);
+      zl = fma2(sz, dup2(S.len_lo_u[2]), zl);
     }
     const unsigned int eb = S.pq_expb;
-    const float u = S.pq_unit;
-    const float dx = fmaf(xl - pq_lox(q), u, xh - pq_hi(q.x, eb));
-    const float dy = fmaf(yl - pq_loy(q), u, yh - pq_hi(q.y, eb));
-    const float dz = fmaf(zl - pq_loz(q), u, zh - pq_hi(q.z, eb));
-    return accum(s, S, fa, i, ent, code, dx, dy, dz, pq_type(q), pq_own(q), ti, eps24, sig2, sh6, tab, T, band);
+    const float2 u = dup2(S.pq_unit);
+    const float2 dx = fma2(add2(xl, make_float2(pq_nlox(q0), pq_nlox(q1))), u,
+                           add2(xh, make_float2(pq_nhi(q0.x, eb), pq_nhi(q1.x, eb))));
+    const float2 dy = fma2(add2(yl, make_float2(pq_nloy(q0), pq_nloy(q1))), u,
+                           add2(yh, make_float2(pq_nhi(q0.y, eb), pq_nhi(q1.y, eb))));
+    const float2 dz = fma2(add2(zl, make_float2(pq_nloz(q0), pq_nloz(q1))), u,
+                           add2(zh, make_float2(pq_nhi(q0.z, eb), pq_nhi(q1.z, eb))));
+    return accum2(s, S, fa, i, e0, e1, dx, dy, dz, pq_type(q0), pq_type(q1), pq_own(q0), pq_own(q1), ti, eps24,
+                  sig2, sh6, tab, T, band, two);
   }
 
   __device__ __forceinline__ void flush() {
+    const float px = bx.x + bx.y, py = by.x + by.y, pz = bz.x + bz.y;
     if (KAHAN) {
-      kahan_add(fxs, fxc, bx);
-      kahan_add(fys, fyc, by);
-      kahan_add(fzs, fzc, bz);
+      kahan_add(fxs, fxc, px);
+      kahan_add(fys, fyc, py);
+      kahan_add(fzs, fzc, pz);
     } else {
-      fxs += bx;
-      fys += by;
-      fzs += bz;
+      fxs += px;
+      fys += py;
+      fzs += pz;
     }
-    bx = by = bz = 0.f;
+    bx = by = bz = make_float2(0.f, 0.f);
   }
+  // the force on i and the globals, signs restored (exact)
+  __device__ __forceinline__ float force_x() const { return fxc - fxs; }
+  __device__ __forceinline__ float force_y() const { return fyc - fys; }
+  __device__ __forceinline__ float force_z() const { return fzc - fzs; }
+  __device__ __forceinline__ float upot(float sh6) const {
+    return ONE_TYPE ? fmaf(sh6, (float)hits, pot.x + pot.y) : pot.x + pot.y;
+  }
+  __device__ __forceinline__ float vir_x() const { return -(vx.x + vx.y); }
+  __device__ __forceinline__ float vir_y() const { return -(vy.x + vy.y); }
+  __device__ __forceinline__ float vir_z() const { return -(vz.x + vz.y); }
 };
 
 // List entries are read once per launch: with STREAM they are loaded with the evict-first (streaming) cache
@@ -431,7 +484,7 @@ __device__ __forceinline__ void list_load(const uint32_t *p, uint32_t (&e)[U]) {
 // One thread's walk over its list.  Entries arrive UNROLL (2 or 4) at a time in one vector load, the next
 // UNROLL being loaded while the current ones are evaluated; the position gathers of a batch are all issued
 // before its arithmetic.  Leftover entries (n mod UNROLL) are read one by one.
-template <int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM>
+template <int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM, bool PF>
 __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                            const float (&iq)[6], int ti, const uint32_t *__restrict__ list, int n,
                                            float eps24, float sig2, float sh6,
@@ -442,39 +495,67 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
   const uint32_t *base = list + i * kPlistBlock;
   const int64_t bstride = stride * kPlistBlock;
   int k = 0;
-  uint32_t e[UNROLL];
+  // e: the current batch; nx (PF only): the next one, whose position records (qn) are gathered while the
+  // current batch (records q) is evaluated
+  uint32_t e[UNROLL], nx[UNROLL];
+  uint4 q[UNROLL];
 #pragma unroll
-  for (int u = 0; u < UNROLL; ++u) e[u] = 0u;
+  for (int u = 0; u < UNROLL; ++u) {
+    e[u] = nx[u] = 0u;
+    q[u] = make_uint4(0u, 0u, 0u, 0u);
+  }
   if (UNROLL <= n) list_load<UNROLL, STREAM>(base, e);
+  if (PF && 2 * UNROLL <= n) list_load<UNROLL, STREAM>(base + (UNROLL >> 3) * bstride + (UNROLL & 7), nx);
+  if (PF && UNROLL <= n) {
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) q[u] = __ldg(s.pq + (e[u] >> 5));
+  }
   for (; k + UNROLL <= n; k += UNROLL) {
     const int kn = k + UNROLL;
-    uint32_t nx[UNROLL];
+    const int kl = PF ? kn + UNROLL : kn;  // first entry of the batch whose entries are loaded now
+    uint32_t nl[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) nx[u] = 0u;
-    if (kn + UNROLL <= n) list_load<UNROLL, STREAM>(base + (int64_t)(kn >> 3) * bstride + (kn & 7), nx);
-    uint4 qj[UNROLL];
+    for (int u = 0; u < UNROLL; ++u) nl[u] = 0u;
+    if (kl + UNROLL <= n) list_load<UNROLL, STREAM>(base + (int64_t)(kl >> 3) * bstride + (kl & 7), nl);
+    uint4 qj[UNROLL], qn[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) qj[u] = __ldg(s.pq + (e[u] >> 5));
+    for (int u = 0; u < UNROLL; ++u) {
+      qn[u] = make_uint4(0u, 0u, 0u, 0u);
+      qj[u] = PF ? q[u] : __ldg(s.pq + (e[u] >> 5));
+    }
+    if (PF && kn + UNROLL <= n) {
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) qn[u] = __ldg(s.pq + (nx[u] >> 5));
+    }
     bool shifted = false;
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) shifted |= (e[u] & 31u) != (uint32_t)kShiftNone;
     // a warp-uniform choice: most batches of most warps hold no image-shifted entry
     if (__any_sync(__activemask(), shifted)) {
 #pragma unroll
-      for (int u = 0; u < UNROLL; ++u)
-        acc.template pair_q<true>(s, S, fa, i, iq, ti, e[u], qj[u], eps24, sig2, sh6, tab, T, band);
+      for (int u = 0; u < UNROLL; u += 2)
+        acc.template pair_q2<true>(s, S, fa, i, iq, ti, e[u], e[u + 1], qj[u], qj[u + 1], eps24, sig2, sh6, tab,
+                                   T, band);
     } else {
 #pragma unroll
-      for (int u = 0; u < UNROLL; ++u)
-        acc.template pair_q<false>(s, S, fa, i, iq, ti, e[u], qj[u], eps24, sig2, sh6, tab, T, band);
+      for (int u = 0; u < UNROLL; u += 2)
+        acc.template pair_q2<false>(s, S, fa, i, iq, ti, e[u], e[u + 1], qj[u], qj[u + 1], eps24, sig2, sh6, tab,
+                                    T, band);
     }
     acc.flush();
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) e[u] = nx[u];
+    for (int u = 0; u < UNROLL; ++u) {
+      e[u] = PF ? nx[u] : nl[u];
+      nx[u] = nl[u];
+      q[u] = qn[u];
+    }
   }
-  for (; k < n; ++k) {
-    const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    acc.template pair_q<true>(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
+  for (; k < n; k += 2) {
+    const bool two = k + 1 < n;
+    const uint32_t e0 = __ldg(list + plist_index(stride, i, k));
+    const uint32_t e1 = two ? __ldg(list + plist_index(stride, i, k + 1)) : e0;
+    acc.template pair_q2<true>(s, S, fa, i, iq, ti, e0, e1, __ldg(s.pq + (e0 >> 5)), __ldg(s.pq + (e1 >> 5)), eps24,
+                               sig2, sh6, tab, T, band, two);
   }
   acc.flush();
 }
@@ -492,8 +573,9 @@ __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const Sy
   int m = 0;
   for (int k = 0; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    const float r2 =
-        acc.template pair_q<true>(s, S, fa, i, iq, ti, en, __ldg(s.pq + (en >> 5)), eps24, sig2, sh6, tab, T, band);
+    const uint4 q = __ldg(s.pq + (en >> 5));
+    const float r2 = acc.template pair_q2<true>(s, S, fa, i, iq, ti, en, en, q, q, eps24, sig2, sh6, tab, T, band,
+                                                false).x;
     if (r2 <= lim) out[plist_index(stride, i, m++)] = en;
     if ((k & 1) == 1) acc.flush();
   }
@@ -508,7 +590,9 @@ __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const Sy
 // buffer since the rebuild) to the inner lists and records the positions of the prune.  The flag is read
 // by every thread and cleared by a later launch, so all threads take the same branch.
 // STREAM: list entries loaded with the streaming (evict-first) hint
-template <int C, int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, bool STREAM>
+// PF: list entries loaded two batches ahead, the position records of the next batch gathered into registers
+// while the current batch is evaluated
+template <int C, int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, int MINB, bool STREAM, bool PF>
 __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, ForceArgs fa) {
   constexpr bool GLOB = GM > 0;
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
@@ -557,14 +641,14 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       }
     }
   } else {
-    plist_walk<GM, ONE_TYPE, KAHAN, UNROLL, STREAM>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, sh6, tab, T,
-                                                      band, acc);
+    plist_walk<GM, ONE_TYPE, KAHAN, UNROLL, STREAM, PF>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, sh6, tab,
+                                                         T, band, acc);
   }
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
   // epilogue keeps to the FP64 work the state needs: the force rounded once from its compensated sum, the
   // velocity half in FP64 with the reference's operation order.  Per-particle globals, the kinetic energy
   // included, are float values summed over the cluster's lanes in float and widened once per cluster.
-  const double Fx = (double)(acc.fxs - acc.fxc), Fy = (double)(acc.fys - acc.fyc), Fz = (double)(acc.fzs - acc.fzc);
+  const double Fx = (double)acc.force_x(), Fy = (double)acc.force_y(), Fz = (double)acc.force_z();
   float ek = 0.f;
   if (oi == 1) {
     s.fx[i] = Fx;
@@ -608,8 +692,8 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   }
   if (GLOB) {
     const bool owned = oi == 1;
-    float g0 = owned ? acc.pot : 0.f, g1 = owned ? acc.vx : 0.f, g2 = owned ? acc.vy : 0.f;
-    float g3 = owned ? acc.vz : 0.f;
+    float g0 = owned ? acc.upot(sh6) : 0.f, g1 = owned ? acc.vir_x() : 0.f, g2 = owned ? acc.vir_y() : 0.f;
+    float g3 = owned ? acc.vir_z() : 0.f;
     int h = owned ? acc.hits + acc.hhalo : 0;
 #pragma unroll
     for (int o = 1; o < C; o <<= 1) {
@@ -732,24 +816,24 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
       k_lj_fp64_plist<C, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);
     return;
   }
-  // kernel variants, chosen by the engine's tuner: positions gathered in batches of 2 under a cap of 64
-  // registers (8 blocks of 128 threads per SM) or of 4 under a cap of 80 (6 blocks) or 72 (7 blocks, a few
-  // spills); list entries cached or streamed.
-#define PE_PLIST(G, O)                                                                   \
-  do {                                                                                   \
-    switch (s.variant) {                                                                 \
-      case 1:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 4, 6, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
-        break;                                                                           \
-      case 2:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 4, 7, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
-        break;                                                                           \
-      case 3:                                                                            \
-        k_lj_mixed_plist<C, G, O, true, 4, 6, true><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
-        break;                                                                           \
-      default:                                                                           \
-        k_lj_mixed_plist<C, G, O, true, 2, 8, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
-    }                                                                                    \
+  // kernel variants, chosen by the engine's tuner: positions gathered in batches of 4 under a cap of 96
+  // registers (5 blocks of 128 threads per SM) or 80 (6 blocks), list entries cached or streamed; or the next
+  // batch's positions gathered while the current one is evaluated (128 registers, 4 blocks).
+#define PE_PLIST(G, O)                                                                          \
+  do {                                                                                          \
+    switch (s.variant) {                                                                        \
+      case 1:                                                                                   \
+        k_lj_mixed_plist<C, G, O, true, 4, 6, false, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
+        break;                                                                                  \
+      case 2:                                                                                   \
+        k_lj_mixed_plist<C, G, O, true, 4, 4, false, true><<<(unsigned)nb, 128, 0, st>>>(s, fa); \
+        break;                                                                                  \
+      case 3:                                                                                   \
+        k_lj_mixed_plist<C, G, O, true, 4, 6, true, false><<<(unsigned)nb, 128, 0, st>>>(s, fa); \
+        break;                                                                                  \
+      default:                                                                                  \
+        k_lj_mixed_plist<C, G, O, true, 4, 5, false, false><<<(unsigned)nb, 128, 0, st>>>(s, fa);\
+    }                                                                                           \
   } while (0)
   // globals mode: none, globals, or globals with the owned-halo pair count (engines holding a system with
   // explicit halos)

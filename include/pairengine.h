@@ -91,9 +91,10 @@ typedef struct {
   double prune_buffer;     /* > 0 (particle lists only): the force kernels read inner lists holding the pairs within
                               cutoff + prune_buffer, refreshed on the device from the rc+skin lists whenever a
                               particle has moved prune_buffer/2 since the last refresh; 0: off */
-  int kernel_variant;      /* particle-list force kernel variant used when the tuner does not run (0: batches
-                              of 2 entries, 1: of 4, 2: of 4 under a tighter register cap, 3: of 4 with list
-                              entries streamed past the caches); the tuner picks its own */
+  int kernel_variant;      /* particle-list force kernel variant used when the tuner does not run (batches of
+                              4 entries; 0: 96 registers, 5 blocks per SM, 1: 80 registers, 6 blocks, 2: the
+                              next batch gathered during the current one, 4 blocks, 3: as 1 with list entries
+                              streamed past the caches); the tuner picks its own */
 } pe_config;
 
 /* One particle system of the ensemble. */
