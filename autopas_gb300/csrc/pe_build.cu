@@ -478,9 +478,11 @@ void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st) {
 template <int C>
 __global__ void __launch_bounds__(128) k_plist_build(DeviceState s) {
   constexpr int G = 32 / C;
-  // the group's current j-cluster, decoded (hi parts); one float4 of padding per group keeps the four groups of
-  // a warp in different shared-memory banks
-  __shared__ float4 sj[4][G][C + 1];
+  // the group's current j-cluster, decoded (hi parts, negated) in pairs of particles: (x0, x1, y0, y1) and
+  // (z0, z1), so that one packed instruction serves two tests; one element of padding per group keeps the
+  // groups of a warp in different shared-memory banks
+  __shared__ float4 sxy[4][G][C / 2 + 1];
+  __shared__ float2 sz[4][G][C / 2 + 1];
   // each lane's last two blocks of entries (a ring of 16: up to C <= 8 appends per cluster pair complete at
   // most one block)
   // (17 words per lane: lanes appending at the same ring position hit different banks)
@@ -534,7 +536,10 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s) {
     const bool act = e < n;
     const uint32_t ent = ent_next;
     if (act) {
-      sj[w][g][ii] = make_float4(pq_hi(pj.x, eb), pq_hi(pj.y, eb), pq_hi(pj.z, eb), 0.f);
+      float *pxy = reinterpret_cast<float *>(&sxy[w][g][ii >> 1]);
+      pxy[ii & 1] = pq_nhi(pj.x, eb);
+      pxy[2 + (ii & 1)] = pq_nhi(pj.y, eb);
+      reinterpret_cast<float *>(&sz[w][g][ii >> 1])[ii & 1] = pq_nhi(pj.z, eb);
     }
     const int e1 = e + 1;
     if ((e1 & (C - 1)) == 0) {
@@ -548,21 +553,25 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s) {
       const int code = ent & 31;
       // i's position moved by minus the image shift (exact: hi parts on the ulp(B) grid)
       const float4 us = c_unit_shift[code];
-      const float xh = fmaf(-us.x, S.len_hi[0], hxi), yh = fmaf(-us.y, S.len_hi[1], hyi);
-      const float zh = fmaf(-us.z, S.len_hi[2], hzi);
+      const float2 xh = dup2(fmaf(-us.x, S.len_hi[0], hxi)), yh = dup2(fmaf(-us.y, S.len_hi[1], hyi));
+      const float2 zh = dup2(fmaf(-us.z, S.len_hi[2], hzi));
       const uint32_t ebase = (((ent >> 5) * (uint32_t)C) << 5) | (uint32_t)code;
       const int before = cnt;
       // dummies sit at x' = B, at least 2(rc+skin) + 4 from every real particle, so the distance test
       // excludes them; r2 > 0 excludes i itself.  Branch-free append: a predicated store at the ring position,
       // which advances when the entry is kept (lanes that drop it take no shared-memory bandwidth).
 #pragma unroll
-      for (int jj = 0; jj < C; ++jj) {
-        const float4 hj = sj[w][g][jj];
-        const float dx = xh - hj.x, dy = yh - hj.y, dz = zh - hj.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const bool keep = (r2 > 0.f) && (r2 <= r2max);
-        if (keep) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
-        cnt += keep ? 1 : 0;
+      for (int p = 0; p < C / 2; ++p) {
+        const float4 hxy = sxy[w][g][p];
+        const float2 dx = add2(xh, make_float2(hxy.x, hxy.y)), dy = add2(yh, make_float2(hxy.z, hxy.w));
+        const float2 dz = add2(zh, sz[w][g][p]);
+        const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const bool k0 = (r2.x > 0.f) && (r2.x <= r2max);
+        if (k0) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)(2 * p) << 5);
+        cnt += k0 ? 1 : 0;
+        const bool k1 = (r2.y > 0.f) && (r2.y <= r2max);
+        if (k1) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)(2 * p + 1) << 5);
+        cnt += k1 ? 1 : 0;
       }
       if ((before ^ cnt) & ~(kPlistBlock - 1)) put_block(before / kPlistBlock);
     }

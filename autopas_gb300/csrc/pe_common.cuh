@@ -120,6 +120,13 @@ __device__ __forceinline__ uint4 pq_pack(const SysDev &S, double x, double y, do
   return pq_encode(xp, type, own);
 }
 
+// Packed FP32 pairs: the Blackwell f32x2 instructions evaluate two operations (.x and .y) per instruction,
+// each lane an IEEE round-to-nearest operation, so a packed pair gives the bits of two scalar ones.
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // hi as the float it stands for, given the exponent bits of B
 __device__ __forceinline__ float pq_hi(unsigned int w, unsigned int expb) { return __uint_as_float((w & 0x7FFFFFu) | expb); }
 // the low parts as integer-valued floats biased by 2^23 (exact; differences of two are the integer difference)
@@ -127,6 +134,15 @@ __device__ __forceinline__ float pq_lox(const uint4 &q) { return __uint_as_float
 __device__ __forceinline__ float pq_loy(const uint4 &q) { return __uint_as_float((q.w >> 16) | 0x4B000000u); }
 __device__ __forceinline__ float pq_loz(const uint4 &q) {
   return __uint_as_float(((q.y >> 23) | ((q.z >> 23) << 9)) | 0x4B000000u);
+}
+// the decoded fields of a record with the sign flipped (the sign bit set in the same logic operation)
+__device__ __forceinline__ float pq_nhi(unsigned int w, unsigned int expb) {
+  return __uint_as_float((w & 0x7FFFFFu) | expb | 0x80000000u);
+}
+__device__ __forceinline__ float pq_nlox(const uint4 &q) { return __uint_as_float((q.w & 0xFFFFu) | 0xCB000000u); }
+__device__ __forceinline__ float pq_nloy(const uint4 &q) { return __uint_as_float((q.w >> 16) | 0xCB000000u); }
+__device__ __forceinline__ float pq_nloz(const uint4 &q) {
+  return __uint_as_float(((q.y >> 23) | ((q.z >> 23) << 9)) | 0xCB000000u);
 }
 __device__ __forceinline__ int pq_type(const uint4 &q) { return (int)((q.x >> 23) & 15u); }
 __device__ __forceinline__ int pq_own(const uint4 &q) { return (int)((q.x >> 27) & 3u); }

@@ -322,28 +322,12 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
 // ---------------------------------------------------------------------------------------------
 // one pair of the mixed kernels: displacement from the compact position records, LJ in FP32, compensated sums.
 // GM: 0 no globals, 1 globals, 2 globals and the owned-halo pair count of systems with explicit halos.
-// Packed FP32 pairs: the Blackwell f32x2 instructions evaluate two list entries (.x and .y) per instruction,
-// each lane an IEEE round-to-nearest operation, so a packed pair gives the bits of two scalar ones.
-__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 // minus the reciprocal, refined by one Newton-Raphson step: the same magnitude as rcp_nr, sign flipped
 __device__ __forceinline__ float nrcp_approx(float x) {
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(-x));
   return r;
 }
-// the decoded fields of a record with the sign flipped (the sign bit set in the same logic operation)
-__device__ __forceinline__ float pq_nhi(unsigned int w, unsigned int expb) {
-  return __uint_as_float((w & 0x7FFFFFu) | expb | 0x80000000u);
-}
-__device__ __forceinline__ float pq_nlox(const uint4 &q) { return __uint_as_float((q.w & 0xFFFFu) | 0xCB000000u); }
-__device__ __forceinline__ float pq_nloy(const uint4 &q) { return __uint_as_float((q.w >> 16) | 0xCB000000u); }
-__device__ __forceinline__ float pq_nloz(const uint4 &q) {
-  return __uint_as_float(((q.y >> 23) | ((q.z >> 23) << 9)) | 0xCB000000u);
-}
-
 template <int GM, bool ONE_TYPE, bool KAHAN>
 struct MixedAcc {
   static constexpr bool GLOB = GM > 0;

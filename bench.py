@@ -103,6 +103,35 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def host_link_rates(nbytes):
+    """Copy-engine bandwidth between page-locked host memory and the device for one step's position (or
+    force) bytes: the floor under the end-to-end step, whose transfers cross the same link."""
+    try:
+        import torch
+        h = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+        d = torch.empty(nbytes // 8, dtype=torch.float64, device="cuda")
+        st = torch.cuda.Stream()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        with torch.cuda.stream(st):
+            for _ in range(2):
+                d.copy_(h, non_blocking=True)
+                h.copy_(d, non_blocking=True)
+            ev[0].record(st)
+            for _ in range(5):
+                d.copy_(h, non_blocking=True)
+            ev[1].record(st)
+            for _ in range(5):
+                h.copy_(d, non_blocking=True)
+            ev[2].record(st)
+        st.synchronize()
+        t_h2d, t_d2h = ev[0].elapsed_time(ev[1]) / 5, ev[1].elapsed_time(ev[2]) / 5
+        return {"h2d_gbs": nbytes / (t_h2d * 1e6), "d2h_gbs": nbytes / (t_d2h * 1e6),
+                "transfer_floor_ms": t_h2d + t_d2h,
+                "what": f"cudaMemcpyAsync of {nbytes} bytes each way between page-locked host and device memory"}
+    except Exception as ex:  # a host without torch or CUDA: no figure
+        return {"unavailable": str(ex)}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -334,7 +363,8 @@ def run_ours(args):
                "h2d_bytes_per_step": 3 * 8 * n, "d2h_bytes_per_step": 3 * 8 * n + 48,
                "steps": nst, "ms_per_step": 1e3 * t_e2e / nst,
                "what": "per step: pe_update_positions from pinned host x,y,z + pe_compute_forces (pe_rebuild every "
-                       f"{REBUILD} steps) + pe_get_forces into pinned host fx,fy,fz; host wall clock"}
+                       f"{REBUILD} steps) + pe_get_forces into pinned host fx,fy,fz; host wall clock",
+               "host_link": host_link_rates(3 * 8 * n)}
 
     # ---- CPU baseline (rank 0, N = 1)
     cpu = None
