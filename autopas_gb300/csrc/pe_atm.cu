@@ -46,6 +46,7 @@ __device__ __forceinline__ double img_dist2(const DeviceState &s, const SysDev &
 __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs aa, double *__restrict__ slot_glob,
                                                          int *__restrict__ err) {
   __shared__ float4 nb[kAtmWarps][kAtmMaxNeigh];
+  __shared__ float ni[kAtmWarps][kAtmMaxNeigh];  // 1/d^2 of each neighbour, rounded once
   __shared__ uint32_t ne[kAtmWarps][kAtmMaxNeigh];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t i = blockIdx.x * (int64_t)kAtmWarps + w;
@@ -85,6 +86,7 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
     if (keep) {
       if (pos < kAtmMaxNeigh) {
         nb[w][pos] = d;
+        ni[w][pos] = __frcp_rn(d.w);
         ne[w][pos] = ent;
       } else {
         overflow = true;
@@ -97,43 +99,69 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
     return;
   }
   __syncwarp();
-  // phase 2: pairs (a, b), a < b, of the neighbour set
+  // phase 2: pairs (a, b), a < b, of the neighbour set, enumerated row by row (row a holds b = a+1 .. m-1) and
+  // dealt to the lanes round robin, so that all lanes stay busy whatever the row lengths.  The divisions of the
+  // reference's expressions become products with the neighbours' reciprocals (1/d^2, 1/d) and one reciprocal
+  // square root of the j-k distance per triplet.  Contributions are summed plainly in batches of 8 pairs and the
+// batch sums compensated.
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f, ps = 0.f, pc = 0.f;
-  int trip = 0;
+  // plain sums of the current batch of 8 pairs, added to the compensated sums when the batch is full
+  float bx = 0.f, by = 0.f, bz = 0.f, bp = 0.f;
+  int trip = 0, it = 0;
   const float nu3 = 3.0f * aa.nu;
-  for (int a = 0; a < m; ++a) {
-    const float4 dj = nb[w][a];
-    for (int b = a + 1 + lane; b < m; b += 32) {
-      const float4 dk = nb[w][b];
-      // reference vectors: IJ = r_j - r_i = -d_j, KI = r_i - r_k = d_k, JK = r_k - r_j = d_j - d_k
+  int a = 0, off = lane;  // this lane's pair: row a, offset off (b = a + 1 + off)
+  while (a < m - 1 && off >= m - 1 - a) {
+    off -= m - 1 - a;
+    ++a;
+  }
+  while (a < m - 1) {
+    const int b = a + 1 + off;
+    const float4 dj = nb[w][a], dk = nb[w][b];
+    // reference vectors: IJ = r_j - r_i = -d_j, KI = r_i - r_k = d_k, JK = r_k - r_j = d_j - d_k
+    const float JKx = dj.x - dk.x, JKy = dj.y - dk.y, JKz = dj.z - dk.z;
+    const float d2JK = fmaf(JKz, JKz, fmaf(JKy, JKy, JKx * JKx));
+    bool in = d2JK <= aa.rc2f;
+    if (fabsf(d2JK - aa.rc2f) <= band) {
+      const uint32_t ej = ne[w][a], ek = ne[w][b];
+      in = img_dist2(s, S, (int64_t)(ej >> 5), ej & 31, (int64_t)(ek >> 5), ek & 31) <= aa.rc2;
+    }
+    if (in) {
+      const float rj = ni[w][a], rk = ni[w][b];
       const float IJx = -dj.x, IJy = -dj.y, IJz = -dj.z;
       const float KIx = dk.x, KIy = dk.y, KIz = dk.z;
-      const float JKx = dj.x - dk.x, JKy = dj.y - dk.y, JKz = dj.z - dk.z;
       const float d2IJ = dj.w, d2KI = dk.w;
-      float d2JK = fmaf(JKz, JKz, fmaf(JKy, JKy, JKx * JKx));
-      bool in = d2JK <= aa.rc2f;
-      if (fabsf(d2JK - aa.rc2f) <= band) {
-        const uint32_t ej = ne[w][a], ek = ne[w][b];
-        in = img_dist2(s, S, (int64_t)(ej >> 5), ej & 31, (int64_t)(ek >> 5), ek & 31) <= aa.rc2;
-      }
-      if (!in) continue;
       const float all2 = d2IJ * d2JK * d2KI;
-      const float all5 = all2 * all2 * sqrtf(all2);
-      const float factor = nu3 / all5;
+      const float factor = nu3 / (all2 * all2 * sqrtf(all2));
       const float IJdotKI = IJx * KIx + IJy * KIy + IJz * KIz;
       const float IJdotJK = IJx * JKx + IJy * JKy + IJz * JKz;
       const float JKdotKI = JKx * KIx + JKy * KIy + JKz * KIz;
       const float allDots = IJdotKI * IJdotJK * JKdotKI;
       const float cJK = IJdotKI * (IJdotJK - JKdotKI);
-      const float cIJ = IJdotJK * JKdotKI - d2JK * d2KI + 5.0f * allDots / d2IJ;
-      const float cKI = -IJdotJK * JKdotKI + d2IJ * d2JK - 5.0f * allDots / d2KI;
-      kahan(fxs, fxc, (JKx * cJK + IJx * cIJ + KIx * cKI) * factor);
-      kahan(fys, fyc, (JKy * cJK + IJy * cIJ + KIy * cKI) * factor);
-      kahan(fzs, fzc, (JKz * cJK + IJz * cIJ + KIz * cKI) * factor);
-      kahan(ps, pc, factor * (all2 - 3.0f * allDots));
+      const float cIJ = IJdotJK * JKdotKI - d2JK * d2KI + 5.0f * allDots * rj;
+      const float cKI = -IJdotJK * JKdotKI + d2IJ * d2JK - 5.0f * allDots * rk;
+      bx = fmaf(JKx * cJK + IJx * cIJ + KIx * cKI, factor, bx);
+      by = fmaf(JKy * cJK + IJy * cIJ + KIy * cKI, factor, by);
+      bz = fmaf(JKz * cJK + IJz * cIJ + KIz * cKI, factor, bz);
+      bp = fmaf(factor, all2 - 3.0f * allDots, bp);
       ++trip;
     }
+    if ((++it & 7) == 0) {
+      kahan(fxs, fxc, bx);
+      kahan(fys, fyc, by);
+      kahan(fzs, fzc, bz);
+      kahan(ps, pc, bp);
+      bx = by = bz = bp = 0.f;
+    }
+    off += 32;
+    while (a < m - 1 && off >= m - 1 - a) {
+      off -= m - 1 - a;
+      ++a;
+    }
   }
+  kahan(fxs, fxc, bx);
+  kahan(fys, fyc, by);
+  kahan(fzs, fzc, bz);
+  kahan(ps, pc, bp);
   double Fx = (double)fxs - (double)fxc, Fy = (double)fys - (double)fyc, Fz = (double)fzs - (double)fzc;
   double P = (double)ps - (double)pc;
   long long T = trip;
