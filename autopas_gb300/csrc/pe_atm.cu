@@ -100,10 +100,9 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
   }
   __syncwarp();
   // phase 2: pairs (a, b), a < b, of the neighbour set, enumerated row by row (row a holds b = a+1 .. m-1) and
-  // dealt to the lanes round robin, so that all lanes stay busy whatever the row lengths.  The divisions of the
-  // reference's expressions become products with the neighbours' reciprocals (1/d^2, 1/d) and one reciprocal
-  // square root of the j-k distance per triplet.  Contributions are summed plainly in batches of 8 pairs and the
-// batch sums compensated.
+  // dealt to the lanes round robin, so that all lanes stay busy whatever the row lengths.  The divisions by the
+  // i-j and i-k squared distances become products with the neighbours' reciprocals (rounded once each).
+  // Contributions are summed plainly in batches of 8 pairs and the batch sums compensated.
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f, ps = 0.f, pc = 0.f;
   // plain sums of the current batch of 8 pairs, added to the compensated sums when the batch is full
   float bx = 0.f, by = 0.f, bz = 0.f, bp = 0.f;
