@@ -179,6 +179,12 @@ struct TypeTable {
   double eps24[kMaxTypes * kMaxTypes];
   double sig2[kMaxTypes * kMaxTypes];
   double shift6[kMaxTypes * kMaxTypes];
+  // the same rounded to float once on the host (a conversion in a kernel runs on the FP64 pipe), and the shift
+  // as a multiple of eps24 (0 where eps24 is 0)
+  float eps24f[kMaxTypes * kMaxTypes];
+  float sig2f[kMaxTypes * kMaxTypes];
+  float shift6f[kMaxTypes * kMaxTypes];
+  float shrf[kMaxTypes * kMaxTypes];
 };
 
 __host__ __device__ inline int shift_code(int sx, int sy, int sz) { return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1); }

@@ -1196,6 +1196,10 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
       } else {
         t.shift6[k] = 0.;
       }
+      t.eps24f[k] = (float)t.eps24[k];
+      t.sig2f[k] = (float)t.sig2[k];
+      t.shift6f[k] = (float)t.shift6[k];
+      t.shrf[k] = t.eps24[k] != 0.0 ? (float)(t.shift6[k] / t.eps24[k]) : 0.f;
     }
   h->sys.resize(num_systems);
   for (int q = 0; q < num_systems; ++q) {

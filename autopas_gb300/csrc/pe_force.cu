@@ -82,9 +82,9 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
   const int T = s.ntypes;
   if (!ONE_TYPE) {
     for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
-      tab[0][q] = (float)s.types->eps24[q];
-      tab[1][q] = (float)s.types->sig2[q];
-      tab[2][q] = (float)s.types->shift6[q];
+      tab[0][q] = s.types->eps24f[q];
+      tab[1][q] = s.types->sig2f[q];
+      tab[2][q] = s.types->shift6f[q];
     }
     __syncthreads();
   }
@@ -103,9 +103,9 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
   const bool halos = !S.periodic;
   float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
   if (ONE_TYPE) {
-    eps24 = (float)s.types->eps24[0];
-    sig2 = (float)s.types->sig2[0];
-    sh6 = (float)s.types->shift6[0];
+    eps24 = s.types->eps24f[0];
+    sig2 = s.types->sig2f[0];
+    sh6 = s.types->shift6f[0];
   }
   const float rc2f = fa.rc2f;
   const float band = rc2f * 2e-6f;
@@ -334,7 +334,7 @@ struct MixedAcc {
   // minus the force: compensated running sums and the plain sums of the current batch (two entries wide)
   float fxs = 0.f, fys = 0.f, fzs = 0.f, fxc = 0.f, fyc = 0.f, fzc = 0.f;
   float2 bx = {0.f, 0.f}, by = {0.f, 0.f}, bz = {0.f, 0.f};
-  // globals, two entries wide: the potential without the per-pair shift, minus the virial
+  // globals, two entries wide: 6 Upot, minus the virial
   float2 pot = {0.f, 0.f}, vx = {0.f, 0.f}, vy = {0.f, 0.f}, vz = {0.f, 0.f};
   int hits = 0, hhalo = 0;
 
@@ -345,7 +345,7 @@ struct MixedAcc {
   //   -fac = eps24 t ninv, so that the pair force on i is fac * d (LJFunctor.h:141-150)
   __device__ __forceinline__ float2 accum2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
                                            uint32_t e0, uint32_t e1, float2 dx, float2 dy, float2 dz, int tj0,
-                                           int tj1, int oj0, int oj1, int ti, float eps24, float sig2, float sh6,
+                                           int tj1, int oj0, int oj1, int ti, float eps24, float sig2, float shr,
                                            const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
                                            bool two) {
     const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
@@ -356,7 +356,7 @@ struct MixedAcc {
       if (n0) m0 = exact_within(s, S, i, (int64_t)(e0 >> 5), e0 & 31, fa.rc2);
       if (n1) m1 = exact_within(s, S, i, (int64_t)(e1 >> 5), e1 & 31, fa.rc2);
     }
-    float2 ep = dup2(eps24), sg = dup2(sig2), sh = dup2(sh6);
+    float2 ep = dup2(eps24), sg = dup2(sig2), sh = dup2(shr);
     if (!ONE_TYPE) {
       const int k0 = ti * T + tj0, k1 = ti * T + tj1;
       ep = make_float2(tab[0][k0], tab[0][k1]);
@@ -376,8 +376,9 @@ struct MixedAcc {
     by = add2(by, py);
     bz = add2(bz, pz);
     if (GLOB) {
-      if (!ONE_TYPE) pot = add2(pot, make_float2(m0 ? sh.x : 0.f, m1 ? sh.y : 0.f));
-      pot = fma2(em, lj12m6, pot);
+      // 6 Upot = eps24 (lj12m6 + shift6/eps24): the shift joins lj12m6 before the product, so a pair near a
+      // shifted cutoff adds its small energy, rounded once, and no large terms cancel in the sum
+      pot = fma2(em, add2(lj12m6, sh), pot);
       vx = fma2(px, dx, vx);
       vy = fma2(py, dy, vy);
       vz = fma2(pz, dz, vz);
@@ -395,8 +396,8 @@ struct MixedAcc {
   // otherwise (the shift of code kShiftNone is zero, so every lane applies its entries' shifts unconditionally).
   template <bool SHIFT>
   __device__ __forceinline__ float2 pair_q2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                            const float (&iq)[6], int ti, uint32_t e0, uint32_t e1, const uint4 &q0,
-                                            const uint4 &q1, float eps24, float sig2, float sh6,
+                                            const float (&iq)[8], int ti, uint32_t e0, uint32_t e1, const uint4 &q0,
+                                            const uint4 &q1, float eps24, float sig2, float shr,
                                             const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
                                             bool two = true) {
     float2 xh = dup2(iq[0]), yh = dup2(iq[1]), zh = dup2(iq[2]), xl = dup2(iq[3]), yl = dup2(iq[4]),
@@ -411,8 +412,8 @@ struct MixedAcc {
       yl = fma2(sy, dup2(S.len_lo_u[1]), yl);
       zl = fma2(sz, dup2(S.len_lo_u[2]), zl);
     }
-    const unsigned int eb = S.pq_expb;
-    const float2 u = dup2(S.pq_unit);
+    const unsigned int eb = __float_as_uint(iq[7]);
+    const float2 u = dup2(iq[6]);
     const float2 dx = fma2(add2(xl, make_float2(pq_nlox(q0), pq_nlox(q1))), u,
                            add2(xh, make_float2(pq_nhi(q0.x, eb), pq_nhi(q1.x, eb))));
     const float2 dy = fma2(add2(yl, make_float2(pq_nloy(q0), pq_nloy(q1))), u,
@@ -420,7 +421,7 @@ struct MixedAcc {
     const float2 dz = fma2(add2(zl, make_float2(pq_nloz(q0), pq_nloz(q1))), u,
                            add2(zh, make_float2(pq_nhi(q0.z, eb), pq_nhi(q1.z, eb))));
     return accum2(s, S, fa, i, e0, e1, dx, dy, dz, pq_type(q0), pq_type(q1), pq_own(q0), pq_own(q1), ti, eps24,
-                  sig2, sh6, tab, T, band, two);
+                  sig2, shr, tab, T, band, two);
   }
 
   __device__ __forceinline__ void flush() {
@@ -440,9 +441,7 @@ struct MixedAcc {
   __device__ __forceinline__ float force_x() const { return fxc - fxs; }
   __device__ __forceinline__ float force_y() const { return fyc - fys; }
   __device__ __forceinline__ float force_z() const { return fzc - fzs; }
-  __device__ __forceinline__ float upot(float sh6) const {
-    return ONE_TYPE ? fmaf(sh6, (float)hits, pot.x + pot.y) : pot.x + pot.y;
-  }
+  __device__ __forceinline__ float upot() const { return pot.x + pot.y; }
   __device__ __forceinline__ float vir_x() const { return -(vx.x + vx.y); }
   __device__ __forceinline__ float vir_y() const { return -(vy.x + vy.y); }
   __device__ __forceinline__ float vir_z() const { return -(vz.x + vz.y); }
@@ -470,8 +469,8 @@ __device__ __forceinline__ void list_load(const uint32_t *p, uint32_t (&e)[U]) {
 // before its arithmetic.  Leftover entries (n mod UNROLL) are read one by one.
 template <int GM, bool ONE_TYPE, bool KAHAN, int UNROLL, bool STREAM, bool PF>
 __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                           const float (&iq)[6], int ti, const uint32_t *__restrict__ list, int n,
-                                           float eps24, float sig2, float sh6,
+                                           const float (&iq)[8], int ti, const uint32_t *__restrict__ list, int n,
+                                           float eps24, float sig2, float shr,
                                            const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
                                            MixedAcc<GM, ONE_TYPE, KAHAN> &acc) {
   static_assert(UNROLL == 2 || UNROLL == 4, "batches of 2 or 4 entries");
@@ -518,12 +517,12 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
     if (__any_sync(__activemask(), shifted)) {
 #pragma unroll
       for (int u = 0; u < UNROLL; u += 2)
-        acc.template pair_q2<true>(s, S, fa, i, iq, ti, e[u], e[u + 1], qj[u], qj[u + 1], eps24, sig2, sh6, tab,
+        acc.template pair_q2<true>(s, S, fa, i, iq, ti, e[u], e[u + 1], qj[u], qj[u + 1], eps24, sig2, shr, tab,
                                    T, band);
     } else {
 #pragma unroll
       for (int u = 0; u < UNROLL; u += 2)
-        acc.template pair_q2<false>(s, S, fa, i, iq, ti, e[u], e[u + 1], qj[u], qj[u + 1], eps24, sig2, sh6, tab,
+        acc.template pair_q2<false>(s, S, fa, i, iq, ti, e[u], e[u + 1], qj[u], qj[u + 1], eps24, sig2, shr, tab,
                                     T, band);
     }
     acc.flush();
@@ -539,7 +538,7 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
     const uint32_t e0 = __ldg(list + plist_index(stride, i, k));
     const uint32_t e1 = two ? __ldg(list + plist_index(stride, i, k + 1)) : e0;
     acc.template pair_q2<true>(s, S, fa, i, iq, ti, e0, e1, __ldg(s.pq + (e0 >> 5)), __ldg(s.pq + (e1 >> 5)), eps24,
-                               sig2, sh6, tab, T, band, two);
+                               sig2, shr, tab, T, band, two);
   }
   acc.flush();
 }
@@ -548,9 +547,9 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
 // out.  Returns their number.
 template <int GM, bool ONE_TYPE, bool KAHAN>
 __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const SysDev &S, const ForceArgs &fa,
-                                                  int64_t i, const float (&iq)[6], int ti,
+                                                  int64_t i, const float (&iq)[8], int ti,
                                                   const uint32_t *__restrict__ list, int n, float eps24, float sig2,
-                                                  float sh6, const float (*tab)[kMaxTypes * kMaxTypes], int T,
+                                                  float shr, const float (*tab)[kMaxTypes * kMaxTypes], int T,
                                                   float band, MixedAcc<GM, ONE_TYPE, KAHAN> &acc,
                                                   uint32_t *__restrict__ out, float lim) {
   const int64_t stride = s.pl_stride;
@@ -558,7 +557,7 @@ __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const Sy
   for (int k = 0; k < n; ++k) {
     const uint32_t en = __ldg(list + plist_index(stride, i, k));
     const uint4 q = __ldg(s.pq + (en >> 5));
-    const float r2 = acc.template pair_q2<true>(s, S, fa, i, iq, ti, en, en, q, q, eps24, sig2, sh6, tab, T, band,
+    const float r2 = acc.template pair_q2<true>(s, S, fa, i, iq, ti, en, en, q, q, eps24, sig2, shr, tab, T, band,
                                                 false).x;
     if (r2 <= lim) out[plist_index(stride, i, m++)] = en;
     if ((k & 1) == 1) acc.flush();
@@ -583,9 +582,9 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   const int T = s.ntypes;
   if (!ONE_TYPE) {
     for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
-      tab[0][q] = (float)s.types->eps24[q];
-      tab[1][q] = (float)s.types->sig2[q];
-      tab[2][q] = (float)s.types->shift6[q];
+      tab[0][q] = s.types->eps24f[q];
+      tab[1][q] = s.types->sig2f[q];
+      tab[2][q] = s.types->shrf[q];
     }
     __syncthreads();
   }
@@ -602,19 +601,25 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   }
   const int sy = inrange ? s.sys[i] : 0;
   const SysDev &S = s.sysd[sy];
-  const float iq[6] = {pq_hi(qi.x, S.pq_expb), pq_hi(qi.y, S.pq_expb), pq_hi(qi.z, S.pq_expb),
-                       pq_lox(qi), pq_loy(qi), pq_loz(qi)};
-  float eps24 = 0.f, sig2 = 0.f, sh6 = 0.f;
+  // i's decoded record, then the system's record unit and exponent bits
+  float iq[8] = {pq_hi(qi.x, S.pq_expb), pq_hi(qi.y, S.pq_expb), pq_hi(qi.z, S.pq_expb),
+                 pq_lox(qi), pq_loy(qi), pq_loz(qi), S.pq_unit, __uint_as_float(S.pq_expb)};
+  float eps24 = 0.f, sig2 = 0.f, shr = 0.f;  // shr: the energy shift over eps24 (TypeTable::shrf)
   if (ONE_TYPE) {
-    eps24 = (float)s.types->eps24[0];
-    sig2 = (float)s.types->sig2[0];
-    sh6 = (float)s.types->shift6[0];
+    eps24 = s.types->eps24f[0];
+    sig2 = s.types->sig2f[0];
+    shr = s.types->shrf[0];
   }
+  // loop invariants made opaque to the compiler, which otherwise may reload them from global memory at each
+  // use (a dependent load in the loop) rather than keep them in registers
+#pragma unroll
+  for (int k = 0; k < 8; ++k) asm volatile("" : "+f"(iq[k]));
+  asm volatile("" : "+f"(eps24), "+f"(sig2), "+f"(shr));
   const float band = fa.rc2f * 2e-6f;
   MixedAcc<GM, ONE_TYPE, KAHAN> acc;
   if (reprune) {
     const float lim = s.disp_bits[1] <= f2bits(s.reb_limit2) ? s.r_in2f : s.r_out2f;
-    const int m = plist_walk_reprune<GM, ONE_TYPE, KAHAN>(s, S, fa, i, iq, ti, s.pl_list, n, eps24, sig2, sh6, tab,
+    const int m = plist_walk_reprune<GM, ONE_TYPE, KAHAN>(s, S, fa, i, iq, ti, s.pl_list, n, eps24, sig2, shr, tab,
                                                            T, band, acc, s.pi_list, lim);
     if (inrange) {
       s.pi_count[i] = m;
@@ -625,7 +630,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       }
     }
   } else {
-    plist_walk<GM, ONE_TYPE, KAHAN, UNROLL, STREAM, PF>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, sh6, tab,
+    plist_walk<GM, ONE_TYPE, KAHAN, UNROLL, STREAM, PF>(s, S, fa, i, iq, ti, s.fl_list, n, eps24, sig2, shr, tab,
                                                          T, band, acc);
   }
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
@@ -676,7 +681,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   }
   if (GLOB) {
     const bool owned = oi == 1;
-    float g0 = owned ? acc.upot(sh6) : 0.f, g1 = owned ? acc.vir_x() : 0.f, g2 = owned ? acc.vir_y() : 0.f;
+    float g0 = owned ? acc.upot() : 0.f, g1 = owned ? acc.vir_x() : 0.f, g2 = owned ? acc.vir_y() : 0.f;
     float g3 = owned ? acc.vir_z() : 0.f;
     int h = owned ? acc.hits + acc.hhalo : 0;
 #pragma unroll
