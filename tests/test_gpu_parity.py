@@ -176,6 +176,31 @@ def test_multi_type_mixing_and_shift(eng_mod, orc):
         assert g["upot"] == pytest.approx(glob[0], rel=tol)
 
 
+@pytest.mark.parametrize("ntypes", [1, 3])
+def test_shifted_energy_keeps_fp64_accuracy_in_mixed_precision(eng_mod, orc, ntypes):
+    """With the shifted potential, each pair's energy is eps24 lj12m6 + shift6, the two terms nearly cancelling
+    near rc; the mixed kernels form the pair energy before summing it.  On a dense 3,000-particle system the FP32
+    rounding of the pair terms alone gives ~8e-8 relative (a float emulation of the sums agrees), so the bound
+    is 2e-7; a lost or doubled shift would be off by 0.2 (single type)."""
+    from autopas_gb300 import workloads
+    rng = np.random.default_rng(33)
+    bmin, bmax = np.zeros(3), np.full(3, 16.0)
+    pos = workloads.rsa(3000, bmin, bmax, bmin, bmax, 0.85, seed=8)
+    types = rng.integers(0, ntypes, size=len(pos)).astype(np.int32)
+    eps, sig = [1.0, 0.8, 1.2][:ntypes], [1.0, 1.1, 0.9][:ntypes]
+    rc, skin = 3.0, 0.3
+    lj = orc.LJ(rc, epsilon=eps, sigma=sig, shift=True)
+    allpos, own, allt, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin, types=types)
+    _, glob, _ = orc.lj_forces(allpos, lj, own=own, types=allt)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=eps, sigma=sig, mass=[1.0] * ntypes,
+                           shift=True, precision=eng_mod.PRECISION_MIXED)
+    e.set_particles(pos, types=types)
+    g = e.compute_forces()[0]
+    e.close()
+    assert abs(g["upot"] - glob[0]) <= 2e-7 * abs(glob[0])
+    assert abs(g["virial"] - glob[1]) <= 2e-7 * abs(glob[1])
+
+
 def test_md_trajectory_fp64_matches_oracle(eng_mod, orc):
     pos, vel, bmin, bmax = liquid(5, seed=13, jitter=0.02)
     rc, skin, dt, nsteps = 2.5, 0.3, 0.002, 40
