@@ -543,8 +543,8 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
   acc.flush();
 }
 
-// The re-prune walk: the outer list (rc + skin) entry by entry; entries within lim also go to the inner list
-// out.  Returns their number.
+// The re-prune walk: the outer list (rc + skin) two entries at a time; entries within lim also go to the
+// inner list out, in list order.  Returns their number.
 template <int GM, bool ONE_TYPE, bool KAHAN>
 __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const SysDev &S, const ForceArgs &fa,
                                                   int64_t i, const float (&iq)[8], int ti,
@@ -554,13 +554,16 @@ __device__ __forceinline__ int plist_walk_reprune(const DeviceState &s, const Sy
                                                   uint32_t *__restrict__ out, float lim) {
   const int64_t stride = s.pl_stride;
   int m = 0;
-  for (int k = 0; k < n; ++k) {
-    const uint32_t en = __ldg(list + plist_index(stride, i, k));
-    const uint4 q = __ldg(s.pq + (en >> 5));
-    const float r2 = acc.template pair_q2<true>(s, S, fa, i, iq, ti, en, en, q, q, eps24, sig2, shr, tab, T, band,
-                                                false).x;
-    if (r2 <= lim) out[plist_index(stride, i, m++)] = en;
-    if ((k & 1) == 1) acc.flush();
+  for (int k = 0; k < n; k += 2) {
+    const bool two = k + 1 < n;
+    const uint32_t e0 = __ldg(list + plist_index(stride, i, k));
+    const uint32_t e1 = two ? __ldg(list + plist_index(stride, i, k + 1)) : e0;
+    const uint4 q0 = __ldg(s.pq + (e0 >> 5)), q1 = __ldg(s.pq + (e1 >> 5));
+    const float2 r2 = acc.template pair_q2<true>(s, S, fa, i, iq, ti, e0, e1, q0, q1, eps24, sig2, shr, tab, T,
+                                                 band, two);
+    if (r2.x <= lim) out[plist_index(stride, i, m++)] = e0;
+    if (two && r2.y <= lim) out[plist_index(stride, i, m++)] = e1;
+    if ((k & 2) == 2) acc.flush();
   }
   acc.flush();
   return m;
