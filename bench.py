@@ -384,7 +384,7 @@ def run_ours(args):
         with open(os.path.join(ROOT, "profiles", "force_kernel_traffic.json")) as f:
             tr = json.load(f)
         if tr.get("kernel_prefix") and info["traversal"] == 1:
-            traffic = tr["dram_bytes_per_particle"] * n
+            traffic = tr["forces_only"]["dram_bytes_per_particle"] * n
     except Exception:
         traffic = None
     sm_max = peaks.get("sm_max_mhz", 2070.0)
@@ -409,8 +409,14 @@ def run_ours(args):
         "tuning": tuning,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per launch, scaled by particle count "
-                                     "from profiles/force_kernel_traffic.json (same kernel, 400,000-particle slab)",
+                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per forces-and-globals launch (the "
+                                     "launch force_kernel times), scaled by particle count from "
+                                     "profiles/force_kernel_traffic.json (same kernel, 400,000-particle slab)",
+                     "hbm_view": ({"achieved_gbs": traffic / (force_ms_per_launch * 1e-3) / 1e9,
+                                   "peak_gbs": peaks.get("hbm_gbs"),
+                                   "frac": traffic / (force_ms_per_launch * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)"}
+                                  if traffic and peaks.get("hbm_gbs") else None),
                      "kernel": ("k_lj_mixed_plist" if info["traversal"] == 1 else "k_lj_mixed_full") +
                                f"<{info['cluster_size']}>",
                      "algorithmic": f"{FLOP_PER_PAIR} FLOP per interacting pair (reference convention)",
