@@ -895,23 +895,50 @@ void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_vel
 }
 
 // ---------------------------------------------------------------------------------------------
-// per-system globals: the clusters of each system are cut into chunks of at most kChunk clusters; one block
-// reduces each chunk (fixed thread assignment and tree), then one block per system reduces its chunk sums
-// the same way, so the result is bitwise reproducible.  LJFunctor::endTraversal post-processing (x0.5, /6;
-// LJFunctor.h:661-685) is applied at the end.
+// per-system globals: the clusters of each system are cut into chunks of at most kChunk clusters; one warp
+// reduces each chunk, then one block per system reduces its chunk sums, each with a fixed thread assignment
+// (sequential per thread, then butterflies over the warps), so the result is bitwise reproducible.
+// LJFunctor::endTraversal post-processing (x0.5, /6; LJFunctor.h:661-685) is applied at the end.  A warp per
+// chunk keeps the FP64 work low: this GPU's FP64 pipe issues 2 lanes per clock per SM, and a block-wide tree
+// per chunk cost more FP64 operations than the sums themselves.
 // ---------------------------------------------------------------------------------------------
-// fixed-order sum of kGlob doubles and a count over a 256-thread block: warp trees, then warp 0 over the
-// eight warp sums.  Thread 0 returns the result.
-__device__ __forceinline__ void block_sum6(double (&g)[kGlob], long long &h) {
-  __shared__ double wred[8][kGlob];
-  __shared__ long long wh[8];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+constexpr int kRedWarps = 8;  // warps per reduction block
+
+__device__ __forceinline__ void warp_sum6(double (&g)[kGlob], long long &h) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
     for (int q = 0; q < kGlob; ++q) g[q] += __shfl_xor_sync(0xffffffffu, g[q], o);
     h += __shfl_xor_sync(0xffffffffu, h, o);
   }
+}
+
+// one warp per chunk of at most kChunk = 256 clusters: lane l sums clusters c0 + l + 32 m
+__global__ void __launch_bounds__(kRedWarps * 32)
+    k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, int nchunks, double *__restrict__ cpart) {
+  const int k = blockIdx.x * kRedWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (k >= nchunks) return;  // a whole warp
+  const int64_t c0 = chunks[3 * k + 1], c1 = chunks[3 * k + 2];
+  double g[kGlob] = {0, 0, 0, 0, 0};
+  long long h = 0;
+  for (int64_t c = c0 + lane; c < c1; c += 32) {
+#pragma unroll
+    for (int q = 0; q < kGlob; ++q) g[q] += s.cl_glob[kGlob * c + q];
+    h += (long long)s.cl_hits[c];
+  }
+  warp_sum6(g, h);
+  if (lane == 0) {
+    for (int q = 0; q < kGlob; ++q) cpart[(kGlob + 1) * k + q] = g[q];
+    cpart[(kGlob + 1) * k + kGlob] = (double)h;
+  }
+}
+
+// fixed-order sum of kGlob doubles and a count over a block: warp butterflies, then thread 0 over the warp sums
+__device__ __forceinline__ void block_sum6(double (&g)[kGlob], long long &h) {
+  __shared__ double wred[kRedWarps][kGlob];
+  __shared__ long long wh[kRedWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  warp_sum6(g, h);
   if (lane == 0) {
     for (int q = 0; q < kGlob; ++q) wred[w][q] = g[q];
     wh[w] = h;
@@ -927,31 +954,14 @@ __device__ __forceinline__ void block_sum6(double (&g)[kGlob], long long &h) {
   }
 }
 
-// one block of 256 threads per chunk of at most kChunk = 256 clusters: one cluster per thread
-__global__ void __launch_bounds__(256) k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks,
-                                                        double *__restrict__ cpart) {
-  const int64_t c0 = chunks[3 * blockIdx.x + 1], c1 = chunks[3 * blockIdx.x + 2];
-  double g[kGlob] = {0, 0, 0, 0, 0};
-  long long h = 0;
-  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
-#pragma unroll
-    for (int q = 0; q < kGlob; ++q) g[q] += s.cl_glob[kGlob * c + q];
-    h += (long long)s.cl_hits[c];
-  }
-  block_sum6(g, h);
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < kGlob; ++q) cpart[(kGlob + 1) * blockIdx.x + q] = g[q];
-    cpart[(kGlob + 1) * blockIdx.x + kGlob] = (double)h;
-  }
-}
-
 // one block per system over its chunk partials (fixed assignment and tree), then the endTraversal scaling
-__global__ void __launch_bounds__(256) k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0,
-                                                         const double *__restrict__ cpart) {
+__global__ void __launch_bounds__(kRedWarps * 32)
+    k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0, const double *__restrict__ cpart) {
   const int sy = blockIdx.x;
   double g[kGlob] = {0, 0, 0, 0, 0};
   long long hh = 0;
   for (int k = sys_chunk0[sy] + threadIdx.x; k < sys_chunk0[sy + 1]; k += blockDim.x) {
+#pragma unroll
     for (int q = 0; q < kGlob; ++q) g[q] += cpart[(kGlob + 1) * k + q];
     hh += (long long)cpart[(kGlob + 1) * k + kGlob];
   }
@@ -972,8 +982,9 @@ __global__ void __launch_bounds__(256) k_reduce_systems(DeviceState s, const int
 
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
                            double *cpart, cudaStream_t st) {
-  if (nchunks > 0) k_reduce_chunks<<<nchunks, 256, 0, st>>>(s, chunks, cpart);
-  if (s.nsys > 0) k_reduce_systems<<<s.nsys, 256, 0, st>>>(s, sys_chunk0, cpart);
+  if (nchunks > 0)
+    k_reduce_chunks<<<(nchunks + kRedWarps - 1) / kRedWarps, kRedWarps * 32, 0, st>>>(s, chunks, nchunks, cpart);
+  if (s.nsys > 0) k_reduce_systems<<<s.nsys, kRedWarps * 32, 0, st>>>(s, sys_chunk0, cpart);
 }
 
 }  // namespace pe

@@ -154,7 +154,7 @@ void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, con
 // forces (pe_force.cu)
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
                   const VVFactors *vv = nullptr, bool fuse_positions = false);
-constexpr int kChunk = 256;  // clusters per globals-reduction chunk (one per thread of a reduction block)
+constexpr int kChunk = 256;  // clusters per globals-reduction chunk (8 per lane of a reduction warp)
 constexpr int kGlob = 5;      // per-cluster partials: 6*Upot, virial x, y, z, kinetic energy
 constexpr int kSysGlob = 6;   // per system: Upot, virial, virial x, y, z, kinetic energy
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
