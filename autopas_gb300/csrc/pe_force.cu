@@ -488,6 +488,7 @@ __device__ __forceinline__ void plist_walk(const DeviceState &s, const SysDev &S
     q[u] = make_uint4(0u, 0u, 0u, 0u);
   }
   if (UNROLL <= n) list_load<UNROLL, STREAM>(base, e);
+  if (8 < n) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + bstride));  // the second block (see below)
   if (PF && 2 * UNROLL <= n) list_load<UNROLL, STREAM>(base + (UNROLL >> 3) * bstride + (UNROLL & 7), nx);
   if (PF && UNROLL <= n) {
 #pragma unroll
@@ -606,6 +607,24 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
     ti = pq_type(qi);
     oi = pq_own(qi);
     if (oi == 1) n = reprune ? min(s.pl_count[i], s.pl_cap) : s.fl_count[i];
+  }
+  if (inrange && oi == 1) {
+    // the FP64 state the epilogue reads, into L2 while the list is walked
+    if (GLOB || fa.fuse_velocity) {
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.vx + i));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.vy + i));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.vz + i));
+    }
+    if (fa.fuse_velocity) {
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.ofx + i));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.ofy + i));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.ofz + i));
+    }
+    if (fa.fuse_positions) {
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.x + i));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.y + i));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(s.z + i));
+    }
   }
   const int sy = inrange ? s.sys[i] : 0;
   const SysDev &S = s.sysd[sy];
