@@ -1,0 +1,97 @@
+"""Edge cases of the engine on the GPU: empty and single-particle systems, a pair exactly at the cutoff, and a
+large sparse box (coarse position encoding) whose pair sets must still equal the oracle's."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng_mod():
+    from autopas_gb300.build import build
+    build()
+    from autopas_gb300 import engine
+    return engine
+
+
+@pytest.fixture(scope="module")
+def orc():
+    from oracle import oracle
+    oracle.build()
+    return oracle
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_empty_and_single_particle(eng_mod, prec):
+    p = eng_mod.PRECISION_MIXED if prec == "mixed" else eng_mod.PRECISION_FP64
+    bmin, bmax = np.zeros(3), np.full(3, 10.0)
+    for n in (0, 1):
+        e = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=p)
+        pos = np.full((n, 3), 5.0)
+        e.set_particles(pos, np.zeros((n, 3)))
+        g = e.compute_forces()[0]
+        F = e.forces()
+        assert F.shape == (n, 3) and not np.any(F)
+        assert g["num_pairs"] == 0 and g["upot"] == 0.0 and g["virial"] == 0.0
+        if n:
+            e.step(0.002, 3)
+            P, V = e.state()
+            assert np.array_equal(P, pos)
+        e.close()
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_pair_exactly_at_the_cutoff(eng_mod, orc, prec):
+    """dr2 == rc^2 interacts (LJFunctor.h mask dr2 <= cutoffSquared); one ulp further apart does not."""
+    p = eng_mod.PRECISION_MIXED if prec == "mixed" else eng_mod.PRECISION_FP64
+    rc, skin = 2.5, 0.3
+    bmin, bmax = np.zeros(3), np.full(3, 20.0)
+    lj = orc.LJ(rc)
+    x0 = 5.0
+    for x1, interacts in ((x0 + rc, True), (np.nextafter(x0 + rc, 10.0), False)):
+        pos = np.array([[x0, 6.0, 7.0], [x1, 6.0, 7.0]])
+        assert ((pos[1, 0] - pos[0, 0]) ** 2 <= rc * rc) == interacts
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=p)
+        e.set_particles(pos, np.zeros((2, 3)))
+        g = e.compute_forces()[0]
+        F = e.forces()
+        e.close()
+        R, glob, _ = orc.lj_forces(pos, lj)
+        assert g["num_pairs"] == (1 if interacts else 0)
+        if interacts:
+            np.testing.assert_allclose(F, R, rtol=1e-6 if prec == "mixed" else 1e-13)
+            assert g["upot"] == pytest.approx(glob[0], rel=1e-6 if prec == "mixed" else 1e-13)
+        else:
+            assert not np.any(F) and g["upot"] == 0.0
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_large_sparse_box_pair_sets(eng_mod, orc, traversal):
+    """A 600-wide periodic box puts the encoding base B at 2048 (ulp(B) = 2.4e-4): the particle lists, built
+    from the hi parts of the records alone, must still hold every pair within rc+skin, and the interacting
+    set must be the FP64 one."""
+    from autopas_gb300 import workloads
+    rc, skin = 3.0, 0.4
+    bmin, bmax = np.zeros(3), np.array([600.0, 40.0, 40.0])
+    pos = workloads.rsa(12000, bmin, bmax, bmin, bmax, 0.9, seed=23)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, traversal=traversal)
+    e.set_particles(pos, np.zeros_like(pos))
+    e.rebuild()
+    for which in (0, 1):
+        a, b, c = e.pair_set(which)
+        dev = np.unique(np.stack([a, b, c], 1), axis=0)
+        allpos, own, allt, owner, code = orc.periodic_system(pos, bmin, bmax, rc, skin)
+        n = len(pos)
+        if which == 0:
+            ra, rb = orc.pair_set(allpos, rc + skin, own=own)
+        else:
+            ra, rb = orc.interacting_set(allpos, rc, own=own)
+        halo_b = rb >= n
+        bb = np.where(halo_b, owner[np.where(halo_b, rb - n, 0)], rb)
+        cc = np.where(halo_b, code[np.where(halo_b, rb - n, 0)], 13)
+        ref = np.unique(np.stack([ra, bb, cc], 1), axis=0)
+        assert np.array_equal(dev, ref)
+    g = e.compute_forces()[0]
+    e.close()
+    ia, ib = orc.interacting_set(allpos, rc, own=own)
+    assert g["num_pairs"] == int(np.sum(ib < n)) + int(np.sum(ib >= n)) // 2
