@@ -211,10 +211,12 @@ class PairEngine:
     def rebuild(self):
         self._check(self._L.pe_rebuild(self._h))
 
-    def compute_forces(self):
-        g = (PeGlobals * self.num_systems)()
+    def compute_forces(self, want_globals=True):
+        """Forces of the current positions; with want_globals the per-system globals are read back (a host
+        wait for the device), without it the call returns at once (None) and the forces are read later."""
+        g = (PeGlobals * self.num_systems)() if want_globals else None
         self._check(self._L.pe_compute_forces(self._h, g))
-        return _globals(g)
+        return _globals(g) if want_globals else None
 
     def compute_atm(self, nu, cutoff3):
         """Adds Axilrod-Teller-Muto forces to the current forces; returns per-system ATM globals."""

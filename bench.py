@@ -353,7 +353,7 @@ def run_ours(args):
             if k % REBUILD == 0:
                 ee.rebuild()
             ee._check(ee._L.pe_update_positions(ee._h, hx.ctypes.data, hy.ctypes.data, hz.ctypes.data))
-            ee.compute_forces()
+            ee.compute_forces(want_globals=False)
             ee.forces_into(fx, fy, fz)
         t_e2e = time.perf_counter() - t0
         st3 = ee.stats(reset=True)
@@ -362,8 +362,9 @@ def run_ours(args):
         e2e = {"value": sum_over_ranks(pg, st3["pairs_total"]) / t_e2e, "unit": "pair interactions/s",
                "h2d_bytes_per_step": 3 * 8 * n, "d2h_bytes_per_step": 3 * 8 * n + 48,
                "steps": nst, "ms_per_step": 1e3 * t_e2e / nst,
-               "what": "per step: pe_update_positions from pinned host x,y,z + pe_compute_forces (pe_rebuild every "
-                       f"{REBUILD} steps) + pe_get_forces into pinned host fx,fy,fz; host wall clock",
+               "what": "per step: pe_update_positions from pinned host x,y,z + pe_compute_forces (forces and "
+                       f"globals on the device, pe_rebuild every {REBUILD} steps) + pe_get_forces into pinned host "
+                       "fx,fy,fz; host wall clock",
                "host_link": host_link_rates(3 * 8 * n)}
 
     # ---- CPU baseline (rank 0, N = 1)
