@@ -1,25 +1,29 @@
-// pe_force.cu -- Lennard-Jones cluster-pair force kernels and the globals reduction.
+// pe_force.cu -- Lennard-Jones force kernels and the globals reduction.
 //
 // Replaces the VCL traversal's SoAFunctorSingle / SoAFunctorPair calls on cluster views
-// (src/autopas/containers/verletClusterLists/traversals/VCLClusterFunctor.h:38-89) with the LJ arithmetic of
+// (src/autopas/containers/verletClusterLists/traversals/VCLClusterFunctor.h:38-89) and the Verlet-list
+// functor (LJFunctor.h:812-1115) with the LJ arithmetic of
 // applicationLibrary/molecularDynamics/molecularDynamicsLibrary/LJFunctor.h:204-559 and the globals of
 // LJFunctor.h:641-720.
 //
-// Work decomposition: one warp per i-cluster.  lane = ii + C*jl with ii the i-particle (C of them) and
-// jl in [0, 32/C) a j-lane; the warp walks the i-cluster's list as a flat sequence of j-particles,
-// 32/C of them per step, so all lanes of a step read the same j-cluster (coalesced / broadcast loads).
-//
-//  * full lists (newton3 off): every pair is evaluated from both sides; the i-force is accumulated in
-//    registers (compensated FP32 for the mixed form) and written once -- no atomics, deterministic.
-//    This is the only list mode the kernels implement.
+// Two traversals:
+//  * cluster pairs (k_lj_mixed_full, k_lj_fp64_full): one warp per i-cluster, lane = ii + C*jl with ii the
+//    i-particle and jl a j-lane; the warp walks the i-cluster's list as a flat sequence of j-particles, 32/C
+//    of them per step, so all lanes of a step read the same j-cluster (broadcast loads).
+//  * particle lists (k_lj_mixed_plist, k_lj_fp64_plist; the tuner's choice on the benchmark systems): one
+//    thread per slot walking its own list of j entries; the list is laid out so that a warp's loads are
+//    coalesced, its next block is prefetched into L2, and the mixed kernel evaluates two entries per packed
+//    FP32x2 instruction.
+// Both use full lists (newton3 off): every pair is evaluated from both sides; the i-force is accumulated in
+// registers (compensated FP32 for the mixed form) and written once -- no atomics, deterministic.
 //
 // Precision forms:
 //  * FP64 ("plain FP64 GPU form"): positions, displacements and LJ arithmetic in FP64 with the reference's
 //    operation order; per-pair forces are bit-identical to LJFunctor's (strict evaluation).
-//  * MIXED: positions are stored as hi+lo float pairs inside one binade [B,2B) per system so that the
-//    hi difference is exact and the displacement is rounded once to FP32; the LJ arithmetic is FP32 and the
-//    i-force sum is Kahan-compensated.  Pairs within 2e-6 (relative) of the cutoff repeat the cutoff test in
-//    FP64 so that the interacting set equals the FP64 one.
+//  * MIXED: positions are encoded in 16-byte records inside one binade [B,2B) per system (hi parts and
+//    integer low parts) so that each displacement is formed exactly and rounded once to FP32; the LJ
+//    arithmetic is FP32 and the i-force sum is Kahan-compensated.  Pairs within 2e-6 (relative) of the cutoff
+//    repeat the cutoff test in FP64 so that the interacting set equals the FP64 one.
 #include "pe_state.cuh"
 
 namespace pe {
