@@ -136,7 +136,8 @@ int pe_update_positions(pe_engine *h, const double *x, const double *y, const do
 int pe_rebuild(pe_engine *h);
 
 /* Replaces: functor.initTraversal(); container->computeInteractions(&traversal); functor.endTraversal()
- * (LogicHandler.h:1092-1122).  Forces are overwritten.  globals: [num_systems] or NULL. */
+ * (LogicHandler.h:1092-1122).  Forces are overwritten.  globals: [num_systems], read back (the call waits
+ * for the device), or NULL (the call returns once the work is queued; pe_get_forces waits for it). */
 int pe_compute_forces(pe_engine *h, pe_globals *globals);
 
 /* Forces in the order of the last pe_set_particles (halo/dummy entries: 0).  Any pointer may be NULL. */
