@@ -38,18 +38,21 @@ __device__ __forceinline__ int tower_coord(double p, const SysDev &S, int d) {
 
 __global__ void k_bin(DeviceState s, int64_t nslots_old, uint64_t *__restrict__ key, int32_t *__restrict__ tower_of) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nslots_old) return;
-  if (s.own[i] == 0) {
-    tower_of[i] = -1;
-    return;
+  int t = -1;
+  if (i < nslots_old) {
+    if (s.own[i] != 0) {
+      const SysDev &S = s.sysd[s.sys[i]];
+      const int tx = tower_coord(s.x[i], S, 0);
+      const int ty = tower_coord(s.y[i], S, 1);
+      t = S.tower_base + ty * S.nt[0] + tx;
+      key[i] = dbl_key(s.z[i]);
+    }
+    tower_of[i] = t;
   }
-  const SysDev &S = s.sysd[s.sys[i]];
-  const int tx = tower_coord(s.x[i], S, 0);
-  const int ty = tower_coord(s.y[i], S, 1);
-  const int t = S.tower_base + ty * S.nt[0] + tx;
-  tower_of[i] = t;
-  key[i] = dbl_key(s.z[i]);
-  atomicAdd(&s.tw_count[t], 1);
+  // one atomic per distinct tower of the warp (consecutive slots mostly share a tower; one atomic per particle
+  // serialised on the same counters)
+  const unsigned peers = __match_any_sync(0xffffffffu, t);
+  if (t >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&s.tw_count[t], __popc(peers));
 }
 
 void launch_bin(DeviceState &s, int64_t nslots_old, uint64_t *key, int32_t *tower_of, cudaStream_t st) {
@@ -75,10 +78,17 @@ __global__ void k_scatter(DeviceState s, int64_t nslots_old, const int32_t *__re
                           const uint64_t *__restrict__ key, int32_t *__restrict__ fill, uint64_t *__restrict__ skey,
                           int32_t *__restrict__ sval) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nslots_old) return;
-  const int t = tower_of[i];
+  const int lane = threadIdx.x & 31;
+  const int t = i < nslots_old ? tower_of[i] : -1;
+  // places within a tower's segment: one atomic per distinct tower of the warp, ranks inside the warp (the
+  // order inside a segment does not matter: the tower sort that follows orders by (z, particle index))
+  const unsigned peers = __match_any_sync(0xffffffffu, t);
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (t >= 0 && lane == leader) base = atomicAdd(&fill[t], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
   if (t < 0) return;
-  const int p = s.tw_start[t] + atomicAdd(&fill[t], 1);
+  const int p = s.tw_start[t] + base + __popc(peers & ((1u << lane) - 1));
   skey[p] = key[i];
   sval[p] = (int32_t)i;
 }
