@@ -3,7 +3,7 @@
 Tolerances:
 * FP64 form: forces within 1e-12 of the largest force magnitude (the per-pair arithmetic is the reference's
   operation order; only the summation order differs), Upot and virial within 1e-12 relative.
-* mixed form: force RMS error relative to the RMS force <= 1e-6 (the spec bar), Upot within 1e-6.
+* mixed form: force RMS error relative to the RMS force <= 1e-6 (the stated accuracy target), Upot within 1e-6.
 * pair sets (rc+skin Verlet rule and the rc interacting set): bit-exact set equality.
 """
 import numpy as np
