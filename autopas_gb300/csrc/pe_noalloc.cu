@@ -1,9 +1,10 @@
 // pe_noalloc.cu -- an LJ force entry point that allocates no memory.
 //
 // Who needs it: callers that must not allocate device memory at the point where they compute forces --
-// code that runs while a CUDA stream is being captured into a graph (cudaMalloc is not allowed inside a
-// capture), hosts that hand all device memory to a framework's pool up front and forbid further allocations,
-// and latency-critical loops that may not block in the allocator.  Such callers keep their particle data in
+// hosts that hand all device memory to a framework's pool up front and forbid further allocations (an MD
+// code running next to a machine-learning framework that reserved the GPU), plug-in hosts whose rules keep
+// plug-ins from allocating, and latency-critical loops that may not block in cudaMalloc, which can
+// synchronise the whole device.  Such callers keep their particle data in
 // memory they already own and only need the force, Upot and virial of it.
 //
 // What it computes: the plain FP64 form of the engine's force path for one small non-periodic particle set

@@ -223,9 +223,9 @@ int pe_tune(pe_engine *h, int samples);
 int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, int *chosen);
 
 /* Forces without any memory allocation.  This entry point has no counterpart in the reference: it exists
- * for callers that cannot allocate device memory where they need forces -- code running while a stream is
- * captured into a CUDA graph, hosts whose device memory is all handed out by a framework's pool, loops that
- * must not block in an allocator.  It computes, in the plain FP64 form, the forces on the owned particles of
+ * for callers that cannot allocate device memory where they need forces -- hosts whose device memory is all
+ * handed out by a framework's pool, plug-in hosts that forbid plug-ins to allocate, loops that must not block
+ * in cudaMalloc (which can synchronise the whole device).  It computes, in the plain FP64 form, the forces on the owned particles of
  * one small non-periodic set (owned + halo, AutoPas container semantics; every pair with dr2 <= rc^2 from both
  * sides, reference LJ arithmetic) and writes globals[0..5] = {Upot, virial, virial_x, virial_y, virial_z,
  * interacting pairs}.  All arrays are device memory owned by the caller (type and ownership may be NULL:

@@ -1,7 +1,7 @@
 """pe_lj_forces_noalloc: forces for callers that cannot allocate device memory.
 
-Such callers (code running under CUDA-graph stream capture, hosts whose device memory is handed out by a
-framework's pool, loops that must not block in an allocator) own their particle buffers and call this entry
+Such callers (hosts whose device memory is all handed out by a framework's pool, plug-in hosts that forbid
+plug-ins to allocate, loops that must not block in cudaMalloc) own their particle buffers and call this entry
 point, which itself allocates nothing.  The test checks it through the C ABI against the engine's regular
 entry point (pe_compute_forces in the FP64 form) on the same owned + halo particles, on two calls in a row,
 with the FP64 tolerance of the other parity tests: forces within 1e-12 of the largest force, Upot and virial
