@@ -44,6 +44,46 @@ struct DBuf {
   }
 };
 
+// Page-locked host memory for the rebuild's small read-backs and uploads.  A copy between the device and
+// pageable memory waits for the whole stream first; into page-locked memory it stays asynchronous, so the
+// rebuild's kernels queue behind the running steps and one synchronisation serves several read-backs.
+struct PinnedBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  // at least n bytes; the stream is drained before an old buffer is freed (copies may still use it)
+  bool ensure(size_t n, cudaStream_t st) {
+    if (n <= bytes && p) return true;
+    if (p) {
+      cudaStreamSynchronize(st);
+      cudaFreeHost(p);
+    }
+    p = nullptr;
+    bytes = 0;
+    if (cudaHostAlloc(&p, std::max<size_t>(n, 64), cudaHostAllocDefault) != cudaSuccess) {
+      p = nullptr;
+      return false;
+    }
+    bytes = std::max<size_t>(n, 64);
+    return true;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+// the words the rebuild reads back, followed (in the same buffer) by the per-system cluster ranges
+struct RebuildWords {
+  int32_t e_steps;     // device error flags raised by the position updates since the last rebuild
+  int32_t total_cl;    // clusters after binning
+  int32_t maxt;        // largest tower
+  int32_t list_err;    // error flags of the cluster-pair list build
+  int32_t plist_max;   // longest particle list
+  int32_t pad;
+  unsigned long long list_total;  // cluster pairs written
+};
+
 struct ParticleArrays {
   DBuf<double> x, y, z, vx, vy, vz, fx, fy, fz, ofx, ofy, ofz;
   DBuf<int32_t> type, sys, orig;
@@ -104,6 +144,8 @@ struct pe_engine {
   int pos_parity = 0;
   cudaGraphExec_t fused_graph[2] = {nullptr, nullptr};
   bool fused_graph_valid[2] = {false, false};
+  PinnedBuf hwords;   // RebuildWords + 2 int64 per system
+  PinnedBuf hchunks;  // the reduction-chunk tables uploaded at each rebuild
   double fused_graph_dt = 0;
   int fused_graph_launches = 0;
   DBuf<int32_t> slot_of;
@@ -798,10 +840,13 @@ static int build_particle_lists(pe_engine *h) {
     DeviceState s = h->state();
     launch_plist_build(s, st);
     h->launches += 1;
-    int mx = 0;
-    PE_CUDA(h, cudaMemcpyAsync(&mx, h->pl_max.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (!h->hwords.ensure(sizeof(RebuildWords) + sizeof(int64_t) * 2 * h->sys.size(), st))
+      return h->fail(PE_ERR_OOM, "page-locked rebuild words");
+    RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
+    PE_CUDA(h, cudaMemcpyAsync(&w->plist_max, h->pl_max.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     PE_CUDA(h, cudaStreamSynchronize(st));
     PE_TRY(h->cuda_check("particle list build"));
+    const int mx = w->plist_max;
     if (mx <= h->pl_cap) {
       h->pl_entries = 0;
       if (h->cfg.prune_buffer > 0 && h->traversal == 1) {
@@ -833,8 +878,11 @@ static int do_rebuild(pe_engine *h) {
   DeviceState s = h->state();
   const int64_t nold = h->nslots;
   h->launches += 1;
-  int e_steps = 0;  // errors flagged by the position updates since the last rebuild
-  PE_CUDA(h, cudaMemcpyAsync(&e_steps, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  const int ns_sys = (int)h->sys.size();
+  if (!h->hwords.ensure(sizeof(RebuildWords) + sizeof(int64_t) * 2 * (size_t)ns_sys, st))
+    return h->fail(PE_ERR_OOM, "page-locked rebuild words");
+  RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
+  PE_CUDA(h, cudaMemcpyAsync(&w->e_steps, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (nold > 0) k_wrap<<<(unsigned)((nold + 255) / 256), 256, 0, st>>>(s, nold);
   PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
   launch_bin(s, nold, h->key.p, h->tower_of.p, st);
@@ -844,12 +892,14 @@ static int do_rebuild(pe_engine *h) {
   PE_CUDA(h, cudaMemsetAsync(h->dmax.p, 0, sizeof(int), st));
   if (h->ntowers > 0) k_max_i32<<<64, 256, 0, st>>>(h->tw_count.p, h->ntowers, h->dmax.p);
   h->launches += 10;
-  int32_t total_cl = 0;
-  int maxt = 0;
-  PE_CUDA(h, cudaMemcpyAsync(&total_cl, h->tw_cl_start.p + h->ntowers, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  PE_CUDA(h, cudaMemcpyAsync(&maxt, h->dmax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PE_CUDA(h, cudaMemcpyAsync(&w->total_cl, h->tw_cl_start.p + h->ntowers, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             st));
+  PE_CUDA(h, cudaMemcpyAsync(&w->maxt, h->dmax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   PE_CUDA(h, cudaStreamSynchronize(st));
   PE_TRY(h->cuda_check("binning"));
+  const int e_steps = w->e_steps;
+  const int32_t total_cl = w->total_cl;
+  const int maxt = w->maxt;
   if (e_steps & kErrEncode)
     return h->fail(PE_ERR_DOMAIN, "a particle moved beyond the encodable range of its system between rebuilds");
   if (maxt > kTowerSortMax)
@@ -886,12 +936,13 @@ static int do_rebuild(pe_engine *h) {
     if (attempt > 0) PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
     launch_list_build(s, h->list_buf, st);
     h->launches += 1;
-    int e = 0;
-    unsigned long long tot = 0;
-    PE_CUDA(h, cudaMemcpyAsync(&e, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    PE_CUDA(h, cudaMemcpyAsync(&tot, h->cp_total.p, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaMemcpyAsync(&w->list_err, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaMemcpyAsync(&w->list_total, h->cp_total.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               st));
     PE_CUDA(h, cudaStreamSynchronize(st));
     PE_TRY(h->cuda_check("list build"));
+    const int e = w->list_err;
+    const unsigned long long tot = w->list_total;
     if (e & kErrTowerOverflow) return h->fail(PE_ERR_TOWER_OVERFLOW, "tower overflow in sort");
     if (e & kErrEncode)
       return h->fail(PE_ERR_DOMAIN, "a particle lies beyond the encodable range of its system (more than "
@@ -921,8 +972,9 @@ static int do_rebuild(pe_engine *h) {
   h->launches += 1;
   {
     // reduction chunks for the per-system globals
-    std::vector<int64_t> rng(2 * ns);
-    PE_CUDA(h, cudaMemcpyAsync(rng.data(), h->sys_cl_range.p, sizeof(int64_t) * 2 * ns, cudaMemcpyDeviceToHost, st));
+    const int64_t *rng = reinterpret_cast<const int64_t *>(static_cast<char *>(h->hwords.p) + sizeof(RebuildWords));
+    PE_CUDA(h, cudaMemcpyAsync(const_cast<int64_t *>(rng), h->sys_cl_range.p, sizeof(int64_t) * 2 * ns,
+                               cudaMemcpyDeviceToHost, st));
     PE_CUDA(h, cudaStreamSynchronize(st));
     std::vector<int64_t> ch;
     std::vector<int32_t> c0(ns + 1);
@@ -940,10 +992,15 @@ static int do_rebuild(pe_engine *h) {
     if (!h->chunks.ensure(std::max<size_t>(ch.size(), 3)) || !h->sys_chunk0.ensure(ns + 1) ||
         !h->chunk_part.ensure((kGlob + 1) * (size_t)std::max(k, 1)))
       return h->fail(PE_ERR_OOM, "reduction chunks");
-    if (!ch.empty())
-      PE_CUDA(h, cudaMemcpyAsync(h->chunks.p, ch.data(), sizeof(int64_t) * ch.size(), cudaMemcpyHostToDevice, st));
-    PE_CUDA(h, cudaMemcpyAsync(h->sys_chunk0.p, c0.data(), sizeof(int32_t) * (ns + 1), cudaMemcpyHostToDevice, st));
-    PE_CUDA(h, cudaStreamSynchronize(st));
+    // uploaded from page-locked memory without waiting: the next rebuild writes that memory only after its
+    // first synchronisation, when these copies are long done
+    const size_t ch_bytes = sizeof(int64_t) * ch.size(), c0_bytes = sizeof(int32_t) * (ns + 1);
+    if (!h->hchunks.ensure(ch_bytes + c0_bytes, st)) return h->fail(PE_ERR_OOM, "page-locked reduction chunks");
+    char *up = static_cast<char *>(h->hchunks.p);
+    std::memcpy(up, ch.data(), ch_bytes);
+    std::memcpy(up + ch_bytes, c0.data(), c0_bytes);
+    if (!ch.empty()) PE_CUDA(h, cudaMemcpyAsync(h->chunks.p, up, ch_bytes, cudaMemcpyHostToDevice, st));
+    PE_CUDA(h, cudaMemcpyAsync(h->sys_chunk0.p, up + ch_bytes, c0_bytes, cudaMemcpyHostToDevice, st));
   }
   PE_TRY(h->cuda_check("rebuild"));
   h->lists_valid = true;
@@ -1234,6 +1291,8 @@ int pe_destroy(pe_engine *h) {
   h->pq2.release();
   for (auto &g : h->fused_graph)
     if (g) cudaGraphExecDestroy(g);
+  h->hwords.release();
+  h->hchunks.release();
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})
@@ -1460,11 +1519,23 @@ static int step_forces(pe_engine *h, double dt, const VVFactors &vv, bool timed)
   return force_eval(h, true, dt, timed);
 }
 
-static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
-  if (h->step_graph) {
-    cudaGraphExecDestroy(h->step_graph);
-    h->step_graph = nullptr;
+// Makes gx execute the captured graph g: an existing executable graph is updated in place when g has its
+// topology (after a rebuild only launch sizes and kernel arguments differ), which costs far less than a new
+// instantiation; otherwise it is replaced.
+static cudaError_t install_graph(cudaGraphExec_t &gx, cudaGraph_t g) {
+  if (gx) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(gx, g, &info) == cudaSuccess) return cudaSuccess;
+    (void)cudaGetLastError();  // a refused update only means a new instantiation
+    cudaGraphExecDestroy(gx);
+    gx = nullptr;
   }
+  const cudaError_t e = cudaGraphInstantiate(&gx, g, 0);
+  if (e != cudaSuccess) gx = nullptr;
+  return e;
+}
+
+static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
   h->step_graph_valid = false;
   if (h->cfg.atm_nu > 0) PE_TRY(ensure_atm(h));
   const int64_t launches0 = h->launches;
@@ -1478,7 +1549,7 @@ static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
   const cudaError_t ce = cudaStreamEndCapture(h->st, &g);
   if (rc != PE_OK) return rc;
   if (ce != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-  const cudaError_t ie = cudaGraphInstantiate(&h->step_graph, g, 0);
+  const cudaError_t ie = install_graph(h->step_graph, g);
   cudaGraphDestroy(g);
   if (ie != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
   h->step_graph_launches = (int)(h->launches - launches0);
@@ -1493,10 +1564,6 @@ static int capture_step_graph(pe_engine *h, double dt, const VVFactors &vv) {
 // positions) and the globals reduction
 static int capture_fused_graph(pe_engine *h, double dt, int parity) {
   cudaGraphExec_t &gx = h->fused_graph[parity];
-  if (gx) {
-    cudaGraphExecDestroy(gx);
-    gx = nullptr;
-  }
   h->fused_graph_valid[parity] = false;
   const int64_t launches0 = h->launches;
   const int steps0 = h->steps_since_rebuild;
@@ -1506,7 +1573,7 @@ static int capture_fused_graph(pe_engine *h, double dt, int parity) {
   const cudaError_t ce = cudaStreamEndCapture(h->st, &g);
   if (rc != PE_OK) return rc;
   if (ce != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-  const cudaError_t ie = cudaGraphInstantiate(&gx, g, 0);
+  const cudaError_t ie = install_graph(gx, g);
   cudaGraphDestroy(g);
   if (ie != cudaSuccess) return h->fail(PE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
   h->fused_graph_launches = (int)(h->launches - launches0);
