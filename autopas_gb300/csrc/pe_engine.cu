@@ -73,7 +73,7 @@ struct PinnedBuf {
   }
 };
 
-// the words the rebuild reads back, followed (in the same buffer) by the per-system cluster ranges
+// the words the rebuild reads back
 struct RebuildWords {
   int32_t e_steps;     // device error flags raised by the position updates since the last rebuild
   int32_t total_cl;    // clusters after binning
@@ -144,8 +144,7 @@ struct pe_engine {
   int pos_parity = 0;
   cudaGraphExec_t fused_graph[2] = {nullptr, nullptr};
   bool fused_graph_valid[2] = {false, false};
-  PinnedBuf hwords;   // RebuildWords + 2 int64 per system
-  PinnedBuf hchunks;  // the reduction-chunk tables uploaded at each rebuild
+  PinnedBuf hwords;  // RebuildWords
   double fused_graph_dt = 0;
   int fused_graph_launches = 0;
   DBuf<int32_t> slot_of;
@@ -176,7 +175,7 @@ struct pe_engine {
   DBuf<int64_t> chunks;        // (system, first cluster, end cluster) per reduction chunk
   DBuf<int32_t> sys_chunk0;    // first chunk of each system, [nsys+1]
   DBuf<double> chunk_part;     // [nchunks*5]
-  int nchunks = 0;
+  int nchunks = 0;  // a bound on the reduction chunks (their count is sys_chunk0[nsys] on the device)
   DBuf<int32_t> sys_tower_base;
   int64_t max_tower = 0;
   int64_t num_cluster_pairs = 0;
@@ -518,6 +517,64 @@ __global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int3
   range[2 * sy + 1] = tw_cl_start[tower_base[sy + 1]];
 }
 
+// The chunk table of the per-system globals reduction, built on the device from the systems' cluster ranges:
+// system q's clusters [range[2q], range[2q+1]) are cut into chunks of kChunk clusters, chunk k of all systems
+// being (system, first cluster, end cluster); sys_chunk0[q] is system q's first chunk and sys_chunk0[nsys] the
+// number of chunks.  One block of 1024 threads, a thread per system, systems in tiles of 1024 carried over by a
+// running offset.  The host sizes the table for max_chunks = clusters / kChunk + nsys + 1, a bound on the count
+// (each system adds at most one partial chunk); entries beyond it are not written.
+__global__ void __launch_bounds__(1024) k_chunk_table(const int64_t *__restrict__ range, int nsys,
+                                                      int64_t *__restrict__ chunks, int32_t *__restrict__ sys_chunk0,
+                                                      int max_chunks) {
+  __shared__ int32_t wsum[32];
+  __shared__ int32_t base;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  for (int t0 = 0; t0 < nsys; t0 += blockDim.x) {
+    const int q = t0 + threadIdx.x;
+    int64_t a = 0, b = 0;
+    int cnt = 0;
+    if (q < nsys) {
+      a = range[2 * q];
+      b = range[2 * q + 1];
+      cnt = (int)((b - a + kChunk - 1) / kChunk);
+    }
+    int x = cnt;  // inclusive scan within the warp, then over the warps
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      const int nw = blockDim.x >> 5;
+      int v = lane < nw ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+      }
+      if (lane < nw) wsum[lane] = v;
+    }
+    __syncthreads();
+    const int first = base + (wid > 0 ? wsum[wid - 1] : 0) + x - cnt;
+    if (q < nsys) {
+      sys_chunk0[q] = first;
+      for (int c = 0; c < cnt; ++c) {
+        const int k = first + c;
+        if (k >= max_chunks) break;
+        chunks[3 * k] = q;
+        chunks[3 * k + 1] = a + (int64_t)c * kChunk;
+        chunks[3 * k + 2] = min(a + (int64_t)(c + 1) * kChunk, b);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) base = first + cnt;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sys_chunk0[nsys] = base;
+}
+
 // velocity-Verlet position half (TimeDiscretization.cpp:17-66 with globalForce 0) fused with the re-encode
 __global__ void k_positions(DeviceState s, double dt, VVFactors vv) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -840,7 +897,7 @@ static int build_particle_lists(pe_engine *h) {
     DeviceState s = h->state();
     launch_plist_build(s, st);
     h->launches += 1;
-    if (!h->hwords.ensure(sizeof(RebuildWords) + sizeof(int64_t) * 2 * h->sys.size(), st))
+    if (!h->hwords.ensure(sizeof(RebuildWords), st))
       return h->fail(PE_ERR_OOM, "page-locked rebuild words");
     RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
     PE_CUDA(h, cudaMemcpyAsync(&w->plist_max, h->pl_max.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -878,8 +935,7 @@ static int do_rebuild(pe_engine *h) {
   DeviceState s = h->state();
   const int64_t nold = h->nslots;
   h->launches += 1;
-  const int ns_sys = (int)h->sys.size();
-  if (!h->hwords.ensure(sizeof(RebuildWords) + sizeof(int64_t) * 2 * (size_t)ns_sys, st))
+  if (!h->hwords.ensure(sizeof(RebuildWords), st))
     return h->fail(PE_ERR_OOM, "page-locked rebuild words");
   RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
   PE_CUDA(h, cudaMemcpyAsync(&w->e_steps, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -971,36 +1027,15 @@ static int do_rebuild(pe_engine *h) {
   k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
   h->launches += 1;
   {
-    // reduction chunks for the per-system globals
-    const int64_t *rng = reinterpret_cast<const int64_t *>(static_cast<char *>(h->hwords.p) + sizeof(RebuildWords));
-    PE_CUDA(h, cudaMemcpyAsync(const_cast<int64_t *>(rng), h->sys_cl_range.p, sizeof(int64_t) * 2 * ns,
-                               cudaMemcpyDeviceToHost, st));
-    PE_CUDA(h, cudaStreamSynchronize(st));
-    std::vector<int64_t> ch;
-    std::vector<int32_t> c0(ns + 1);
-    int k = 0;
-    for (int q = 0; q < ns; ++q) {
-      c0[q] = k;
-      for (int64_t a = rng[2 * q]; a < rng[2 * q + 1]; a += kChunk, ++k) {
-        ch.push_back(q);
-        ch.push_back(a);
-        ch.push_back(std::min<int64_t>(a + kChunk, rng[2 * q + 1]));
-      }
-    }
-    c0[ns] = k;
-    h->nchunks = k;
-    if (!h->chunks.ensure(std::max<size_t>(ch.size(), 3)) || !h->sys_chunk0.ensure(ns + 1) ||
-        !h->chunk_part.ensure((kGlob + 1) * (size_t)std::max(k, 1)))
+    // reduction chunks for the per-system globals, built on the device (no read-back): the table is sized for
+    // a bound on the chunk count, and the reduction reads the count itself from sys_chunk0[ns]
+    const int max_chunks = total_cl / kChunk + ns + 1;
+    h->nchunks = max_chunks;
+    if (!h->chunks.ensure(3 * (size_t)max_chunks) || !h->sys_chunk0.ensure(ns + 1) ||
+        !h->chunk_part.ensure((kGlob + 1) * (size_t)max_chunks))
       return h->fail(PE_ERR_OOM, "reduction chunks");
-    // uploaded from page-locked memory without waiting: the next rebuild writes that memory only after its
-    // first synchronisation, when these copies are long done
-    const size_t ch_bytes = sizeof(int64_t) * ch.size(), c0_bytes = sizeof(int32_t) * (ns + 1);
-    if (!h->hchunks.ensure(ch_bytes + c0_bytes, st)) return h->fail(PE_ERR_OOM, "page-locked reduction chunks");
-    char *up = static_cast<char *>(h->hchunks.p);
-    std::memcpy(up, ch.data(), ch_bytes);
-    std::memcpy(up + ch_bytes, c0.data(), c0_bytes);
-    if (!ch.empty()) PE_CUDA(h, cudaMemcpyAsync(h->chunks.p, up, ch_bytes, cudaMemcpyHostToDevice, st));
-    PE_CUDA(h, cudaMemcpyAsync(h->sys_chunk0.p, up + ch_bytes, c0_bytes, cudaMemcpyHostToDevice, st));
+    k_chunk_table<<<1, 1024, 0, st>>>(h->sys_cl_range.p, ns, h->chunks.p, h->sys_chunk0.p, max_chunks);
+    h->launches += 1;
   }
   PE_TRY(h->cuda_check("rebuild"));
   h->lists_valid = true;
@@ -1292,7 +1327,6 @@ int pe_destroy(pe_engine *h) {
   for (auto &g : h->fused_graph)
     if (g) cudaGraphExecDestroy(g);
   h->hwords.release();
-  h->hchunks.release();
   for (auto *b : {&h->slot_of, &h->tw_count, &h->tw_start, &h->tw_cl_start, &h->tw_ncl, &h->tw_fill, &h->cl_sys,
                   &h->cl_tower, &h->cl_flags, &h->cp_count, &h->tower_of, &h->sval, &h->perm_src, &h->sys_tower_base,
                   &h->dump_c})

@@ -941,11 +941,13 @@ __device__ __forceinline__ void warp_sum6(double (&g)[kGlob], long long &h) {
   }
 }
 
-// one warp per chunk of at most kChunk = 256 clusters: lane l sums clusters c0 + l + 32 m
+// one warp per chunk of at most kChunk = 256 clusters: lane l sums clusters c0 + l + 32 m.  The grid covers a
+// bound on the chunk count; the count itself is sys_chunk0[nsys], written by the rebuild on the device.
 __global__ void __launch_bounds__(kRedWarps * 32)
-    k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, int nchunks, double *__restrict__ cpart) {
+    k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, const int32_t *__restrict__ sys_chunk0,
+                    double *__restrict__ cpart) {
   const int k = blockIdx.x * kRedWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (k >= nchunks) return;  // a whole warp
+  if (k >= sys_chunk0[s.nsys]) return;  // a whole warp
   const int64_t c0 = chunks[3 * k + 1], c1 = chunks[3 * k + 2];
   double g[kGlob] = {0, 0, 0, 0, 0};
   long long h = 0;
@@ -1008,10 +1010,11 @@ __global__ void __launch_bounds__(kRedWarps * 32)
   atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)pairs);
 }
 
-void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int nchunks, const int32_t *sys_chunk0,
+void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int max_chunks, const int32_t *sys_chunk0,
                            double *cpart, cudaStream_t st) {
-  if (nchunks > 0)
-    k_reduce_chunks<<<(nchunks + kRedWarps - 1) / kRedWarps, kRedWarps * 32, 0, st>>>(s, chunks, nchunks, cpart);
+  if (max_chunks > 0)
+    k_reduce_chunks<<<(max_chunks + kRedWarps - 1) / kRedWarps, kRedWarps * 32, 0, st>>>(s, chunks, sys_chunk0,
+                                                                                        cpart);
   if (s.nsys > 0) k_reduce_systems<<<s.nsys, kRedWarps * 32, 0, st>>>(s, sys_chunk0, cpart);
 }
 
