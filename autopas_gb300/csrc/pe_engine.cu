@@ -981,7 +981,10 @@ static int do_rebuild(pe_engine *h) {
   if (nnew > 0) k_pack<<<(unsigned)((nnew + 255) / 256), 256, 0, st>>>(s, nnew);
   launch_cluster_bbox(s, st);
   h->launches += 5;
-  // cluster-pair lists (grow the buffer and retry when it is too small)
+  // cluster-pair lists (grow the buffer and retry when it is too small), then the particle lists.  The list
+  // build's flags are read at the particle-list build's synchronisation: a cluster-pair list that overflowed is
+  // left empty (count 0), so the particle-list build still reads only valid entries, and both are redone.
+  bool listed = false;
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (h->cp_list.cap == 0) {
       const int64_t est = std::max<int64_t>(h->nclusters * (h->newton3 ? 48 : 96), 1024);
@@ -995,6 +998,7 @@ static int do_rebuild(pe_engine *h) {
     PE_CUDA(h, cudaMemcpyAsync(&w->list_err, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     PE_CUDA(h, cudaMemcpyAsync(&w->list_total, h->cp_total.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                st));
+    const int prc = (h->traversal == 1 || h->need_plist) ? build_particle_lists(h) : PE_OK;
     PE_CUDA(h, cudaStreamSynchronize(st));
     PE_TRY(h->cuda_check("list build"));
     const int e = w->list_err;
@@ -1016,13 +1020,12 @@ static int do_rebuild(pe_engine *h) {
       if (!h->cp_list.ensure(want)) return h->fail(PE_ERR_OOM, "cluster-pair list (%zu)", want);
       continue;
     }
+    if (prc != PE_OK) return prc;
     h->num_cluster_pairs = (int64_t)tot;
-    if (h->num_cluster_pairs * 2 + 1024 < (int64_t)h->cp_list.cap / 4) {
-      // keep the buffer within 4x of need
-    }
+    listed = true;
     break;
   }
-  if (h->traversal == 1 || h->need_plist) PE_TRY(build_particle_lists(h));
+  if (!listed) return h->fail(PE_ERR_LIST_OVERFLOW, "cluster-pair lists kept overflowing");
   const int ns = (int)h->sys.size();
   k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
   h->launches += 1;
