@@ -245,6 +245,36 @@ def test_ensemble_systems_are_independent(eng_mod, orc, traversal):
                 assert gs[k]["upot"] == pytest.approx(glob[0], rel=1e-6)
 
 
+def test_more_systems_than_one_block_of_the_chunk_table(eng_mod, orc):
+    """1,100 small systems in one engine: the globals reduction's chunk table is built on the device by one
+    block of 1,024 threads, a thread per system, so these systems span two tiles of it.  Each system's Upot and
+    virial (FP64 form) must be its own oracle's within 1e-12 of the sum of the magnitudes of their terms (in
+    some of these systems attraction and repulsion cancel to 1e-4 of that sum).  With a = sum of
+    eps24 (sigma^2/r^2)^6 and b = sum of eps24 (sigma^2/r^2)^3, Upot = (a - b)/6 and virial = 2a - b; a second
+    oracle run with sigma^2 scaled by 2^(1/3) gives Upot' = (4a - 2b)/6, hence a and b."""
+    from autopas_gb300 import workloads
+    systems = workloads.ensemble(1100, nmin=300, nmax=700, seed=5)
+    rc, skin = 2.5, 0.3
+    boxes = [(s["bmin"], s["bmax"]) for s in systems]
+    pos = np.concatenate([s["pos"] for s in systems])
+    sysid = np.concatenate([np.full(len(s["pos"]), k, np.int32) for k, s in enumerate(systems)])
+    e = eng_mod.PairEngine(rc, skin, boxes, periodic=True, precision=eng_mod.PRECISION_FP64, cluster_size=8,
+                           traversal=1)
+    e.set_particles(pos, system=sysid)
+    gs = e.compute_forces()
+    e.close()
+    assert len(gs) == len(systems)
+    lj, lj2 = orc.LJ(rc), orc.LJ.single(rc, 24.0, 2.0 ** (1.0 / 3.0))
+    for k, s in enumerate(systems):
+        allpos, own, allt, _, _ = orc.periodic_system(s["pos"], s["bmin"], s["bmax"], rc, skin)
+        _, glob, _ = orc.cpu_lc_c08(allpos, lj, skin, own=own, types=allt)
+        _, glob2, _ = orc.cpu_lc_c08(allpos, lj2, skin, own=own, types=allt)
+        a = 3.0 * glob2[0] - 6.0 * glob[0]
+        b = a - 6.0 * glob[0]
+        assert abs(gs[k]["upot"] - glob[0]) <= 1e-12 * max(abs(glob[0]), (a + b) / 6.0), k
+        assert abs(gs[k]["virial"] - glob[1]) <= 1e-12 * max(abs(glob[1]), 2.0 * a + b), k
+
+
 def test_long_cutoff_grows_the_list_buffer(eng_mod, orc):
     """rc 6, skin 1, C = 4 at density 0.9: a cluster has more candidate cluster pairs than the list build's
     first on-chip buffer holds; the build grows the buffer and the forces stay the oracle's."""
