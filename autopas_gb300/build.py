@@ -20,6 +20,9 @@ LIB = os.path.join(LIBDIR, "libpairengine.so")
 
 SOURCES = ["pe_engine.cu", "pe_build.cu", "pe_force.cu", "pe_noalloc.cu", "pe_atm.cu", "pe_inputs.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# the input generator is compiled without FMA contraction, as the oracle library compiles the same file, so that
+# both give the same positions for the same seed on any host
+EXTRA = {"pe_inputs.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
 
@@ -51,7 +54,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
         o = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _newer(o, [s] + headers):
-            cmd = [nv, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o]
+            cmd = [nv, *ARCH, *NVCC_FLAGS, *EXTRA.get(src, []), "-c", s, "-o", o]
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

@@ -40,7 +40,7 @@ __device__ __forceinline__ double img_dist2(const DeviceState &s, const SysDev &
   const double dx = image_coord(s.x[b], bx, S.len[0]) - image_coord(s.x[a], ax, S.len[0]);
   const double dy = image_coord(s.y[b], by, S.len[1]) - image_coord(s.y[a], ay, S.len[1]);
   const double dz = image_coord(s.z[b], bz, S.len[2]) - image_coord(s.z[a], az, S.len[2]);
-  return dist2_mode(dx, dy, dz, 0);
+  return dist2_mode(dx, dy, dz, kDistStrict);
 }
 
 __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs aa, double *__restrict__ slot_glob,

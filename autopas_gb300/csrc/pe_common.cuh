@@ -194,11 +194,15 @@ __host__ __device__ inline void shift_of(int code, int &sx, int &sy, int &sz) {
   sz = code / 9 - 1;
 }
 
+// Distance expressions (PE_DIST_* of pairengine.h): the reference's SoA loops as GCC contracts them, the
+// uncontracted source expression, and the contracted ArrayMath::dot.
+constexpr int kDistFmaSoa = 0, kDistStrict = 1, kDistFmaDot = 2;
+
 // FP64 squared distance with the selected contraction.  The explicit __dmul_rn/__dadd_rn/__fma_rn
 // intrinsics keep nvcc from fusing or reordering, so the bits equal those of the host expression.
 __device__ __forceinline__ double dist2_mode(double dx, double dy, double dz, int mode) {
-  if (mode == 1) return __fma_rn(dz, dz, __fma_rn(dx, dx, __dmul_rn(dy, dy)));
-  if (mode == 2) return __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+  if (mode == kDistFmaSoa) return __fma_rn(dz, dz, __fma_rn(dx, dx, __dmul_rn(dy, dy)));
+  if (mode == kDistFmaDot) return __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 

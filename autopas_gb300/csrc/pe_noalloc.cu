@@ -50,10 +50,23 @@ __global__ void __launch_bounds__(kThreads) k_direct_forces(LJTable tab, int n, 
   __shared__ double sx[kThreads], sy[kThreads], sz[kThreads];
   __shared__ int st[kThreads], so[kThreads];
   __shared__ double red[kPartials][kThreads];
+  __shared__ int bad_type;
+  if (threadIdx.x == 0) bad_type = 0;
+  // OwnershipState: only owned (1) and halo (2) particles take part; any other value counts as a dummy
+  auto real_state = [](int o) { return (o == PE_OWNED || o == PE_HALO) ? o : PE_DUMMY; };
+  // a type outside [0, ntypes) would index past the mixing table: it is clamped and the block reports it
+  auto checked_type = [&](int t) {
+    if (t < 0 || t >= tab.ntypes) {
+      bad_type = 1;
+      return 0;
+    }
+    return t;
+  };
+  __syncthreads();
   const int i = blockIdx.x * kThreads + threadIdx.x;
   const bool live = i < n;
-  const int oi = live ? (own ? own[i] : PE_OWNED) : PE_DUMMY;
-  const int ti = live && type ? type[i] : 0;
+  const int oi = live ? (own ? real_state(own[i]) : PE_OWNED) : PE_DUMMY;
+  const int ti = (live && type && oi != PE_DUMMY) ? checked_type(type[i]) : 0;
   const double xi = live ? x[i] : 0.0, yi = live ? y[i] : 0.0, zi = live ? z[i] : 0.0;
   double f0 = 0, f1 = 0, f2 = 0, pot = 0, v0 = 0, v1 = 0, v2 = 0, hits = 0;
   for (int base = 0; base < n; base += kThreads) {
@@ -63,8 +76,9 @@ __global__ void __launch_bounds__(kThreads) k_direct_forces(LJTable tab, int n, 
       sx[threadIdx.x] = x[j];
       sy[threadIdx.x] = y[j];
       sz[threadIdx.x] = z[j];
-      st[threadIdx.x] = type ? type[j] : 0;
-      so[threadIdx.x] = own ? own[j] : PE_OWNED;
+      const int oj = own ? real_state(own[j]) : PE_OWNED;
+      so[threadIdx.x] = oj;
+      st[threadIdx.x] = (type && oj != PE_DUMMY) ? checked_type(type[j]) : 0;
     } else {
       so[threadIdx.x] = PE_DUMMY;
     }
@@ -111,7 +125,8 @@ __global__ void __launch_bounds__(kThreads) k_direct_forces(LJTable tab, int n, 
       for (int c = 0; c < kPartials; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x < kPartials) scratch[blockIdx.x * kPartials + threadIdx.x] = red[threadIdx.x][0];
+  // a block that met an invalid type makes every global of the call NaN
+  if (threadIdx.x < kPartials) scratch[blockIdx.x * kPartials + threadIdx.x] = bad_type ? nan("") : red[threadIdx.x][0];
 }
 
 // Adds the block rows of this call in block order and applies the endTraversal post-processing.
@@ -180,9 +195,25 @@ extern "C" int pe_lj_forces_noalloc(const pe_config *cfg, int64_t n, const doubl
       tab.shift6[k] = sh;
     }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int nblocks = (int)((n + kThreads - 1) / kThreads);
-  if (nblocks > 0)
-    k_direct_forces<<<nblocks, kThreads, 0, st>>>(tab, (int)n, x, y, z, type, ownership, fx, fy, fz, scratch);
-  k_direct_globals<<<1, 32, 0, st>>>(nblocks, scratch, globals);
-  return cudaGetLastError() == cudaSuccess ? PE_OK : PE_ERR_CUDA;
+  // the scratch address belongs to the current device, so the stream must too (the legacy and per-thread
+  // default streams always do)
+  if (st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread) {
+    int sdev = -1, cur = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess || cudaGetDevice(&cur) != cudaSuccess) return PE_ERR_ARG;
+    if (sdev != cur) return PE_ERR_ARG;
+  }
+  // Each launch's own status: cudaLaunchKernel reports this launch's error rather than a pending error that
+  // earlier, unrelated work left behind (a context that has faulted still fails every call).
+  int nblocks = (int)((n + kThreads - 1) / kThreads);
+  int ni = (int)n;
+  if (nblocks > 0) {
+    void *args[] = {&tab, &ni, (void *)&x, (void *)&y, (void *)&z, (void *)&type, (void *)&ownership,
+                    (void *)&fx, (void *)&fy, (void *)&fz, &scratch};
+    if (cudaLaunchKernel((const void *)k_direct_forces, dim3(nblocks), dim3(kThreads), args, 0, st) != cudaSuccess)
+      return PE_ERR_CUDA;
+  }
+  void *gargs[] = {&nblocks, &scratch, (void *)&globals};
+  if (cudaLaunchKernel((const void *)k_direct_globals, dim3(1), dim3(32), gargs, 0, st) != cudaSuccess)
+    return PE_ERR_CUDA;
+  return PE_OK;
 }

@@ -20,7 +20,7 @@ ERRORS = {
 }
 NOALLOC_MAX_PARTICLES = 16384
 PRECISION_FP64, PRECISION_MIXED = 0, 1
-DIST_STRICT, DIST_FMA_SOA, DIST_FMA_DOT = 0, 1, 2
+DIST_FMA_SOA, DIST_STRICT, DIST_FMA_DOT = 0, 1, 2
 DUMMY, OWNED, HALO = 0, 1, 2
 
 # every symbol include/pairengine.h declares
@@ -128,7 +128,7 @@ class PairEngine:
     """One engine instance (one CUDA stream) holding one or more particle systems."""
 
     def __init__(self, cutoff, skin, boxes, periodic=True, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,),
-                 shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_STRICT,
+                 shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_FMA_SOA,
                  rebuild_frequency=10, calc_globals=True, tower_sizing=1, traversal=1, atm_nu=0.0, atm_cutoff=0.0,
                  use_graphs=True, prune_buffer=0.0, kernel_variant=0):
         L = load()
@@ -296,7 +296,7 @@ class PairEngine:
         return ms.value
 
 
-def make_config(cutoff, skin=0.0, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,), shift=False, dist_mode=DIST_STRICT):
+def make_config(cutoff, skin=0.0, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,), shift=False, dist_mode=DIST_FMA_SOA):
     """A PeConfig for calls that take one without an engine (pe_lj_forces_noalloc).  Returns (cfg, keepalive)."""
     eps = np.ascontiguousarray(epsilon, np.float64)
     sig = np.ascontiguousarray(sigma, np.float64)

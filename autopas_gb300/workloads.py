@@ -67,8 +67,10 @@ def rsa(n, bmin, bmax, rmin, rmax, dmin, seed, existing=None):
     return pos
 
 
-def slab(n_total=2_000_000, rho_liq=0.75, rho_vap=0.02, dmin=0.8, T=0.8, seed=7):
-    """Vapour-liquid slab in a 3:1:1 box (x long), liquid in the middle third.  Returns (pos, vel, bmin, bmax)."""
+def slab(n_total=2_000_000, rho_liq=0.75, rho_vap=0.02, dmin=0.8, T=0.8, seed=7, rsa_fn=None):
+    """Vapour-liquid slab in a 3:1:1 box (x long), liquid in the middle third.  Returns (pos, vel, bmin, bmax).
+    rsa_fn: the random-sequential-addition routine (signature of `rsa`); the engine library's by default."""
+    rsa_fn = rsa if rsa_fn is None else rsa_fn
     # n_total = rho_liq * V/3 + rho_vap * 2V/3 with V = 3 l^3
     V = n_total / (rho_liq / 3.0 + 2.0 * rho_vap / 3.0)
     ell = (V / 3.0) ** (1.0 / 3.0)
@@ -76,8 +78,8 @@ def slab(n_total=2_000_000, rho_liq=0.75, rho_vap=0.02, dmin=0.8, T=0.8, seed=7)
     bmax = np.array([3 * ell, ell, ell])
     n_liq = int(round(rho_liq * V / 3.0))
     n_vap = n_total - n_liq
-    liq = rsa(n_liq, bmin, bmax, [ell, 0, 0], [2 * ell, ell, ell], dmin, seed)
-    both = rsa(n_vap, bmin, bmax, bmin, bmax, dmin, seed + 1, existing=liq)
+    liq = rsa_fn(n_liq, bmin, bmax, [ell, 0, 0], [2 * ell, ell, ell], dmin, seed)
+    both = rsa_fn(n_vap, bmin, bmax, bmin, bmax, dmin, seed + 1, existing=liq)
     # vapour candidates may land in the slab region too; keep the count per region as drawn
     vel = mb_velocities(n_total, T, seed=seed + 2)
     return both, vel, bmin, bmax

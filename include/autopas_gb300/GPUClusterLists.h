@@ -199,7 +199,7 @@ class GPUClusterLists {
     cfg.precision = _precision;
     cfg.cluster_size = (int)_clusterSize;
     cfg.newton3 = 0;
-    cfg.dist_mode = PE_DIST_STRICT;
+    cfg.dist_mode = PE_DIST_FMA_SOA;
     cfg.rebuild_frequency = 1;
     cfg.tower_sizing = 1;
     cfg.traversal = toEngineTraversal(t);

@@ -47,9 +47,14 @@ extern "C" {
 #define PE_PRECISION_FP64 0   /* plain FP64 form: FP64 positions, FP64 LJ arithmetic, FP64 sums */
 #define PE_PRECISION_MIXED 1  /* FP64 state, FP32 LJ on hi/lo-split displacements, compensated FP32 sums */
 
-#define PE_DIST_STRICT 0   /* dr2 = (dx*dx + dy*dy) + dz*dz, every operation rounded (source semantics) */
-#define PE_DIST_FMA_SOA 1  /* dr2 = fma(dz,dz, fma(dx,dx, dy*dy)) (GCC -O3 -march=native contraction) */
-#define PE_DIST_FMA_DOT 2  /* dr2 = fma(dz,dz, fma(dy,dy, dx*dx)) (contracted ArrayMath::dot) */
+/* Distance expression of every FP64 distance test.  The reference writes dr2 = drx*drx + dry*dry + drz*drz
+ * (LJFunctor.h:287-293, 475-481; VerletListHelpers.h:104-110); the bits depend on the FMA contraction its
+ * compiler applies.  GCC with the reference's flags (-O3, FMA available: -march=native on x86-64, always on
+ * aarch64) contracts those SoA loops to fma(drz,drz, fma(drx,drx, dry*dry)), which is therefore the default
+ * (0, what a zero-initialised pe_config selects); oracle/contraction_probe.cpp pins it on each host. */
+#define PE_DIST_FMA_SOA 0  /* dr2 = fma(dz,dz, fma(dx,dx, dy*dy)): the reference's SoA loops as GCC builds them */
+#define PE_DIST_STRICT 1   /* dr2 = (dx*dx + dy*dy) + dz*dz, every operation rounded (no contraction) */
+#define PE_DIST_FMA_DOT 2  /* dr2 = fma(dz,dz, fma(dy,dy, dx*dx)): contracted ArrayMath::dot (AoSFunctor) */
 
 /* OwnershipState values (src/autopas/particles/OwnershipState.h:20-29) */
 #define PE_DUMMY 0
@@ -230,12 +235,17 @@ int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, i
  * sides, reference LJ arithmetic) and writes globals[0..5] = {Upot, virial, virial_x, virial_y, virial_z,
  * interacting pairs}.  All arrays are device memory owned by the caller (type and ownership may be NULL:
  * type 0, owned); cfg supplies cutoff, types, epsilon, sigma, apply_shift and dist_mode; stream is a
- * cudaStream_t (NULL: the default stream).  The call is asynchronous on that stream.
+ * cudaStream_t of the current device (NULL: the default stream; a stream of another device gives PE_ERR_ARG).
+ * The call is asynchronous on that stream.  Ownership values other than PE_OWNED and PE_HALO count as dummies
+ * (ignored).  Types must lie in [0, num_types): a particle with another type makes every global of the call
+ * NaN (its forces use type 0).
  * Limits: n <= PE_NOALLOC_MAX_PARTICLES, else PE_ERR_TOO_LARGE.  The only scratch is a fixed 5 KB array of
  * per-block partial sums in the library's device memory, shared by every call on a device and held by every
  * device that loads the library until the process exits; calls that overlap on the GPU race on it, so issue
  * them on one stream or wait for one before the next.  The first call on a device looks up that array's
- * device address (with the device current) and caches it: make that first call before any stream capture. */
+ * device address (with the device current) and caches it; under CUDA's lazy module loading that lookup also
+ * loads the library's device code and the array, which takes device memory once.  So make the first call on
+ * each device at set-up, before a memory pool takes the rest of the device and before any stream capture. */
 #define PE_NOALLOC_MAX_PARTICLES 16384
 int pe_lj_forces_noalloc(const pe_config *cfg, int64_t n, const double *x, const double *y, const double *z,
                          const int32_t *type, const int8_t *ownership, double *fx, double *fy, double *fz,

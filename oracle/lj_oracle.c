@@ -12,6 +12,7 @@
 double orc_dist2(double dx, double dy, double dz, int mode) {
   if (mode == ORC_DIST_FMA_SOA) return fma(dz, dz, fma(dx, dx, dy * dy));
   if (mode == ORC_DIST_FMA_DOT) return fma(dz, dz, fma(dy, dy, dx * dx));
+  /* ORC_DIST_STRICT */
   const double x2 = dx * dx;
   const double y2 = dy * dy;
   const double z2 = dz * dz;
@@ -272,6 +273,37 @@ int64_t orc_pair_set(int64_t n, const double *x, const double *y, const double *
 int64_t orc_interacting_set(int64_t n, const double *x, const double *y, const double *z, const int8_t *own,
                             double rc, int dist_mode, int64_t cap, int64_t *pa, int64_t *pb) {
   return pair_set_impl(n, x, y, z, own, rc, 0, dist_mode, cap, pa, pb);
+}
+
+/* ---- interacting-pair counts by ownership (the metric's pair count, without storing the pairs) ---- */
+typedef struct {
+  const double *x, *y, *z;
+  const int8_t *own;
+  double lim;
+  int dist_mode;
+  int64_t counts[3]; /* owned-owned, owned-halo, halo-halo */
+} count_ctx;
+
+static void count_cb(int64_t a, int64_t b, void *vctx) {
+  count_ctx *c = (count_ctx *)vctx;
+  const double d2 = orc_dist2(c->x[a] - c->x[b], c->y[a] - c->y[b], c->z[a] - c->z[b], c->dist_mode);
+  if (!(d2 <= c->lim)) return;
+  const int halos = (c->own[a] == ORC_HALO) + (c->own[b] == ORC_HALO);
+  c->counts[halos]++;
+}
+
+/* LJFunctor.h:149 / :300 mask dr2 <= cutoff^2, counted per ownership class: out[0] owned-owned, out[1]
+ * owned-halo, out[2] halo-halo pairs.  The unique physical pairs of a periodic system given as owned + halo
+ * images are out[0] + out[1]/2.  Returns 0, or -1 if the cell list could not be allocated. */
+int orc_count_interacting(int64_t n, const double *x, const double *y, const double *z, const int8_t *own,
+                          double rc, int dist_mode, int64_t *out) {
+  cell_list cl;
+  if (cl_build(&cl, n, x, y, z, own, rc) != 0) return -1;
+  count_ctx c = {x, y, z, own, rc * rc, dist_mode, {0, 0, 0}};
+  cl_for_pairs(&cl, count_cb, &c);
+  cl_free(&cl);
+  for (int k = 0; k < 3; ++k) out[k] = c.counts[k];
+  return 0;
 }
 
 /* ---- periodic halos (RegularGridDecomposition.cpp:159-236 and :486-531) ---- */

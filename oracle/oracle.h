@@ -32,9 +32,11 @@
  *
  * Distance expression: the reference computes dr2 = drx*drx + dry*dry + drz*drz.
  * Which FMA contraction a C++ compiler applies is not fixed by the source, so
- * the expression is a parameter (ORC_DIST_*); the default is the plain IEEE
- * evaluation ((dx*dx + dy*dy) + dz*dz) with every operation rounded.  This file
- * is compiled with -ffp-contract=off so that the C compiler cannot change it.
+ * the expression is a parameter (ORC_DIST_*).  The default (0) is the form GCC
+ * gives the reference's SoA loops with the reference's flags,
+ * fma(dz,dz, fma(dx,dx, dy*dy)); contraction_probe.cpp, compiled with those
+ * flags, shows which form the host compiler produces.  This file is compiled
+ * with -ffp-contract=off so that the C compiler cannot change any form.
  */
 #ifndef AUTOPAS_GB300_ORACLE_H
 #define AUTOPAS_GB300_ORACLE_H
@@ -46,8 +48,8 @@ extern "C" {
 #endif
 
 enum {
-  ORC_DIST_STRICT = 0,   /* (dx*dx + dy*dy) + dz*dz, every operation rounded */
-  ORC_DIST_FMA_SOA = 1,  /* fma(dz,dz, fma(dx,dx, dy*dy)): GCC -O3 -march=native contraction of the SoA loops */
+  ORC_DIST_FMA_SOA = 0,  /* fma(dz,dz, fma(dx,dx, dy*dy)): GCC -O3 -march=native contraction of the SoA loops */
+  ORC_DIST_STRICT = 1,   /* (dx*dx + dy*dy) + dz*dz, every operation rounded */
   ORC_DIST_FMA_DOT = 2   /* fma(dz,dz, fma(dy,dy, dx*dx)): contraction of ArrayMath::dot */
 };
 
@@ -64,6 +66,16 @@ typedef struct {
 } orc_lj_params;
 
 double orc_dist2(double dx, double dy, double dz, int mode);
+
+/* Interacting pairs (dr2 <= rc^2) of an owned + halo set counted per ownership class:
+ * out[0] owned-owned, out[1] owned-halo, out[2] halo-halo. */
+int orc_count_interacting(int64_t n, const double *x, const double *y, const double *z, const int8_t *own,
+                          double rc, int dist_mode, int64_t *out);
+
+/* Seeded random sequential addition (autopas_gb300/csrc/pe_inputs.cpp, compiled into this library from the
+ * same source with contraction off, so both libraries give the same positions for the same seed). */
+int64_t pe_gen_rsa(int64_t existing, int64_t n, const double *bmin, const double *bmax, const double *rmin,
+                   const double *rmax, double dmin, uint64_t seed, int64_t max_attempts, double *pos);
 
 /* ParticlePropertiesLibrary::calculateMixingCoefficients + calcShift6 */
 void orc_mixing(int ntypes, const double *epsilon, const double *sigma, double cutoff, int apply_shift,

@@ -17,7 +17,7 @@ _LIB_PATH = os.path.join(_HERE, "build", "liboracle.so")
 _lib = None
 
 ORC_DUMMY, ORC_OWNED, ORC_HALO = 0, 1, 2
-DIST_STRICT, DIST_FMA_SOA, DIST_FMA_DOT = 0, 1, 2
+DIST_FMA_SOA, DIST_STRICT, DIST_FMA_DOT = 0, 1, 2
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
@@ -40,6 +40,24 @@ def build() -> str:
     """Compile the oracle with its Makefile (gcc only)."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
+
+
+def contraction_probe():
+    """The reference's dr2 expression compiled with the reference's flags (contraction_probe.c):
+    f(xi, yi, zi, xj, yj, zj) -> dr2 over arrays."""
+    path = os.path.join(_HERE, "build", "libcontraction.so")
+    if not os.path.exists(path):
+        build()
+    L = C.CDLL(path)
+    L.probe_dist2.restype = None
+    L.probe_dist2.argtypes = [C.c_int64] + [_dp] * 7
+
+    def dist2(xi, yi, zi, xj, yj, zj):
+        a = [np.ascontiguousarray(v, np.float64) for v in (xi, yi, zi, xj, yj, zj)]
+        out = np.empty(len(a[0]))
+        L.probe_dist2(len(out), *a, out)
+        return out
+    return dist2
 
 
 def lib():
@@ -76,6 +94,10 @@ def lib():
                                   _dp, _dp, _dp]
         L.orc_atm_forces.restype = C.c_int64
         L.orc_atm_forces.argtypes = [C.c_int64, _dp, _dp, _dp, _i8p, C.c_double, C.c_double, _dp, _dp, _dp, _dp]
+        L.orc_count_interacting.restype = C.c_int
+        L.orc_count_interacting.argtypes = [C.c_int64, _dp, _dp, _dp, _i8p, C.c_double, C.c_int, _i64p]
+        L.pe_gen_rsa.restype = C.c_int64
+        L.pe_gen_rsa.argtypes = [C.c_int64, C.c_int64, _dp, _dp, _dp, _dp, C.c_double, C.c_uint64, C.c_int64, _dp]
         L.orc_cpu_lc_c08.restype = C.c_int64
         L.orc_cpu_lc_c08.argtypes = [C.c_int64, _dp, _dp, _dp, _i32p, _i8p, C.POINTER(LJParams), C.c_double,
                                      C.c_int, _dp, _dp, _dp, _dp]
@@ -86,7 +108,7 @@ def lib():
 class LJ:
     """Mixing table + parameters (ParticlePropertiesLibrary.h:444-473, LJFunctor constructor)."""
 
-    def __init__(self, cutoff, epsilon=(1.0,), sigma=(1.0,), shift=False, dist_mode=DIST_STRICT, table=None):
+    def __init__(self, cutoff, epsilon=(1.0,), sigma=(1.0,), shift=False, dist_mode=DIST_FMA_SOA, table=None):
         self.cutoff = float(cutoff)
         eps = np.ascontiguousarray(epsilon, dtype=np.float64)
         sig = np.ascontiguousarray(sigma, dtype=np.float64)
@@ -106,7 +128,7 @@ class LJ:
                           self.shift6.ctypes.data_as(C.POINTER(C.c_double)), int(dist_mode))
 
     @classmethod
-    def single(cls, cutoff, epsilon24, sigma_squared, shift=False, dist_mode=DIST_STRICT):
+    def single(cls, cutoff, epsilon24, sigma_squared, shift=False, dist_mode=DIST_FMA_SOA):
         """LJFunctor::setParticleProperties(epsilon24, sigmaSquared) (LJFunctor.h:583-590)."""
         c2 = cutoff * cutoff
         sh = 0.0
@@ -158,14 +180,40 @@ def _set(fn, pos, own, radius, dist_mode):
         cap = int(cnt)
 
 
-def pair_set(pos, L, own=None, dist_mode=DIST_STRICT):
+def pair_set(pos, L, own=None, dist_mode=DIST_FMA_SOA):
     """VerletListHelpers.h:64-123 rule: dr2 < L^2.  Returns (a, b) index arrays, a < b."""
     return _set(lib().orc_pair_set, pos, own, L, dist_mode)
 
 
-def interacting_set(pos, rc, own=None, dist_mode=DIST_STRICT):
+def interacting_set(pos, rc, own=None, dist_mode=DIST_FMA_SOA):
     """LJFunctor mask dr2 <= rc^2."""
     return _set(lib().orc_interacting_set, pos, own, rc, dist_mode)
+
+
+def count_interacting(pos, rc, own=None, dist_mode=DIST_FMA_SOA):
+    """Interacting pairs per ownership class: (owned-owned, owned-halo, halo-halo)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    n = len(pos)
+    own = np.full(n, ORC_OWNED, np.int8) if own is None else _c(own, np.int8)
+    x, y, z = (np.ascontiguousarray(pos[:, d]) for d in range(3))
+    out = np.zeros(3, np.int64)
+    if lib().orc_count_interacting(n, x, y, z, own, float(rc), int(dist_mode), out) != 0:
+        raise MemoryError("cell list")
+    return tuple(int(v) for v in out)
+
+
+def gen_rsa(n, bmin, bmax, rmin, rmax, dmin, seed, existing=None):
+    """The benchmark's random sequential addition (same source as the engine library's pe_gen_rsa)."""
+    m = 0 if existing is None else len(existing)
+    pos = np.zeros((m + n, 3))
+    if m:
+        pos[:m] = existing
+    arrs = [_c(v, np.float64) for v in (bmin, bmax, rmin, rmax)]
+    flat = pos.reshape(-1)
+    placed = lib().pe_gen_rsa(m, n, *arrs, float(dmin), int(seed), int(200 * n + 10000), flat)
+    if placed != n:
+        raise RuntimeError(f"random sequential addition placed {placed} of {n} particles")
+    return pos
 
 
 def make_halos(pos, bmin, bmax, cutoff, skin):

@@ -68,3 +68,15 @@ def test_rsa_generator_min_distance(lib):
     np.fill_diagonal(r2, 1e9)
     assert r2.min() >= 0.64 - 1e-12
     assert pos.min() >= 0 and pos.max() < 12
+
+
+def test_reference_arm_generates_the_same_slab_without_the_engine_library(lib, orc):
+    """The benchmark's reference arm builds its slab with the oracle library's copy of the generator (the same
+    source file, compiled the same way), so both arms time identical positions and the reference arm never
+    loads the engine library."""
+    import numpy as np
+    from autopas_gb300 import workloads
+    a = workloads.slab(n_total=6000, seed=7)
+    b = workloads.slab(n_total=6000, seed=7, rsa_fn=orc.gen_rsa)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

@@ -95,3 +95,35 @@ def test_large_sparse_box_pair_sets(eng_mod, orc, traversal):
     e.close()
     ia, ib = orc.interacting_set(allpos, rc, own=own)
     assert g["num_pairs"] == int(np.sum(ib < n)) + int(np.sum(ib >= n)) // 2
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_default_distance_form_is_the_references_contraction(eng_mod, orc, straddling_pairs, traversal):
+    """Pairs straddling (rc+skin)^2 and rc^2 by an ulp, where the uncontracted expression and the reference's
+    contracted one (fma(dz,dz, fma(dx,dx, dy*dy)), what GCC makes of LJFunctor.h:287-293 with the reference's
+    flags) disagree: an engine with the default options reproduces the contracted pair sets and interacting
+    count, bit for bit, in both precision forms."""
+    rc, skin = 2.5, 0.3
+    spacing = 3 * (rc + skin)
+    pos_l, _ = straddling_pairs(orc, rc + skin, 27, seed=3, spacing=spacing)
+    pos_c, _ = straddling_pairs(orc, rc, 27, seed=4, spacing=spacing)
+    pos_c = pos_c + np.array([3 * spacing + spacing, 0.0, 0.0])  # a second block of sites beside the first
+    pos = np.concatenate([pos_l, pos_c])
+    bmin, bmax = np.zeros(3), np.array([8 * spacing, 4 * spacing, 4 * spacing])
+    own = np.ones(len(pos), np.int8)
+    for which, rule, radius in ((0, orc.pair_set, rc + skin), (1, orc.interacting_set, rc)):
+        ra, rb = rule(pos, radius)  # the oracle's default form
+        sa, sb = rule(pos, radius, dist_mode=orc.DIST_STRICT)
+        assert len(ra) != len(sa) or not np.array_equal(ra, sa), "the case no longer separates the forms"
+        ref = np.unique(np.stack([ra, rb], 1), axis=0)
+        for prec in (eng_mod.PRECISION_FP64, eng_mod.PRECISION_MIXED):
+            e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, precision=prec, traversal=traversal)
+            e.set_particles(pos, ownership=own)
+            e.rebuild()
+            a, b, c = e.pair_set(which)
+            dev = np.unique(np.stack([np.minimum(a, b), np.maximum(a, b)], 1), axis=0)
+            assert np.array_equal(dev, ref), (which, prec)
+            g = e.compute_forces()[0]
+            ia, _ = orc.interacting_set(pos, rc)
+            assert g["num_pairs"] == len(ia), (which, prec)
+            e.close()

@@ -217,12 +217,48 @@ def test_dist_modes_differ_only_by_contraction(orc):
     diff = 0
     for _ in range(2000):
         dx, dy, dz = rng.uniform(-3, 3, 3)
-        s = L.orc_dist2(dx, dy, dz, 0)
-        f = L.orc_dist2(dx, dy, dz, 1)
+        s = L.orc_dist2(dx, dy, dz, orc.DIST_STRICT)
+        f = L.orc_dist2(dx, dy, dz, orc.DIST_FMA_SOA)
         assert s == pytest.approx(f, rel=1e-15)
         diff += s != f
         assert s == (dx * dx + dy * dy) + dz * dz
     assert diff > 0
+
+
+def test_reference_flags_contract_dr2_to_the_default_form(orc):
+    """The reference's SoA distance expression (LJFunctor.h:287-293), compiled by this host's C compiler with the
+    reference's flags, gives exactly fma(dz,dz, fma(dx,dx, dy*dy)): the engine's default distance form
+    (PE_DIST_FMA_SOA) is the one the reference binary computes on this host."""
+    probe = orc.contraction_probe()
+    L = orc.lib()
+    rng = np.random.default_rng(12)
+    n = 20000
+    pi = rng.uniform(0, 50, (n, 3))
+    # displacements of every scale, many near the cutoff radii the engine tests against
+    pj = pi + rng.normal(0, 1, (n, 3)) * rng.choice([1e-3, 0.5, 1.0, 3.4], (n, 1))
+    got = probe(pi[:, 0], pi[:, 1], pi[:, 2], pj[:, 0], pj[:, 1], pj[:, 2])
+    d = pi - pj
+    forms = {m: np.array([L.orc_dist2(*d[k], m) for k in range(n)])
+             for m in (orc.DIST_FMA_SOA, orc.DIST_STRICT, orc.DIST_FMA_DOT)}
+    assert np.array_equal(got, forms[orc.DIST_FMA_SOA])
+    # the test can tell the forms apart: the uncontracted and the dot forms differ on many of these inputs
+    assert (got != forms[orc.DIST_STRICT]).sum() > n // 20
+    assert (got != forms[orc.DIST_FMA_DOT]).sum() > n // 20
+
+
+def test_contraction_changes_the_pair_sets_of_straddling_pairs(orc, straddling_pairs):
+    """Pairs built to straddle (rc+skin)^2 and rc^2: the oracle's Verlet and interacting sets differ between the
+    uncontracted expression and the reference's contracted one, so a parity test on them can tell a wrong
+    default distance form."""
+    rc, skin = 2.5, 0.3
+    for radius, rule in ((rc + skin, orc.pair_set), (rc, orc.interacting_set)):
+        pos, flags = straddling_pairs(orc, radius, 27, seed=3, spacing=3 * (rc + skin))
+        arg = rc + skin if rule is orc.pair_set else rc
+        a_s, b_s = rule(pos, arg, dist_mode=orc.DIST_STRICT)
+        a_f, b_f = rule(pos, arg, dist_mode=orc.DIST_FMA_SOA)
+        col = (0, 2) if rule is orc.pair_set else (1, 3)
+        assert len(a_s) == flags[:, col[0]].sum() and len(a_f) == flags[:, col[1]].sum()
+        assert len(a_s) != len(a_f) or not np.array_equal(a_s, a_f)
 
 
 def test_tower_grid_geometry(orc):
