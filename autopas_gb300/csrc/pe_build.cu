@@ -609,6 +609,129 @@ void launch_plist_build(DeviceState &s, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// 6b. pair-group half lists for the newton3 force path (traversal 2).  Group g is slots 2g and 2g+1, two
+//     consecutive particles of one cluster (C is even).  Built like the particle lists from the full cluster-pair
+//     lists, keeping each unordered pair in exactly one group's list, as the reference's newton3 lists keep only
+//     forward neighbours (VerletClusterListsRebuilder.h:339-354): a j of a later cluster; of the same cluster,
+//     only beyond the group (the group's own pair needs no entry); of an image of the same cluster, only for
+//     image codes above kShiftNone (the opposite code gives the same pair).  A j is kept when it lies within the
+//     widened rc+skin threshold of either member, both tested in one packed instruction on the hi parts.
+//     Systems with explicit halo particles use the full lists; this traversal serves periodic systems.
+// ---------------------------------------------------------------------------------------------
+template <int C>
+__global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
+  constexpr int GL = C / 2;   // groups (lanes) per cluster
+  constexpr int G = 32 / GL;  // clusters per warp
+  // the current j-cluster of each cluster of the warp, hi parts negated, one row per coordinate (one word of
+  // padding keeps the rows of neighbouring clusters in different banks)
+  __shared__ float sj[4][G][3][C + 1];
+  // each lane's last two blocks of entries (a ring of 16; up to C <= 8 appends per cluster pair complete at most one
+  // block); 17 words per lane keep lanes that append at the same ring position in different banks
+  __shared__ uint32_t stage[4][32][2 * kPlistBlock + 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cg = lane / GL, gl = lane % GL;
+  const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + cg;
+  const bool validA = A < s.nclusters;
+  const int64_t g = A * GL + gl;
+  int n = 0;
+  const uint32_t *lst = s.cp_list;
+  uint4 q0 = make_uint4(0u, 0u, 0u, 0u), q1 = q0;
+  int sy = 0;
+  if (validA) {
+    n = s.cp_count[A];
+    lst = s.cp_list + s.cp_start[A];
+    q0 = s.pq[2 * g];
+    q1 = s.pq[2 * g + 1];
+    sy = s.cl_sys[A];
+  }
+  const SysDev &S = s.sysd[sy];
+  const unsigned int eb = S.pq_expb;
+  const float2 hx = make_float2(pq_hi(q0.x, eb), pq_hi(q1.x, eb));
+  const float2 hy = make_float2(pq_hi(q0.y, eb), pq_hi(q1.y, eb));
+  const float2 hz = make_float2(pq_hi(q0.z, eb), pq_hi(q1.z, eb));
+  const float r2max = S.plist_r2max;
+  // padding dummies close a cluster, so a group whose first member is a dummy has a dummy second member too
+  const bool real = validA && pq_own(q0) != 0;
+  int nmax = n;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+  const int cap = s.gl_cap;
+  const int64_t stride = s.gl_stride;
+  uint32_t *stg = stage[w][lane];
+  auto put_block = [&](int b) {
+    if (b * kPlistBlock < cap) {
+      const uint32_t *src = stg + (b & 1) * kPlistBlock;
+      uint4 *dst = reinterpret_cast<uint4 *>(s.gl_list + plist_index(stride, g, b * kPlistBlock));
+      dst[0] = make_uint4(src[0], src[1], src[2], src[3]);
+      dst[1] = make_uint4(src[4], src[5], src[6], src[7]);
+    }
+  };
+  int cnt = 0;
+  uint32_t ent_next = 0 < n ? __ldg(lst) : 0u;
+  for (int e = 0; e < nmax; ++e) {
+    const bool act = e < n;
+    const uint32_t ent = ent_next;
+    ent_next = e + 1 < n ? __ldg(lst + e + 1) : 0u;
+    const int64_t B = ent >> 5;
+    const int code = ent & 31;
+    // the forward rule; every lane of a cluster reads the same entry, so the decision is uniform over them
+    const bool fwd = act && (B > A || (B == A && code >= kShiftNone));
+    if (fwd) {
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int jj = 2 * gl + u;
+        const uint4 pj = __ldg(&s.pq[B * C + jj]);
+        sj[w][cg][0][jj] = pq_nhi(pj.x, eb);
+        sj[w][cg][1][jj] = pq_nhi(pj.y, eb);
+        sj[w][cg][2][jj] = pq_nhi(pj.z, eb);
+      }
+    }
+    __syncwarp();
+    if (fwd && real) {
+      // both members moved by minus the image shift (exact: hi parts and shifts on the ulp(B) grid)
+      const float4 us = c_unit_shift[code];
+      const float2 xh = fma2(dup2(-us.x), dup2(S.len_hi[0]), hx);
+      const float2 yh = fma2(dup2(-us.y), dup2(S.len_hi[1]), hy);
+      const float2 zh = fma2(dup2(-us.z), dup2(S.len_hi[2]), hz);
+      const uint32_t ebase = (((uint32_t)B * (uint32_t)C) << 5) | (uint32_t)code;
+      const int jfirst = (B == A && code == kShiftNone) ? 2 * gl + 2 : 0;
+      const int before = cnt;
+#pragma unroll
+      for (int jj = 0; jj < C; ++jj) {
+        const float2 dx = add2(xh, dup2(sj[w][cg][0][jj]));
+        const float2 dy = add2(yh, dup2(sj[w][cg][1][jj]));
+        const float2 dz = add2(zh, dup2(sj[w][cg][2][jj]));
+        const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const bool keep = jj >= jfirst && ((r2.x > 0.f && r2.x <= r2max) || (r2.y > 0.f && r2.y <= r2max));
+        if (keep) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
+        cnt += keep ? 1 : 0;
+      }
+      if ((before ^ cnt) & ~(kPlistBlock - 1)) put_block(before / kPlistBlock);
+    }
+    __syncwarp();
+  }
+  if (validA) {
+    if (cnt & (kPlistBlock - 1)) put_block(cnt / kPlistBlock);  // the last block; entries past cnt are never read
+    s.gl_count[g] = cnt;
+  }
+  int mx = cnt;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0 && mx > 0) atomicMax(s.pl_max, mx);
+}
+
+void launch_glist_build(DeviceState &s, cudaStream_t st) {
+  cudaMemsetAsync(s.pl_max, 0, sizeof(int), st);
+  const int64_t per_block = 4 * (64 / s.C);  // i-clusters per block of 4 warps
+  const int64_t nb = (s.nclusters + per_block - 1) / per_block;
+  if (nb == 0) return;
+  if (s.C == 4)
+    k_glist_build<4><<<(unsigned)nb, 128, 0, st>>>(s);
+  else
+    k_glist_build<8><<<(unsigned)nb, 128, 0, st>>>(s);
+}
+
+// ---------------------------------------------------------------------------------------------
 // 7. rolling pruning (the inner lists the force kernels read)
 //    Invariant: every pair within rc at a force evaluation is in the inner list.  It holds because (a) the
 //    inner list holds every pair within rc + b at the last prune, b the prune buffer, and (b) no particle has
@@ -835,9 +958,69 @@ __global__ void k_pair_dump_plist(DeviceState s, int which, int64_t cap, int64_t
   }
 }
 
+// the pairs covered by the pair-group half lists: every pair sits in one group's list (or is a group's own pair),
+// so each is reported from there, with both halo views of a periodic-image pair (j's image seen by i, and i's
+// image seen by j, each when md-flexible's halo rule creates it), evaluated in FP64 with the distance form
+__device__ __forceinline__ void dump_one(const DeviceState &s, const SysDev &S, int which, int64_t cap, int64_t i,
+                                         int64_t j, int code, int64_t *__restrict__ oa, int64_t *__restrict__ ob,
+                                         int32_t *__restrict__ oc, unsigned long long *__restrict__ count) {
+  const double L = s.cutoff + s.skin;
+  const double lim = which == 0 ? L * L : s.cutoff * s.cutoff;
+  const double pi[3] = {s.x[i], s.y[i], s.z[i]};
+  const double pj[3] = {s.x[j], s.y[j], s.z[j]};
+  int sx, sy, sz;
+  shift_of(code, sx, sy, sz);
+  for (int view = 0; view < 2; ++view) {
+    if (code == kShiftNone && view == 1) break;
+    const double *a = view == 0 ? pi : pj, *b = view == 0 ? pj : pi;
+    const int tx = view == 0 ? sx : -sx, ty = view == 0 ? sy : -sy, tz = view == 0 ? sz : -sz;
+    if (code != kShiftNone && !image_exists(S, b, tx, ty, tz)) continue;
+    const double d2 = dist2_mode(a[0] - image_coord(b[0], tx, S.len[0]), a[1] - image_coord(b[1], ty, S.len[1]),
+                                 a[2] - image_coord(b[2], tz, S.len[2]), s.dist_mode);
+    const bool in = which == 0 ? (d2 < lim) : (d2 <= lim);
+    if (!in) continue;
+    const unsigned long long k = atomicAdd(count, 1ull);
+    if (k < (unsigned long long)cap) {
+      int64_t ga = s.orig[view == 0 ? i : j], gb = s.orig[view == 0 ? j : i];
+      if (code == kShiftNone && gb < ga) {
+        const int64_t t = ga;
+        ga = gb;
+        gb = t;
+      }
+      oa[k] = ga;
+      ob[k] = gb;
+      oc[k] = code == kShiftNone ? kShiftNone : shift_code(tx, ty, tz);
+    }
+  }
+}
+
+__global__ void k_pair_dump_glist(DeviceState s, int which, int64_t cap, int64_t *__restrict__ oa,
+                                  int64_t *__restrict__ ob, int32_t *__restrict__ oc,
+                                  unsigned long long *__restrict__ count) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (2 * g >= s.nslots) return;
+  const int64_t i0 = 2 * g, i1 = 2 * g + 1;
+  if (s.own[i0] == 0) return;
+  const SysDev &S = s.sysd[s.sys[i0]];
+  if (s.own[i1] != 0) dump_one(s, S, which, cap, i0, i1, kShiftNone, oa, ob, oc, count);
+  const int n = min(s.gl_count[g], s.gl_cap);
+  for (int k = 0; k < n; ++k) {
+    const uint32_t ent = s.gl_list[plist_index(s.gl_stride, g, k)];
+    const int64_t j = ent >> 5;
+    const int code = ent & 31;
+    dump_one(s, S, which, cap, i0, j, code, oa, ob, oc, count);
+    if (s.own[i1] != 0) dump_one(s, S, which, cap, i1, j, code, oa, ob, oc, count);
+  }
+}
+
 void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_t *b, int32_t *code,
                       unsigned long long *count, cudaStream_t st) {
   cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  if (s.traversal == 2) {
+    const int64_t nb = (s.nslots / 2 + 127) / 128;
+    if (nb > 0) k_pair_dump_glist<<<(unsigned)nb, 128, 0, st>>>(s, which, cap, a, b, code, count);
+    return;
+  }
   if (s.traversal == 1) {
     const int64_t nb = (s.nslots + 127) / 128;
     if (nb > 0) k_pair_dump_plist<<<(unsigned)nb, 128, 0, st>>>(s, which, cap, a, b, code, count);

@@ -186,6 +186,12 @@ struct pe_engine {
   int pl_cap = 0;
   int64_t pl_entries = 0;
   bool need_plist = false;       // particle lists needed besides the force traversal (three-body forces)
+  // pair-group half lists and the newton3 force sums (traversal 2)
+  DBuf<uint32_t> gl_list;
+  DBuf<int32_t> gl_count;
+  int gl_cap = 0;
+  int64_t gl_entries = 0;
+  DBuf<float4> fown, facc;
   DBuf<uint32_t> pi_list;        // pruned inner lists
   DBuf<int32_t> pi_count;
   DBuf<double> x_prune, x_reb;
@@ -269,6 +275,12 @@ struct pe_engine {
     s.pl_cap = pl_cap;
     s.pl_stride = pcap;
     s.pl_max = pl_max.p;
+    s.gl_list = gl_list.p;
+    s.gl_count = gl_count.p;
+    s.gl_cap = gl_cap;
+    s.gl_stride = pcap / 2;
+    s.fown = fown.p;
+    s.facc = facc.p;
     s.prune = (cfg.prune_buffer > 0 && traversal == 1) ? 1 : 0;
     s.any_halo_sys = 0;
     for (const auto &S : sys) s.any_halo_sys |= S.desc.periodic ? 0 : 1;
@@ -926,6 +938,49 @@ static int build_particle_lists(pe_engine *h) {
   return h->fail(PE_ERR_LIST_OVERFLOW, "particle lists kept overflowing");
 }
 
+// pair-group half lists (newton3) from the full cluster-pair lists; the per-group capacity grows when exceeded.
+// The reaction accumulators are cleared here: the slot order has changed.
+static int build_group_lists(pe_engine *h) {
+  cudaStream_t st = h->st;
+  const size_t groups = (size_t)(h->pcap / 2);
+  if (!h->gl_count.ensure(groups) || !h->pl_max.ensure(1) || !h->fown.ensure((size_t)h->pcap) ||
+      !h->facc.ensure((size_t)h->pcap))
+    return h->fail(PE_ERR_OOM, "pair-group lists");
+  PE_CUDA(h, cudaMemsetAsync(h->facc.p, 0, sizeof(float4) * (size_t)h->pcap, st));
+  if (h->gl_cap == 0) {
+    double rho = 0;
+    for (auto &S : h->sys) {
+      double vol = 1;
+      for (int d = 0; d < 3; ++d) vol *= S.desc.box_max[d] - S.desc.box_min[d];
+      rho = std::max(rho, std::max(S.density, (double)S.count / vol));
+    }
+    const double L = h->cfg.cutoff + h->cfg.skin;
+    // the forward half of the neighbours of two close particles: about as many as one particle's full list
+    h->gl_cap = (int)std::min(4096.0, 4.18879 * L * L * L * rho * 1.2 + 32);
+  }
+  h->gl_cap = (h->gl_cap + kPlistBlock - 1) / kPlistBlock * kPlistBlock;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    const size_t need = (size_t)h->gl_cap * groups;
+    if (!h->gl_list.ensure(need)) return h->fail(PE_ERR_OOM, "pair-group lists (%zu entries)", need);
+    DeviceState s = h->state();
+    launch_glist_build(s, st);
+    h->launches += 1;
+    if (!h->hwords.ensure(sizeof(RebuildWords), st)) return h->fail(PE_ERR_OOM, "page-locked rebuild words");
+    RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
+    PE_CUDA(h, cudaMemcpyAsync(&w->plist_max, h->pl_max.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PE_CUDA(h, cudaStreamSynchronize(st));
+    PE_TRY(h->cuda_check("pair-group list build"));
+    const int mx = w->plist_max;
+    if (mx <= h->gl_cap) {
+      h->gl_entries = 0;
+      return PE_OK;
+    }
+    h->gl_cap = ((int)(mx * 1.2) + 8 + kPlistBlock - 1) / kPlistBlock * kPlistBlock;
+    h->gl_list.release();
+  }
+  return h->fail(PE_ERR_LIST_OVERFLOW, "pair-group lists kept overflowing");
+}
+
 static int normalize_positions(pe_engine *h);
 
 static int do_rebuild(pe_engine *h) {
@@ -998,7 +1053,8 @@ static int do_rebuild(pe_engine *h) {
     PE_CUDA(h, cudaMemcpyAsync(&w->list_err, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     PE_CUDA(h, cudaMemcpyAsync(&w->list_total, h->cp_total.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                st));
-    const int prc = (h->traversal == 1 || h->need_plist) ? build_particle_lists(h) : PE_OK;
+    int prc = (h->traversal == 1 || h->need_plist) ? build_particle_lists(h) : PE_OK;
+    if (prc == PE_OK && h->traversal == 2) prc = build_group_lists(h);
     PE_CUDA(h, cudaStreamSynchronize(st));
     PE_TRY(h->cuda_check("list build"));
     const int e = w->list_err;
@@ -1069,7 +1125,18 @@ static int normalize_positions(pe_engine *h) {
 // new velocity of its particle); the other kernels, rolling pruning (which tracks displacements in the
 // position update) and three-body forces (which add to the force after the pair kernel) take the plain path.
 static bool fused_positions_ok(const pe_engine *h) {
-  return h->precision != PE_PRECISION_FP64 && h->traversal == 1 && !pruning(h) && !(h->cfg.atm_nu > 0);
+  return h->precision != PE_PRECISION_FP64 && (h->traversal == 1 || h->traversal == 2) && !pruning(h) &&
+         !(h->cfg.atm_nu > 0);
+}
+
+// The newton3 traversal (pair-group half lists) serves the mixed form on periodic systems without three-body
+// forces or rolling pruning, when the configuration allows newton3.
+static bool newton3_allowed(const pe_engine *h) {
+  if (h->cfg.newton3 == 0 || h->precision != PE_PRECISION_MIXED || h->cfg.atm_nu > 0 || h->cfg.prune_buffer > 0)
+    return false;
+  for (const auto &S : h->sys)
+    if (!S.desc.periodic) return false;
+  return true;
 }
 
 static VVFactors vv_factors(const pe_engine *h, double dt) {
@@ -1172,7 +1239,7 @@ static int apply_config(pe_engine *h, int C, int traversal, int variant) {
   h->C = C;
   h->traversal = traversal;
   h->variant = variant;
-  h->newton3 = (h->cfg.newton3 == 1 && traversal == 0) ? 1 : 0;
+  h->newton3 = traversal == 2 ? 1 : 0;
   if (regrid) {
     PE_TRY(setup_grids(h));
     PE_TRY(ensure_particle_capacity(h));
@@ -1187,6 +1254,8 @@ static int tune(pe_engine *h, int samples) {
   samples = std::max(1, samples);
   std::vector<int> Cs = h->cfg.cluster_size == 0 ? std::vector<int>{4, 8} : std::vector<int>{h->cfg.cluster_size};
   std::vector<int> Ts = h->cfg.traversal == -1 ? std::vector<int>{0, 1} : std::vector<int>{h->traversal};
+  if (h->cfg.newton3 == 1) Ts = {2};  // newton3 required: the pair-group half lists only
+  else if (h->cfg.traversal == -1 && newton3_allowed(h)) Ts.push_back(2);
   h->tune_log.clear();
   const int rebuilds = (int)h->rebuilds;
   const double per_step = 1.0 / std::max(1, h->cfg.rebuild_frequency);
@@ -1250,12 +1319,19 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->cluster_size != 0 && cfg->cluster_size != 4 && cfg->cluster_size != 8) return PE_ERR_ARG;
   if (cfg->dist_mode < 0 || cfg->dist_mode > 2) return PE_ERR_ARG;
   if (cfg->tower_sizing < 0 || cfg->tower_sizing > 1) return PE_ERR_ARG;
-  if (cfg->traversal < -1 || cfg->traversal > 1) return PE_ERR_ARG;
+  if (cfg->traversal < -1 || cfg->traversal > 2) return PE_ERR_ARG;
+  if (cfg->newton3 < -1 || cfg->newton3 > 1) return PE_ERR_ARG;
   if (cfg->atm_nu > 0 && !(cfg->atm_cutoff > 0 && cfg->atm_cutoff <= cfg->cutoff + cfg->skin)) return PE_ERR_ARG;
   if (cfg->prune_buffer < 0 || cfg->prune_buffer > cfg->skin) return PE_ERR_ARG;
   if (cfg->kernel_variant < 0 || cfg->kernel_variant > 3) return PE_ERR_ARG;
-  // every force kernel evaluates each pair from both sides (full lists); half lists are not offered
-  if (cfg->newton3 == 1) return PE_ERR_ARG;
+  // newton3 (pair-group half lists): the mixed form, periodic systems, no three-body forces or pruning
+  if (cfg->newton3 == 1 || cfg->traversal == 2) {
+    if (cfg->precision != PE_PRECISION_MIXED || cfg->atm_nu > 0 || cfg->prune_buffer > 0 || cfg->newton3 == 0)
+      return PE_ERR_ARG;
+    if (cfg->traversal == 0 || cfg->traversal == 1) return PE_ERR_ARG;
+    for (int q = 0; q < num_systems; ++q)
+      if (!systems[q].periodic) return PE_ERR_ARG;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PE_ERR_NO_DEVICE;
   pe_engine *h = new pe_engine();
@@ -1267,9 +1343,9 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   h->cfg.sigma = h->sig.data();
   h->cfg.mass = h->mass.data();
   h->C = cfg->cluster_size == 0 ? 8 : cfg->cluster_size;
-  h->traversal = cfg->traversal == 0 ? 0 : 1;
+  h->traversal = cfg->traversal == 0 ? 0 : (cfg->traversal == 2 || cfg->newton3 == 1) ? 2 : 1;
   h->need_plist = cfg->atm_nu > 0;
-  h->newton3 = (cfg->newton3 == 1 && h->traversal == 0) ? 1 : 0;
+  h->newton3 = h->traversal == 2 ? 1 : 0;
   h->precision = cfg->precision;
   h->variant = cfg->kernel_variant;
   cudaGetDevice(&h->device);
@@ -1360,6 +1436,10 @@ int pe_destroy(pe_engine *h) {
   h->pl_list.release();
   h->pl_count.release();
   h->pl_max.release();
+  h->gl_list.release();
+  h->gl_count.release();
+  h->fown.release();
+  h->facc.release();
   h->atm_slot.release();
   h->pi_list.release();
   h->pi_count.release();
@@ -1735,8 +1815,21 @@ int pe_get_info(pe_engine *h, pe_info *info) {
     }
     PE_TRY(h->cuda_check("list entry count"));
   }
-  info->num_list_entries = h->pl_entries;
-  info->list_capacity = h->pl_cap;
+  if (h->traversal == 2 && h->lists_valid && h->gl_entries == 0 && h->nslots > 0 && h->gl_count.p) {
+    unsigned long long *acc = nullptr;
+    if (cudaMalloc(&acc, sizeof(unsigned long long)) == cudaSuccess) {
+      unsigned long long v = 0;
+      cudaMemsetAsync(acc, 0, sizeof(v), h->st);
+      k_sum_i32<<<304, 256, 0, h->st>>>(h->gl_count.p, h->nslots / 2, acc);
+      cudaMemcpyAsync(&v, acc, sizeof(v), cudaMemcpyDeviceToHost, h->st);
+      cudaStreamSynchronize(h->st);
+      cudaFree(acc);
+      h->gl_entries = (int64_t)v;
+    }
+    PE_TRY(h->cuda_check("list entry count"));
+  }
+  info->num_list_entries = h->traversal == 2 ? h->gl_entries : h->pl_entries;
+  info->list_capacity = h->traversal == 2 ? h->gl_cap : h->pl_cap;
   info->num_particles = h->nuser;
   info->num_slots = h->nslots;
   info->num_clusters = h->nclusters;

@@ -825,6 +825,314 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// newton3 over pair-group half lists (traversal 2, mixed precision).  One thread per group of two consecutive
+// slots (i0, i1): the two members are the two halves of every packed FP32x2 instruction, so each list entry j is
+// gathered and decoded once and evaluated against both.  The i-forces are compensated sums in registers; the
+// reaction on j, summed over both members, goes out as one vector reduction (red.global.add.v4.f32) into facc.
+// The reference's newton3 functor call (SoAFunctorPair with newton3, LJFunctor.h:369-559) accumulates the j side
+// the same way, per pair; here the two members' shares are combined before the reduction.  k_n3_finish adds the
+// group's own part and the reductions, clears facc and runs the velocity half.  Globals use the newton3 energy
+// factor (both members owned: the pair counts twice, LJFunctor.h:327-345).
+// ---------------------------------------------------------------------------------------------
+template <int GM, bool ONE_TYPE>
+struct N3Acc {
+  // minus the force on i0 (.x) and i1 (.y): compensated running sums, plain sums of the current batch
+  float2 fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  float2 fc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  float2 b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  float2 pot = {0.f, 0.f}, vx = {0.f, 0.f}, vy = {0.f, 0.f}, vz = {0.f, 0.f};
+  int hits = 0;
+
+  // LJ of the two pairs (i0, j) and (i1, j) from their displacements; returns minus the forces on i0, i1 (the
+  // forces on j summed over the two are their sum) with the cutoff masks applied.  k0, k1: type-pair indices.
+  __device__ __forceinline__ void lj2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i0,
+                                      int64_t j, int code, float2 dx, float2 dy, float2 dz, bool live1, int k0,
+                                      int k1, float eps24, float sig2, float shr,
+                                      const float (*tab)[kMaxTypes * kMaxTypes], float band, float2 &px, float2 &py,
+                                      float2 &pz, bool &any) {
+    const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+    bool m0 = r2.x <= fa.rc2f, m1 = live1 && r2.y <= fa.rc2f;
+    const float2 off = add2(r2, dup2(-fa.rc2f));
+    const bool n0 = fabsf(off.x) <= band, n1 = live1 && fabsf(off.y) <= band;
+    if (n0 || n1) {
+      if (n0) m0 = exact_within(s, S, i0, j, code, fa.rc2);
+      if (n1) m1 = exact_within(s, S, i0 + 1, j, code, fa.rc2);
+    }
+    float2 ep = dup2(eps24), sg = dup2(sig2), sh = dup2(shr);
+    if (!ONE_TYPE) {
+      ep = make_float2(tab[0][k0], tab[0][k1]);
+      sg = make_float2(tab[1][k0], tab[1][k1]);
+      sh = make_float2(tab[2][k0], tab[2][k1]);
+    }
+    const float2 rn = make_float2(nrcp_approx(r2.x), nrcp_approx(r2.y));
+    const float2 ninv = fma2(rn, fma2(r2, rn, dup2(1.0f)), rn);
+    const float2 nlj2 = mul2(sg, ninv);
+    const float2 nlj6 = mul2(mul2(nlj2, nlj2), nlj2);
+    const float2 lj12m6 = fma2(nlj6, nlj6, nlj6);
+    const float2 t = fma2(nlj6, nlj6, lj12m6);
+    const float2 em = make_float2(m0 ? ep.x : 0.f, m1 ? ep.y : 0.f);
+    const float2 nfac = mul2(mul2(em, t), ninv);
+    px = mul2(dx, nfac);
+    py = mul2(dy, nfac);
+    pz = mul2(dz, nfac);
+    if (GM > 0) {
+      pot = fma2(em, add2(lj12m6, sh), pot);
+      vx = fma2(px, dx, vx);
+      vy = fma2(py, dy, vy);
+      vz = fma2(pz, dz, vz);
+      hits += (m0 ? 1 : 0) + (m1 ? 1 : 0);
+    }
+    any = m0 || m1;
+  }
+
+  // one list entry: j (image code) against both members; iq holds the members' decoded records, packed
+  template <bool SHIFT>
+  __device__ __forceinline__ void entry(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i0,
+                                        const float2 (&iq)[6], float u, unsigned int eb, bool live1, int2 ti,
+                                        uint32_t e, const uint4 &qj, float eps24, float sig2, float shr,
+                                        const float (*tab)[kMaxTypes * kMaxTypes], int T, float band) {
+    const int code = e & 31;
+    const int64_t j = e >> 5;
+    float2 xh = iq[0], yh = iq[1], zh = iq[2], xl = iq[3], yl = iq[4], zl = iq[5];
+    if (SHIFT) {
+      // the members moved by minus the image shift (exact on the ulp(B) grid and in integer low parts)
+      const float4 us = c_unit_shift[code];
+      xh = fma2(dup2(-us.x), dup2(S.len_hi[0]), xh);
+      yh = fma2(dup2(-us.y), dup2(S.len_hi[1]), yh);
+      zh = fma2(dup2(-us.z), dup2(S.len_hi[2]), zh);
+      xl = fma2(dup2(-us.x), dup2(S.len_lo_u[0]), xl);
+      yl = fma2(dup2(-us.y), dup2(S.len_lo_u[1]), yl);
+      zl = fma2(dup2(-us.z), dup2(S.len_lo_u[2]), zl);
+    }
+    const float2 uu = dup2(u);
+    const float2 dx = fma2(add2(xl, dup2(pq_nlox(qj))), uu, add2(xh, dup2(pq_nhi(qj.x, eb))));
+    const float2 dy = fma2(add2(yl, dup2(pq_nloy(qj))), uu, add2(yh, dup2(pq_nhi(qj.y, eb))));
+    const float2 dz = fma2(add2(zl, dup2(pq_nloz(qj))), uu, add2(zh, dup2(pq_nhi(qj.z, eb))));
+    const int tj = ONE_TYPE ? 0 : pq_type(qj);
+    float2 px, py, pz;
+    bool any;
+    lj2(s, S, fa, i0, j, code, dx, dy, dz, live1, ti.x * T + tj, ti.y * T + tj, eps24, sig2, shr, tab, band, px, py,
+        pz, any);
+    b[0] = add2(b[0], px);
+    b[1] = add2(b[1], py);
+    b[2] = add2(b[2], pz);
+    // the reaction on j: minus the forces on the members, i.e. px + py of both halves
+    if (any) atomicAdd(s.facc + j, make_float4(px.x + px.y, py.x + py.y, pz.x + pz.y, 0.f));
+  }
+
+  __device__ __forceinline__ void flush() {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      kahan_add(fs[c].x, fc[c].x, b[c].x);
+      kahan_add(fs[c].y, fc[c].y, b[c].y);
+      b[c] = make_float2(0.f, 0.f);
+    }
+  }
+};
+
+template <int C, int GM, bool ONE_TYPE, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceArgs fa) {
+  constexpr int GL = C / 2;  // groups per cluster
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  const int T = s.ntypes;
+  if (!ONE_TYPE) {
+    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
+      tab[0][q] = s.types->eps24f[q];
+      tab[1][q] = s.types->sig2f[q];
+      tab[2][q] = s.types->shrf[q];
+    }
+    __syncthreads();
+  }
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i0 = 2 * g;
+  const bool inrange = i0 < s.nslots;
+  uint4 q0 = make_uint4(0u, 0u, 0u, 0u), q1 = q0;
+  int n = 0, sy = 0;
+  if (inrange) {
+    q0 = s.pq[i0];
+    q1 = s.pq[i0 + 1];
+    sy = s.sys[i0];
+    if (pq_own(q0) != 0) n = s.gl_count[g];
+  }
+  const bool live0 = pq_own(q0) == 1, live1 = pq_own(q1) == 1;
+  const SysDev &S = s.sysd[sy];
+  const unsigned int eb = S.pq_expb;
+  const float u = S.pq_unit;
+  float2 iq[6] = {make_float2(pq_hi(q0.x, eb), pq_hi(q1.x, eb)), make_float2(pq_hi(q0.y, eb), pq_hi(q1.y, eb)),
+                  make_float2(pq_hi(q0.z, eb), pq_hi(q1.z, eb)), make_float2(pq_lox(q0), pq_lox(q1)),
+                  make_float2(pq_loy(q0), pq_loy(q1)), make_float2(pq_loz(q0), pq_loz(q1))};
+  const int2 ti = make_int2(pq_type(q0), pq_type(q1));
+  float eps24 = 0.f, sig2 = 0.f, shr = 0.f;
+  if (ONE_TYPE) {
+    eps24 = s.types->eps24f[0];
+    sig2 = s.types->sig2f[0];
+    shr = s.types->shrf[0];
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) asm volatile("" : "+f"(iq[k].x), "+f"(iq[k].y));
+  asm volatile("" : "+f"(eps24), "+f"(sig2), "+f"(shr));
+  const float band = fa.rc2f * 2e-6f;
+  N3Acc<GM, ONE_TYPE> acc;
+  // the group's own pair (i0, i1), once
+  if (live0 && live1) {
+    const float dx = fmaf(iq[3].x - iq[3].y, u, iq[0].x - iq[0].y);
+    const float dy = fmaf(iq[4].x - iq[4].y, u, iq[1].x - iq[1].y);
+    const float dz = fmaf(iq[5].x - iq[5].y, u, iq[2].x - iq[2].y);
+    float2 px, py, pz;
+    bool any;
+    acc.lj2(s, S, fa, i0, i0 + 1, kShiftNone, make_float2(dx, dx), make_float2(dy, dy), make_float2(dz, dz), false,
+            ti.x * T + ti.y, ti.x * T + ti.y, eps24, sig2, shr, tab, band, px, py, pz, any);
+    // .x holds minus the force on i0; i1 gets the opposite
+    acc.b[0] = make_float2(px.x, -px.x);
+    acc.b[1] = make_float2(py.x, -py.x);
+    acc.b[2] = make_float2(pz.x, -pz.x);
+    acc.flush();
+  }
+  const uint32_t *base = s.gl_list + g * kPlistBlock;
+  const int64_t bstride = s.gl_stride * kPlistBlock;
+  int k = 0;
+  for (; k + 4 <= n; k += 4) {
+    // four entries in one 16-byte load (an aligned half of a block of 8); the next block into L2 when a block is
+    // first read
+    const uint4 ev = __ldg(reinterpret_cast<const uint4 *>(base + (int64_t)(k >> 3) * bstride + (k & 7)));
+    if ((k & 7) == 0 && k + 8 < n) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (int64_t)((k >> 3) + 1) * bstride));
+    const uint32_t e[4] = {ev.x, ev.y, ev.z, ev.w};
+    uint4 qj[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) qj[q] = __ldg(s.pq + (e[q] >> 5));
+    bool shifted = false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) shifted |= (e[q] & 31u) != (uint32_t)kShiftNone;
+    if (__any_sync(__activemask(), shifted)) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        acc.template entry<true>(s, S, fa, i0, iq, u, eb, live1, ti, e[q], qj[q], eps24, sig2, shr, tab, T, band);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        acc.template entry<false>(s, S, fa, i0, iq, u, eb, live1, ti, e[q], qj[q], eps24, sig2, shr, tab, T, band);
+    }
+    acc.flush();
+  }
+  for (; k < n; ++k) {
+    const uint32_t e = __ldg(s.gl_list + plist_index(s.gl_stride, g, k));
+    acc.template entry<true>(s, S, fa, i0, iq, u, eb, live1, ti, e, __ldg(s.pq + (e >> 5)), eps24, sig2, shr, tab,
+                             T, band);
+  }
+  acc.flush();
+  if (inrange) {
+    // the group's own part of the members' forces, signs restored (exact)
+    s.fown[i0] = make_float4(acc.fc[0].x - acc.fs[0].x, acc.fc[1].x - acc.fs[1].x, acc.fc[2].x - acc.fs[2].x, 0.f);
+    s.fown[i0 + 1] = make_float4(acc.fc[0].y - acc.fs[0].y, acc.fc[1].y - acc.fs[1].y, acc.fc[2].y - acc.fs[2].y, 0.f);
+  }
+  if (GM > 0) {
+    // newton3 energy factor 2 (both members and j owned: the engine runs this path on periodic systems only)
+    float g0 = 2.f * (acc.pot.x + acc.pot.y);
+    float g1 = -2.f * (acc.vx.x + acc.vx.y), g2 = -2.f * (acc.vy.x + acc.vy.y), g3 = -2.f * (acc.vz.x + acc.vz.y);
+    int h = 2 * acc.hits;
+#pragma unroll
+    for (int o = 1; o < GL; o <<= 1) {
+      g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+      g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+      g3 += __shfl_xor_sync(0xffffffffu, g3, o);
+      h += __shfl_xor_sync(0xffffffffu, h, o);
+    }
+    if (inrange && (g % GL) == 0) {
+      const int64_t cl = g / GL;
+      s.cl_glob[kGlob * cl + 0] = (double)g0;
+      s.cl_glob[kGlob * cl + 1] = (double)g1;
+      s.cl_glob[kGlob * cl + 2] = (double)g2;
+      s.cl_glob[kGlob * cl + 3] = (double)g3;
+      s.cl_hits[cl] = (unsigned long long)h;
+    }
+  }
+}
+
+// After the newton3 force kernel: force = own part + reactions (each rounded once to FP64 from its float sum),
+// facc cleared for the next evaluation, then the epilogue of the particle-list kernel: velocity half, the next
+// step's position half and record when fused, and the kinetic energy per cluster.
+template <int C, bool GLOB>
+__global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool inrange = i < s.nslots;
+  float ek = 0.f;
+  if (inrange) {
+    const float4 a = s.fown[i], r = s.facc[i];
+    s.facc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int oi = s.own[i];
+    if (oi == 1) {
+      const int ti = s.type[i];
+      const double Fx = (double)a.x + (double)r.x, Fy = (double)a.y + (double)r.y, Fz = (double)a.z + (double)r.z;
+      s.fx[i] = Fx;
+      s.fy[i] = Fy;
+      s.fz[i] = Fz;
+      double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+      if (fa.fuse_velocity) {
+        const double h = fa.vv.h[ti];
+        vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
+        vy = __dadd_rn(vy, __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
+        vz = __dadd_rn(vz, __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
+        s.vx[i] = vx;
+        s.vy[i] = vy;
+        s.vz[i] = vz;
+        if (fa.fuse_positions) {
+          const double c = fa.vv.c[ti], dt = fa.dt;
+          const double x1 = __dadd_rn(s.x[i], __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(Fx, c)));
+          const double y1 = __dadd_rn(s.y[i], __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(Fy, c)));
+          const double z1 = __dadd_rn(s.z[i], __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(Fz, c)));
+          s.xn[i] = x1;
+          s.yn[i] = y1;
+          s.zn[i] = z1;
+          s.ofx[i] = Fx;
+          s.ofy[i] = Fy;
+          s.ofz[i] = Fz;
+          s.pqn[i] = pq_pack(s.sysd[s.sys[i]], x1, y1, z1, ti, oi, s.err);
+        }
+      }
+      if (GLOB) {
+        const float ux = (float)vx, uy = (float)vy, uz = (float)vz;
+        ek = fa.vv.half_mass[ti] * fmaf(uz, uz, fmaf(uy, uy, ux * ux));
+      }
+    } else if (fa.fuse_positions) {
+      s.xn[i] = s.x[i];
+      s.yn[i] = s.y[i];
+      s.zn[i] = s.z[i];
+      s.pqn[i] = s.pq[i];
+    }
+  }
+  if (GLOB) {
+#pragma unroll
+    for (int o = 1; o < C; o <<= 1) ek += __shfl_xor_sync(0xffffffffu, ek, o);
+    if (inrange && (i % C) == 0) s.cl_glob[kGlob * (i / C) + 4] = (double)ek;
+  }
+}
+
+template <int C>
+static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st) {
+  const int64_t ng = s.nslots / 2;
+  const int64_t nb = (ng + 127) / 128;
+  if (nb == 0) return;
+  const int gm = fa.calc_globals ? 1 : 0;
+  if (s.ntypes == 1) {
+    if (gm)
+      k_lj_mixed_n3<C, 1, true, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_n3<C, 0, true, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+  } else {
+    if (gm)
+      k_lj_mixed_n3<C, 1, false, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_n3<C, 0, false, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
+  }
+  const int64_t nf = (s.nslots + 255) / 256;
+  if (fa.calc_globals)
+    k_n3_finish<C, true><<<(unsigned)nf, 256, 0, st>>>(s, fa);
+  else
+    k_n3_finish<C, false><<<(unsigned)nf, 256, 0, st>>>(s, fa);
+}
+
 template <int C>
 static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st) {
   const int64_t nb = (s.nslots + 127) / 128;
@@ -878,6 +1186,10 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
 
 template <int C>
 static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st) {
+  if (s.traversal == 2) {
+    launch_force_n3<C>(s, fa, st);  // the engine allows this traversal for the mixed form only
+    return;
+  }
   if (s.traversal == 1) {
     launch_force_plist<C>(s, precision, fa, st);
     return;

@@ -59,13 +59,27 @@ struct DeviceState {
   // particle neighbour lists (traversal 1): entry k of slot i at pl_list[plist_index(pl_stride, i, k)],
   // (j slot << 5 | image-shift code), every j within rc+skin of i (FP32 test with a safety margin).  pl_cap is
   // a multiple of kPlistBlock.
-  int traversal = 0;               // 0: cluster-pair lists, 1: particle lists
+  int traversal = 0;               // 0: cluster-pair lists, 1: particle lists, 2: pair-group half lists (newton3)
   int variant = 0;                 // kernel variant inside a traversal (tuner dimension)
   uint32_t *pl_list = nullptr;
   int32_t *pl_count = nullptr;     // [nslots]
   int pl_cap = 0;
   int64_t pl_stride = 0;
   int *pl_max = nullptr;           // device max of pl_count
+  // pair-group half lists (traversal 2, newton3): group g = slots 2g and 2g+1 (two consecutive particles of one
+  // cluster, C even); entry k of group g at gl_list[plist_index(gl_stride, g, k)], (j slot << 5 | image-shift code),
+  // every j within rc+skin of slot 2g or 2g+1 whose pair is not held by another group: j in a later cluster, or
+  // in the same cluster beyond the group, or an image of the same cluster with a code above kShiftNone.  The pair
+  // (2g, 2g+1) itself is evaluated by its group without an entry.
+  uint32_t *gl_list = nullptr;
+  int32_t *gl_count = nullptr;     // [groups]
+  int gl_cap = 0;                  // a multiple of kPlistBlock
+  int64_t gl_stride = 0;           // groups the list layout is sized for
+  // newton3 force sums: the group's own part (its compensated sums, written once per group member) and the
+  // reactions other groups add with vector reductions; the finish kernel adds both, clears facc and runs the
+  // velocity half
+  float4 *fown = nullptr;          // [slots]
+  float4 *facc = nullptr;          // [slots], zero between force evaluations
   // lists the force kernels read: the particle lists themselves, or the pruned inner lists
   uint32_t *fl_list = nullptr;
   int32_t *fl_count = nullptr;
@@ -140,6 +154,7 @@ int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *pe
 void launch_cluster_bbox(DeviceState &s, cudaStream_t st);
 void launch_list_build(DeviceState &s, int buf_per_warp, cudaStream_t st);
 void launch_plist_build(DeviceState &s, cudaStream_t st);
+void launch_glist_build(DeviceState &s, cudaStream_t st);  // pair-group half lists (traversal 2)
 void launch_prune_reset_refs(DeviceState &s, cudaStream_t st);   // x_prune = x_reb = x, force the next prune
 void launch_displacement(DeviceState &s, cudaStream_t st);       // update disp_bits from the current positions
 void launch_prune(DeviceState &s, cudaStream_t st);              // prune if needed, then clear the flag

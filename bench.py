@@ -44,7 +44,9 @@ def parse():
     p.add_argument("--n", type=int, default=2_000_000, help="particles of the slab workload")
     p.add_argument("--fp64-steps", type=int, default=10)
     p.add_argument("--cluster-size", type=int, default=0, help="0: the engine's tuner picks 4 or 8")
-    p.add_argument("--traversal", type=int, default=-1, help="-1: tuner; 0 cluster pairs; 1 particle lists")
+    p.add_argument("--traversal", type=int, default=-1,
+                   help="-1: tuner; 0 cluster pairs; 1 particle lists; 2 pair-group half lists (newton3)")
+    p.add_argument("--newton3", type=int, default=-1, help="-1: the tuner may pick newton3; 0 off; 1 required")
     p.add_argument("--prune", type=float, default=0.0, help="rolling-prune buffer of the particle lists (0: off)")
     p.add_argument("--variant", type=int, default=0, help="particle-list kernel variant when the tuner is off")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -230,7 +232,8 @@ def config_dict(args):
             "particles": args.n, "cutoff": RC, "skin": SKIN, "rebuild_frequency": REBUILD,
             "cluster_size": args.cluster_size or "tuned", "traversal": "tuned" if args.traversal < 0 else args.traversal,
             "prune_buffer": args.prune,
-            "newton3": False, "l2_policy": "inputs larger than L2 (no flush)"}
+            "newton3": {-1: "tuned", 0: False, 1: True}.get(args.newton3, args.newton3),
+            "l2_policy": "inputs larger than L2 (no flush)"}
 
 
 # ---------------------------------------------------------------------------------------------- our arm
@@ -246,7 +249,8 @@ def run_ours(args):
 
     def new_engine(prec, use_graphs=True):
         e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
-                         newton3=0, rebuild_frequency=REBUILD, calc_globals=True, traversal=args.traversal,
+                         newton3=args.newton3 if prec == E.PRECISION_MIXED else 0, rebuild_frequency=REBUILD,
+                         calc_globals=True, traversal=args.traversal,
                          prune_buffer=args.prune, use_graphs=use_graphs, kernel_variant=args.variant)
         e.set_particles(pos, vel)
         return e
@@ -404,7 +408,7 @@ def run_ours(args):
         "force_error": err,
         "upot_last_step": g_last["upot"], "rebuilds_in_timed_region": st["rebuilds"],
         "prunes_in_timed_region": st["prunes"],
-        "engine": {k: info[k] for k in ("cluster_size", "traversal", "num_clusters", "num_cluster_pairs",
+        "engine": {k: info[k] for k in ("cluster_size", "traversal", "newton3", "num_clusters", "num_cluster_pairs",
                                         "max_tower_size", "num_towers", "list_capacity", "num_list_entries")},
         "tuning": tuning,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
