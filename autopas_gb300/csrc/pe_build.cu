@@ -40,7 +40,9 @@ __global__ void k_bin(DeviceState s, int64_t nslots_old, uint64_t *__restrict__ 
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int t = -1;
   if (i < nslots_old) {
-    if (s.own[i] != 0) {
+    // every user particle keeps a slot, dummies included (their records sit far outside every box, so they join
+    // no list, and a later ownership change finds them); only the cluster padding (orig < 0) is dropped
+    if (s.orig[i] >= 0) {
       const SysDev &S = s.sysd[s.sys[i]];
       const int tx = tower_coord(s.x[i], S, 0);
       const int ty = tower_coord(s.y[i], S, 1);

@@ -166,6 +166,47 @@ __device__ __forceinline__ void pq_disp(const PQPos &pi, const SysDev &S, int co
   dz = fmaf(fmaf(-us.z, S.len_lo_u[2], pi.lz) - pq_loz(qj), u, fmaf(-us.z, S.len_hi[2], pi.hz) - pq_hi(qj.z, eb));
 }
 
+// Squared length of displacements d = a + b u formed from two exact terms (a: the difference of hi parts, b: the
+// integer difference of low parts, u the low-part unit) and rounded once, with the rounding of d taken into
+// account: r2 = |d|^2 + 2 d.delta, delta = (a + b u) - d per component.  a - d is exact where it matters (for
+// |a| >= 2 ulp(B), d lies within a factor 2 of a; a component below that adds nothing measurable to r2).  The
+// LJ force scales like r^-14, so the rounding of d moved into r2 would be amplified sevenfold; with the
+// correction, what remains of it is second order.
+__device__ __forceinline__ float2 r2_resid2(float2 dx, float2 dy, float2 dz, float2 ax, float2 ay, float2 az,
+                                           float2 bx, float2 by, float2 bz, float2 u) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 ex = __ffma2_rn(bx, u, __ffma2_rn(dx, m1, ax));
+  const float2 ey = __ffma2_rn(by, u, __ffma2_rn(dy, m1, ay));
+  const float2 ez = __ffma2_rn(bz, u, __ffma2_rn(dz, m1, az));
+  const float2 c = __ffma2_rn(dz, ez, __ffma2_rn(dy, ey, __fmul2_rn(dx, ex)));
+  const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+  return __ffma2_rn(c, make_float2(2.f, 2.f), r2);
+}
+__device__ __forceinline__ float r2_resid(float dx, float dy, float dz, float ax, float ay, float az, float bx, float by,
+                                          float bz, float u) {
+  const float ex = fmaf(bx, u, ax - dx), ey = fmaf(by, u, ay - dy), ez = fmaf(bz, u, az - dz);
+  const float c = fmaf(dz, ez, fmaf(dy, ey, dx * ex));
+  return fmaf(2.f, c, fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+}
+
+// The displacement r_i - (r_j + s len) of pq_disp and its residual-corrected squared length (r2_resid).
+__device__ __forceinline__ float pq_disp_r2(const PQPos &pi, const SysDev &S, int code, const uint4 &qj, float &dx,
+                                            float &dy, float &dz) {
+  const float4 us = c_unit_shift[code];
+  const unsigned int eb = S.pq_expb;
+  const float u = S.pq_unit;
+  const float ax = fmaf(-us.x, S.len_hi[0], pi.hx) - pq_hi(qj.x, eb);
+  const float ay = fmaf(-us.y, S.len_hi[1], pi.hy) - pq_hi(qj.y, eb);
+  const float az = fmaf(-us.z, S.len_hi[2], pi.hz) - pq_hi(qj.z, eb);
+  const float bx = fmaf(-us.x, S.len_lo_u[0], pi.lx) - pq_lox(qj);
+  const float by = fmaf(-us.y, S.len_lo_u[1], pi.ly) - pq_loy(qj);
+  const float bz = fmaf(-us.z, S.len_lo_u[2], pi.lz) - pq_loz(qj);
+  dx = fmaf(bx, u, ax);
+  dy = fmaf(by, u, ay);
+  dz = fmaf(bz, u, az);
+  return r2_resid(dx, dy, dz, ax, ay, az, bx, by, bz, u);
+}
+
 // Velocity-Verlet factors per type, computed on the host with the reference's operation order
 // (TimeDiscretization.cpp:42: dt*dt/(2*m); :160: dt/(2*m)) so that no kernel divides in FP64.
 struct VVFactors {

@@ -191,7 +191,9 @@ struct pe_engine {
   DBuf<int32_t> gl_count;
   int gl_cap = 0;
   int64_t gl_entries = 0;
-  DBuf<float4> fown, facc;
+  DBuf<float4> facc;
+  DBuf<int8_t> own_reb;          // ownership of each slot at the last rebuild
+  DBuf<int8_t> own_tmp;          // user-order ownership upload
   DBuf<uint32_t> pi_list;        // pruned inner lists
   DBuf<int32_t> pi_count;
   DBuf<double> x_prune, x_reb;
@@ -279,7 +281,6 @@ struct pe_engine {
     s.gl_count = gl_count.p;
     s.gl_cap = gl_cap;
     s.gl_stride = pcap / 2;
-    s.fown = fown.p;
     s.facc = facc.p;
     s.prune = (cfg.prune_buffer > 0 && traversal == 1) ? 1 : 0;
     s.any_halo_sys = 0;
@@ -637,6 +638,12 @@ __global__ void k_from_user(double *__restrict__ a, const int32_t *__restrict__ 
   if (u < n) a[slot_of[u]] = in[u];
 }
 
+__global__ void k_from_user_i8(int8_t *__restrict__ a, const int32_t *__restrict__ slot_of, int64_t n,
+                               const int8_t *__restrict__ in) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u < n) a[slot_of[u]] = in[u];
+}
+
 // user-order positions read straight from page-locked host memory (device mapping of the host buffers),
 // scattered into slot order and re-encoded in the same pass
 __global__ void k_positions_from_host(DeviceState s, int64_t n, const double *__restrict__ hx,
@@ -649,6 +656,22 @@ __global__ void k_positions_from_host(DeviceState s, int64_t n, const double *__
   s.y[q] = y;
   s.z[q] = z;
   pack_xyz(s, q, x, y, z);
+}
+
+// New ownership states in user order (LeavingParticleCollector::collectParticlesAndMarkNonOwnedAsDummy's marking,
+// src/autopas/containers/LeavingParticleCollector.h:85-118, and the revival of a halo particle by
+// updateHaloParticle).  A slot that held a dummy at the last list build is in no list, so it may not become
+// real again before the next rebuild: such a change raises bit 0 of *flag.
+__global__ void k_update_own(DeviceState s, int64_t n, const int8_t *__restrict__ own, const int8_t *__restrict__ own_reb,
+                             int *__restrict__ flag) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= n) return;
+  const int32_t q = s.slot_of[u];
+  const int o = own[u];
+  if (o != 0 && own_reb[q] == 0) atomicOr(flag, 1);
+  if (o == s.own[q]) return;
+  s.own[q] = (int8_t)o;
+  pack_one(s, q);
 }
 
 // forces of owned particles in user order, written straight into page-locked host memory
@@ -943,8 +966,7 @@ static int build_particle_lists(pe_engine *h) {
 static int build_group_lists(pe_engine *h) {
   cudaStream_t st = h->st;
   const size_t groups = (size_t)(h->pcap / 2);
-  if (!h->gl_count.ensure(groups) || !h->pl_max.ensure(1) || !h->fown.ensure((size_t)h->pcap) ||
-      !h->facc.ensure((size_t)h->pcap))
+  if (!h->gl_count.ensure(groups) || !h->pl_max.ensure(1) || !h->facc.ensure((size_t)h->pcap))
     return h->fail(PE_ERR_OOM, "pair-group lists");
   PE_CUDA(h, cudaMemsetAsync(h->facc.p, 0, sizeof(float4) * (size_t)h->pcap, st));
   if (h->gl_cap == 0) {
@@ -1096,6 +1118,9 @@ static int do_rebuild(pe_engine *h) {
     k_chunk_table<<<1, 1024, 0, st>>>(h->sys_cl_range.p, ns, h->chunks.p, h->sys_chunk0.p, max_chunks);
     h->launches += 1;
   }
+  if (!h->own_reb.ensure((size_t)std::max<int64_t>(h->nslots, 1))) return h->fail(PE_ERR_OOM, "ownership record");
+  if (h->nslots > 0)
+    PE_CUDA(h, cudaMemcpyAsync(h->own_reb.p, h->A.own.p, (size_t)h->nslots, cudaMemcpyDeviceToDevice, st));
   PE_TRY(h->cuda_check("rebuild"));
   h->lists_valid = true;
   h->steps_since_rebuild = 0;
@@ -1261,7 +1286,7 @@ static int tune(pe_engine *h, int samples) {
   const double per_step = 1.0 / std::max(1, h->cfg.rebuild_frequency);
   for (int C : Cs)
     for (int T : Ts) {
-      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : 1;
+      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : (T == 2 ? 3 : 1);
       double reb_ms = 0;
       for (int v = 0; v < nv; ++v) {
         PE_TRY(apply_config(h, C, T, v));
@@ -1438,8 +1463,9 @@ int pe_destroy(pe_engine *h) {
   h->pl_max.release();
   h->gl_list.release();
   h->gl_count.release();
-  h->fown.release();
   h->facc.release();
+  h->own_reb.release();
+  h->own_tmp.release();
   h->atm_slot.release();
   h->pi_list.release();
   h->pi_count.release();
@@ -1553,6 +1579,49 @@ int pe_update_positions(pe_engine *h, const double *x, const double *y, const do
   if (h->nslots > 0) k_pack<<<(unsigned)((h->nslots + 255) / 256), 256, 0, st>>>(s, h->nslots);
   PE_CUDA(h, cudaStreamSynchronize(st));
   return h->cuda_check("update_positions");
+}
+
+int pe_update_ownership(pe_engine *h, const int8_t *ownership, int *lists_valid) {
+  if (!h || !ownership) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  const int64_t n = h->nuser;
+  for (int64_t i = 0; i < n; ++i)
+    if (ownership[i] < 0 || ownership[i] > 2)
+      return h->fail(PE_ERR_ARG, "particle %lld has ownership %d", (long long)i, ownership[i]);
+  PE_TRY(normalize_positions(h));
+  if (!h->own_tmp.ensure((size_t)std::max<int64_t>(n, 1)) || !h->derr.ensure(1))
+    return h->fail(PE_ERR_OOM, "ownership upload");
+  if (!h->hwords.ensure(sizeof(RebuildWords), h->st)) return h->fail(PE_ERR_OOM, "page-locked rebuild words");
+  RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
+  DBuf<int> flag;
+  if (!flag.ensure(1)) return h->fail(PE_ERR_OOM, "flag");
+  cudaStream_t st = h->st;
+  PE_CUDA(h, cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+  if (n > 0) {
+    PE_CUDA(h, cudaMemcpyAsync(h->own_tmp.p, ownership, (size_t)n, cudaMemcpyHostToDevice, st));
+    if (h->lists_valid) {
+      DeviceState s = h->state();
+      k_update_own<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s, n, h->own_tmp.p, h->own_reb.p, flag.p);
+      h->launches += 1;
+    }
+  }
+  PE_CUDA(h, cudaMemcpyAsync(&w->pad, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PE_CUDA(h, cudaStreamSynchronize(st));
+  flag.release();
+  PE_TRY(h->cuda_check("update_ownership"));
+  if (!h->lists_valid) {
+    // no lists to keep: the new states take effect at the next rebuild, from the user-order copy
+    if (n > 0) {
+      DeviceState s = h->state();
+      k_from_user_i8<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s.own, h->slot_of.p, n, h->own_tmp.p);
+      PE_CUDA(h, cudaStreamSynchronize(st));
+    }
+  } else if (w->pad & 1) {
+    h->lists_valid = false;  // a particle that was a dummy at the rebuild became real
+  }
+  h->forces_valid = false;
+  if (lists_valid) *lists_valid = h->lists_valid ? 1 : 0;
+  return h->cuda_check("update_ownership");
 }
 
 int pe_rebuild(pe_engine *h) {

@@ -130,8 +130,7 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
       const int code = ent & 31;
       const uint4 qj = __ldg(&s.pq[j]);
       float dx, dy, dz;
-      pq_disp(pi, S, code, qj, dx, dy, dz);
-      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const float r2 = pq_disp_r2(pi, S, code, qj, dx, dy, dz);
       bool mask = (r2 <= rc2f) && (r2 > 0.f);
       if (fabsf(r2 - rc2f) <= band) mask = (r2 > 0.f) && exact_within(s, S, i, j, code, fa.rc2);
       if (!ONE_TYPE) {
@@ -348,11 +347,10 @@ struct MixedAcc {
   //   ninv = -1/r2, nlj2 = -(sig2/r2), nlj6 = -(sig2/r2)^3, lj12m6 = lj6^2 - lj6, t = 2 lj6^2 - lj6,
   //   -fac = eps24 t ninv, so that the pair force on i is fac * d (LJFunctor.h:141-150)
   __device__ __forceinline__ float2 accum2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i,
-                                           uint32_t e0, uint32_t e1, float2 dx, float2 dy, float2 dz, int tj0,
-                                           int tj1, int oj0, int oj1, int ti, float eps24, float sig2, float shr,
-                                           const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
+                                           uint32_t e0, uint32_t e1, float2 dx, float2 dy, float2 dz, float2 r2,
+                                           int tj0, int tj1, int oj0, int oj1, int ti, float eps24, float sig2,
+                                           float shr, const float (*tab)[kMaxTypes * kMaxTypes], int T, float band,
                                            bool two) {
-    const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
     bool m0 = r2.x <= fa.rc2f, m1 = two && r2.y <= fa.rc2f;
     const float2 off = add2(r2, dup2(-fa.rc2f));
     const bool n0 = fabsf(off.x) <= band, n1 = two && fabsf(off.y) <= band;
@@ -418,13 +416,15 @@ struct MixedAcc {
     }
     const unsigned int eb = __float_as_uint(iq[7]);
     const float2 u = dup2(iq[6]);
-    const float2 dx = fma2(add2(xl, make_float2(pq_nlox(q0), pq_nlox(q1))), u,
-                           add2(xh, make_float2(pq_nhi(q0.x, eb), pq_nhi(q1.x, eb))));
-    const float2 dy = fma2(add2(yl, make_float2(pq_nloy(q0), pq_nloy(q1))), u,
-                           add2(yh, make_float2(pq_nhi(q0.y, eb), pq_nhi(q1.y, eb))));
-    const float2 dz = fma2(add2(zl, make_float2(pq_nloz(q0), pq_nloz(q1))), u,
-                           add2(zh, make_float2(pq_nhi(q0.z, eb), pq_nhi(q1.z, eb))));
-    return accum2(s, S, fa, i, e0, e1, dx, dy, dz, pq_type(q0), pq_type(q1), pq_own(q0), pq_own(q1), ti, eps24,
+    const float2 ax = add2(xh, make_float2(pq_nhi(q0.x, eb), pq_nhi(q1.x, eb)));
+    const float2 ay = add2(yh, make_float2(pq_nhi(q0.y, eb), pq_nhi(q1.y, eb)));
+    const float2 az = add2(zh, make_float2(pq_nhi(q0.z, eb), pq_nhi(q1.z, eb)));
+    const float2 bx = add2(xl, make_float2(pq_nlox(q0), pq_nlox(q1)));
+    const float2 by = add2(yl, make_float2(pq_nloy(q0), pq_nloy(q1)));
+    const float2 bz = add2(zl, make_float2(pq_nloz(q0), pq_nloz(q1)));
+    const float2 dx = fma2(bx, u, ax), dy = fma2(by, u, ay), dz = fma2(bz, u, az);
+    const float2 r2 = r2_resid2(dx, dy, dz, ax, ay, az, bx, by, bz, u);
+    return accum2(s, S, fa, i, e0, e1, dx, dy, dz, r2, pq_type(q0), pq_type(q1), pq_own(q0), pq_own(q1), ti, eps24,
                   sig2, shr, tab, T, band, two);
   }
 
@@ -831,8 +831,8 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
 // gathered and decoded once and evaluated against both.  The i-forces are compensated sums in registers; the
 // reaction on j, summed over both members, goes out as one vector reduction (red.global.add.v4.f32) into facc.
 // The reference's newton3 functor call (SoAFunctorPair with newton3, LJFunctor.h:369-559) accumulates the j side
-// the same way, per pair; here the two members' shares are combined before the reduction.  k_n3_finish adds the
-// group's own part and the reductions, clears facc and runs the velocity half.  Globals use the newton3 energy
+// the same way, per pair; here the two members' shares are combined before the reduction.  The group adds its
+// own part to facc at the end; k_n3_finish reads the sums, clears facc and runs the velocity half.  Globals use the newton3 energy
 // factor (both members owned: the pair counts twice, LJFunctor.h:327-345).
 // ---------------------------------------------------------------------------------------------
 template <int GM, bool ONE_TYPE>
@@ -847,11 +847,10 @@ struct N3Acc {
   // LJ of the two pairs (i0, j) and (i1, j) from their displacements; returns minus the forces on i0, i1 (the
   // forces on j summed over the two are their sum) with the cutoff masks applied.  k0, k1: type-pair indices.
   __device__ __forceinline__ void lj2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i0,
-                                      int64_t j, int code, float2 dx, float2 dy, float2 dz, bool live1, int k0,
-                                      int k1, float eps24, float sig2, float shr,
+                                      int64_t j, int code, float2 dx, float2 dy, float2 dz, float2 r2, bool live1,
+                                      int k0, int k1, float eps24, float sig2, float shr,
                                       const float (*tab)[kMaxTypes * kMaxTypes], float band, float2 &px, float2 &py,
                                       float2 &pz, bool &any) {
-    const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
     bool m0 = r2.x <= fa.rc2f, m1 = live1 && r2.y <= fa.rc2f;
     const float2 off = add2(r2, dup2(-fa.rc2f));
     const bool n0 = fabsf(off.x) <= band, n1 = live1 && fabsf(off.y) <= band;
@@ -906,14 +905,16 @@ struct N3Acc {
       zl = fma2(dup2(-us.z), dup2(S.len_lo_u[2]), zl);
     }
     const float2 uu = dup2(u);
-    const float2 dx = fma2(add2(xl, dup2(pq_nlox(qj))), uu, add2(xh, dup2(pq_nhi(qj.x, eb))));
-    const float2 dy = fma2(add2(yl, dup2(pq_nloy(qj))), uu, add2(yh, dup2(pq_nhi(qj.y, eb))));
-    const float2 dz = fma2(add2(zl, dup2(pq_nloz(qj))), uu, add2(zh, dup2(pq_nhi(qj.z, eb))));
+    const float2 ax = add2(xh, dup2(pq_nhi(qj.x, eb))), ay = add2(yh, dup2(pq_nhi(qj.y, eb)));
+    const float2 az = add2(zh, dup2(pq_nhi(qj.z, eb)));
+    const float2 bx = add2(xl, dup2(pq_nlox(qj))), by = add2(yl, dup2(pq_nloy(qj))), bz = add2(zl, dup2(pq_nloz(qj)));
+    const float2 dx = fma2(bx, uu, ax), dy = fma2(by, uu, ay), dz = fma2(bz, uu, az);
+    const float2 r2 = r2_resid2(dx, dy, dz, ax, ay, az, bx, by, bz, uu);
     const int tj = ONE_TYPE ? 0 : pq_type(qj);
     float2 px, py, pz;
     bool any;
-    lj2(s, S, fa, i0, j, code, dx, dy, dz, live1, ti.x * T + tj, ti.y * T + tj, eps24, sig2, shr, tab, band, px, py,
-        pz, any);
+    lj2(s, S, fa, i0, j, code, dx, dy, dz, r2, live1, ti.x * T + tj, ti.y * T + tj, eps24, sig2, shr, tab, band, px,
+        py, pz, any);
     b[0] = add2(b[0], px);
     b[1] = add2(b[1], py);
     b[2] = add2(b[2], pz);
@@ -976,13 +977,14 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceA
   N3Acc<GM, ONE_TYPE> acc;
   // the group's own pair (i0, i1), once
   if (live0 && live1) {
-    const float dx = fmaf(iq[3].x - iq[3].y, u, iq[0].x - iq[0].y);
-    const float dy = fmaf(iq[4].x - iq[4].y, u, iq[1].x - iq[1].y);
-    const float dz = fmaf(iq[5].x - iq[5].y, u, iq[2].x - iq[2].y);
+    const float ax = iq[0].x - iq[0].y, ay = iq[1].x - iq[1].y, az = iq[2].x - iq[2].y;
+    const float bx = iq[3].x - iq[3].y, by = iq[4].x - iq[4].y, bz = iq[5].x - iq[5].y;
+    const float dx = fmaf(bx, u, ax), dy = fmaf(by, u, ay), dz = fmaf(bz, u, az);
+    const float r2 = r2_resid(dx, dy, dz, ax, ay, az, bx, by, bz, u);
     float2 px, py, pz;
     bool any;
-    acc.lj2(s, S, fa, i0, i0 + 1, kShiftNone, make_float2(dx, dx), make_float2(dy, dy), make_float2(dz, dz), false,
-            ti.x * T + ti.y, ti.x * T + ti.y, eps24, sig2, shr, tab, band, px, py, pz, any);
+    acc.lj2(s, S, fa, i0, i0 + 1, kShiftNone, make_float2(dx, dx), make_float2(dy, dy), make_float2(dz, dz),
+            make_float2(r2, r2), false, ti.x * T + ti.y, ti.x * T + ti.y, eps24, sig2, shr, tab, band, px, py, pz, any);
     // .x holds minus the force on i0; i1 gets the opposite
     acc.b[0] = make_float2(px.x, -px.x);
     acc.b[1] = make_float2(py.x, -py.x);
@@ -1022,9 +1024,14 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceA
   }
   acc.flush();
   if (inrange) {
-    // the group's own part of the members' forces, signs restored (exact)
-    s.fown[i0] = make_float4(acc.fc[0].x - acc.fs[0].x, acc.fc[1].x - acc.fs[1].x, acc.fc[2].x - acc.fs[2].x, 0.f);
-    s.fown[i0 + 1] = make_float4(acc.fc[0].y - acc.fs[0].y, acc.fc[1].y - acc.fs[1].y, acc.fc[2].y - acc.fs[2].y, 0.f);
+    // the group's own part of the members' forces (signs restored, exact), added to the reactions the other
+    // groups deliver: facc then holds each member's whole force for the finish kernel
+    if (live0)
+      atomicAdd(s.facc + i0, make_float4(acc.fc[0].x - acc.fs[0].x, acc.fc[1].x - acc.fs[1].x,
+                                         acc.fc[2].x - acc.fs[2].x, 0.f));
+    if (live1)
+      atomicAdd(s.facc + i0 + 1, make_float4(acc.fc[0].y - acc.fs[0].y, acc.fc[1].y - acc.fs[1].y,
+                                             acc.fc[2].y - acc.fs[2].y, 0.f));
   }
   if (GM > 0) {
     // newton3 energy factor 2 (both members and j owned: the engine runs this path on periodic systems only)
@@ -1050,45 +1057,60 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceA
   }
 }
 
-// After the newton3 force kernel: force = own part + reactions (each rounded once to FP64 from its float sum),
-// facc cleared for the next evaluation, then the epilogue of the particle-list kernel: velocity half, the next
-// step's position half and record when fused, and the kinetic energy per cluster.
+// After the newton3 force kernel: the force of each particle is its accumulator (own part and reactions, one
+// float sum each), widened to FP64; the accumulator is cleared for the next evaluation; then the epilogue of the
+// particle-list kernel: velocity half, the next step's position half and record when fused, and the kinetic
+// energy per cluster.  A streaming pass over the state: every load is issued before the first use, so that the
+// thread's requests are in flight together.
 template <int C, bool GLOB>
 __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool inrange = i < s.nslots;
   float ek = 0.f;
   if (inrange) {
-    const float4 a = s.fown[i], r = s.facc[i];
-    s.facc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int oi = s.own[i];
+    const int64_t k = i;
+    const float4 r = __ldcg(s.facc + k);
+    const int oi = s.own[k];
+    const int ti = s.type[k];
+    const double vx0 = s.vx[k], vy0 = s.vy[k], vz0 = s.vz[k];
+    double ox = 0, oy = 0, oz = 0, px = 0, py = 0, pz = 0;
+    if (fa.fuse_velocity) {
+      ox = s.ofx[k];
+      oy = s.ofy[k];
+      oz = s.ofz[k];
+    }
+    if (fa.fuse_positions) {
+      px = s.x[k];
+      py = s.y[k];
+      pz = s.z[k];
+    }
+    __stcg(s.facc + k, make_float4(0.f, 0.f, 0.f, 0.f));
     if (oi == 1) {
-      const int ti = s.type[i];
-      const double Fx = (double)a.x + (double)r.x, Fy = (double)a.y + (double)r.y, Fz = (double)a.z + (double)r.z;
-      s.fx[i] = Fx;
-      s.fy[i] = Fy;
-      s.fz[i] = Fz;
-      double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+      const double Fx = (double)r.x, Fy = (double)r.y, Fz = (double)r.z;
+      s.fx[k] = Fx;
+      s.fy[k] = Fy;
+      s.fz[k] = Fz;
+      double vx = vx0, vy = vy0, vz = vz0;
       if (fa.fuse_velocity) {
         const double h = fa.vv.h[ti];
-        vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
-        vy = __dadd_rn(vy, __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
-        vz = __dadd_rn(vz, __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
-        s.vx[i] = vx;
-        s.vy[i] = vy;
-        s.vz[i] = vz;
+        vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, ox), h));
+        vy = __dadd_rn(vy, __dmul_rn(__dadd_rn(Fy, oy), h));
+        vz = __dadd_rn(vz, __dmul_rn(__dadd_rn(Fz, oz), h));
+        s.vx[k] = vx;
+        s.vy[k] = vy;
+        s.vz[k] = vz;
         if (fa.fuse_positions) {
           const double c = fa.vv.c[ti], dt = fa.dt;
-          const double x1 = __dadd_rn(s.x[i], __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(Fx, c)));
-          const double y1 = __dadd_rn(s.y[i], __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(Fy, c)));
-          const double z1 = __dadd_rn(s.z[i], __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(Fz, c)));
-          s.xn[i] = x1;
-          s.yn[i] = y1;
-          s.zn[i] = z1;
-          s.ofx[i] = Fx;
-          s.ofy[i] = Fy;
-          s.ofz[i] = Fz;
-          s.pqn[i] = pq_pack(s.sysd[s.sys[i]], x1, y1, z1, ti, oi, s.err);
+          const double x1 = __dadd_rn(px, __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(Fx, c)));
+          const double y1 = __dadd_rn(py, __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(Fy, c)));
+          const double z1 = __dadd_rn(pz, __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(Fz, c)));
+          s.xn[k] = x1;
+          s.yn[k] = y1;
+          s.zn[k] = z1;
+          s.ofx[k] = Fx;
+          s.ofy[k] = Fy;
+          s.ofz[k] = Fz;
+          s.pqn[k] = pq_pack(s.sysd[s.sys[k]], x1, y1, z1, ti, oi, s.err);
         }
       }
       if (GLOB) {
@@ -1096,10 +1118,10 @@ __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) 
         ek = fa.vv.half_mass[ti] * fmaf(uz, uz, fmaf(uy, uy, ux * ux));
       }
     } else if (fa.fuse_positions) {
-      s.xn[i] = s.x[i];
-      s.yn[i] = s.y[i];
-      s.zn[i] = s.z[i];
-      s.pqn[i] = s.pq[i];
+      s.xn[k] = px;
+      s.yn[k] = py;
+      s.zn[k] = pz;
+      s.pqn[k] = s.pq[k];
     }
   }
   if (GLOB) {
@@ -1109,23 +1131,35 @@ __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) 
   }
 }
 
+template <int C, int MINB>
+static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, unsigned nb, cudaStream_t st) {
+  const bool glob = fa.calc_globals != 0;
+  if (s.ntypes == 1) {
+    if (glob)
+      k_lj_mixed_n3<C, 1, true, MINB><<<nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_n3<C, 0, true, MINB><<<nb, 128, 0, st>>>(s, fa);
+  } else {
+    if (glob)
+      k_lj_mixed_n3<C, 1, false, MINB><<<nb, 128, 0, st>>>(s, fa);
+    else
+      k_lj_mixed_n3<C, 0, false, MINB><<<nb, 128, 0, st>>>(s, fa);
+  }
+}
+
+// kernel variants (the tuner's choice): the register cap for 5 (variant 0), 6 (1) or 4 (2) resident blocks of
+// 128 threads per SM
 template <int C>
 static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st) {
   const int64_t ng = s.nslots / 2;
   const int64_t nb = (ng + 127) / 128;
   if (nb == 0) return;
-  const int gm = fa.calc_globals ? 1 : 0;
-  if (s.ntypes == 1) {
-    if (gm)
-      k_lj_mixed_n3<C, 1, true, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
-    else
-      k_lj_mixed_n3<C, 0, true, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
-  } else {
-    if (gm)
-      k_lj_mixed_n3<C, 1, false, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
-    else
-      k_lj_mixed_n3<C, 0, false, 5><<<(unsigned)nb, 128, 0, st>>>(s, fa);
-  }
+  if (s.variant == 1)
+    launch_n3_kernel<C, 6>(s, fa, (unsigned)nb, st);
+  else if (s.variant == 2)
+    launch_n3_kernel<C, 4>(s, fa, (unsigned)nb, st);
+  else
+    launch_n3_kernel<C, 5>(s, fa, (unsigned)nb, st);
   const int64_t nf = (s.nslots + 255) / 256;
   if (fa.calc_globals)
     k_n3_finish<C, true><<<(unsigned)nf, 256, 0, st>>>(s, fa);

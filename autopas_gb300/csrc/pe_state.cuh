@@ -75,10 +75,8 @@ struct DeviceState {
   int32_t *gl_count = nullptr;     // [groups]
   int gl_cap = 0;                  // a multiple of kPlistBlock
   int64_t gl_stride = 0;           // groups the list layout is sized for
-  // newton3 force sums: the group's own part (its compensated sums, written once per group member) and the
-  // reactions other groups add with vector reductions; the finish kernel adds both, clears facc and runs the
-  // velocity half
-  float4 *fown = nullptr;          // [slots]
+  // newton3 force sums: the reactions other groups add with vector reductions and the group's own part (its
+  // compensated sums), added at its end; the finish kernel reads them, clears facc and runs the velocity half
   float4 *facc = nullptr;          // [slots], zero between force evaluations
   // lists the force kernels read: the particle lists themselves, or the pruned inner lists
   uint32_t *fl_list = nullptr;

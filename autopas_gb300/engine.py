@@ -28,7 +28,7 @@ EXPORTS = [
     "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
     "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning", "pe_lj_forces_noalloc",
-    "pe_compute_atm",
+    "pe_compute_atm", "pe_update_ownership",
 ]
 
 
@@ -94,6 +94,7 @@ def load(path: str | None = None):
     L.pe_set_particles.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pe_update_positions.argtypes = [vp, vp, vp, vp]
     L.pe_rebuild.argtypes = [vp]
+    L.pe_update_ownership.argtypes = [vp, vp, C.POINTER(C.c_int)]
     L.pe_compute_forces.argtypes = [vp, vp]
     L.pe_get_forces.argtypes = [vp, vp, vp, vp]
     L.pe_get_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
@@ -210,6 +211,13 @@ class PairEngine:
 
     def rebuild(self):
         self._check(self._L.pe_rebuild(self._h))
+
+    def update_ownership(self, ownership):
+        """New OwnershipState values (user order); returns whether the lists stayed valid."""
+        o = np.ascontiguousarray(ownership, np.int8)
+        v = C.c_int()
+        self._check(self._L.pe_update_ownership(self._h, _ptr(o), C.byref(v)))
+        return bool(v.value)
 
     def compute_forces(self, want_globals=True):
         """Forces of the current positions; with want_globals the per-system globals are read back (a host

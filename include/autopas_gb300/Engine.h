@@ -62,6 +62,17 @@ class Engine {
     check(pe_update_positions(_h, x, y, z), "pe_update_positions");
   }
   void rebuild() { check(pe_rebuild(_h), "pe_rebuild"); }
+  /** New ownership states (order of the last setParticles); returns whether the lists stayed valid. */
+  bool updateOwnership(const int8_t *own) {
+    int valid = 0;
+    check(pe_update_ownership(_h, own, &valid), "pe_update_ownership");
+    return valid != 0;
+  }
+  pe_stats stats(bool reset = false) {
+    pe_stats st{};
+    check(pe_get_stats(_h, reset ? 1 : 0, &st), "pe_get_stats");
+    return st;
+  }
   std::vector<pe_globals> computeForces() {
     std::vector<pe_globals> g(_numSystems);
     check(pe_compute_forces(_h, g.data()), "pe_compute_forces");

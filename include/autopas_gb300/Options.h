@@ -17,8 +17,9 @@ namespace autopas_gb300 {
 /** The container option the engine registers (patched into ContainerOption::Value as gpuClusterLists). */
 enum class ContainerOption { gpuClusterLists };
 
-/** The traversal options the engine registers; gpu_tuned lets the engine's tuner pick between the other two. */
-enum class TraversalOption { gpu_cluster_pairs, gpu_particle_lists, gpu_tuned };
+/** The traversal options the engine registers; gpu_tuned lets the engine's tuner pick among the others (the
+ *  newton3 pair-group lists serve periodic systems of the mixed form only). */
+enum class TraversalOption { gpu_cluster_pairs, gpu_particle_lists, gpu_newton3_pair_groups, gpu_tuned };
 
 inline std::string toString(ContainerOption) { return "GPUClusterLists"; }
 inline std::string toString(TraversalOption t) {
@@ -27,12 +28,23 @@ inline std::string toString(TraversalOption t) {
       return "gpu_cluster_pairs";
     case TraversalOption::gpu_particle_lists:
       return "gpu_particle_lists";
+    case TraversalOption::gpu_newton3_pair_groups:
+      return "gpu_newton3_pair_groups";
     default:
       return "gpu_tuned";
   }
 }
 inline int toEngineTraversal(TraversalOption t) {
-  return t == TraversalOption::gpu_cluster_pairs ? 0 : (t == TraversalOption::gpu_particle_lists ? 1 : -1);
+  switch (t) {
+    case TraversalOption::gpu_cluster_pairs:
+      return 0;
+    case TraversalOption::gpu_particle_lists:
+      return 1;
+    case TraversalOption::gpu_newton3_pair_groups:
+      return 2;
+    default:
+      return -1;
+  }
 }
 
 /** IteratorBehavior bits with the reference's meaning (owned = 1, halo = 2, dummy = 4). */

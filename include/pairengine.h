@@ -136,6 +136,15 @@ int pe_set_particles(pe_engine *h, int64_t n, const double *x, const double *y, 
  * invalidating the lists (particles must not have moved more than skin/2 since the last rebuild). */
 int pe_update_positions(pe_engine *h, const double *x, const double *y, const double *z);
 
+/* Replaces: marking particles as dummies while the lists stay valid -- updateContainer(keepNeighborListsValid =
+ * true) through LeavingParticleCollector::collectParticlesAndMarkNonOwnedAsDummy
+ * (src/autopas/containers/LeavingParticleCollector.h:85-118) -- and reviving a halo particle in place
+ * (ParticleContainerInterface::updateHaloParticle, VerletClusterLists.h:194-212).  ownership: new
+ * OwnershipState of every particle of the last pe_set_particles, in that order.  The lists stay valid, except
+ * when a particle that was a dummy at the last rebuild becomes owned or halo (it is in no list): then the next
+ * force evaluation rebuilds them.  *lists_valid (may be NULL) receives whether they stayed valid. */
+int pe_update_ownership(pe_engine *h, const int8_t *ownership, int *lists_valid);
+
 /* Replaces: VerletClusterLists::rebuildNeighborLists (VerletClusterLists.h:779-800) -- binning by radix
  * sort on tower index, per-tower z order, clusters, bounding boxes and the cluster-pair lists. */
 int pe_rebuild(pe_engine *h);

@@ -1,7 +1,8 @@
 // C++ tests of the AutoPas-facing mirror (include/autopas_gb300/*.h) over the engine's C ABI.
 //   test_mirror cpu : host-side logic only (options, checks, error reporting without a GPU)
 //   test_mirror gpu : the reference's own force and globals known answers through the container pipeline
-//                     (ForceCalculationTest.cpp:45-95, LJFunctorTestGlobals.cpp:12-73) and mixed vs FP64
+//                     (ForceCalculationTest.cpp:45-95, LJFunctorTestGlobals.cpp:12-73), mixed vs FP64, and an
+//                     md-flexible-style loop that keeps the lists valid between rebuilds (buffers + remainder)
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -47,8 +48,38 @@ static void checkpoint_roundtrip() {
   std::remove(fn.c_str());
 }
 
+// LJFunctor::AoSFunctor known answer (LJFunctorTestNoGlobals.h:27-29): p1 = 0, p2 = (0.1, 0.2, 0.3), cutoff 1,
+// setParticleProperties(24, 1), abs tol 1e-7; with newton3 p2 gets the opposite force, without it none
+static void aos_functor_known_answer() {
+  const double expected[3] = {-4547248.8989645941, -9094497.7979291882, -13641746.696893783};
+  for (int n3 = 0; n3 < 2; ++n3) {
+    Functor f(1.0);
+    f.setParticleProperties(24, 1);
+    f.initTraversal();
+    MoleculeLJ a({0, 0, 0}, {0, 0, 0}, 0), b({0.1, 0.2, 0.3}, {0, 0, 0}, 1);
+    f.AoSFunctor(a, b, n3 == 1);
+    for (int d = 0; d < 3; ++d) {
+      CHECK(std::fabs(a.getF()[d] - expected[d]) <= 1e-7, "AoS newton3=%d dim %d: %.17g", n3, d, a.getF()[d]);
+      CHECK(std::fabs(b.getF()[d] - (n3 ? -expected[d] : 0.0)) <= 1e-7, "AoS newton3=%d j dim %d", n3, d);
+    }
+    f.endTraversal(n3 == 1);
+    CHECK(f.getNumInteractingPairs() == (n3 ? 1 : 0) || (n3 == 0 && f.getNumInteractingPairs() == 0),
+          "pair count newton3=%d: %lld", n3, (long long)f.getNumInteractingPairs());
+  }
+  // beyond the cutoff nothing happens; dummies are skipped
+  Functor f(1.0);
+  f.setParticleProperties(24, 1);
+  f.initTraversal();
+  MoleculeLJ a({0, 0, 0}, {0, 0, 0}, 0), b({1.1, 0, 0}, {0, 0, 0}, 1), c({0.1, 0, 0}, {0, 0, 0}, 2);
+  c.setOwnershipState(PE_DUMMY);
+  f.AoSFunctor(a, b, true);
+  f.AoSFunctor(a, c, true);
+  CHECK(a.getF()[0] == 0 && b.getF()[0] == 0 && c.getF()[0] == 0, "cutoff / dummy");
+}
+
 static void cpu_tests() {
   checkpoint_roundtrip();
+  aos_functor_known_answer();
   CHECK(toString(ContainerOption::gpuClusterLists) == "GPUClusterLists", "container name");
   CHECK(toString(TraversalOption::gpu_particle_lists) == "gpu_particle_lists", "traversal name");
   CHECK(toEngineTraversal(TraversalOption::gpu_tuned) == -1, "tuned traversal");
@@ -196,6 +227,122 @@ static void mixed_vs_fp64() {
   std::printf("mixed vs FP64 force RMS relative error: %.3e\n", rel);
 }
 
+// md-flexible's periodic halo copies of an owned particle: one image per shift whose coordinates lie within the
+// interaction length outside the box (RegularGridDecomposition.cpp:159-236), with the particle's own id
+static void add_images(GPUClusterLists<MoleculeLJ> &c, const MoleculeLJ &p, double box, double L) {
+  const auto r = p.getR();
+  for (int sx = -1; sx <= 1; ++sx)
+    for (int sy = -1; sy <= 1; ++sy)
+      for (int sz = -1; sz <= 1; ++sz) {
+        if (!sx && !sy && !sz) continue;
+        const int s[3] = {sx, sy, sz};
+        std::array<double, 3> q{};
+        bool near = true;
+        for (int d = 0; d < 3; ++d) {
+          q[d] = s[d] == 0 ? r[d] : r[d] + (s[d] > 0 ? box : -box);
+          near = near && q[d] >= -L && q[d] < box + L;
+        }
+        if (near) c.addHaloParticle(MoleculeLJ(q, p.getV(), p.getID(), p.getTypeId()));
+      }
+}
+
+// The container driven as LogicHandler drives it over many steps (LogicHandler.h:165-224, 1064-1165): velocity
+// Verlet on the host, updateContainer(keepNeighborListsValid) with a rebuild every 10 steps, leaving particles
+// wrapped and re-added, halo images re-added every step.  Between rebuilds the halo particles are revived in
+// place or buffered, leavers are buffered, and the buffers interact through AoSFunctor on the host.  Every step,
+// the forces on all owned particles (container and buffer) and Upot must equal a brute-force FP64 sum over the
+// same owned + halo set (1e-10 of the largest force; 1e-10 relative), and the engine may rebuild only when the
+// container asks it to.
+static void kept_lists_md_loop() {
+  const int nc = 5;
+  const double rho = 0.8442, a = std::cbrt(4.0 / rho), box = nc * a, rc = 2.5, skin = 0.3, L = rc + skin;
+  const double dt = 0.004;
+  std::mt19937_64 rng(11);
+  std::normal_distribution<double> g(0.0, std::sqrt(1.2));
+  GPUClusterLists<MoleculeLJ> c({0, 0, 0}, {box, box, box}, rc, skin, 8, PE_PRECISION_FP64);
+  const double base[4][3] = {{0, 0, 0}, {0.5, 0.5, 0}, {0.5, 0, 0.5}, {0, 0.5, 0.5}};
+  uint64_t id = 0;
+  for (int i = 0; i < nc; ++i)
+    for (int j = 0; j < nc; ++j)
+      for (int k = 0; k < nc; ++k)
+        for (auto &b : base)
+          c.addParticle(MoleculeLJ({(i + b[0]) * a + a / 4, (j + b[1]) * a + a / 4, (k + b[2]) * a + a / 4},
+                                   {g(rng), g(rng), g(rng)}, id++));
+  std::vector<MoleculeLJ> snapshot;
+  c.forEach([&](MoleculeLJ &p) { snapshot.push_back(p); }, IteratorBehavior::owned);
+  for (auto &p : snapshot) add_images(c, p, box, L);
+  Functor f(rc);
+  f.setParticleProperties(24, 1);
+  computeInteractionsPipeline(c, f);
+  int rebuildSteps = 1, bufferedSteps = 0;
+  size_t maxBuffered = 0;
+  for (int step = 1; step <= 30; ++step) {
+    c.forEach(
+        [&](MoleculeLJ &p) {
+          auto r = p.getR(), v = p.getV(), F = p.getF();
+          for (int d = 0; d < 3; ++d) r[d] += v[d] * dt + F[d] * (dt * dt / 2.0);
+          p.setR(r);
+          p.setOldF(F);
+          p.setF({0, 0, 0});
+        },
+        IteratorBehavior::owned);
+    const bool keep = step % 10 != 0;
+    rebuildSteps += keep ? 0 : 1;
+    auto leaving = c.updateContainer(keep);
+    for (auto &p : leaving) {
+      auto r = p.getR();
+      for (auto &v : r) v = v < 0 ? v + box : (v >= box ? v - box : v);
+      p.setR(r);
+      c.addParticle(p);
+    }
+    snapshot.clear();
+    c.forEach([&](MoleculeLJ &p) { snapshot.push_back(p); }, IteratorBehavior::owned);
+    for (auto &p : snapshot) add_images(c, p, box, L);
+    maxBuffered = std::max(maxBuffered, c.numBufferedParticles());
+    bufferedSteps += c.numBufferedParticles() > 0 ? 1 : 0;
+    computeInteractionsPipeline(c, f);
+    // brute-force reference over the same owned + halo set, with the functor's own host arithmetic
+    std::vector<MoleculeLJ> owned, all;
+    c.forEach([&](MoleculeLJ &p) { owned.push_back(p); }, IteratorBehavior::owned);
+    c.forEach([&](MoleculeLJ &p) { all.push_back(p); }, IteratorBehavior::ownedOrHalo);
+    Functor ref(rc);
+    ref.setParticleProperties(24, 1);
+    ref.initTraversal();
+    double fmax = 0, err = 0;
+    for (auto &o : owned) {
+      MoleculeLJ i = o;
+      i.setF({0, 0, 0});
+      for (auto &q : all) {
+        if (q.getID() == o.getID() && q.isOwned()) continue;
+        MoleculeLJ j = q;
+        ref.AoSFunctor(i, j, false);
+      }
+      for (int d = 0; d < 3; ++d) {
+        fmax = std::max(fmax, std::fabs(i.getF()[d]));
+        err = std::max(err, std::fabs(i.getF()[d] - o.getF()[d]));
+      }
+    }
+    ref.endTraversal(false);
+    CHECK(err <= 1e-10 * fmax, "step %d: max force difference %.3g of %.3g", step, err, fmax);
+    CHECK(std::fabs(f.getPotentialEnergy() - ref.getPotentialEnergy()) <= 1e-10 * std::fabs(ref.getPotentialEnergy()),
+          "step %d: Upot %.15g vs %.15g", step, f.getPotentialEnergy(), ref.getPotentialEnergy());
+    c.forEach(
+        [&](MoleculeLJ &p) {
+          auto v = p.getV();
+          const auto F = p.getF(), oF = p.getOldF();
+          for (int d = 0; d < 3; ++d) v[d] += (F[d] + oF[d]) * (dt / 2.0);
+          p.setV(v);
+        },
+        IteratorBehavior::owned);
+  }
+  const auto st = c.engine()->stats();
+  CHECK(bufferedSteps > 0 && maxBuffered > 0, "the loop must exercise the buffers (%d steps)", bufferedSteps);
+  CHECK(st.rebuilds == rebuildSteps + c.rebuildsRequested(), "engine rebuilds %lld, container rebuilds %d",
+        (long long)st.rebuilds, rebuildSteps);
+  std::printf("kept-lists loop: %d rebuilds in 31 force evaluations, buffers used in %d steps (max %zu particles)\n",
+              (int)st.rebuilds, bufferedSteps, maxBuffered);
+}
+
 int main(int argc, char **argv) {
   const std::string mode = argc > 1 ? argv[1] : "cpu";
   if (mode == "cpu") {
@@ -207,6 +354,7 @@ int main(int argc, char **argv) {
     force_calculation_test(std::pow(2.0, 1.0 / 6.0), 1.3, e0);
     globals_where_factor();
     mixed_vs_fp64();
+    kept_lists_md_loop();
   }
   std::printf("%s: %d failure(s)\n", mode.c_str(), failures);
   return failures == 0 ? 0 : 1;
