@@ -1,0 +1,31 @@
+"""A slab rank's force evaluation on the GPU: the engine with an explicit-halo system over the rank's owned
+particles and the halos the decomposition exchanged (here one rank, exchanging with itself) gives the periodic
+engine's forces: FP64 form within 1e-12 of the largest force, the same Upot, virial and pair count."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_engine_as_slab_rank_force_function(orc):
+    from autopas_gb300 import decomposition as D
+    from autopas_gb300 import engine
+    from autopas_gb300.build import build
+    build()
+    rc, skin = 2.5, 0.3
+    ell = 12.0
+    bmin, bmax = np.zeros(3), np.array([3 * ell, ell, ell])
+    pos = orc.gen_rsa(int(0.7 * 3 * ell ** 3), bmin, bmax, bmin, bmax, 0.8, seed=31)
+    dec = D.SlabDecomposition(0, 1, bmin, bmax, rc, skin)
+    halos = dec.exchange_halos(D.Comm(None), np.concatenate([pos, np.arange(len(pos))[:, None]], 1))
+    F, glob = D.engine_forces(engine, rc, skin, dec.lmin - rc - skin, dec.lmax + rc + skin,
+                              precision=engine.PRECISION_FP64)(pos, halos[:, :3])
+    e = engine.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=engine.PRECISION_FP64)
+    e.set_particles(pos)
+    g = e.compute_forces()[0]
+    R = e.forces()
+    e.close()
+    np.testing.assert_allclose(F, R, rtol=0, atol=1e-12 * np.abs(R).max())
+    assert glob[0] == pytest.approx(g["upot"], rel=1e-12)
+    assert glob[1] == pytest.approx(g["virial"], rel=1e-12)
+    assert glob[2] == g["num_pairs"]
