@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libpairengine.so")
 
-SOURCES = ["pe_engine.cu", "pe_build.cu", "pe_force.cu", "pe_noalloc.cu", "pe_atm.cu", "pe_inputs.cpp"]
+SOURCES = ["pe_engine.cu", "pe_build.cu", "pe_force.cu", "pe_noalloc.cu", "pe_atm.cu", "pe_peak.cu", "pe_inputs.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # the input generator is compiled without FMA contraction, as the oracle library compiles the same file, so that
 # both give the same positions for the same seed on any host

@@ -22,6 +22,7 @@ struct AtmArgs {
   float nu;
   float rc2f;
   double rc2;
+  double nu_fp64;
 };
 
 __device__ __forceinline__ void kahan(float &s, float &c, float v) {
@@ -76,8 +77,8 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
       ent = s.pl_list[plist_index(s.pl_stride, i, k)];
       const int64_t j = ent >> 5;
       const int code = ent & 31;
-      pq_disp(pi, S, code, s.pq[j], d.x, d.y, d.z);
-      d.w = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+      // the squared distance with the rounding of the displacement folded in (pq_disp_r2)
+      d.w = pq_disp_r2(pi, S, code, s.pq[j], d.x, d.y, d.z);
       keep = d.w <= aa.rc2f;
       if (fabsf(d.w - aa.rc2f) <= band) keep = img_dist2(s, S, i, kShiftNone, j, code) <= aa.rc2;
     }
@@ -182,6 +183,127 @@ __global__ void __launch_bounds__(kAtmWarps * 32) k_atm(DeviceState s, AtmArgs a
   }
 }
 
+// The plain FP64 form of the triplet kernel: the same walk as k_atm on FP64 image positions (x + s len as the
+// reference's halo copies hold them) with the reference's expressions in their order (AxilrodTellerMutoFunctor.h
+// :197-240, 268-286): the difference vectors IJ = r_j - r_i, JK = r_k - r_j, KI = r_i - r_k, dot products summed
+// component by component, the two divisions by the squared distances, and FP64 sums.  Each triplet is evaluated
+// once from each owned vertex (forceI only), so the per-vertex sums need no atomics.
+__device__ __forceinline__ double dot3d(double ax, double ay, double az, double bx, double by, double bz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
+
+__global__ void __launch_bounds__(kAtmWarps * 32) k_atm_fp64(DeviceState s, AtmArgs aa,
+                                                              double *__restrict__ slot_glob, int *__restrict__ err) {
+  __shared__ double4 nb[kAtmWarps][kAtmMaxNeigh];  // image position of each neighbour, |r_j - r_i|^2
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = blockIdx.x * (int64_t)kAtmWarps + w;
+  if (i >= s.nslots) return;
+  if (s.own[i] != 1) {
+    if (lane == 0) {
+      slot_glob[3 * i] = 0;
+      slot_glob[3 * i + 1] = 0;
+      slot_glob[3 * i + 2] = 0;
+    }
+    return;
+  }
+  const SysDev &S = s.sysd[s.sys[i]];
+  const double xi = s.x[i], yi = s.y[i], zi = s.z[i];
+  const int n = min(s.pl_count[i], s.pl_cap);
+  int m = 0;
+  bool overflow = false;
+  for (int base = 0; base < n; base += 32) {
+    const int k = base + lane;
+    bool keep = false;
+    double4 q = make_double4(0, 0, 0, 0);
+    if (k < n) {
+      const uint32_t ent = s.pl_list[plist_index(s.pl_stride, i, k)];
+      const int64_t j = ent >> 5;
+      int sx, sy, sz;
+      shift_of(ent & 31, sx, sy, sz);
+      q.x = image_coord(s.x[j], sx, S.len[0]);
+      q.y = image_coord(s.y[j], sy, S.len[1]);
+      q.z = image_coord(s.z[j], sz, S.len[2]);
+      const double ex = __dsub_rn(q.x, xi), ey = __dsub_rn(q.y, yi), ez = __dsub_rn(q.z, zi);
+      q.w = dot3d(ex, ey, ez, ex, ey, ez);
+      keep = q.w <= aa.rc2;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    const int pos = m + __popc(bal & ((1u << lane) - 1));
+    if (keep) {
+      if (pos < kAtmMaxNeigh)
+        nb[w][pos] = q;
+      else
+        overflow = true;
+    }
+    m += __popc(bal);
+  }
+  if (__any_sync(0xffffffffu, overflow)) {
+    if (lane == 0) atomicOr(err, 1);
+    return;
+  }
+  __syncwarp();
+  double Fx = 0, Fy = 0, Fz = 0, P = 0;
+  long long T = 0;
+  const double nu3 = 3.0 * (double)aa.nu_fp64;
+  int a = 0, off = lane;
+  while (a < m - 1 && off >= m - 1 - a) {
+    off -= m - 1 - a;
+    ++a;
+  }
+  while (a < m - 1) {
+    const int b = a + 1 + off;
+    const double4 pj = nb[w][a], pk = nb[w][b];
+    const double IJx = __dsub_rn(pj.x, xi), IJy = __dsub_rn(pj.y, yi), IJz = __dsub_rn(pj.z, zi);
+    const double JKx = __dsub_rn(pk.x, pj.x), JKy = __dsub_rn(pk.y, pj.y), JKz = __dsub_rn(pk.z, pj.z);
+    const double KIx = __dsub_rn(xi, pk.x), KIy = __dsub_rn(yi, pk.y), KIz = __dsub_rn(zi, pk.z);
+    const double d2IJ = pj.w, d2KI = dot3d(KIx, KIy, KIz, KIx, KIy, KIz);
+    const double d2JK = dot3d(JKx, JKy, JKz, JKx, JKy, JKz);
+    if (d2JK <= aa.rc2 && d2KI <= aa.rc2) {
+      const double all2 = __dmul_rn(__dmul_rn(d2IJ, d2JK), d2KI);
+      const double all5 = __dmul_rn(__dmul_rn(all2, all2), __dsqrt_rn(all2));
+      const double factor = __ddiv_rn(nu3, all5);
+      const double IJdotKI = dot3d(IJx, IJy, IJz, KIx, KIy, KIz);
+      const double IJdotJK = dot3d(IJx, IJy, IJz, JKx, JKy, JKz);
+      const double JKdotKI = dot3d(JKx, JKy, JKz, KIx, KIy, KIz);
+      const double allDots = __dmul_rn(__dmul_rn(IJdotKI, IJdotJK), JKdotKI);
+      const double cJK = __dmul_rn(IJdotKI, __dsub_rn(IJdotJK, JKdotKI));
+      const double cIJ = __dadd_rn(__dsub_rn(__dmul_rn(IJdotJK, JKdotKI), __dmul_rn(d2JK, d2KI)),
+                                   __ddiv_rn(__dmul_rn(5.0, allDots), d2IJ));
+      const double cKI = __dsub_rn(__dadd_rn(__dmul_rn(-IJdotJK, JKdotKI), __dmul_rn(d2IJ, d2JK)),
+                                   __ddiv_rn(__dmul_rn(5.0, allDots), d2KI));
+      Fx = __dadd_rn(Fx, __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(JKx, cJK), __dmul_rn(IJx, cIJ)), __dmul_rn(KIx, cKI)),
+                                   factor));
+      Fy = __dadd_rn(Fy, __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(JKy, cJK), __dmul_rn(IJy, cIJ)), __dmul_rn(KIy, cKI)),
+                                   factor));
+      Fz = __dadd_rn(Fz, __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(JKz, cJK), __dmul_rn(IJz, cIJ)), __dmul_rn(KIz, cKI)),
+                                   factor));
+      P = __dadd_rn(P, __dmul_rn(factor, __dsub_rn(all2, __dmul_rn(3.0, allDots))));
+      ++T;
+    }
+    off += 32;
+    while (a < m - 1 && off >= m - 1 - a) {
+      off -= m - 1 - a;
+      ++a;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Fx += __shfl_xor_sync(0xffffffffu, Fx, o);
+    Fy += __shfl_xor_sync(0xffffffffu, Fy, o);
+    Fz += __shfl_xor_sync(0xffffffffu, Fz, o);
+    P += __shfl_xor_sync(0xffffffffu, P, o);
+    T += __shfl_xor_sync(0xffffffffu, T, o);
+  }
+  if (lane == 0) {
+    s.fx[i] += Fx;
+    s.fy[i] += Fy;
+    s.fz[i] += Fz;
+    slot_glob[3 * i] = P;
+    slot_glob[3 * i + 1] = Fx * xi + Fy * yi + Fz * zi;
+    slot_glob[3 * i + 2] = (double)T;
+  }
+}
+
 // per-system sums over the system's slots in a fixed order, endTraversal post-processing (/3/3)
 __global__ void k_reduce_atm(DeviceState s, const int64_t *__restrict__ sys_cl_range, const double *__restrict__ slot_glob,
                              double *__restrict__ out) {
@@ -205,14 +327,20 @@ __global__ void k_reduce_atm(DeviceState s, const int64_t *__restrict__ sys_cl_r
   }
 }
 
-void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, const int64_t *sys_cl_range, double *out,
-                int *err, cudaStream_t st) {
+void launch_atm(DeviceState &s, int precision, double nu, double cutoff, double *slot_glob,
+                const int64_t *sys_cl_range, double *out, int *err, cudaStream_t st) {
   AtmArgs aa;
   aa.nu = (float)nu;
+  aa.nu_fp64 = nu;
   aa.rc2 = cutoff * cutoff;
   aa.rc2f = (float)aa.rc2;
   const int64_t nb = (s.nslots + kAtmWarps - 1) / kAtmWarps;
-  if (nb > 0) k_atm<<<(unsigned)nb, kAtmWarps * 32, 0, st>>>(s, aa, slot_glob, err);
+  if (nb > 0) {
+    if (precision == 0)
+      k_atm_fp64<<<(unsigned)nb, kAtmWarps * 32, 0, st>>>(s, aa, slot_glob, err);
+    else
+      k_atm<<<(unsigned)nb, kAtmWarps * 32, 0, st>>>(s, aa, slot_glob, err);
+  }
   if (s.nsys > 0) k_reduce_atm<<<s.nsys, 256, 0, st>>>(s, sys_cl_range, slot_glob, out);
 }
 

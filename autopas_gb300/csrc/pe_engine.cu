@@ -226,6 +226,7 @@ struct pe_engine {
   int64_t force_launches = 0;
   int64_t rebuilds = 0;
   cudaEvent_t timer_ev[2] = {nullptr, nullptr};
+  double force_cap = 0;  // > 0: forces capped at this magnitude before the integrator uses them
   // CUDA graph of one step without list rebuild, captured once per rebuild
   cudaGraphExec_t step_graph = nullptr;
   bool step_graph_valid = false;
@@ -611,6 +612,33 @@ __global__ void k_positions(DeviceState s, double dt, VVFactors vv) {
   }
   pack_one(s, i);
   if (s.prune) track_displacement(s, i, s.own[i] != 0);
+}
+
+// Caps the force on every owned particle at |F| <= fmax, keeping its direction (the capped-force soft start of
+// the benchmark's mixture): F *= fmax / |F| where |F| > fmax.
+__global__ void k_cap_forces(DeviceState s, double fmax) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.nslots || s.own[i] != 1) return;
+  const double fx = s.fx[i], fy = s.fy[i], fz = s.fz[i];
+  const double f2 = fx * fx + fy * fy + fz * fz;
+  if (!(f2 > fmax * fmax)) return;
+  const double k = fmax / sqrt(f2);
+  s.fx[i] = fx * k;
+  s.fy[i] = fy * k;
+  s.fz[i] = fz * k;
+}
+
+// Velocities scaled per type (the velocity scaling of md-flexible's Thermostat::apply, Thermostat.h:229-268)
+struct TypeFactors {
+  double f[kMaxTypes];
+};
+__global__ void k_scale_velocities(DeviceState s, TypeFactors tf) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= s.nslots || s.own[i] != 1) return;
+  const double k = tf.f[s.type[i]];
+  s.vx[i] *= k;
+  s.vy[i] *= k;
+  s.vz[i] *= k;
 }
 
 // velocity half when it is not fused into the force kernel
@@ -1151,7 +1179,7 @@ static int normalize_positions(pe_engine *h) {
 // position update) and three-body forces (which add to the force after the pair kernel) take the plain path.
 static bool fused_positions_ok(const pe_engine *h) {
   return h->precision != PE_PRECISION_FP64 && (h->traversal == 1 || h->traversal == 2) && !pruning(h) &&
-         !(h->cfg.atm_nu > 0);
+         !(h->cfg.atm_nu > 0) && !(h->force_cap > 0);
 }
 
 // The newton3 traversal (pair-group half lists) serves the mixed form on periodic systems without three-body
@@ -1214,6 +1242,13 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, b
   return h->cuda_check("force kernel");
 }
 
+static void cap_forces(pe_engine *h) {
+  if (!(h->force_cap > 0) || h->nslots == 0) return;
+  DeviceState s = h->state();
+  k_cap_forces<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, h->force_cap);
+  h->launches += 1;
+}
+
 // three-body buffers; allocated outside any stream capture (a graph capture may not allocate)
 static int ensure_atm(pe_engine *h) {
   const int ns = (int)h->sys.size();
@@ -1227,7 +1262,8 @@ static int atm_eval(pe_engine *h, double nu, double cutoff3) {
   PE_TRY(ensure_atm(h));
   DeviceState s = h->state();
   PE_CUDA(h, cudaMemsetAsync(h->atm_err.p, 0, sizeof(int), h->st));
-  launch_atm(s, nu, cutoff3, h->atm_slot.p, h->sys_cl_range.p, h->atm_out.p, h->atm_err.p, h->st);
+  launch_atm(s, h->precision == PE_PRECISION_FP64 ? 0 : 1, nu, cutoff3, h->atm_slot.p, h->sys_cl_range.p,
+             h->atm_out.p, h->atm_err.p, h->st);
   h->launches += 2;
   return h->cuda_check("three-body kernel");
 }
@@ -1624,6 +1660,29 @@ int pe_update_ownership(pe_engine *h, const int8_t *ownership, int *lists_valid)
   return h->cuda_check("update_ownership");
 }
 
+int pe_set_force_cap(pe_engine *h, double max_force) {
+  if (!h || max_force < 0 || std::isnan(max_force)) return PE_ERR_ARG;
+  h->force_cap = max_force;
+  h->step_graph_valid = false;
+  h->fused_graph_valid[0] = h->fused_graph_valid[1] = false;
+  return PE_OK;
+}
+
+int pe_scale_velocities(pe_engine *h, const double *factor) {
+  if (!h || !factor) return PE_ERR_ARG;
+  if (!h->have_particles) return h->fail(PE_ERR_STATE, "no particles");
+  TypeFactors tf{};
+  for (int t = 0; t < h->table.ntypes; ++t) {
+    if (!(factor[t] >= 0) || std::isinf(factor[t])) return h->fail(PE_ERR_ARG, "type %d factor %g", t, factor[t]);
+    tf.f[t] = factor[t];
+  }
+  PE_TRY(normalize_positions(h));
+  DeviceState s = h->state();
+  if (h->nslots > 0) k_scale_velocities<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s, tf);
+  h->launches += 1;
+  return h->cuda_check("scale_velocities");
+}
+
 int pe_rebuild(pe_engine *h) {
   if (!h) return PE_ERR_ARG;
   return do_rebuild(h);
@@ -1641,6 +1700,7 @@ int pe_compute_forces(pe_engine *h, pe_globals *globals) {
     h->launches += 1;
   }
   PE_TRY(force_eval(h, false, 0.0, true));
+  cap_forces(h);
   return read_globals(h, globals);
 }
 
@@ -1693,6 +1753,16 @@ int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, doub
 // ATM is on, else the velocity half is fused into the force kernel) and the globals reduction.
 static int step_forces(pe_engine *h, double dt, const VVFactors &vv, bool timed) {
   // with pruning on, the displacement since the last prune was tracked by k_positions
+  if (h->force_cap > 0) {
+    // capped forces: forces, the cap, then the velocity half
+    PE_TRY(force_eval(h, false, dt, timed));
+    if (h->cfg.atm_nu > 0) PE_TRY(atm_eval(h, h->cfg.atm_nu, h->cfg.atm_cutoff));
+    cap_forces(h);
+    DeviceState s2 = h->state();
+    if (h->nslots > 0) k_velocities<<<(unsigned)((h->nslots + 255) / 256), 256, 0, h->st>>>(s2, vv);
+    h->launches += 1;
+    return h->cuda_check("capped step");
+  }
   if (h->cfg.atm_nu > 0) {
     // the velocity update needs the total force: pair forces, then three-body forces, then velocities
     PE_TRY(force_eval(h, false, dt, timed));

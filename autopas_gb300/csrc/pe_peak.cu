@@ -1,0 +1,59 @@
+// pe_peak.cu -- the FP32 CUDA-core throughput of this GPU, measured: the denominator of the force kernels'
+// roofline (their work is FP32 arithmetic on the CUDA cores, not tensor-core contractions).
+//
+// Every thread runs 8 independent chains of packed FP32x2 fused multiply-adds (16 FLOP per instruction pair of
+// lanes), enough independent work per warp to keep the FMA pipes issuing back to back; the grid fills every SM
+// with 8 blocks of 256 threads.  Timed with CUDA events after a warm-up launch.
+#include <cuda_runtime.h>
+
+#include "../../include/pairengine.h"
+
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kUnroll = 16;
+
+__global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters, float a, float b) {
+  float2 x[kChains];
+  for (int q = 0; q < kChains; ++q) x[q] = make_float2(threadIdx.x + q, threadIdx.x - q);
+  const float2 A = make_float2(a, a), B = make_float2(b, b);
+  for (int k = 0; k < iters; ++k) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+#pragma unroll
+      for (int q = 0; q < kChains; ++q) x[q] = __ffma2_rn(x[q], A, B);
+    }
+  }
+  float s = 0.f;
+  for (int q = 0; q < kChains; ++q) s += x[q].x + x[q].y;
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the chains live
+}
+
+}  // namespace
+
+extern "C" int pe_measure_fp32_peak(double *tflops) {
+  if (!tflops) return PE_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PE_ERR_NO_DEVICE;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PE_ERR_CUDA;
+  const int blocks = sms * 8, threads = 256, iters = 2048;
+  float *out = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * blocks * threads) != cudaSuccess) return PE_ERR_OOM;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fma_peak<<<blocks, threads>>>(out, 64, 1.0001f, 0.5f);
+  cudaEventRecord(a);
+  k_fma_peak<<<blocks, threads>>>(out, iters, 1.0001f, 0.5f);
+  cudaEventRecord(b);
+  const cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (e != cudaSuccess || !(ms > 0)) return PE_ERR_CUDA;
+  const double flop = 2.0 * 2.0 * kChains * kUnroll * (double)iters * blocks * threads;
+  *tflops = flop / (ms * 1e-3) / 1e12;
+  return PE_OK;
+}

@@ -161,8 +161,9 @@ void launch_pair_dump(DeviceState &s, int which, int64_t cap, int64_t *a, int64_
                       unsigned long long *count, cudaStream_t st);
 
 // three-body forces (pe_atm.cu)
-void launch_atm(DeviceState &s, double nu, double cutoff, double *slot_glob, const int64_t *sys_cl_range, double *out,
-                int *err, cudaStream_t st);
+// precision 0: the plain FP64 form (k_atm_fp64), else FP32 triplet arithmetic (k_atm)
+void launch_atm(DeviceState &s, int precision, double nu, double cutoff, double *slot_glob,
+                const int64_t *sys_cl_range, double *out, int *err, cudaStream_t st);
 
 // forces (pe_force.cu)
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,

@@ -28,7 +28,7 @@ EXPORTS = [
     "pe_create", "pe_destroy", "pe_last_error", "pe_set_particles", "pe_update_positions", "pe_rebuild",
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
     "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning", "pe_lj_forces_noalloc",
-    "pe_compute_atm", "pe_update_ownership",
+    "pe_compute_atm", "pe_update_ownership", "pe_set_force_cap", "pe_scale_velocities", "pe_measure_fp32_peak",
 ]
 
 
@@ -95,6 +95,9 @@ def load(path: str | None = None):
     L.pe_update_positions.argtypes = [vp, vp, vp, vp]
     L.pe_rebuild.argtypes = [vp]
     L.pe_update_ownership.argtypes = [vp, vp, C.POINTER(C.c_int)]
+    L.pe_set_force_cap.argtypes = [vp, C.c_double]
+    L.pe_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    L.pe_scale_velocities.argtypes = [vp, vp]
     L.pe_compute_forces.argtypes = [vp, vp]
     L.pe_get_forces.argtypes = [vp, vp, vp, vp]
     L.pe_get_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
@@ -212,6 +215,34 @@ class PairEngine:
     def rebuild(self):
         self._check(self._L.pe_rebuild(self._h))
 
+    def set_force_cap(self, max_force):
+        """Caps each particle's force at max_force before integration (0: off)."""
+        self._check(self._L.pe_set_force_cap(self._h, float(max_force)))
+
+    def scale_velocities(self, factors):
+        """Velocities times factors[type] (a scalar applies to every type)."""
+        f = np.ascontiguousarray(np.broadcast_to(np.asarray(factors, np.float64), (len(self._eps),)))
+        self._check(self._L.pe_scale_velocities(self._h, _ptr(f)))
+
+    def soft_start(self, dt, nsteps, max_force, temperature, mass=1.0):
+        """Capped-force steps from overlapping positions, each followed by a velocity scaling to the target
+        temperature (the thermostat), then the cap is switched off.  Returns the globals of the last step."""
+        n_owned = None
+        self.set_force_cap(max_force)
+        self.compute_forces()
+        g = None
+        for _ in range(nsteps):
+            g = self.step(dt, 1)
+            ekin = sum(x["ekin"] for x in g)
+            if n_owned is None:
+                n_owned = self.n
+            t_now = 2.0 * ekin / (3.0 * n_owned)
+            if t_now > 0:
+                self.scale_velocities((temperature / t_now) ** 0.5)
+        self.set_force_cap(0.0)
+        self.compute_forces()
+        return g
+
     def update_ownership(self, ownership):
         """New OwnershipState values (user order); returns whether the lists stayed valid."""
         o = np.ascontiguousarray(ownership, np.int8)
@@ -313,6 +344,15 @@ def make_config(cutoff, skin=0.0, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,), shi
     cfg = PeConfig(cutoff, skin, len(eps), eps.ctypes.data_as(dp), sig.ctypes.data_as(dp), ms.ctypes.data_as(dp),
                    int(shift), PRECISION_FP64, 8, 0, int(dist_mode), 1, 1, 1, 1, 0.0, 0.0, 0, 0.0, 0)
     return cfg, (eps, sig, ms)
+
+
+def measure_fp32_peak():
+    """FP32 CUDA-core FMA throughput of the current device, TFLOP/s (pe_measure_fp32_peak)."""
+    v = C.c_double()
+    rc = load().pe_measure_fp32_peak(C.byref(v))
+    if rc != PE_OK:
+        raise EngineError(rc, "pe_measure_fp32_peak failed")
+    return v.value
 
 
 def lj_forces_noalloc(cfg, n, x, y, z, type_ptr, own_ptr, fx, fy, fz, globals_ptr, stream=None):

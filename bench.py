@@ -383,17 +383,21 @@ def run_ours(args):
         return 0
     peaks = measured_peaks()
     traffic = None
+    tr_source = None
     try:
-        # DRAM bytes per particle of the force kernel from an ncu capture of the same kernel on a smaller slab
+        # DRAM bytes per particle of the force evaluation (per traversal) from an ncu capture of the same kernels
+        # on a 400,000-particle slab, scaled by the particle count
         with open(os.path.join(ROOT, "profiles", "force_kernel_traffic.json")) as f:
-            tr = json.load(f)
-        if tr.get("kernel_prefix") and info["traversal"] == 1:
-            traffic = tr["forces_only"]["dram_bytes_per_particle"] * n
+            tr = json.load(f)["traversals"].get(str(info["traversal"]))
+        if tr:
+            traffic = tr["dram_bytes_per_particle"] * n
+            tr_source = tr["kernels"]
     except Exception:
         traffic = None
-    sm_max = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    # the FP32 CUDA-core peak of this GPU, measured now (the best of three ~10 ms runs)
+    fp32_peak = max(E.measure_fp32_peak() for _ in range(3))
     achieved = FLOP_PER_PAIR * pairs_per_launch / (force_ms_per_launch * 1e-3) / 1e12
+    kernel = {0: "k_lj_mixed_full", 1: "k_lj_mixed_plist", 2: "k_lj_mixed_n3 + k_n3_finish"}[info["traversal"]]
     line = {
         "metric": metric_name(), "value": value, "unit": "pair interactions/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -413,20 +417,20 @@ def run_ours(args):
         "tuning": tuning,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per forces-and-globals launch (the "
-                                     "launch force_kernel times), scaled by particle count from "
-                                     "profiles/force_kernel_traffic.json (same kernel, 400,000-particle slab)",
+                     "traffic_note": (f"dram__bytes_read.sum + dram__bytes_write.sum per force evaluation ({tr_source})"
+                                      ", scaled by particle count from profiles/force_kernel_traffic.json (the same "
+                                      "kernels on a 400,000-particle slab)") if traffic else None,
                      "hbm_view": ({"achieved_gbs": traffic / (force_ms_per_launch * 1e-3) / 1e9,
                                    "peak_gbs": peaks.get("hbm_gbs"),
                                    "frac": traffic / (force_ms_per_launch * 1e-3) / 1e9 / peaks["hbm_gbs"],
                                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)"}
                                   if traffic and peaks.get("hbm_gbs") else None),
-                     "kernel": ("k_lj_mixed_plist" if info["traversal"] == 1 else "k_lj_mixed_full") +
-                               f"<{info['cluster_size']}>",
-                     "algorithmic": f"{FLOP_PER_PAIR} FLOP per interacting pair (reference convention)",
-                     "peak_source": f"nominal CUDA-core FP32: 152 SM x 128 lanes x 2 FLOP x {sm_max:.0f} MHz "
-                                    "(MEASURED_PEAKS.json holds no CUDA-core figure; hbm/bf16 peaks do not bound "
-                                    "this kernel)"},
+                     "kernel": f"{kernel} (C = {info['cluster_size']})",
+                     "algorithmic": f"{FLOP_PER_PAIR} FLOP per interacting pair (reference convention), "
+                                    f"{pairs_per_launch:.0f} pairs per force evaluation",
+                     "peak_source": "measured in this run: FP32 CUDA-core FMA throughput (pe_measure_fp32_peak, "
+                                    "packed FP32x2 FMA chains on every SM, CUDA events) -- the force kernels' work "
+                                    "is CUDA-core FP32 arithmetic; MEASURED_PEAKS.json holds HBM and tensor figures"},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["kernel_launches"], "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -507,8 +511,10 @@ def run_mixture(args):
     """4,000,000 particles of 4 types (fractions 0.4/0.3/0.2/0.1, sigma 1.0/1.1/0.9/1.2, epsilon
     1.0/0.8/1.2/0.6), Lorentz-Berthelot mixing, shifted potential, rc = 2.5 x max sigma = 3.0, skin 0.3, density
     0.7 in a periodic cube, rebuild every 10; cluster size, traversal and kernel variant tuned.  Positions are
-    random sequential addition with a minimum distance of 0.8 (they stand in for the capped-force soft start);
-    FP32-mixed against the engine's FP64 form on the same configuration."""
+    uniform random (seeded), then 200 soft-start steps with every force capped at |F| <= 100 and the velocities
+    scaled to T* 1.0 after each step (the thermostat's scaling), run in the FP64 form (overlapping starts put pair
+    terms beyond FP32's range before the cap applies); the timed FP32-mixed run starts from the result and is
+    compared with the engine's FP64 form on the same configuration."""
     import numpy as np
     import __graft_entry__
     __graft_entry__.build()
@@ -518,11 +524,21 @@ def run_mixture(args):
     rho, rc, skin, reb = 0.7, 3.0, 0.3, 10
     side = (n / rho) ** (1.0 / 3.0)
     bmin, bmax = np.zeros(3), np.full(3, side)
-    pos = workloads.rsa(n, bmin, bmax, bmin, bmax, 0.8, seed=23)
     rng = np.random.default_rng(23)
+    pos = bmin + rng.uniform(0.0, 1.0, (n, 3)) * (bmax - bmin)
     types = rng.choice(4, size=len(pos), p=[0.4, 0.3, 0.2, 0.1]).astype(np.int32)
     vel = workloads.mb_velocities(len(pos), 1.0, seed=23)
     eps, sig = [1.0, 0.8, 1.2, 0.6], [1.0, 1.1, 0.9, 1.2]
+    # the capped-force soft start (FP64 form)
+    es = E.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=eps, sigma=sig, mass=[1, 1, 1, 1], shift=True,
+                      precision=E.PRECISION_FP64, rebuild_frequency=reb, cluster_size=8, traversal=1)
+    es.set_particles(pos, vel, types=types)
+    t0 = time.perf_counter()
+    es.soft_start(DT, 200, 100.0, 1.0)
+    t_soft = time.perf_counter() - t0
+    pos, vel = es.state()
+    pos = np.mod(pos, bmax)
+    es.close()
 
     def engine(prec, **kw):
         e = E.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=eps, sigma=sig, mass=[1, 1, 1, 1],
@@ -565,8 +581,9 @@ def run_mixture(args):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 LJ arithmetic on f64 state", "data": "synthetic",
             "config": {"workload": f"4-type LJ mixture: {len(pos)} particles, density {rho}, Lorentz-Berthelot, "
-                                   f"shifted, rc {rc}, skin {skin}, rebuild every {reb}, RSA positions dmin 0.8",
-                       "particles": int(len(pos))},
+                                   f"shifted, rc {rc}, skin {skin}, rebuild every {reb}, uniform random start + 200 "
+                                   "capped-force (|F| <= 100) soft-start steps at T* 1.0",
+                       "particles": int(len(pos)), "soft_start_s": t_soft},
             "fp64_gpu": {"value": st2["pairs_total"] / (ms2 * 1e-3), "unit": "pair interactions/s",
                          "ms_per_step": ms2 / 5},
             "force_error": err, "engine": {k: info[k] for k in ("cluster_size", "traversal", "num_list_entries")},
@@ -579,10 +596,12 @@ def run_mixture(args):
 def run_atm(args):
     """LJ plus Axilrod-Teller-Muto: 200,000 particles (an FCC lattice jittered by 0.02 with MB velocities at a
     liquid state point, where it melts; a jitter of 0.1 already puts some of the 2.4 million nearest-neighbour
-    pairs at overlapping distances) at
-    density 0.8, T* 1.0, nu 0.073, pair rc 2.5 with skin 0.3, triplet cutoff 2.5; whole MD steps with both
-    force kernels.  The three-body error is stated against the oracle's FP64 AxilrodTellerMuto restatement on a
-    4,000-particle system of the same density (the oracle's neighbour search is quadratic)."""
+    pairs at overlapping distances) at density 0.8, T* 1.0, nu 0.073, pair rc 2.5 with skin 0.3, triplet cutoff
+    2.5.  value: whole MD steps per second with both force kernels (FP32 triplet arithmetic, FP64 sums).  Beside
+    it, for the three-body evaluation alone on the same configuration: the FP32 kernel, the plain FP64 kernel and
+    the oracle's FP64 restatement on the host cores (cell list, OpenMP, each triplet evaluated from every owned
+    vertex), all as interacting triplets per second; and the FP32 kernel's error against that FP64 oracle on the
+    whole 200,000-particle system."""
     import numpy as np
     import __graft_entry__
     __graft_entry__.build()
@@ -607,31 +626,55 @@ def run_atm(args):
     e.close()
     if rank != 0:
         return 0
-    # three-body error against the oracle on a small system of the same kind
+    # the three-body evaluation alone (pair term off: epsilon 0), FP32 and FP64 kernels, same positions
+    three = {}
+    for name, prec in (("fp32", E.PRECISION_MIXED), ("fp64", E.PRECISION_FP64)):
+        e3 = E.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=prec, epsilon=[0.0], sigma=[1.0])
+        e3.set_particles(pos, vel)
+        e3.compute_forces()
+        f0 = e3.forces()
+        g = e3.compute_atm(nu, rc)[0]
+        F3 = e3.forces() - f0
+        reps = 3 if prec == E.PRECISION_MIXED else 1
+        e3.compute_forces()
+        e3.timer_start()
+        for _ in range(reps):
+            e3.compute_atm(nu, rc)
+        t3 = e3.timer_stop() / reps
+        e3.close()
+        three[name] = {"F": F3, "upot": g["upot"], "triplets": g["num_pairs"], "ms": t3}
     from oracle import oracle as orc
     orc.build()
-    p2, v2, b0, b1 = workloads.fcc_lj(10, rho, 1.0, seed=31)
-    p2 = np.mod(p2 + np.random.default_rng(31).normal(0, 0.02, p2.shape), b1)
-    e2 = E.PairEngine(rc, skin, (b0, b1), periodic=True, precision=E.PRECISION_MIXED, atm_nu=nu, atm_cutoff=rc)
-    e2.set_particles(p2, v2)
-    e2.compute_forces()
-    f_pair = e2.forces()
-    g3 = e2.compute_atm(nu, rc)[0]
-    f_tot = e2.forces()
-    e2.close()
-    allpos, own, _, _, _ = orc.periodic_system(p2, b0, b1, rc, skin)
-    R3, glob3, _ = orc.atm_forces(allpos, nu, rc, own=own)
-    R3 = R3[: len(p2)]
-    d3 = (f_tot - f_pair) - R3
-    err = {"force_rms_rel": float(np.sqrt((d3 ** 2).sum(1).mean() / (R3 ** 2).sum(1).mean())),
-           "upot3_rel": abs(g3["upot"] - glob3[0]) / abs(glob3[0]), "sample": f"{len(p2)} particles, same density"}
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    R3, glob3, vertex_evals = orc.atm_forces_cells(allpos, nu, rc, own=own, nthreads=nthreads)
+    t_cpu = time.perf_counter() - t0
+    R3 = R3[: len(pos)]
+    triplets = vertex_evals / 3.0  # each triplet was evaluated from each of its three owned vertices
+
+    def err(F, upot):
+        return {"force_rms_rel": float(np.sqrt(((F - R3) ** 2).sum(1).mean() / (R3 ** 2).sum(1).mean())),
+                "upot3_rel": abs(upot - glob3[0]) / abs(glob3[0])}
+    rate = lambda ms: triplets / (ms * 1e-3)  # noqa: E731
     line = {"metric": "MD steps/s, LJ + Axilrod-Teller-Muto (FP32 triplets, FP64 accumulation)",
             "value": nst / (ms * 1e-3), "unit": "steps/s", "n_gpus": world, "steps": nst, "warmup": args.warmup,
             "ms_per_step": ms / nst, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 triplet arithmetic, f64 sums", "data": "synthetic",
             "config": {"workload": f"{len(pos)} particles, FCC start (jitter 0.02), density {rho}, T* 1.0, nu {nu}, "
                                    f"pair rc {rc} skin {skin}, triplet cutoff {rc}", "particles": int(len(pos))},
-            "pair_interactions_per_s": st["pairs_total"] / (ms * 1e-3), "atm_error": err,
+            "pair_interactions_per_s": st["pairs_total"] / (ms * 1e-3),
+            "three_body": {"triplets": triplets,
+                           "fp32_gpu": {"ms": three["fp32"]["ms"], "triplets_per_s": rate(three["fp32"]["ms"]),
+                                        "error": err(three["fp32"]["F"], three["fp32"]["upot"])},
+                           "fp64_gpu": {"ms": three["fp64"]["ms"], "triplets_per_s": rate(three["fp64"]["ms"]),
+                                        "error": err(three["fp64"]["F"], three["fp64"]["upot"])},
+                           "speedup_fp32_vs_fp64": three["fp64"]["ms"] / three["fp32"]["ms"],
+                           "error_against": f"the oracle's FP64 AxilrodTellerMuto restatement on all {len(pos)} "
+                                            "particles"},
+            "cpu_baseline": {"value": triplets / t_cpu, "unit": "triplet interactions/s", "cores": nthreads,
+                             "kind": "port", "sample": f"one three-body evaluation of all {len(pos)} particles "
+                             f"(cell list, OpenMP, each triplet from every owned vertex), {t_cpu:.1f} s"},
             "gpu_launches": st["kernel_launches"]}
     print(json.dumps(line), flush=True)
     return 0

@@ -165,6 +165,15 @@ int pe_get_state(pe_engine *h, double *x, double *y, double *z, double *vx, doub
  * (pe_compute_forces) before the first step.  globals of the last step: [num_systems] or NULL. */
 int pe_step(pe_engine *h, double dt, int nsteps, pe_globals *globals);
 
+/* Caps the force on every owned particle at |F| <= max_force (direction kept) before the integrator uses it, in
+ * pe_step and in the forces pe_compute_forces reports; 0 switches the cap off.  With the thermostat below it gives
+ * a capped-force soft start from overlapping positions; no reference counterpart (md-flexible starts from its
+ * generators' non-overlapping objects). */
+int pe_set_force_cap(pe_engine *h, double max_force);
+/* Replaces: the velocity scaling of md-flexible's Thermostat::apply (examples/md-flexible/src/Thermostat.h:229-268):
+ * every owned particle's velocity times factor[type] ([num_types]). */
+int pe_scale_velocities(pe_engine *h, const double *factor);
+
 /* Replaces: computeInteractions(&atmFunctor) for AxilrodTellerMutoFunctor (AxilrodTellerMutoFunctor.h:186-385):
  * adds the three-body forces of every triplet with all distances <= cutoff3 to the current forces (call after
  * pe_compute_forces) and returns per system {Upot_ATM, virial_ATM = sum over owned i of F_i . r_i, -, -, -,
@@ -259,6 +268,11 @@ int pe_get_tuning(pe_engine *h, int cap, pe_tuning_entry *entries, int *count, i
 int pe_lj_forces_noalloc(const pe_config *cfg, int64_t n, const double *x, const double *y, const double *z,
                          const int32_t *type, const int8_t *ownership, double *fx, double *fy, double *fz,
                          double *globals, void *stream);
+
+/* A measurement utility with no counterpart in the reference: the FP32 CUDA-core FMA throughput of the current
+ * device at its present clock (packed FP32x2 fused multiply-adds on every SM, CUDA-event timed), in TFLOP/s --
+ * the denominator of the force kernels' roofline.  Takes about 10 ms of device time. */
+int pe_measure_fp32_peak(double *tflops);
 
 /* Device timer on the engine's stream: op 0 records a start event; op 1 records a stop event, waits for it and
  * returns the elapsed milliseconds between the two in *ms. */

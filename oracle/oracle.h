@@ -72,6 +72,12 @@ double orc_dist2(double dx, double dy, double dz, int mode);
 int orc_count_interacting(int64_t n, const double *x, const double *y, const double *z, const int8_t *own,
                           double rc, int dist_mode, int64_t *out);
 
+/* ATM forces of the owned particles (owned + halo input) through a cell list, OpenMP over owned particles, each
+ * triplet evaluated from every owned vertex without newton3 (full size; see atm_oracle.c). */
+int64_t orc_atm_forces_cells(int64_t n, const double *x, const double *y, const double *z, const int8_t *own,
+                             double nu, double cutoff, int nthreads, double *fx, double *fy, double *fz,
+                             double *glob);
+
 /* Seeded random sequential addition (autopas_gb300/csrc/pe_inputs.cpp, compiled into this library from the
  * same source with contraction off, so both libraries give the same positions for the same seed). */
 int64_t pe_gen_rsa(int64_t existing, int64_t n, const double *bmin, const double *bmax, const double *rmin,

@@ -98,6 +98,9 @@ def lib():
         L.orc_count_interacting.argtypes = [C.c_int64, _dp, _dp, _dp, _i8p, C.c_double, C.c_int, _i64p]
         L.pe_gen_rsa.restype = C.c_int64
         L.pe_gen_rsa.argtypes = [C.c_int64, C.c_int64, _dp, _dp, _dp, _dp, C.c_double, C.c_uint64, C.c_int64, _dp]
+        L.orc_atm_forces_cells.restype = C.c_int64
+        L.orc_atm_forces_cells.argtypes = [C.c_int64, _dp, _dp, _dp, _i8p, C.c_double, C.c_double, C.c_int, _dp, _dp,
+                                           _dp, _dp]
         L.orc_cpu_lc_c08.restype = C.c_int64
         L.orc_cpu_lc_c08.argtypes = [C.c_int64, _dp, _dp, _dp, _i32p, _i8p, C.POINTER(LJParams), C.c_double,
                                      C.c_int, _dp, _dp, _dp, _dp]
@@ -294,6 +297,19 @@ def atm_forces(pos, nu, cutoff, own=None):
     fx, fy, fz = np.zeros(n), np.zeros(n), np.zeros(n)
     glob = np.zeros(2)
     hits = lib().orc_atm_forces(n, x, y, z, own, nu, cutoff, fx, fy, fz, glob)
+    return np.stack([fx, fy, fz], 1), glob, hits
+
+
+def atm_forces_cells(pos, nu, cutoff, own=None, nthreads=0):
+    """ATM forces on the owned particles via a cell list (OpenMP).  Returns (F, glob[2], triplet evaluations
+    summed over owned vertices)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    n = len(pos)
+    own = np.full(n, ORC_OWNED, np.int8) if own is None else _c(own, np.int8)
+    x, y, z = (np.ascontiguousarray(pos[:, d]) for d in range(3))
+    fx, fy, fz = np.zeros(n), np.zeros(n), np.zeros(n)
+    glob = np.zeros(2)
+    hits = lib().orc_atm_forces_cells(n, x, y, z, own, nu, cutoff, int(nthreads), fx, fy, fz, glob)
     return np.stack([fx, fy, fz], 1), glob, hits
 
 

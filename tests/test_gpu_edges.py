@@ -127,3 +127,34 @@ def test_default_distance_form_is_the_references_contraction(eng_mod, orc, strad
             ia, _ = orc.interacting_set(pos, rc)
             assert g["num_pairs"] == len(ia), (which, prec)
             e.close()
+
+
+def test_capped_force_soft_start_separates_overlaps(eng_mod):
+    """Uniform random positions (overlapping pairs) at density 0.7: forces reported under the cap never exceed it,
+    and 200 capped-force steps with the velocity scaling (FP64 form) leave no pair closer than 0.7 sigma and a
+    finite, uncapped force field at the thermostat's temperature."""
+    rng = np.random.default_rng(5)
+    n, rho = 3000, 0.7
+    side = (n / rho) ** (1.0 / 3.0)
+    bmin, bmax = np.zeros(3), np.full(3, side)
+    pos = rng.uniform(0, side, (n, 3))
+    vel = rng.normal(0, 1.0, (n, 3))
+    e = eng_mod.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_FP64,
+                           rebuild_frequency=10, traversal=1)
+    e.set_particles(pos, vel)
+    e.set_force_cap(100.0)
+    e.compute_forces()
+    F = e.forces()
+    assert np.sqrt((F ** 2).sum(1)).max() <= 100.0 * (1 + 1e-12)
+    e.soft_start(0.002, 200, 100.0, 1.0)
+    P, V = e.state()
+    F = e.forces()
+    e.close()
+    assert np.all(np.isfinite(F))
+    d = P[:, None, :] - P[None, :, :]
+    d -= side * np.round(d / side)
+    r2 = (d ** 2).sum(-1)
+    np.fill_diagonal(r2, np.inf)
+    assert np.sqrt(r2.min()) > 0.7
+    t = (V ** 2).sum() / (3 * n)
+    assert 0.5 < t < 2.0

@@ -424,6 +424,52 @@ def test_atm_periodic_liquid_matches_oracle(eng_mod, orc):
     assert g["upot"] == pytest.approx(glob[0], rel=1e-5)
 
 
+def test_atm_fp64_form_matches_oracle(eng_mod, orc):
+    """The plain FP64 triplet kernel against the oracle's FP64 AxilrodTellerMuto restatement (cell-list form,
+    checked against the quadratic one in the oracle tests): forces within 1e-12 of the largest, Upot and virial
+    within 1e-12 relative."""
+    from autopas_gb300 import workloads
+    pos, vel, bmin, bmax = workloads.fcc_lj(6, 0.8, 1.0, seed=3)
+    pos = np.mod(pos + np.random.default_rng(3).normal(0, 0.05, pos.shape), bmax)
+    rc, skin, nu = 2.5, 0.3, 0.073
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=[0.0], sigma=[1.0],
+                           precision=eng_mod.PRECISION_FP64)
+    e.set_particles(pos, vel)
+    e.compute_forces()
+    g = e.compute_atm(nu, rc)[0]
+    F = e.forces()
+    e.close()
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.atm_forces_cells(allpos, nu, rc, own=own)
+    R = R[: len(pos)]
+    np.testing.assert_allclose(F, R, rtol=0, atol=1e-12 * np.abs(R).max())
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-12)
+    assert g["virial"] == pytest.approx(glob[1], rel=1e-12)
+
+
+def test_atm_mixed_form_error_on_32k_particles(eng_mod, orc):
+    """The FP32 triplet kernel on a 32,000-particle melted FCC liquid (density 0.8, nu 0.073, triplet cutoff
+    2.5): three-body force RMS error relative to the RMS three-body force <= 1e-6, three-body energy within 1e-6."""
+    from autopas_gb300 import workloads
+    pos, vel, bmin, bmax = workloads.fcc_lj(20, 0.8, 1.0, seed=29)
+    pos = np.mod(pos + np.random.default_rng(29).normal(0, 0.02, pos.shape), bmax)
+    rc, skin, nu = 2.5, 0.3, 0.073
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, epsilon=[0.0], sigma=[1.0])
+    e.set_particles(pos, vel)
+    e.compute_forces()
+    g = e.compute_atm(nu, rc)[0]
+    F = e.forces()
+    e.close()
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.atm_forces_cells(allpos, nu, rc, own=own)
+    R = R[: len(pos)]
+    err = rel_rms(F, R)
+    print(f"ATM mixed form on {len(pos)} particles: force RMS error {err:.3g}, "
+          f"energy {abs(g['upot'] - glob[0]) / abs(glob[0]):.3g}")
+    assert err <= 1e-6
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
+
+
 def test_graph_replay_matches_eager_steps(eng_mod):
     """Steps replayed from the captured CUDA graph give the same bits as steps launched one kernel at a time."""
     pos, vel, bmin, bmax = liquid(5, seed=21)

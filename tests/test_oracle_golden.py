@@ -261,6 +261,20 @@ def test_contraction_changes_the_pair_sets_of_straddling_pairs(orc, straddling_p
         assert len(a_s) != len(a_f) or not np.array_equal(a_s, a_f)
 
 
+def test_atm_cell_list_oracle_matches_the_quadratic_one(orc):
+    """The cell-list ATM restatement (full-size checks, CPU baseline) against the quadratic enumeration."""
+    from autopas_gb300 import workloads
+    p, v, b0, b1 = workloads.fcc_lj(6, 0.8, 1.0, seed=31)
+    p = np.mod(p + np.random.default_rng(31).normal(0, 0.03, p.shape), b1)
+    allpos, own, _, _, _ = orc.periodic_system(p, b0, b1, 2.5, 0.3)
+    R, g, _ = orc.atm_forces(allpos, 0.073, 2.5, own=own)
+    R2, g2, _ = orc.atm_forces_cells(allpos, 0.073, 2.5, own=own)
+    n = len(p)
+    np.testing.assert_allclose(R2[:n], R[:n], rtol=0, atol=1e-13 * np.abs(R[:n]).max())
+    assert g2[0] == pytest.approx(g[0], rel=1e-13)
+    assert g2[1] == pytest.approx(g[1], rel=1e-11)  # the virial sum cancels: 11.5 from terms of ~1e3
+
+
 def test_tower_grid_geometry(orc):
     """ClusterTowerBlock2D::estimateOptimalGridSideLength restated (side, towers incl. halo)."""
     side, num, halo = orc.tower_grid([0, 0, 0], [33.0, 34.0, 35.0], 32000, 4, 2.8)
