@@ -26,6 +26,8 @@
 //    repeat the cutoff test in FP64 so that the interacting set equals the FP64 one.
 #include "pe_state.cuh"
 
+#include <algorithm>
+
 namespace pe {
 
 struct ForceArgs {
@@ -832,7 +834,8 @@ __global__ void __launch_bounds__(128) k_lj_fp64_plist(DeviceState s, ForceArgs 
 // reaction on j, summed over both members, goes out as one vector reduction (red.global.add.v4.f32) into facc.
 // The reference's newton3 functor call (SoAFunctorPair with newton3, LJFunctor.h:369-559) accumulates the j side
 // the same way, per pair; here the two members' shares are combined before the reduction.  The group adds its
-// own part to facc at the end; k_n3_finish reads the sums, clears facc and runs the velocity half.  Globals use the newton3 energy
+// own part to facc at the end; the finish of a slot (n3_finish_slot) reads the sum, clears facc and runs the velocity
+// half.  Globals use the newton3 energy
 // factor (both members owned: the pair counts twice, LJFunctor.h:327-345).
 // ---------------------------------------------------------------------------------------------
 template <int GM, bool ONE_TYPE>
@@ -932,20 +935,13 @@ struct N3Acc {
   }
 };
 
-template <int C, int GM, bool ONE_TYPE, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceArgs fa) {
+// One group's force work: the group's own pair, its list walk, its own part into facc and the cluster globals.
+// Every thread of a warp calls it (the globals are reduced over the groups of a cluster with shuffles).
+template <int C, int GM, bool ONE_TYPE>
+__device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &fa, int64_t g,
+                                         const float (*tab)[kMaxTypes * kMaxTypes]) {
   constexpr int GL = C / 2;  // groups per cluster
-  __shared__ float tab[3][kMaxTypes * kMaxTypes];
   const int T = s.ntypes;
-  if (!ONE_TYPE) {
-    for (int q = threadIdx.x; q < T * T; q += blockDim.x) {
-      tab[0][q] = s.types->eps24f[q];
-      tab[1][q] = s.types->sig2f[q];
-      tab[2][q] = s.types->shrf[q];
-    }
-    __syncthreads();
-  }
-  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i0 = 2 * g;
   const bool inrange = i0 < s.nslots;
   uint4 q0 = make_uint4(0u, 0u, 0u, 0u), q1 = q0;
@@ -1057,14 +1053,14 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceA
   }
 }
 
-// After the newton3 force kernel: the force of each particle is its accumulator (own part and reactions, one
+// After the force work of the slots' groups: the force of each particle is its accumulator (own part and reactions, one
 // float sum each), widened to FP64; the accumulator is cleared for the next evaluation; then the epilogue of the
 // particle-list kernel: velocity half, the next step's position half and record when fused, and the kinetic
 // energy per cluster.  A streaming pass over the state: every load is issued before the first use, so that the
 // thread's requests are in flight together.
+// The finish of one slot (all threads of a warp call it: the kinetic energy is reduced over a cluster's slots).
 template <int C, bool GLOB>
-__global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const ForceArgs &fa, int64_t i) {
   const bool inrange = i < s.nslots;
   float ek = 0.f;
   if (inrange) {
@@ -1131,40 +1127,155 @@ __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// The newton3 evaluation as one wavefront.  A group's list holds only j of later clusters (or later in its own
+// cluster), so every reaction on slot j comes from a group at or below j: once the force tiles (128 groups each)
+// up to j's tile are complete, j's force is final.  Resident blocks claim force tiles in increasing order from a
+// counter; after a tile the block publishes it (its reductions fenced first) and advances the count of leading
+// complete tiles; between force tiles a block claims a finish tile (256 slots) when that tile lies below the
+// complete prefix.  No block ever waits: a block that finds neither kind of work returns, and k_n3_finish_tail
+// finishes every tile nobody claimed.  The FP64 finish work (velocity half, next positions) so runs beside the
+// FP32 pair work of other warps instead of in a pass of its own.
+// ---------------------------------------------------------------------------------------------
+constexpr int kN3Tile = 128;  // groups per force tile; a finish tile is the tile's 256 slots
+
+struct N3Wave {
+  unsigned int next_force;
+  unsigned int next_finish;
+  unsigned int prefix;  // leading force tiles complete
+  unsigned int pad;
+  unsigned int *done;   // [tiles]
+};
+
+template <int C, int GM, bool ONE_TYPE, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3_wave(DeviceState s, ForceArgs fa, N3Wave *w,
+                                                                 unsigned int tiles) {
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  __shared__ unsigned int task, kind;  // kind 0: none, 1: force tile, 2: finish tile
+  if (!ONE_TYPE) {
+    for (int q = threadIdx.x; q < s.ntypes * s.ntypes; q += blockDim.x) {
+      tab[0][q] = s.types->eps24f[q];
+      tab[1][q] = s.types->sig2f[q];
+      tab[2][q] = s.types->shrf[q];
+    }
+  }
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      kind = 0;
+      // a ready finish tile first (claimed only while it lies below the complete prefix; the loop ends when the
+      // claim succeeds or no tile is ready, and every failed attempt means another block claimed one)
+      for (int attempt = 0; attempt < 64; ++attempt) {
+        const unsigned int p = atomicAdd(&w->prefix, 0u);
+        const unsigned int f = atomicAdd(&w->next_finish, 0u);
+        if (f >= p) break;
+        if (atomicCAS(&w->next_finish, f, f + 1) == f) {
+          kind = 2;
+          task = f;
+          break;
+        }
+      }
+      if (kind == 0) {
+        const unsigned int t = atomicAdd(&w->next_force, 1u);
+        if (t < tiles) {
+          kind = 1;
+          task = t;
+        }
+      }
+    }
+    __syncthreads();
+    const unsigned int k = kind, t = task;
+    if (k == 0) return;
+    if (k == 1) {
+      n3_group<C, GM, ONE_TYPE>(s, fa, (int64_t)t * kN3Tile + threadIdx.x, tab);
+      __threadfence();  // this thread's reductions before the tile is published
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        atomicExch(&w->done[t], 1u);
+        // advance the complete prefix over every published tile (each pass of the loop advances it by one or
+        // finds another block advancing it)
+        for (unsigned int it = 0; it < tiles; ++it) {
+          const unsigned int p = atomicAdd(&w->prefix, 0u);
+          if (p >= tiles || atomicAdd(&w->done[p], 0u) == 0u) break;
+          atomicCAS(&w->prefix, p, p + 1);
+        }
+      }
+    } else {
+      __threadfence();
+      const int64_t base = (int64_t)t * (2 * kN3Tile);
+      n3_finish_slot<C, GM != 0>(s, fa, base + threadIdx.x);
+      n3_finish_slot<C, GM != 0>(s, fa, base + kN3Tile + threadIdx.x);
+    }
+  }
+}
+
+// The finish tiles no block of the wavefront claimed: [next_finish, tiles), grid-stride.
+template <int C, bool GLOB>
+__global__ void __launch_bounds__(256) k_n3_finish_tail(DeviceState s, ForceArgs fa, const N3Wave *w) {
+  const int64_t first = (int64_t)w->next_finish * (2 * kN3Tile);
+  for (int64_t i = first + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i - threadIdx.x < s.nslots;
+       i += (int64_t)gridDim.x * blockDim.x)
+    n3_finish_slot<C, GLOB>(s, fa, i);
+}
+
+template <int C, int GM, bool ONE_TYPE, int MINB>
+static void launch_n3_wave(DeviceState &s, const ForceArgs &fa, unsigned int tiles, cudaStream_t st) {
+  static int resident = 0;  // blocks of this instantiation that fit on the GPU at once
+  if (resident == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lj_mixed_n3_wave<C, GM, ONE_TYPE, MINB>, 128, 0);
+    resident = std::max(1, sms * std::max(1, per_sm));
+  }
+  const unsigned int grid = std::min<unsigned int>(tiles, (unsigned int)resident);
+  k_lj_mixed_n3_wave<C, GM, ONE_TYPE, MINB><<<grid, 128, 0, st>>>(s, fa, reinterpret_cast<N3Wave *>(s.wave), tiles);
+}
+
 template <int C, int MINB>
-static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, unsigned nb, cudaStream_t st) {
+static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, unsigned int tiles, cudaStream_t st) {
   const bool glob = fa.calc_globals != 0;
   if (s.ntypes == 1) {
     if (glob)
-      k_lj_mixed_n3<C, 1, true, MINB><<<nb, 128, 0, st>>>(s, fa);
+      launch_n3_wave<C, 1, true, MINB>(s, fa, tiles, st);
     else
-      k_lj_mixed_n3<C, 0, true, MINB><<<nb, 128, 0, st>>>(s, fa);
+      launch_n3_wave<C, 0, true, MINB>(s, fa, tiles, st);
   } else {
     if (glob)
-      k_lj_mixed_n3<C, 1, false, MINB><<<nb, 128, 0, st>>>(s, fa);
+      launch_n3_wave<C, 1, false, MINB>(s, fa, tiles, st);
     else
-      k_lj_mixed_n3<C, 0, false, MINB><<<nb, 128, 0, st>>>(s, fa);
+      launch_n3_wave<C, 0, false, MINB>(s, fa, tiles, st);
   }
 }
 
 // kernel variants (the tuner's choice): the register cap for 5 (variant 0), 6 (1) or 4 (2) resident blocks of
-// 128 threads per SM
+// 128 threads per SM.  The wavefront's counters are cleared first (stream-ordered memsets, captured with the step
+// graphs), the tail kernel finishes what the wavefront left.
 template <int C>
 static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st) {
   const int64_t ng = s.nslots / 2;
-  const int64_t nb = (ng + 127) / 128;
-  if (nb == 0) return;
+  const unsigned int tiles = (unsigned int)((ng + kN3Tile - 1) / kN3Tile);
+  if (tiles == 0) return;
+  cudaMemsetAsync(s.wave, 0, 4 * sizeof(unsigned int), st);
+  cudaMemsetAsync(s.wave_done, 0, sizeof(unsigned int) * tiles, st);
   if (s.variant == 1)
-    launch_n3_kernel<C, 6>(s, fa, (unsigned)nb, st);
+    launch_n3_kernel<C, 6>(s, fa, tiles, st);
   else if (s.variant == 2)
-    launch_n3_kernel<C, 4>(s, fa, (unsigned)nb, st);
+    launch_n3_kernel<C, 4>(s, fa, tiles, st);
   else
-    launch_n3_kernel<C, 5>(s, fa, (unsigned)nb, st);
-  const int64_t nf = (s.nslots + 255) / 256;
+    launch_n3_kernel<C, 5>(s, fa, tiles, st);
+  static int tail_grid = 0;
+  if (tail_grid == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    tail_grid = std::max(1, sms * 4);
+  }
+  const N3Wave *w = reinterpret_cast<const N3Wave *>(s.wave);
   if (fa.calc_globals)
-    k_n3_finish<C, true><<<(unsigned)nf, 256, 0, st>>>(s, fa);
+    k_n3_finish_tail<C, true><<<tail_grid, 256, 0, st>>>(s, fa, w);
   else
-    k_n3_finish<C, false><<<(unsigned)nf, 256, 0, st>>>(s, fa);
+    k_n3_finish_tail<C, false><<<tail_grid, 256, 0, st>>>(s, fa, w);
 }
 
 template <int C>

@@ -150,8 +150,10 @@ class SlabDecomposition:
 
 
 def engine_forces(engine_module, cutoff, skin, lmin, lmax, precision=1, **kw):
-    """A force function on the GPU engine: one explicit-halo system covering the local box, owned + halo
-    particles uploaded as AutoPas containers receive them.  Returns f(owned_pos, halo_pos) -> (F_owned, globals)."""
+    """A force function on the GPU engine: one explicit-halo system over the local box [lmin, lmax), owned + halo
+    particles uploaded as AutoPas containers receive them.  Returns f(owned_pos, halo_pos) -> (F_owned, globals)
+    with globals = (Upot, virial, interacting pairs as the container counts them: owned-owned pairs plus every
+    owned-halo pair once; a pair across a rank boundary is thus counted on both ranks)."""
     def f(owned_pos, halo_pos):
         e = engine_module.PairEngine(cutoff, skin, (lmin, lmax), periodic=False, precision=precision, **kw)
         allpos = np.concatenate([owned_pos, halo_pos])
@@ -165,7 +167,8 @@ def engine_forces(engine_module, cutoff, skin, lmin, lmax, precision=1, **kw):
 
 
 def oracle_forces(orc, cutoff):
-    """The same interface on the CPU oracle (FP64, explicit halos): for tests."""
+    """The same interface on the CPU oracle (FP64, explicit halos): for tests.  Its pair count is the rank's share of
+    the unique pairs (owned-owned plus half the owned-halo pairs), which sums over the ranks to the system's count."""
     lj = orc.LJ(cutoff)
 
     def f(owned_pos, halo_pos):
