@@ -98,7 +98,14 @@ __global__ void __launch_bounds__(128) k_lj_mixed_full(DeviceState s, ForceArgs 
   const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
   if (A >= s.nclusters) return;
   const int n = s.cp_count[A];
-  if (n == 0) return;
+  if (n == 0) {
+    // a cluster without a list (only halo or dummy members) still owes the reduction its zero partials
+    if (GLOB && lane == 0) {
+      for (int q = 0; q < kGlob; ++q) s.cl_glob[kGlob * A + q] = 0.0;
+      s.cl_hits[A] = 0ull;
+    }
+    return;
+  }
   const uint32_t *__restrict__ lst = s.cp_list + s.cp_start[A];
   const int ii = lane % C, jl = lane / C;
   const int64_t i = A * C + ii;
@@ -226,7 +233,14 @@ __global__ void __launch_bounds__(128) k_lj_fp64_full(DeviceState s, ForceArgs f
   const int64_t A = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
   if (A >= s.nclusters) return;
   const int n = s.cp_count[A];
-  if (n == 0) return;
+  if (n == 0) {
+    // a cluster without a list (only halo or dummy members) still owes the reduction its zero partials
+    if (GLOB && lane == 0) {
+      for (int q = 0; q < kGlob; ++q) s.cl_glob[kGlob * A + q] = 0.0;
+      s.cl_hits[A] = 0ull;
+    }
+    return;
+  }
   const int64_t lst = s.cp_start[A];
   const int ii = lane % C, jl = lane / C;
   const int64_t i = A * C + ii;

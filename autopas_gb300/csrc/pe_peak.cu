@@ -29,7 +29,49 @@ __global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters, float a
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps the chains live
 }
 
+__global__ void __launch_bounds__(256) k_dfma_peak(double *out, int iters, double a, double b) {
+  double x[kChains];
+  for (int q = 0; q < kChains; ++q) x[q] = threadIdx.x + q;
+  for (int k = 0; k < iters; ++k) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+#pragma unroll
+      for (int q = 0; q < kChains; ++q) x[q] = fma(x[q], a, b);
+    }
+  }
+  double s = 0.0;
+  for (int q = 0; q < kChains; ++q) s += x[q];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
+
+extern "C" int pe_measure_fp64_peak(double *tflops) {
+  if (!tflops) return PE_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PE_ERR_NO_DEVICE;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PE_ERR_CUDA;
+  const int blocks = sms * 4, threads = 256, iters = 16;
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return PE_ERR_OOM;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_dfma_peak<<<blocks, threads>>>(out, 2, 1.0001, 0.5);
+  cudaEventRecord(a);
+  k_dfma_peak<<<blocks, threads>>>(out, iters, 1.0001, 0.5);
+  cudaEventRecord(b);
+  const cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (e != cudaSuccess || !(ms > 0)) return PE_ERR_CUDA;
+  const double flop = 2.0 * kChains * kUnroll * (double)iters * blocks * threads;
+  *tflops = flop / (ms * 1e-3) / 1e12;
+  return PE_OK;
+}
 
 extern "C" int pe_measure_fp32_peak(double *tflops) {
   if (!tflops) return PE_ERR_ARG;

@@ -29,6 +29,7 @@ EXPORTS = [
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
     "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning", "pe_lj_forces_noalloc",
     "pe_compute_atm", "pe_update_ownership", "pe_set_force_cap", "pe_scale_velocities", "pe_measure_fp32_peak",
+    "pe_measure_fp64_peak",
 ]
 
 
@@ -97,6 +98,7 @@ def load(path: str | None = None):
     L.pe_update_ownership.argtypes = [vp, vp, C.POINTER(C.c_int)]
     L.pe_set_force_cap.argtypes = [vp, C.c_double]
     L.pe_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    L.pe_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     L.pe_scale_velocities.argtypes = [vp, vp]
     L.pe_compute_forces.argtypes = [vp, vp]
     L.pe_get_forces.argtypes = [vp, vp, vp, vp]
@@ -352,6 +354,15 @@ def measure_fp32_peak():
     rc = load().pe_measure_fp32_peak(C.byref(v))
     if rc != PE_OK:
         raise EngineError(rc, "pe_measure_fp32_peak failed")
+    return v.value
+
+
+def measure_fp64_peak():
+    """FP64 FMA throughput of the current device, TFLOP/s (pe_measure_fp64_peak)."""
+    v = C.c_double()
+    rc = load().pe_measure_fp64_peak(C.byref(v))
+    if rc != PE_OK:
+        raise EngineError(rc, "pe_measure_fp64_peak failed")
     return v.value
 
 

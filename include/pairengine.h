@@ -273,6 +273,8 @@ int pe_lj_forces_noalloc(const pe_config *cfg, int64_t n, const double *x, const
  * device at its present clock (packed FP32x2 fused multiply-adds on every SM, CUDA-event timed), in TFLOP/s --
  * the denominator of the force kernels' roofline.  Takes about 10 ms of device time. */
 int pe_measure_fp32_peak(double *tflops);
+/* The same for FP64 fused multiply-adds (the FP64 form's roofline denominator). */
+int pe_measure_fp64_peak(double *tflops);
 
 /* Device timer on the engine's stream: op 0 records a start event; op 1 records a stop event, waits for it and
  * returns the elapsed milliseconds between the two in *ms. */
