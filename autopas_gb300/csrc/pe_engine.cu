@@ -192,9 +192,6 @@ struct pe_engine {
   int gl_cap = 0;
   int64_t gl_entries = 0;
   DBuf<float4> facc;
-  DBuf<unsigned long long> wave;  // the wavefront's counter block (32 bytes: three counters, a pad word, a pointer)
-  DBuf<unsigned int> wave_done;
-  unsigned int *wave_set_for = nullptr;  // the flag array whose address the counter block holds
   DBuf<int8_t> own_reb;          // ownership of each slot at the last rebuild
   DBuf<int8_t> own_tmp;          // user-order ownership upload
   DBuf<uint32_t> pi_list;        // pruned inner lists
@@ -286,8 +283,6 @@ struct pe_engine {
     s.gl_cap = gl_cap;
     s.gl_stride = pcap / 2;
     s.facc = facc.p;
-    s.wave = wave.p;
-    s.wave_done = wave_done.p;
     s.prune = (cfg.prune_buffer > 0 && traversal == 1) ? 1 : 0;
     s.any_halo_sys = 0;
     for (const auto &S : sys) s.any_halo_sys |= S.desc.periodic ? 0 : 1;
@@ -1001,17 +996,6 @@ static int build_group_lists(pe_engine *h) {
   const size_t groups = (size_t)(h->pcap / 2);
   if (!h->gl_count.ensure(groups) || !h->pl_max.ensure(1) || !h->facc.ensure((size_t)h->pcap))
     return h->fail(PE_ERR_OOM, "pair-group lists");
-  {
-    // the wavefront's counter block with the address of its per-tile flags (one flag per 128 groups)
-    const size_t tiles = groups / 128 + 1;
-    const bool grow = h->wave_done.cap < tiles;
-    if (!h->wave.ensure(4) || !h->wave_done.ensure(tiles)) return h->fail(PE_ERR_OOM, "newton3 wavefront");
-    if (grow || h->wave_set_for != h->wave_done.p) {
-      unsigned long long hdr[4] = {0, 0, (unsigned long long)(uintptr_t)h->wave_done.p, 0};
-      PE_CUDA(h, cudaMemcpy(h->wave.p, hdr, sizeof hdr, cudaMemcpyHostToDevice));
-      h->wave_set_for = h->wave_done.p;
-    }
-  }
   PE_CUDA(h, cudaMemsetAsync(h->facc.p, 0, sizeof(float4) * (size_t)h->pcap, st));
   if (h->gl_cap == 0) {
     double rho = 0;
@@ -1518,8 +1502,6 @@ int pe_destroy(pe_engine *h) {
   h->facc.release();
   h->own_reb.release();
   h->own_tmp.release();
-  h->wave.release();
-  h->wave_done.release();
   h->atm_slot.release();
   h->pi_list.release();
   h->pi_count.release();

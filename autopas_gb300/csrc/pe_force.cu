@@ -1142,154 +1142,73 @@ __device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const Force
 }
 
 // ---------------------------------------------------------------------------------------------
-// The newton3 evaluation as one wavefront.  A group's list holds only j of later clusters (or later in its own
-// cluster), so every reaction on slot j comes from a group at or below j: once the force tiles (128 groups each)
-// up to j's tile are complete, j's force is final.  Resident blocks claim force tiles in increasing order from a
-// counter; after a tile the block publishes it (its reductions fenced first) and advances the count of leading
-// complete tiles; between force tiles a block claims a finish tile (256 slots) when that tile lies below the
-// complete prefix.  No block ever waits: a block that finds neither kind of work returns, and k_n3_finish_tail
-// finishes every tile nobody claimed.  The FP64 finish work (velocity half, next positions) so runs beside the
-// FP32 pair work of other warps instead of in a pass of its own.
+// The newton3 evaluation: one thread per group over the pair-group half lists (k_lj_mixed_n3), then the finish of
+// every slot (k_n3_finish).  A group's list holds only j of later clusters (or later in its own cluster), so the
+// reactions are complete only when every group has run: the finish is a second kernel.  (Running the finish inside
+// the force kernel, tile by tile behind a published prefix of completed force tiles, was measured slower on the
+// 2M-particle slab: the ticket order, the prefix scans and their fences cost more L1 reuse and issue slots than
+// the overlap saved.)
 // ---------------------------------------------------------------------------------------------
-constexpr int kN3Tile = 128;  // groups per force tile; a finish tile is the tile's 256 slots
-
-struct N3Wave {
-  unsigned int next_force;
-  unsigned int next_finish;
-  unsigned int prefix;  // leading force tiles complete
-  unsigned int pad;
-  unsigned int *done;   // [tiles]
-};
-
 template <int C, int GM, bool ONE_TYPE, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3_wave(DeviceState s, ForceArgs fa, N3Wave *w,
-                                                                 unsigned int tiles) {
+__global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceArgs fa) {
   __shared__ float tab[3][kMaxTypes * kMaxTypes];
-  __shared__ unsigned int task, kind;  // kind 0: none, 1: force tile, 2: finish tile
   if (!ONE_TYPE) {
     for (int q = threadIdx.x; q < s.ntypes * s.ntypes; q += blockDim.x) {
       tab[0][q] = s.types->eps24f[q];
       tab[1][q] = s.types->sig2f[q];
       tab[2][q] = s.types->shrf[q];
     }
-  }
-  for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) {
-      kind = 0;
-      // a ready finish tile first (claimed only while it lies below the complete prefix; the loop ends when the
-      // claim succeeds or no tile is ready, and every failed attempt means another block claimed one)
-      for (int attempt = 0; attempt < 64; ++attempt) {
-        const unsigned int p = atomicAdd(&w->prefix, 0u);
-        const unsigned int f = atomicAdd(&w->next_finish, 0u);
-        if (f >= p) break;
-        if (atomicCAS(&w->next_finish, f, f + 1) == f) {
-          kind = 2;
-          task = f;
-          break;
-        }
-      }
-      if (kind == 0) {
-        const unsigned int t = atomicAdd(&w->next_force, 1u);
-        if (t < tiles) {
-          kind = 1;
-          task = t;
-        }
-      }
-    }
-    __syncthreads();
-    const unsigned int k = kind, t = task;
-    if (k == 0) return;
-    if (k == 1) {
-      n3_group<C, GM, ONE_TYPE>(s, fa, (int64_t)t * kN3Tile + threadIdx.x, tab);
-      __threadfence();  // this thread's reductions before the tile is published
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        atomicExch(&w->done[t], 1u);
-        // advance the complete prefix over every published tile (each pass of the loop advances it by one or
-        // finds another block advancing it)
-        for (unsigned int it = 0; it < tiles; ++it) {
-          const unsigned int p = atomicAdd(&w->prefix, 0u);
-          if (p >= tiles || atomicAdd(&w->done[p], 0u) == 0u) break;
-          atomicCAS(&w->prefix, p, p + 1);
-        }
-      }
-    } else {
-      __threadfence();
-      const int64_t base = (int64_t)t * (2 * kN3Tile);
-      n3_finish_slot<C, GM != 0>(s, fa, base + threadIdx.x);
-      n3_finish_slot<C, GM != 0>(s, fa, base + kN3Tile + threadIdx.x);
-    }
   }
+  n3_group<C, GM, ONE_TYPE>(s, fa, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, tab);
 }
 
-// The finish tiles no block of the wavefront claimed: [next_finish, tiles), grid-stride.
+// one thread per slot; a warp past the last slot leaves whole (the kinetic energy is reduced with shuffles)
 template <int C, bool GLOB>
-__global__ void __launch_bounds__(256) k_n3_finish_tail(DeviceState s, ForceArgs fa, const N3Wave *w) {
-  const int64_t first = (int64_t)w->next_finish * (2 * kN3Tile);
-  for (int64_t i = first + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i - threadIdx.x < s.nslots;
-       i += (int64_t)gridDim.x * blockDim.x)
-    n3_finish_slot<C, GLOB>(s, fa, i);
+__global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) {
+  const int64_t w0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31u);
+  if (w0 >= s.nslots) return;
+  n3_finish_slot<C, GLOB>(s, fa, w0 + (threadIdx.x & 31));
 }
 
 template <int C, int GM, bool ONE_TYPE, int MINB>
-static void launch_n3_wave(DeviceState &s, const ForceArgs &fa, unsigned int tiles, cudaStream_t st) {
-  static int resident = 0;  // blocks of this instantiation that fit on the GPU at once
-  if (resident == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lj_mixed_n3_wave<C, GM, ONE_TYPE, MINB>, 128, 0);
-    resident = std::max(1, sms * std::max(1, per_sm));
-  }
-  const unsigned int grid = std::min<unsigned int>(tiles, (unsigned int)resident);
-  k_lj_mixed_n3_wave<C, GM, ONE_TYPE, MINB><<<grid, 128, 0, st>>>(s, fa, reinterpret_cast<N3Wave *>(s.wave), tiles);
+static void launch_n3(DeviceState &s, const ForceArgs &fa, int64_t ng, cudaStream_t st) {
+  k_lj_mixed_n3<C, GM, ONE_TYPE, MINB><<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(s, fa);
 }
 
 template <int C, int MINB>
-static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, unsigned int tiles, cudaStream_t st) {
+static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, int64_t ng, cudaStream_t st) {
   const bool glob = fa.calc_globals != 0;
   if (s.ntypes == 1) {
     if (glob)
-      launch_n3_wave<C, 1, true, MINB>(s, fa, tiles, st);
+      launch_n3<C, 1, true, MINB>(s, fa, ng, st);
     else
-      launch_n3_wave<C, 0, true, MINB>(s, fa, tiles, st);
+      launch_n3<C, 0, true, MINB>(s, fa, ng, st);
   } else {
     if (glob)
-      launch_n3_wave<C, 1, false, MINB>(s, fa, tiles, st);
+      launch_n3<C, 1, false, MINB>(s, fa, ng, st);
     else
-      launch_n3_wave<C, 0, false, MINB>(s, fa, tiles, st);
+      launch_n3<C, 0, false, MINB>(s, fa, ng, st);
   }
 }
 
 // kernel variants (the tuner's choice): the register cap for 5 (variant 0), 6 (1) or 4 (2) resident blocks of
-// 128 threads per SM.  The wavefront's counters are cleared first (stream-ordered memsets, captured with the step
-// graphs), the tail kernel finishes what the wavefront left.
+// 128 threads per SM.  Then the finish of every slot.
 template <int C>
 static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st) {
   const int64_t ng = s.nslots / 2;
-  const unsigned int tiles = (unsigned int)((ng + kN3Tile - 1) / kN3Tile);
-  if (tiles == 0) return;
-  cudaMemsetAsync(s.wave, 0, 4 * sizeof(unsigned int), st);
-  cudaMemsetAsync(s.wave_done, 0, sizeof(unsigned int) * tiles, st);
+  if (ng == 0) return;
   if (s.variant == 1)
-    launch_n3_kernel<C, 6>(s, fa, tiles, st);
+    launch_n3_kernel<C, 6>(s, fa, ng, st);
   else if (s.variant == 2)
-    launch_n3_kernel<C, 4>(s, fa, tiles, st);
+    launch_n3_kernel<C, 4>(s, fa, ng, st);
   else
-    launch_n3_kernel<C, 5>(s, fa, tiles, st);
-  static int tail_grid = 0;
-  if (tail_grid == 0) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    tail_grid = std::max(1, sms * 4);
-  }
-  const N3Wave *w = reinterpret_cast<const N3Wave *>(s.wave);
+    launch_n3_kernel<C, 5>(s, fa, ng, st);
+  const unsigned int grid = (unsigned int)((s.nslots + 255) / 256);
   if (fa.calc_globals)
-    k_n3_finish_tail<C, true><<<tail_grid, 256, 0, st>>>(s, fa, w);
+    k_n3_finish<C, true><<<grid, 256, 0, st>>>(s, fa);
   else
-    k_n3_finish_tail<C, false><<<tail_grid, 256, 0, st>>>(s, fa, w);
+    k_n3_finish<C, false><<<grid, 256, 0, st>>>(s, fa);
 }
 
 template <int C>

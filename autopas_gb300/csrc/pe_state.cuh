@@ -78,10 +78,6 @@ struct DeviceState {
   // newton3 force sums: the reactions other groups add with vector reductions and the group's own part (its
   // compensated sums), added at its end; the finish kernel reads them, clears facc and runs the velocity half
   float4 *facc = nullptr;          // [slots], zero between force evaluations
-  // the newton3 wavefront's counters (next force tile, next finish tile, complete prefix, pointer to the
-  // per-tile flags) and its flags [tiles]; see k_lj_mixed_n3_wave
-  void *wave = nullptr;
-  unsigned int *wave_done = nullptr;
   // lists the force kernels read: the particle lists themselves, or the pruned inner lists
   uint32_t *fl_list = nullptr;
   int32_t *fl_count = nullptr;

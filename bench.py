@@ -250,7 +250,8 @@ def run_ours(args):
     def new_engine(prec, use_graphs=True):
         e = E.PairEngine(RC, SKIN, (bmin, bmax), periodic=True, precision=prec, cluster_size=args.cluster_size,
                          newton3=args.newton3 if prec == E.PRECISION_MIXED else 0, rebuild_frequency=REBUILD,
-                         calc_globals=True, traversal=args.traversal,
+                         calc_globals=True,
+                         traversal=args.traversal if prec == E.PRECISION_MIXED or args.traversal < 2 else -1,
                          prune_buffer=args.prune, use_graphs=use_graphs, kernel_variant=args.variant)
         e.set_particles(pos, vel)
         return e
