@@ -472,19 +472,28 @@ __global__ void k_pack(DeviceState s, int64_t n) {
   if (i < n) pack_one(s, i);
 }
 
-// gather into the new slot order; dummies fill the cluster padding
+// gather into the new slot order; dummies fill the cluster padding.  Every field of a particle is loaded before
+// the first store: the source and destination arrays are reached through plain pointers, so a store between two
+// loads would make the second wait for the first (the compiler cannot rule out that they alias).
 __global__ void k_gather(DeviceState src, DeviceState dst, const int32_t *__restrict__ perm_src, int64_t nnew) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= nnew) return;
   const int32_t p = perm_src[q];
   if (p >= 0) {
-    dst.x[q] = src.x[p]; dst.y[q] = src.y[p]; dst.z[q] = src.z[p];
-    dst.vx[q] = src.vx[p]; dst.vy[q] = src.vy[p]; dst.vz[q] = src.vz[p];
-    dst.fx[q] = src.fx[p]; dst.fy[q] = src.fy[p]; dst.fz[q] = src.fz[p];
-    dst.ofx[q] = src.ofx[p]; dst.ofy[q] = src.ofy[p]; dst.ofz[q] = src.ofz[p];
-    dst.type[q] = src.type[p]; dst.sys[q] = src.sys[p]; dst.own[q] = src.own[p];
-    dst.id[q] = src.id[p];
-    const int32_t o = src.orig[p];
+    const double x = __ldg(src.x + p), y = __ldg(src.y + p), z = __ldg(src.z + p);
+    const double vx = __ldg(src.vx + p), vy = __ldg(src.vy + p), vz = __ldg(src.vz + p);
+    const double fx = __ldg(src.fx + p), fy = __ldg(src.fy + p), fz = __ldg(src.fz + p);
+    const double ofx = __ldg(src.ofx + p), ofy = __ldg(src.ofy + p), ofz = __ldg(src.ofz + p);
+    const int32_t ty = __ldg(src.type + p), sy = __ldg(src.sys + p);
+    const int8_t ow = __ldg(src.own + p);
+    const int64_t id = __ldg(src.id + p);
+    const int32_t o = __ldg(src.orig + p);
+    dst.x[q] = x; dst.y[q] = y; dst.z[q] = z;
+    dst.vx[q] = vx; dst.vy[q] = vy; dst.vz[q] = vz;
+    dst.fx[q] = fx; dst.fy[q] = fy; dst.fz[q] = fz;
+    dst.ofx[q] = ofx; dst.ofy[q] = ofy; dst.ofz[q] = ofz;
+    dst.type[q] = ty; dst.sys[q] = sy; dst.own[q] = ow;
+    dst.id[q] = id;
     dst.orig[q] = o;
     dst.slot_of[o] = (int32_t)q;
   } else {

@@ -76,8 +76,10 @@ typedef struct {
   int apply_shift;         /* truncated-shifted potential (applyShift) */
   int precision;           /* PE_PRECISION_* */
   int cluster_size;        /* 4 or 8; 0 lets the engine's tuner decide */
-  int newton3;             /* 0 or -1: full lists, each pair evaluated from both sides (the only mode the force
-                              kernels implement; 1 is rejected with PE_ERR_ARG) */
+  int newton3;             /* 0: full lists, each pair evaluated from both sides; 1: Newton-3, each pair once
+                              (traversal 2; mixed precision on periodic systems without ATM or pruning, else
+                              PE_ERR_ARG), as the reference's newton3 functor calls (LJFunctor.h:369-559);
+                              -1: the tuner may pick either where newton3 is allowed */
   int dist_mode;           /* PE_DIST_* for every FP64 distance test */
   int rebuild_frequency;   /* steps between list rebuilds inside pe_step (verletRebuildFrequency) */
   int calc_globals;        /* compute Upot and virial with every force evaluation */
@@ -87,8 +89,10 @@ typedef struct {
                               systems.  Only the cluster shapes differ; the pair set is the same. */
   int traversal;           /* 0: cluster-pair lists (VerletClusterLists traversal, vcl_cluster_iteration);
                               1: per-particle lists filtered from the cluster pairs on the device (VerletLists
-                              traversal, vl_list_iteration); -1: the engine's tuner times both and keeps the
-                              faster */
+                              traversal, vl_list_iteration); 2: Newton-3 half lists per group of two
+                              consecutive particles (forward neighbours only, VerletClusterListsRebuilder.h:
+                              339-354), reactions added with vector float reductions and a finish pass (requires
+                              newton3 = 1); -1: the engine's tuner times the allowed ones and keeps the fastest */
   double atm_nu;           /* > 0: pe_step adds Axilrod-Teller-Muto three-body forces with this nu */
   double atm_cutoff;       /* triplet cutoff for ATM (all three distances); <= cutoff + skin */
   int use_graphs;          /* 1: pe_step captures the launches of a step without list rebuild into a CUDA graph
@@ -96,10 +100,11 @@ typedef struct {
   double prune_buffer;     /* > 0 (particle lists only): the force kernels read inner lists holding the pairs within
                               cutoff + prune_buffer, refreshed on the device from the rc+skin lists whenever a
                               particle has moved prune_buffer/2 since the last refresh; 0: off */
-  int kernel_variant;      /* particle-list force kernel variant used when the tuner does not run (batches of
-                              4 entries; 0: 96 registers, 5 blocks per SM, 1: 80 registers, 6 blocks, 2: the
+  int kernel_variant;      /* force kernel variant used when the tuner does not run.  Traversal 1 (batches of
+                              4 entries): 0: 96 registers, 5 blocks per SM, 1: 80 registers, 6 blocks, 2: the
                               next batch gathered during the current one, 4 blocks, 3: as 1 with list entries
-                              streamed past the caches); the tuner picks its own */
+                              streamed past the caches.  Traversal 2: 0, 1, 2 cap the registers for 5, 6, 4
+                              blocks of 128 threads per SM.  The tuner picks its own. */
 } pe_config;
 
 /* One particle system of the ensemble. */
@@ -194,7 +199,7 @@ typedef struct {
   int64_t num_towers;
   int64_t num_cluster_pairs; /* entries in all cluster-pair lists */
   int64_t max_tower_size;
-  int64_t num_list_entries;  /* particle-list entries (traversal 1) */
+  int64_t num_list_entries;  /* particle-list entries (traversal 1) or pair-group list entries (traversal 2) */
   int64_t list_capacity;     /* particle-list entries reserved per particle */
 } pe_info;
 int pe_get_info(pe_engine *h, pe_info *info);
@@ -228,7 +233,8 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out);
 
 /* The engine's tuner (the counterpart of AutoPas's AutoTuner full search, tuning/AutoTuner.cpp:85-175, over
  * the engine-internal dimensions that AutoPas does not tune): every candidate (cluster size 4/8 when
- * cluster_size == 0, traversal 0/1 when traversal == -1, kernel variant) is applied, the lists rebuilt, one
+ * cluster_size == 0, traversal 0/1 (and 2 where newton3 is allowed) when traversal == -1, kernel variant) is
+ * applied, the lists rebuilt, one
  * more rebuild timed (rebuild_ms, once per cluster size and traversal), and `samples` force evaluations timed
  * with CUDA events (ms, the median).  The candidate with the lowest cost per step, score = ms + rebuild_ms /
  * rebuild_frequency, is kept.  It runs by itself at the first pe_compute_forces when cluster_size == 0 or
