@@ -687,15 +687,28 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   const double Fx = (double)acc.force_x(), Fy = (double)acc.force_y(), Fz = (double)acc.force_z();
   float ek = 0.f;
   if (oi == 1) {
+    // every load of the epilogue before its first store (through plain pointers a load after a store is issued
+    // only after it, one more round trip per particle)
+    double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+    double ox = 0, oy = 0, oz = 0, x0 = 0, y0 = 0, z0 = 0;
+    if (fa.fuse_velocity) {
+      ox = s.ofx[i];
+      oy = s.ofy[i];
+      oz = s.ofz[i];
+      if (fa.fuse_positions) {
+        x0 = s.x[i];
+        y0 = s.y[i];
+        z0 = s.z[i];
+      }
+    }
     s.fx[i] = Fx;
     s.fy[i] = Fy;
     s.fz[i] = Fz;
-    double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
     if (fa.fuse_velocity) {
       const double h = fa.vv.h[ti];
-      vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, s.ofx[i]), h));
-      vy = __dadd_rn(vy, __dmul_rn(__dadd_rn(Fy, s.ofy[i]), h));
-      vz = __dadd_rn(vz, __dmul_rn(__dadd_rn(Fz, s.ofz[i]), h));
+      vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, ox), h));
+      vy = __dadd_rn(vy, __dmul_rn(__dadd_rn(Fy, oy), h));
+      vz = __dadd_rn(vz, __dmul_rn(__dadd_rn(Fz, oz), h));
       s.vx[i] = vx;
       s.vy[i] = vy;
       s.vz[i] = vz;
@@ -703,9 +716,9 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
         // the next step's position half (TimeDiscretization.cpp:17-66), the same operations as k_positions:
         // x += v dt + F dt^2/(2m), old force = F; into the next-step buffers
         const double c = fa.vv.c[ti], dt = fa.dt;
-        const double x1 = __dadd_rn(s.x[i], __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(Fx, c)));
-        const double y1 = __dadd_rn(s.y[i], __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(Fy, c)));
-        const double z1 = __dadd_rn(s.z[i], __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(Fz, c)));
+        const double x1 = __dadd_rn(x0, __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(Fx, c)));
+        const double y1 = __dadd_rn(y0, __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(Fy, c)));
+        const double z1 = __dadd_rn(z0, __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(Fz, c)));
         s.xn[i] = x1;
         s.yn[i] = y1;
         s.zn[i] = z1;
@@ -1089,10 +1102,12 @@ __device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const Force
       oy = s.ofy[k];
       oz = s.ofz[k];
     }
+    int sy = 0;
     if (fa.fuse_positions) {
       px = s.x[k];
       py = s.y[k];
       pz = s.z[k];
+      sy = s.sys[k];  // with the other loads: a load after the stores below would wait for its own round trip
     }
     __stcg(s.facc + k, make_float4(0.f, 0.f, 0.f, 0.f));
     if (oi == 1) {
@@ -1120,7 +1135,7 @@ __device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const Force
           s.ofx[k] = Fx;
           s.ofy[k] = Fy;
           s.ofz[k] = Fz;
-          s.pqn[k] = pq_pack(s.sysd[s.sys[k]], x1, y1, z1, ti, oi, s.err);
+          s.pqn[k] = pq_pack(s.sysd[sy], x1, y1, z1, ti, oi, s.err);
         }
       }
       if (GLOB) {
