@@ -624,9 +624,9 @@ template <int C>
 __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
   constexpr int GL = C / 2;   // groups (lanes) per cluster
   constexpr int G = 32 / GL;  // clusters per warp
-  // the current j-cluster of each cluster of the warp, hi parts negated, one row per coordinate (one word of
-  // padding keeps the rows of neighbouring clusters in different banks)
-  __shared__ float sj[4][G][3][C + 1];
+  // the current j-cluster of each cluster of the warp, hi parts negated, one float4 (x, y, z, -) per particle; one
+  // float4 of padding per row puts the rows of the warp's clusters in different banks
+  __shared__ float4 sj[4][G][C + 1];
   // each lane's last two blocks of entries (a ring of 16; up to C <= 8 appends per cluster pair complete at most one
   // block); 17 words per lane keep lanes that append at the same ring position in different banks
   __shared__ uint32_t stage[4][32][2 * kPlistBlock + 1];
@@ -668,28 +668,38 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
       dst[1] = make_uint4(src[4], src[5], src[6], src[7]);
     }
   };
-  int cnt = 0;
-  uint32_t ent_next = 0 < n ? __ldg(lst) : 0u;
-  for (int e = 0; e < nmax; ++e) {
-    const bool act = e < n;
-    const uint32_t ent = ent_next;
-    ent_next = e + 1 < n ? __ldg(lst + e + 1) : 0u;
+  // the forward rule; every lane of a cluster reads the same entry, so the decision is uniform over them
+  auto forward = [&](uint32_t ent) {
     const int64_t B = ent >> 5;
-    const int code = ent & 31;
-    // the forward rule; every lane of a cluster reads the same entry, so the decision is uniform over them
-    const bool fwd = act && (B > A || (B == A && code >= kShiftNone));
+    return B > A || (B == A && (int)(ent & 31) >= kShiftNone);
+  };
+  // software pipeline: the lane's two j records of entry e + 1 are loaded while entry e is tested, and the list
+  // entry e + 2 with them
+  auto load_j = [&](uint32_t ent, bool ok, uint4 (&pj)[2]) {
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      pj[u] = ok ? __ldg(&s.pq[(int64_t)(ent >> 5) * C + 2 * gl + u]) : make_uint4(0u, 0u, 0u, 0u);
+  };
+  int cnt = 0;
+  uint32_t ent_cur = 0 < n ? __ldg(lst) : 0u;
+  uint32_t ent_nxt = 1 < n ? __ldg(lst + 1) : 0u;
+  uint4 pc[2];
+  load_j(ent_cur, 0 < n && forward(ent_cur), pc);
+  for (int e = 0; e < nmax; ++e) {
+    const uint32_t ent = ent_cur;
+    const bool fwd = e < n && forward(ent);
+    uint4 pn[2];
+    load_j(ent_nxt, e + 1 < n && forward(ent_nxt), pn);
+    const uint32_t ent_after = e + 2 < n ? __ldg(lst + e + 2) : 0u;
     if (fwd) {
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int jj = 2 * gl + u;
-        const uint4 pj = __ldg(&s.pq[B * C + jj]);
-        sj[w][cg][0][jj] = pq_nhi(pj.x, eb);
-        sj[w][cg][1][jj] = pq_nhi(pj.y, eb);
-        sj[w][cg][2][jj] = pq_nhi(pj.z, eb);
-      }
+      for (int u = 0; u < 2; ++u)
+        sj[w][cg][2 * gl + u] = make_float4(pq_nhi(pc[u].x, eb), pq_nhi(pc[u].y, eb), pq_nhi(pc[u].z, eb), 0.f);
     }
     __syncwarp();
     if (fwd && real) {
+      const int64_t B = ent >> 5;
+      const int code = ent & 31;
       // both members moved by minus the image shift (exact: hi parts and shifts on the ulp(B) grid)
       const float4 us = c_unit_shift[code];
       const float2 xh = fma2(dup2(-us.x), dup2(S.len_hi[0]), hx);
@@ -700,9 +710,10 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
       const int before = cnt;
 #pragma unroll
       for (int jj = 0; jj < C; ++jj) {
-        const float2 dx = add2(xh, dup2(sj[w][cg][0][jj]));
-        const float2 dy = add2(yh, dup2(sj[w][cg][1][jj]));
-        const float2 dz = add2(zh, dup2(sj[w][cg][2][jj]));
+        const float4 hj = sj[w][cg][jj];
+        const float2 dx = add2(xh, dup2(hj.x));
+        const float2 dy = add2(yh, dup2(hj.y));
+        const float2 dz = add2(zh, dup2(hj.z));
         const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
         const bool keep = jj >= jfirst && ((r2.x > 0.f && r2.x <= r2max) || (r2.y > 0.f && r2.y <= r2max));
         if (keep) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
@@ -711,6 +722,10 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
       if ((before ^ cnt) & ~(kPlistBlock - 1)) put_block(before / kPlistBlock);
     }
     __syncwarp();
+    ent_cur = ent_nxt;
+    ent_nxt = ent_after;
+    pc[0] = pn[0];
+    pc[1] = pn[1];
   }
   if (validA) {
     if (cnt & (kPlistBlock - 1)) put_block(cnt / kPlistBlock);  // the last block; entries past cnt are never read

@@ -701,9 +701,13 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
         z0 = s.z[i];
       }
     }
-    s.fx[i] = Fx;
-    s.fy[i] = Fy;
-    s.fz[i] = Fz;
+    if (!fa.fuse_positions) {
+      // (with the position half fused the force goes to the old-force arrays below; the last step of a fused
+      // loop is a plain evaluation, which leaves the force here)
+      s.fx[i] = Fx;
+      s.fy[i] = Fy;
+      s.fz[i] = Fz;
+    }
     if (fa.fuse_velocity) {
       const double h = fa.vv.h[ti];
       vx = __dadd_rn(vx, __dmul_rn(__dadd_rn(Fx, ox), h));
@@ -1112,9 +1116,11 @@ __device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const Force
     __stcg(s.facc + k, make_float4(0.f, 0.f, 0.f, 0.f));
     if (oi == 1) {
       const double Fx = (double)r.x, Fy = (double)r.y, Fz = (double)r.z;
-      s.fx[k] = Fx;
-      s.fy[k] = Fy;
-      s.fz[k] = Fz;
+      if (!fa.fuse_positions) {  // fused: the force goes to the old-force arrays (as in the particle-list kernel)
+        s.fx[k] = Fx;
+        s.fy[k] = Fy;
+        s.fz[k] = Fz;
+      }
       double vx = vx0, vy = vy0, vz = vz0;
       if (fa.fuse_velocity) {
         const double h = fa.vv.h[ti];
