@@ -36,10 +36,15 @@ template <class Functor>
 class GPUTraversal {
  public:
   GPUTraversal(Functor *f, TraversalOption option, bool newton3 = false) : _functor(f), _option(option) {
-    if (newton3) throw GpuEngineException(PE_ERR_ARG, "GPUTraversal: the GPU traversals evaluate pairs without newton3");
+    if (newton3)
+      throw GpuEngineException(PE_ERR_ARG,
+                               "GPUTraversal: a container with explicit halo copies evaluates pairs without newton3");
   }
   TraversalOption getTraversalType() const { return _option; }
-  bool isApplicableToDomain() const { return true; }
+  // The newton3 pair-group traversal serves periodic systems, whose images the engine forms itself; this container
+  // receives explicit halo copies from AutoPas, so the tuner is told it does not apply here
+  // (TraversalInterface.h:18-83, isApplicable).
+  bool isApplicableToDomain() const { return _option != TraversalOption::gpu_newton3_pair_groups; }
   bool getUseNewton3() const { return false; }
   void initTraversal() {}
   void traverseParticles() {}

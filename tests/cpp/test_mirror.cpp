@@ -83,6 +83,23 @@ static void cpu_tests() {
   CHECK(toString(ContainerOption::gpuClusterLists) == "GPUClusterLists", "container name");
   CHECK(toString(TraversalOption::gpu_particle_lists) == "gpu_particle_lists", "traversal name");
   CHECK(toEngineTraversal(TraversalOption::gpu_tuned) == -1, "tuned traversal");
+  CHECK(toEngineTraversal(TraversalOption::gpu_newton3_pair_groups) == 2, "newton3 traversal");
+  {
+    // the container receives explicit halo copies: the newton3 pair-group traversal (periodic systems only) must
+    // not look applicable to the AutoTuner, the others must
+    Functor fa(1.1);
+    CHECK(!GPUTraversal<Functor>(&fa, TraversalOption::gpu_newton3_pair_groups).isApplicableToDomain(),
+          "newton3 traversal must not apply to an explicit-halo container");
+    CHECK(GPUTraversal<Functor>(&fa, TraversalOption::gpu_particle_lists).isApplicableToDomain(),
+          "particle-list traversal applies");
+    bool n3threw = false;
+    try {
+      GPUTraversal<Functor> t(&fa, TraversalOption::gpu_particle_lists, true);
+    } catch (const GpuEngineException &) {
+      n3threw = true;
+    }
+    CHECK(n3threw, "a newton3 traversal object must be refused");
+  }
   GPUClusterLists<MoleculeLJ> c({0, 0, 0}, {3, 3, 3}, 1.1, 0.2);
   bool threw = false;
   try {
