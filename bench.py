@@ -32,6 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 RC, SKIN, DT, REBUILD = 3.0, 0.4, 0.002, 20
+REFERENCE_BUDGET_S = 150.0  # timed CPU work of the reference arm, at most
 FLOP_PER_PAIR = 38  # 8 distance + 18 newton3 kernel + 12 globals (unshifted), LJFunctor.h:722-789
 
 
@@ -172,7 +173,7 @@ def cpu_reference_rate(pos, bmin, bmax, pairs, nthreads, budget_s=None, warmup=1
     LJ functor with newton3, FP64, OpenMP) on the whole workload: each evaluation bins the owned particles and
     their periodic halo copies into cells and computes all forces and globals.  `pairs` is the workload's
     interacting-pair count (each unordered physical pair once).  Times `steps` evaluations, or as many as fit in
-    budget_s.  Returns (rate, evaluations, seconds)."""
+    budget_s, whichever is fewer (at least three when both are given).  Returns (rate, evaluations, seconds)."""
     from oracle import oracle as orc
     allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, RC, SKIN)
     lj = orc.LJ(RC)
@@ -184,7 +185,9 @@ def cpu_reference_rate(pos, bmin, bmax, pairs, nthreads, budget_s=None, warmup=1
         orc.cpu_lc_c08(allpos, lj, SKIN, own=own, nthreads=nthreads)
         t_total += time.perf_counter() - t0
         evals += 1
-        if (steps is not None and evals >= steps) or (steps is None and t_total >= budget_s):
+        if steps is not None and evals >= steps:
+            break
+        if budget_s is not None and t_total >= budget_s and (steps is None or evals >= 3):
             break
     return pairs * evals / t_total, evals, t_total
 
@@ -204,13 +207,18 @@ def run_reference(args):
     oo, oh, _ = orc.count_interacting(allpos, RC, own=own)
     pairs = oo + oh // 2
     del allpos, own
-    rate, evals, t = cpu_reference_rate(pos, bmin, bmax, pairs, nthreads, warmup=args.warmup, steps=args.steps)
+    # one evaluation of the whole 2M slab takes ~0.6 s on 16 cores: the timed evaluations are bounded by the
+    # requested steps and by a time budget, so that the arm ends within a few minutes for any --steps
+    rate, evals, t = cpu_reference_rate(pos, bmin, bmax, pairs, nthreads, budget_s=REFERENCE_BUDGET_S,
+                                        warmup=min(args.warmup, 2), steps=args.steps)
     sample = (f"the whole workload: one step = one force evaluation (LinkedCells cell binning, c08 colouring, SoA LJ "
               f"with newton3, FP64, OpenMP on {nthreads} threads) of all {args.n} particles of the slab plus their "
-              f"periodic halo copies; {pairs} interacting pairs per step")
+              f"periodic halo copies; {pairs} interacting pairs per step; {evals} of the {args.steps} requested "
+              f"steps timed ({t:.1f} s, budget {REFERENCE_BUDGET_S:.0f} s), after {min(args.warmup, 2)} untimed")
     line = {
         "impl": "reference", "metric": metric_name(), "value": rate, "unit": "pair interactions/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / evals,
+        "n_gpus": args.gpus, "steps": evals, "warmup": min(args.warmup, 2), "ms_per_step": 1e3 * t / evals,
+        "steps_requested": args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_dict(args),
         "cpu_baseline": {"value": rate, "unit": "pair interactions/s", "cores": nthreads, "kind": "port",
