@@ -2,7 +2,7 @@
 //
 // Replaces VerletClusterLists::rebuildNeighborLists (src/autopas/containers/verletClusterLists/
 // VerletClusterLists.h:779-800 -> VerletClusterListsRebuilder.h:67-409):
-//   1. tower index of every particle            (ClusterTowerBlock2D.h:220-245)       k_bin
+//   1. periodic wrap and tower index of every particle (ClusterTowerBlock2D.h:220-245)  k_bin
 //   2. one-digit radix (counting) sort on tower  (histogram, scan, scatter)            k_bin, k_scatter
 //   3. per-tower order by z, tie by particle index (ClusterTower::generateClusters sorts by z,
 //      ClusterTower.h:83-143; here the order is made deterministic), padding to whole clusters
@@ -44,10 +44,23 @@ __global__ void k_bin(DeviceState s, int64_t nslots_old, uint64_t *__restrict__ 
     // no list, and a later ownership change finds them); only the cluster padding (orig < 0) is dropped
     if (s.orig[i] >= 0) {
       const SysDev &S = s.sysd[s.sys[i]];
-      const int tx = tower_coord(s.x[i], S, 0);
-      const int ty = tower_coord(s.y[i], S, 1);
+      double x = s.x[i], y = s.y[i], z = s.z[i];
+      if (S.periodic && s.own[i] != 0) {
+        // the periodic wrap of a particle that left the box (RegularGridDecomposition.cpp:555-590), written back
+        // only when it moved the particle
+        const double wx = wrap1(x, S.bmin[0], S.bmax[0]), wy = wrap1(y, S.bmin[1], S.bmax[1]);
+        const double wz = wrap1(z, S.bmin[2], S.bmax[2]);
+        if (__double_as_longlong(wx) != __double_as_longlong(x)) s.x[i] = wx;
+        if (__double_as_longlong(wy) != __double_as_longlong(y)) s.y[i] = wy;
+        if (__double_as_longlong(wz) != __double_as_longlong(z)) s.z[i] = wz;
+        x = wx;
+        y = wy;
+        z = wz;
+      }
+      const int tx = tower_coord(x, S, 0);
+      const int ty = tower_coord(y, S, 1);
       t = S.tower_base + ty * S.nt[0] + tx;
-      key[i] = dbl_key(s.z[i]);
+      key[i] = dbl_key(z);
     }
     tower_of[i] = t;
   }
@@ -66,6 +79,75 @@ void launch_bin(DeviceState &s, int64_t nslots_old, uint64_t *key, int32_t *towe
 __global__ void k_ncl(const int32_t *__restrict__ cnt, int32_t *__restrict__ ncl, int64_t nt, int C) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t < nt) ncl[t] = (cnt[t] + C - 1) / C;
+}
+
+// One block of 1024 threads: thread q takes a contiguous run of towers, sums its counts and clusters, the block
+// scans the 1024 partial sums (warp shuffles, then the warp totals), and each thread writes its towers' starts.
+__global__ void __launch_bounds__(1024) k_tower_tables(const int32_t *__restrict__ cnt, int32_t *__restrict__ start,
+                                                       int32_t *__restrict__ ncl, int32_t *__restrict__ cl_start,
+                                                       int nt, int C, int *__restrict__ maxc) {
+  __shared__ int32_t wsum[2][32];
+  __shared__ int32_t wmax[32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int per = (nt + 1023) / 1024;
+  const int b = min(tid * per, nt), e = min(b + per, nt);
+  int32_t sc = 0, sn = 0, mx = 0;
+  for (int i = b; i < e; ++i) {
+    const int32_t c = cnt[i];
+    sc += c;
+    sn += (c + C - 1) / C;
+    mx = max(mx, c);
+  }
+  int32_t ic = sc, in = sn;  // inclusive within the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t a = __shfl_up_sync(0xffffffffu, ic, o), bb = __shfl_up_sync(0xffffffffu, in, o);
+    if (lane >= o) {
+      ic += a;
+      in += bb;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 31) {
+    wsum[0][w] = ic;
+    wsum[1][w] = in;
+  }
+  if (lane == 0) wmax[w] = mx;
+  __syncthreads();
+  if (w == 0) {
+    const int32_t a = wsum[0][lane], bb = wsum[1][lane];
+    int32_t ia = a, ib = bb, m = wmax[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t ua = __shfl_up_sync(0xffffffffu, ia, o), ub = __shfl_up_sync(0xffffffffu, ib, o);
+      if (lane >= o) {
+        ia += ua;
+        ib += ub;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    wsum[0][lane] = ia - a;  // exclusive offsets of the warps
+    wsum[1][lane] = ib - bb;
+    if (lane == 0) *maxc = m;
+  }
+  __syncthreads();
+  int32_t oc = wsum[0][w] + ic - sc, on = wsum[1][w] + in - sn;  // exclusive prefix of this thread's run
+  for (int i = b; i < e; ++i) {
+    const int32_t c = cnt[i], k = (c + C - 1) / C;
+    start[i] = oc;
+    ncl[i] = k;
+    cl_start[i] = on;
+    oc += c;
+    on += k;
+  }
+  if (tid == 1023) {  // the totals (this thread's run ends at nt, or it is empty and starts there)
+    start[nt] = oc;
+    cl_start[nt] = on;
+  }
+}
+
+bool launch_tower_tables(DeviceState &s, int32_t *ncl, int *maxc, cudaStream_t st) {
+  if (s.ntowers > kTowerTablesMax) return false;
+  k_tower_tables<<<1, 1024, 0, st>>>(s.tw_count, s.tw_start, ncl, s.tw_cl_start, (int)s.ntowers, s.C, maxc);
+  return true;
 }
 
 void launch_clusters_per_tower(DeviceState &s, int32_t *ncl, cudaStream_t st) {
@@ -119,7 +201,14 @@ __global__ void k_tower_sort(DeviceState s, const uint64_t *__restrict__ skey, c
   const int clb = s.tw_cl_start[t];
   const int cle = s.tw_cl_start[t + 1];
   if (n > kTowerSortMax || n > p2) {
-    if (threadIdx.x == 0) atomicOr(s.err, kErrTowerOverflow);
+    // the tower does not fit: flagged (a hard error beyond kTowerSortMax; beyond a speculative size the host redoes
+    // the rebuild), and its slots left as dummies of a well-formed tower, so that what runs before the host sees
+    // the flag reads valid indices
+    if (threadIdx.x == 0) atomicOr(s.err, n > kTowerSortMax ? kErrTowerOverflow : kErrSpecTower);
+    if (threadIdx.x == 0) s.tw_bbf[t] = make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
+    const int C = s.C;
+    for (int q = threadIdx.x; q < (cle - clb) * C; q += blockDim.x) perm_src[(int64_t)clb * C + q] = -1;
+    for (int c = clb + threadIdx.x; c < cle; c += blockDim.x) s.cl_tower[c] = t;
     return;
   }
   // the tower's own power of two (p2 sizes the shared arrays for the largest tower)
@@ -222,7 +311,7 @@ int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *pe
 // ---------------------------------------------------------------------------------------------
 __global__ void k_cluster_bbox(DeviceState s) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= s.nclusters) return;
+  if (c >= clusters_bound(s)) return;
   const int C = s.C;
   double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   int flags = 0;
@@ -346,7 +435,7 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s, i
   extern __shared__ uint32_t lbuf[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t A = blockIdx.x * (int64_t)kListWarps + warp;
-  if (A >= s.nclusters) return;
+  if (A >= clusters_bound(s)) return;
   uint32_t *buf = lbuf + warp * buf_per_warp;
   const int flagsA = s.cl_flags[A];
   const bool aOwned = flagsA & 1;
@@ -502,7 +591,7 @@ __global__ void __launch_bounds__(128) k_plist_build(DeviceState s) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / C, ii = lane % C;
   const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + g;
-  const bool validA = A < s.nclusters;
+  const bool validA = A < clusters_bound(s);
   const int64_t i = A * C + ii;
   int n = 0, oi = 0;
   const uint32_t *lst = s.cp_list;
@@ -633,7 +722,7 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cg = lane / GL, gl = lane % GL;
   const int64_t A = (blockIdx.x * 4 + w) * (int64_t)G + cg;
-  const bool validA = A < s.nclusters;
+  const bool validA = A < clusters_bound(s);
   const int64_t g = A * GL + gl;
   int n = 0;
   const uint32_t *lst = s.cp_list;

@@ -29,6 +29,7 @@ enum DeviceError : int {
   kErrListCapacity = 2,   // the global list buffer is too small (host regrows and retries)
   kErrTowerOverflow = 4,  // a tower holds more than kTowerSortMax particles
   kErrEncode = 8,         // a particle left the range of the position encoding ([B, 2B) in every dimension)
+  kErrSpecTower = 16,     // a tower outgrew the size a rebuild on the previous rebuild's sizes assumed (redone)
 };
 
 // Per-system constants (device copy).
@@ -260,6 +261,25 @@ __device__ __forceinline__ uint64_t dbl_key(double v) {
 }
 __device__ __forceinline__ double key_dbl(uint64_t k) {
   return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// periodic wrap of a coordinate that left the box (RegularGridDecomposition.cpp:555-590)
+__device__ __forceinline__ double wrap1(double x, double lo, double hi) {
+  // inside the box (the common case), decided on the order-preserving integer keys of the doubles: FP64
+  // compares go through this GPU's FP64 pipe (2 lanes per clock per SM)
+  const uint64_t kx = dbl_key(x);
+  if (kx >= dbl_key(lo) && kx < dbl_key(hi)) return x;
+  const double len = hi - lo;
+  if (x < lo) {
+    const double p = x + len;
+    const double just = nextafter(hi, lo);
+    return p < just ? p : just;
+  }
+  if (x >= hi) {
+    const double p = x - len;
+    return lo > p ? lo : p;
+  }
+  return x;
 }
 
 // ---- launch wrappers implemented in the .cu files (all asynchronous on `st`) ----

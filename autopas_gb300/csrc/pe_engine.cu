@@ -179,6 +179,12 @@ struct pe_engine {
   DBuf<int32_t> sys_tower_base;
   int64_t max_tower = 0;
   int64_t num_cluster_pairs = 0;
+  // rebuilds on the previous rebuild's sizes (one host synchronisation instead of two): the tower-sort size
+  // assumed (0: no previous rebuild to go by) and the tower count and slot capacity it was taken under
+  int spec_p2 = 0;
+  int64_t spec_ntowers = -1, spec_pcap = -1;
+  bool spec_active = false;
+  int64_t spec_rebuilds_redone = 0;
   // particle lists
   DBuf<uint32_t> pl_list;
   DBuf<int32_t> pl_count;
@@ -273,6 +279,7 @@ struct pe_engine {
     s.newton3 = newton3;
     s.traversal = traversal;
     s.variant = variant;
+    s.spec = spec_active ? 1 : 0;
     s.pl_list = pl_list.p;
     s.pl_count = pl_count.p;
     s.pl_cap = pl_cap;
@@ -432,34 +439,7 @@ __global__ void k_init_slots(DeviceState s, int64_t n, int has_type, int has_own
   s.ofx[i] = s.ofy[i] = s.ofz[i] = 0;
 }
 
-// periodic wrap of a coordinate that left the box (RegularGridDecomposition.cpp:555-590)
-__device__ __forceinline__ double wrap1(double x, double lo, double hi) {
-  // inside the box (the common case), decided on the order-preserving integer keys of the doubles: FP64
-  // compares go through this GPU's FP64 pipe (2 lanes per clock per SM)
-  const uint64_t kx = dbl_key(x);
-  if (kx >= dbl_key(lo) && kx < dbl_key(hi)) return x;
-  const double len = hi - lo;
-  if (x < lo) {
-    const double p = x + len;
-    const double just = nextafter(hi, lo);
-    return p < just ? p : just;
-  }
-  if (x >= hi) {
-    const double p = x - len;
-    return lo > p ? lo : p;
-  }
-  return x;
-}
 
-__global__ void k_wrap(DeviceState s, int64_t n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n || s.own[i] == 0) return;
-  const SysDev &S = s.sysd[s.sys[i]];
-  if (!S.periodic) return;
-  s.x[i] = wrap1(s.x[i], S.bmin[0], S.bmax[0]);
-  s.y[i] = wrap1(s.y[i], S.bmin[1], S.bmax[1]);
-  s.z[i] = wrap1(s.z[i], S.bmin[2], S.bmax[2]);
-}
 
 __device__ __forceinline__ void pack_xyz(const DeviceState &s, int64_t i, double px, double py, double pz) {
   s.pq[i] = pq_pack(s.sysd[s.sys[i]], px, py, pz, s.type[i], s.own[i], s.err);
@@ -469,15 +449,16 @@ __device__ __forceinline__ void pack_one(const DeviceState &s, int64_t i) { pack
 
 __global__ void k_pack(DeviceState s, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) pack_one(s, i);
+  if (i < n && (!s.spec || i < clusters_bound(s) * s.C)) pack_one(s, i);
 }
 
-// gather into the new slot order; dummies fill the cluster padding.  Every field of a particle is loaded before
+// gather into the new slot order, with each slot's compact position record; dummies fill the cluster padding.
+// Every field of a particle is loaded before
 // the first store: the source and destination arrays are reached through plain pointers, so a store between two
 // loads would make the second wait for the first (the compiler cannot rule out that they alias).
 __global__ void k_gather(DeviceState src, DeviceState dst, const int32_t *__restrict__ perm_src, int64_t nnew) {
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q >= nnew) return;
+  if (q >= nnew || (dst.spec && q >= clusters_bound(dst) * dst.C)) return;
   const int32_t p = perm_src[q];
   if (p >= 0) {
     const double x = __ldg(src.x + p), y = __ldg(src.y + p), z = __ldg(src.z + p);
@@ -496,11 +477,12 @@ __global__ void k_gather(DeviceState src, DeviceState dst, const int32_t *__rest
     dst.id[q] = id;
     dst.orig[q] = o;
     dst.slot_of[o] = (int32_t)q;
+    dst.pq[q] = pq_pack(dst.sysd[sy], x, y, z, ty, ow, dst.err);  // the compact record of the new slot
   } else {
     // dummy: same system as the first slot of its cluster (always a real particle), parked far outside
     const int64_t first = (q / dst.C) * dst.C;
     const int32_t pf = perm_src[first];
-    const int32_t sy = src.sys[pf];
+    const int32_t sy = pf >= 0 ? src.sys[pf] : 0;  // (a tower that did not fit a speculative sort: all dummies)
     const SysDev &S = dst.sysd[sy];
     dst.x[q] = S.bmin[0] - 1.0e4;
     dst.y[q] = S.bmin[1] - 1.0e4;
@@ -513,6 +495,7 @@ __global__ void k_gather(DeviceState src, DeviceState dst, const int32_t *__rest
     dst.own[q] = 0;
     dst.id[q] = -1;
     dst.orig[q] = -1;
+    dst.pq[q] = pq_pack(S, 0.0, 0.0, 0.0, 0, 0, dst.err);  // a dummy's record ignores the position
   }
 }
 
@@ -1042,47 +1025,82 @@ static int build_group_lists(pe_engine *h) {
 
 static int normalize_positions(pe_engine *h);
 
+static bool pruning(const pe_engine *h);
+
+// The tower-sort size a rebuild on speculative sizes assumes: the largest tower of the last rebuild with room to
+// grow by a quarter, as a power of two; 0 when there is no previous rebuild to go by.
+static int spec_tower_size(int64_t maxt) {
+  const int64_t want = std::max<int64_t>(2, maxt + maxt / 4 + 1);
+  int p2 = 2;
+  while (p2 < want) p2 <<= 1;
+  return p2 <= kTowerSortMax ? p2 : 0;
+}
+
+// One list rebuild (LogicHandler::rebuildNeighborLists, VerletClusterListsRebuilder).  After the binning the
+// rebuild needs the cluster total (the launch sizes of what follows) and the largest tower (the tower sort's
+// shared memory).  Without a previous rebuild to go by it reads them back (a host synchronisation).  Otherwise it
+// runs on the previous sizes: launches cover the slot capacity and bound themselves by the device's own cluster
+// total, the tower sort assumes the last rebuild's largest tower with room to grow, and the counts are read with
+// the list builds' flags at their synchronisation.  A tower that outgrew the assumed size is flagged; the host
+// then puts the old state back (the gather wrote the new order into the second buffers) and redoes the rebuild
+// with the read-back sizes.
 static int do_rebuild(pe_engine *h) {
   if (!h->have_particles) return h->fail(PE_ERR_STATE, "rebuild before pe_set_particles");
   PE_TRY(normalize_positions(h));
   cudaStream_t st = h->st;
+  const bool spec = h->spec_p2 > 0 && h->spec_ntowers == h->ntowers && h->spec_pcap == h->pcap && !pruning(h);
+  h->spec_active = false;
   DeviceState s = h->state();
   const int64_t nold = h->nslots;
+  const int64_t ncl_old = h->nclusters;
   h->launches += 1;
   if (!h->hwords.ensure(sizeof(RebuildWords), st))
     return h->fail(PE_ERR_OOM, "page-locked rebuild words");
   RebuildWords *w = static_cast<RebuildWords *>(h->hwords.p);
   PE_CUDA(h, cudaMemcpyAsync(&w->e_steps, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-  if (nold > 0) k_wrap<<<(unsigned)((nold + 255) / 256), 256, 0, st>>>(s, nold);
   PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
   launch_bin(s, nold, h->key.p, h->tower_of.p, st);
-  scan_exclusive_i32(h->tw_count.p, h->tw_start.p, h->ntowers, st);
-  launch_clusters_per_tower(s, h->tw_ncl.p, st);
-  scan_exclusive_i32(h->tw_ncl.p, h->tw_cl_start.p, h->ntowers, st);
-  PE_CUDA(h, cudaMemsetAsync(h->dmax.p, 0, sizeof(int), st));
-  if (h->ntowers > 0) k_max_i32<<<64, 256, 0, st>>>(h->tw_count.p, h->ntowers, h->dmax.p);
-  h->launches += 10;
+  if (launch_tower_tables(s, h->tw_ncl.p, h->dmax.p, st)) {
+    h->launches += 2;
+  } else {
+    scan_exclusive_i32(h->tw_count.p, h->tw_start.p, h->ntowers, st);
+    launch_clusters_per_tower(s, h->tw_ncl.p, st);
+    scan_exclusive_i32(h->tw_ncl.p, h->tw_cl_start.p, h->ntowers, st);
+    PE_CUDA(h, cudaMemsetAsync(h->dmax.p, 0, sizeof(int), st));
+    if (h->ntowers > 0) k_max_i32<<<64, 256, 0, st>>>(h->tw_count.p, h->ntowers, h->dmax.p);
+    h->launches += 10;
+  }
   PE_CUDA(h, cudaMemcpyAsync(&w->total_cl, h->tw_cl_start.p + h->ntowers, sizeof(int32_t), cudaMemcpyDeviceToHost,
                              st));
   PE_CUDA(h, cudaMemcpyAsync(&w->maxt, h->dmax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-  PE_CUDA(h, cudaStreamSynchronize(st));
-  PE_TRY(h->cuda_check("binning"));
-  const int e_steps = w->e_steps;
-  const int32_t total_cl = w->total_cl;
-  const int maxt = w->maxt;
-  if (e_steps & kErrEncode)
-    return h->fail(PE_ERR_DOMAIN, "a particle moved beyond the encodable range of its system between rebuilds");
-  if (maxt > kTowerSortMax)
-    return h->fail(PE_ERR_TOWER_OVERFLOW, "a tower holds %d particles; the on-chip tower sort supports %d", maxt,
-                   kTowerSortMax);
-  h->max_tower = maxt;
-  h->nclusters = total_cl;
-  const int64_t nnew = (int64_t)total_cl * h->C;
-  if (nnew > h->pcap) return h->fail(PE_ERR_STATE, "slot capacity exceeded (%lld > %lld)", (long long)nnew,
-                                     (long long)h->pcap);
+  // the counts read back and checked (at once after the binning, or with the list builds' flags)
+  auto check_counts = [&]() -> int {
+    if (w->e_steps & kErrEncode)
+      return h->fail(PE_ERR_DOMAIN, "a particle moved beyond the encodable range of its system between rebuilds");
+    if (w->maxt > kTowerSortMax)
+      return h->fail(PE_ERR_TOWER_OVERFLOW, "a tower holds %d particles; the on-chip tower sort supports %d", w->maxt,
+                     kTowerSortMax);
+    if ((int64_t)w->total_cl * h->C > h->pcap)
+      return h->fail(PE_ERR_STATE, "slot capacity exceeded (%lld > %lld)", (long long)w->total_cl * h->C,
+                     (long long)h->pcap);
+    return PE_OK;
+  };
+  int tower_p2 = 0;
+  if (!spec) {
+    PE_CUDA(h, cudaStreamSynchronize(st));
+    PE_TRY(h->cuda_check("binning"));
+    PE_TRY(check_counts());
+    h->nclusters = w->total_cl;
+    tower_p2 = std::max(w->maxt, 1);
+  } else {
+    h->spec_active = true;
+    h->nclusters = h->pcap / h->C;  // a capacity: the kernels bound themselves by the device's total
+    tower_p2 = h->spec_p2;
+  }
+  const int64_t nnew = h->nclusters * h->C;
   s = h->state();
   launch_scatter(s, nold, h->tower_of.p, h->key.p, h->tw_fill.p, h->skey.p, h->sval.p, st);
-  if (launch_tower_sort(s, h->skey.p, h->sval.p, h->perm_src.p, std::max(maxt, 1), st) != 0)
+  if (launch_tower_sort(s, h->skey.p, h->sval.p, h->perm_src.p, tower_p2, st) != 0)
     return h->fail(PE_ERR_TOWER_OVERFLOW, "tower too large");
   // gather into the second buffer set, then swap
   DeviceState dst = s;
@@ -1092,9 +1110,8 @@ static int do_rebuild(pe_engine *h) {
   std::swap(h->A, h->Bk);
   h->nslots = nnew;
   s = h->state();
-  if (nnew > 0) k_pack<<<(unsigned)((nnew + 255) / 256), 256, 0, st>>>(s, nnew);
   launch_cluster_bbox(s, st);
-  h->launches += 5;
+  h->launches += 4;
   // cluster-pair lists (grow the buffer and retry when it is too small), then the particle lists.  The list
   // build's flags are read at the particle-list build's synchronisation: a cluster-pair list that overflowed is
   // left empty (count 0), so the particle-list build still reads only valid entries, and both are redone.
@@ -1112,12 +1129,33 @@ static int do_rebuild(pe_engine *h) {
     PE_CUDA(h, cudaMemcpyAsync(&w->list_err, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     PE_CUDA(h, cudaMemcpyAsync(&w->list_total, h->cp_total.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                st));
-    int prc = (h->traversal == 1 || h->need_plist) ? build_particle_lists(h) : PE_OK;
+    const bool plist = h->traversal == 1 || h->need_plist;
+    int prc = plist ? build_particle_lists(h) : PE_OK;
     if (prc == PE_OK && h->traversal == 2) prc = build_group_lists(h);
-    PE_CUDA(h, cudaStreamSynchronize(st));
+    // the particle-list and pair-group builds synchronise to read their sizes, which also brings the flags above
+    // (a build that failed before its synchronisation leaves that to this one)
+    if (prc != PE_OK || (!plist && h->traversal != 2)) PE_CUDA(h, cudaStreamSynchronize(st));
     PE_TRY(h->cuda_check("list build"));
     const int e = w->list_err;
     const unsigned long long tot = w->list_total;
+    if (h->spec_active) {
+      // the rebuild ran on the previous sizes: the counts arrive now
+      h->spec_active = false;
+      PE_TRY(check_counts());
+      if (e & kErrSpecTower) {
+        // a tower outgrew the assumed size: the old state is intact in the second buffers; back to it, and
+        // rebuild with the read-back sizes
+        std::swap(h->A, h->Bk);
+        h->nslots = nold;
+        h->nclusters = ncl_old;
+        h->spec_p2 = 0;
+        h->spec_rebuilds_redone += 1;
+        PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));  // this attempt's flags are not the steps'
+        return do_rebuild(h);
+      }
+      h->nclusters = w->total_cl;
+      h->nslots = h->nclusters * h->C;
+    }
     if (e & kErrTowerOverflow) return h->fail(PE_ERR_TOWER_OVERFLOW, "tower overflow in sort");
     if (e & kErrEncode)
       return h->fail(PE_ERR_DOMAIN, "a particle lies beyond the encodable range of its system (more than "
@@ -1141,6 +1179,8 @@ static int do_rebuild(pe_engine *h) {
     break;
   }
   if (!listed) return h->fail(PE_ERR_LIST_OVERFLOW, "cluster-pair lists kept overflowing");
+  h->max_tower = w->maxt;
+  const int32_t total_cl = (int32_t)h->nclusters;
   const int ns = (int)h->sys.size();
   k_sys_ranges<<<(ns + 127) / 128, 128, 0, st>>>(h->tw_cl_start.p, h->sys_tower_base.p, ns, h->sys_cl_range.p);
   h->launches += 1;
@@ -1159,6 +1199,10 @@ static int do_rebuild(pe_engine *h) {
   if (h->nslots > 0)
     PE_CUDA(h, cudaMemcpyAsync(h->own_reb.p, h->A.own.p, (size_t)h->nslots, cudaMemcpyDeviceToDevice, st));
   PE_TRY(h->cuda_check("rebuild"));
+  // the sizes the next rebuild may assume
+  h->spec_p2 = spec_tower_size(h->max_tower);
+  h->spec_ntowers = h->ntowers;
+  h->spec_pcap = h->pcap;
   h->lists_valid = true;
   h->steps_since_rebuild = 0;
   h->rebuilds += 1;
@@ -2042,6 +2086,7 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out) {
   if (h->disp_bits.p)
     PE_CUDA(h, cudaMemcpy(&prunes, h->disp_bits.p + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost));
   out->prunes = prunes;
+  out->rebuilds_redone = h->spec_rebuilds_redone;
   if (reset) {
     if (h->disp_bits.p) PE_CUDA(h, cudaMemset(h->disp_bits.p + 2, 0, sizeof(unsigned int)));
     h->force_ev.clear();
@@ -2049,6 +2094,7 @@ int pe_get_stats(pe_engine *h, int reset, pe_stats *out) {
     h->force_launches = 0;
     h->launches = 0;
     h->rebuilds = 0;
+    h->spec_rebuilds_redone = 0;
     if (h->pairs_acc.p) PE_CUDA(h, cudaMemset(h->pairs_acc.p, 0, sizeof(long long)));
   }
   return PE_OK;

@@ -112,7 +112,15 @@ struct DeviceState {
   long long *pairs_acc = nullptr;  // running sum of interacting pairs over force evaluations
 
   int *err = nullptr;              // device error flags (DeviceError bits)
+  // 1 while a rebuild runs on the previous rebuild's sizes: nclusters and nslots are then capacities, and the
+  // rebuild kernels bound themselves by the device's own cluster total, tw_cl_start[ntowers]
+  int spec = 0;
 };
+
+// the number of clusters a rebuild kernel covers (see DeviceState::spec)
+__device__ __forceinline__ int64_t clusters_bound(const DeviceState &s) {
+  return s.spec ? min(s.nclusters, (int64_t)s.tw_cl_start[s.ntowers]) : s.nclusters;
+}
 
 __device__ __forceinline__ unsigned int f2bits(float v) { return __float_as_uint(v); }
 
@@ -145,6 +153,11 @@ void scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t
 // rebuild (pe_build.cu)
 void launch_bin(DeviceState &s, int64_t nslots_old, uint64_t *key, int32_t *tower_of, cudaStream_t st);
 void launch_clusters_per_tower(DeviceState &s, int32_t *ncl, cudaStream_t st);
+// the tower tables of a rebuild in one single-block launch (tower starts, clusters per tower, cluster starts with
+// the totals at index ntowers, the largest tower into *maxc); false beyond kTowerTablesMax towers, where the
+// caller uses the scans
+constexpr int64_t kTowerTablesMax = 32768;
+bool launch_tower_tables(DeviceState &s, int32_t *ncl, int *maxc, cudaStream_t st);
 void launch_scatter(DeviceState &s, int64_t nslots_old, const int32_t *tower_of, const uint64_t *key,
                     int32_t *fill, uint64_t *skey, int32_t *sval, cudaStream_t st);
 int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *perm_src, int max_tower,

@@ -55,7 +55,8 @@ class PeGlobals(C.Structure):
 
 class PeStats(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("force_launches", C.c_int64), ("kernel_launches", C.c_int64),
-                ("pairs_total", C.c_int64), ("rebuilds", C.c_int64), ("prunes", C.c_int64)]
+                ("pairs_total", C.c_int64), ("rebuilds", C.c_int64), ("prunes", C.c_int64),
+                ("rebuilds_redone", C.c_int64)]
 
 
 class PeTuningEntry(C.Structure):

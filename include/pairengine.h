@@ -219,8 +219,9 @@ int pe_pair_set(pe_engine *h, int which, int64_t cap, int64_t *a, int64_t *b, in
 /* Counters of the engine since the last reset: CUDA-event time of the force kernels launched outside CUDA
  * graphs (force_ms) and the number of launches it covers (force_launches), launches of the engine's own
  * kernels including those inside graph replays (kernel_launches), interacting pairs summed over all force
- * evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds, and
- * refreshes of the pruned inner lists (prunes; 0 unless prune_buffer > 0). */
+ * evaluations (each unordered pair once per evaluation; counted when calc_globals is on), rebuilds,
+ * refreshes of the pruned inner lists (prunes; 0 unless prune_buffer > 0), and rebuilds that ran on the previous
+ * rebuild's sizes and were redone because a tower outgrew them (rebuilds_redone). */
 typedef struct {
   double force_ms;
   int64_t force_launches;
@@ -228,6 +229,7 @@ typedef struct {
   int64_t pairs_total;
   int64_t rebuilds;
   int64_t prunes;
+  int64_t rebuilds_redone;
 } pe_stats;
 int pe_get_stats(pe_engine *h, int reset, pe_stats *out);
 

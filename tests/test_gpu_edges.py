@@ -158,3 +158,44 @@ def test_capped_force_soft_start_separates_overlaps(eng_mod):
     assert np.sqrt(r2.min()) > 0.7
     t = (V ** 2).sum() / (3 * n)
     assert 0.5 < t < 2.0
+
+
+def test_rebuild_on_previous_sizes_and_its_redo(eng_mod, orc):
+    """After a first rebuild, a rebuild runs on the previous rebuild's sizes (one host synchronisation); when a
+    tower outgrows the size it assumed (here: 160 particles moved into one tower's column), it is redone with the
+    read-back sizes.  After each rebuild the FP64 forces equal the oracle's to 1e-12 of the largest force."""
+    from autopas_gb300 import workloads
+    bmin, bmax = np.zeros(3), np.full(3, 20.0)
+    rc, skin = 2.5, 0.3
+    pos1 = workloads.rsa(2000, bmin, bmax, bmin, bmax, 0.85, seed=17)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_FP64, cluster_size=8,
+                           traversal=1)
+    e.set_particles(pos1)
+
+    def check(pos):
+        e.rebuild()
+        e.compute_forces()
+        F = e.forces()
+        allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+        R, _, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+        R = R[: len(pos)]
+        np.testing.assert_allclose(F, R, rtol=0, atol=1e-12 * np.abs(R).max())
+        return e.stats(reset=True)["rebuilds_redone"]
+
+    e.compute_forces()                     # the first rebuild reads its sizes back
+    assert check(pos1) == 0                # the same configuration: the previous sizes hold
+    maxt1 = e.info()["max_tower_size"]
+    assumed = 2
+    while assumed < maxt1 + maxt1 // 4 + 1:  # the size the next rebuild assumes (the engine's rule)
+        assumed *= 2
+    assert assumed < 160, "the scenario needs a dense column larger than the assumed tower size"
+    side, num, _, origin = e.tower_grid()
+    lo = np.array([origin[0] + 0.05, origin[1] + 0.05, bmin[2]])
+    hi = np.array([origin[0] + side[0] - 0.05, origin[1] + side[1] - 0.05, bmax[2]])
+    col = workloads.rsa(160, bmin, bmax, lo, hi, 0.7, seed=18)
+    pos2 = workloads.rsa(1840, bmin, bmax, bmin, bmax, 0.85, seed=19, existing=col)
+    e.update_positions(pos2)
+    assert check(pos2) == 1                # one tower outgrew the assumed size: redone
+    assert e.info()["max_tower_size"] >= 160
+    assert check(pos2) == 0                # the new sizes are assumed next time
+    e.close()
