@@ -478,6 +478,7 @@ def run_ensemble(args):
     vel = np.concatenate([s_["vel"] for s_ in systems])
     sysid = np.concatenate([np.full(len(s_["pos"]), k, np.int32) for k, s_ in enumerate(systems)])
     e = E.PairEngine(rc, skin, boxes, periodic=True, precision=E.PRECISION_MIXED, cluster_size=0, traversal=-1,
+                     newton3=args.newton3,
                      rebuild_frequency=reb, use_graphs=True)
     e.set_particles(pos, vel, system=sysid)
     e.compute_forces()
@@ -564,7 +565,7 @@ def run_mixture(args):
         e.set_particles(pos, vel, types=types)
         return e
 
-    e = engine(E.PRECISION_MIXED, cluster_size=0, traversal=-1)
+    e = engine(E.PRECISION_MIXED, cluster_size=0, traversal=-1, newton3=args.newton3)
     g0 = e.compute_forces()[0]
     F = e.forces()
     tuning = e.tuning()
@@ -701,17 +702,22 @@ def run_atm(args):
 # ---------------------------------------------------------------------------------------------- energy drift
 def run_drift(args):
     """Energy drift of the FP32-mixed and FP64 forms over --steps steps (default 10^4) on the FCC case:
-    20^3 unit cells (32,000 particles), density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, rebuild every 10."""
+    20^3 unit cells (32,000 particles), density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, rebuild every 10.
+    Each form also runs from three more starts whose velocities differ by a relative 1e-10: MD is chaotic, so two
+    trajectories part within a few thousand steps whatever their precision, and the spread of the drift over these
+    starts is the scale on which the two forms' drifts can be told apart."""
     import numpy as np
     import __graft_entry__
     __graft_entry__.build()
     from autopas_gb300 import engine as E, workloads
     pos, vel, bmin, bmax = workloads.fcc_lj(20, 0.8442, 0.72, seed=1)
     nsteps = max(args.steps, 10000)
-    out = {}
-    for name, prec in (("fp64", E.PRECISION_FP64), ("mixed", E.PRECISION_MIXED)):
+    rng = np.random.default_rng(5)
+    starts = [vel] + [vel * (1.0 + 1e-10 * rng.standard_normal(vel.shape)) for _ in range(3)]
+
+    def run(prec, v0):
         e = E.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10)
-        e.set_particles(pos, vel)
+        e.set_particles(pos, v0)
         g = e.compute_forces()[0]
         E0 = g["upot"] + g["ekin"]
         series = []
@@ -720,19 +726,31 @@ def run_drift(args):
             g = e.step(0.002, 100)[0]
             series.append(g["upot"] + g["ekin"])
         wall = time.perf_counter() - t0
+        e.close()
         s_ = np.array(series)
         slope = np.polyfit(np.arange(1, len(s_) + 1) * 100 * 0.002, s_ / len(pos), 1)[0]
-        out[name] = {"E0_per_particle": E0 / len(pos), "drift_rel": float((s_[-1] - E0) / abs(E0)),
-                     "max_dev_rel": float(np.abs(s_ - E0).max() / abs(E0)),
-                     "slope_per_particle_per_time": float(slope), "steps": nsteps,
-                     "steps_per_s": nsteps / wall}
-        e.close()
+        return {"E0_per_particle": E0 / len(pos), "drift_rel": float((s_[-1] - E0) / abs(E0)),
+                "max_dev_rel": float(np.abs(s_ - E0).max() / abs(E0)),
+                "slope_per_particle_per_time": float(slope), "steps": nsteps, "steps_per_s": nsteps / wall}
+
+    out, spread = {}, {}
+    for name, prec in (("fp64", E.PRECISION_FP64), ("mixed", E.PRECISION_MIXED)):
+        runs = [run(prec, v0) for v0 in starts]
+        out[name] = runs[0]
+        d = np.array([r["drift_rel"] for r in runs])
+        spread[name] = {"drift_rel": d.tolist(), "mean": float(d.mean()), "std": float(d.std(ddof=1)),
+                        "min": float(d.min()), "max": float(d.max())}
+    gap = abs(spread["mixed"]["mean"] - spread["fp64"]["mean"])
+    scale = spread["fp64"]["max"] - spread["fp64"]["min"]
     line = {"metric": "energy drift over MD steps, FP32-mixed vs FP64 (32,000-particle FCC LJ)",
             "value": out["mixed"]["drift_rel"], "unit": "relative total-energy change", "n_gpus": 1,
             "steps": nsteps, "warmup": 0, "higher_is_better": False, "data": "synthetic",
             "config": {"workload": "FCC 20^3 unit cells, density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, "
                                    "rebuild every 10, truncated LJ"},
-            "mixed": out["mixed"], "fp64": out["fp64"]}
+            "mixed": out["mixed"], "fp64": out["fp64"],
+            "starts": {"what": "drift_rel of each form from the same start and from three starts whose velocities "
+                               "differ by a relative 1e-10 (seeded)", "fp64": spread["fp64"], "mixed": spread["mixed"],
+                       "mean_gap": gap, "fp64_range": scale, "mixed_within_fp64_range": bool(gap <= scale)}}
     print(json.dumps(line), flush=True)
     return 0
 
