@@ -526,8 +526,8 @@ __global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int3
 // The chunk table of the per-system globals reduction, built on the device from the systems' cluster ranges:
 // system q's clusters [range[2q], range[2q+1]) are cut into chunks of kChunk clusters, chunk k of all systems
 // being (system, first cluster, end cluster); sys_chunk0[q] is system q's first chunk and sys_chunk0[nsys] the
-// number of chunks.  One block of 1024 threads, a thread per system, systems in tiles of 1024 carried over by a
-// running offset.  The host sizes the table for max_chunks = clusters / kChunk + nsys + 1, a bound on the count
+// number of chunks.  One block of 1024 threads: a thread per system scans the chunk counts (systems in tiles of
+// 1024 carried over by a running offset), then all threads write the chunks.  The host sizes the table for max_chunks = clusters / kChunk + nsys + 1, a bound on the count
 // (each system adds at most one partial chunk); entries beyond it are not written.
 __global__ void __launch_bounds__(1024) k_chunk_table(const int64_t *__restrict__ range, int nsys,
                                                       int64_t *__restrict__ chunks, int32_t *__restrict__ sys_chunk0,
@@ -564,21 +564,31 @@ __global__ void __launch_bounds__(1024) k_chunk_table(const int64_t *__restrict_
     }
     __syncthreads();
     const int first = base + (wid > 0 ? wsum[wid - 1] : 0) + x - cnt;
-    if (q < nsys) {
-      sys_chunk0[q] = first;
-      for (int c = 0; c < cnt; ++c) {
-        const int k = first + c;
-        if (k >= max_chunks) break;
-        chunks[3 * k] = q;
-        chunks[3 * k + 1] = a + (int64_t)c * kChunk;
-        chunks[3 * k + 2] = min(a + (int64_t)(c + 1) * kChunk, b);
-      }
-    }
+    if (q < nsys) sys_chunk0[q] = first;
     __syncthreads();
     if (threadIdx.x == blockDim.x - 1) base = first + cnt;
     __syncthreads();
   }
   if (threadIdx.x == 0) sys_chunk0[nsys] = base;
+  __syncthreads();
+  // the chunks themselves, by all threads: chunk k belongs to the last system whose first chunk is at or before k
+  // (a system without clusters has the same first chunk as the next one)
+  const int total = min(base, max_chunks);
+  for (int k = threadIdx.x; k < total; k += blockDim.x) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sys_chunk0[mid] <= k)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int64_t a = range[2 * lo], b = range[2 * lo + 1];
+    const int c = k - sys_chunk0[lo];
+    chunks[3 * k] = lo;
+    chunks[3 * k + 1] = a + (int64_t)c * kChunk;
+    chunks[3 * k + 2] = min(a + (int64_t)(c + 1) * kChunk, b);
+  }
 }
 
 // velocity-Verlet position half (TimeDiscretization.cpp:17-66 with globalForce 0) fused with the re-encode

@@ -245,6 +245,39 @@ def test_ensemble_systems_are_independent(eng_mod, orc, traversal):
                 assert gs[k]["upot"] == pytest.approx(glob[0], rel=1e-6)
 
 
+def test_ensemble_with_an_empty_system(eng_mod, orc):
+    """Three systems, the middle one without particles: it gets no reduction chunk (the chunks' systems are found
+    through the table of first chunks, which the empty system shares with the next), its globals are zero, and its
+    neighbours' forces and globals are their own oracle's (FP64 form, 1e-12)."""
+    from autopas_gb300 import workloads
+    systems = workloads.ensemble(2, nmin=600, nmax=3000, seed=8)
+    rc, skin = 2.5, 0.3
+    boxes = [(systems[0]["bmin"], systems[0]["bmax"]), (np.zeros(3), np.full(3, 9.0)),
+             (systems[1]["bmin"], systems[1]["bmax"])]
+    pos = np.concatenate([systems[0]["pos"], systems[1]["pos"]])
+    sysid = np.concatenate([np.zeros(len(systems[0]["pos"]), np.int32), np.full(len(systems[1]["pos"]), 2, np.int32)])
+    for traversal in (1, 2):
+        e = eng_mod.PairEngine(rc, skin, boxes, periodic=True, precision=eng_mod.PRECISION_FP64, traversal=1,
+                               cluster_size=8) if traversal == 1 else \
+            eng_mod.PairEngine(rc, skin, boxes, periodic=True, traversal=2, newton3=1, cluster_size=8)
+        e.set_particles(pos, system=sysid)
+        gs = e.compute_forces()
+        F = e.forces()
+        e.close()
+        assert gs[1]["upot"] == 0.0 and gs[1]["virial"] == 0.0 and gs[1]["num_pairs"] == 0
+        tol = 1e-12 if traversal == 1 else 1e-6
+        for k, s in ((0, systems[0]), (2, systems[1])):
+            allpos, own, _, _, _ = orc.periodic_system(s["pos"], s["bmin"], s["bmax"], rc, skin)
+            R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+            R = R[: len(s["pos"])]
+            Fk = F[sysid == k]
+            if traversal == 1:
+                np.testing.assert_allclose(Fk, R, rtol=0, atol=tol * np.abs(R).max())
+            else:
+                assert rel_rms(Fk, R) <= tol
+            assert gs[k]["upot"] == pytest.approx(glob[0], rel=tol)
+
+
 def test_more_systems_than_one_block_of_the_chunk_table(eng_mod, orc):
     """1,100 small systems in one engine: the globals reduction's chunk table is built on the device by one
     block of 1,024 threads, a thread per system, so these systems span two tiles of it.  Each system's Upot and
