@@ -469,6 +469,12 @@ __global__ void __launch_bounds__(kListWarps * 32) k_list_build(DeviceState s, i
   for (int sb = 0; sb < nseg && !overflow; sb += 32) {
     int cf = 0, ce = 0, code = kShiftNone;
     if (sb + lane < nseg) segment_run(s, S, tx, ty, sb + lane, nseg_z, alo, ahi, L2hi, Lz, cf, ce, code);
+    if (s.newton3) {
+      // forward neighbours only: clusters are numbered in tower order, so the run starts at A (an image of A
+      // itself only for a positive image code; the unshifted self entry is added above)
+      cf = max(cf, (int)A + (code > kShiftNone ? 0 : 1));
+      ce = max(ce, cf);
+    }
     // flatten the runs of the 32 segments into one candidate index space (exclusive prefix over lanes)
     const int len = ce - cf;
     int incl = len;
