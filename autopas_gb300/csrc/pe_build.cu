@@ -743,12 +743,21 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
   }
   const SysDev &S = s.sysd[sy];
   const unsigned int eb = S.pq_expb;
-  const float2 hx = make_float2(pq_hi(q0.x, eb), pq_hi(q1.x, eb));
-  const float2 hy = make_float2(pq_hi(q0.y, eb), pq_hi(q1.y, eb));
-  const float2 hz = make_float2(pq_hi(q0.z, eb), pq_hi(q1.z, eb));
+  float2 hx = make_float2(pq_hi(q0.x, eb), pq_hi(q1.x, eb));
+  float2 hy = make_float2(pq_hi(q0.y, eb), pq_hi(q1.y, eb));
+  float2 hz = make_float2(pq_hi(q0.z, eb), pq_hi(q1.z, eb));
   const float r2max = S.plist_r2max;
   // padding dummies close a cluster, so a group whose first member is a dummy has a dummy second member too
   const bool real = validA && pq_own(q0) != 0;
+  if (pq_own(q1) == 0) {
+    // a dummy second member: moved to 4x the first member's coordinates (encoded positions lie in [B, 2B), so
+    // this is at least 2B from every record), where no distance test keeps anything.  With the group's own
+    // pair excluded by index (jfirst), no test then needs r2 > 0: only dummies share a position.
+    const float far = 4.f * hx.x;
+    hx.y = far;
+    hy.y = far;
+    hz.y = far;
+  }
   int nmax = n;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
@@ -810,7 +819,7 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
         const float2 dy = add2(yh, dup2(hj.y));
         const float2 dz = add2(zh, dup2(hj.z));
         const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-        const bool keep = jj >= jfirst && ((r2.x > 0.f && r2.x <= r2max) || (r2.y > 0.f && r2.y <= r2max));
+        const bool keep = jj >= jfirst && (r2.x <= r2max || r2.y <= r2max);
         if (keep) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
         cnt += keep ? 1 : 0;
       }

@@ -55,6 +55,15 @@ __device__ __forceinline__ void kahan_add(float &sum, float &c, float v) {
   sum = t;
 }
 
+// kahan_add on both lanes of a pair, with packed instructions (a - b is a + (-b) bit for bit)
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void kahan_add2(float2 &sum, float2 &c, float2 v) {
+  const float2 y = add2(v, neg2(c));
+  const float2 t = add2(sum, y);
+  c = add2(add2(t, neg2(sum)), neg2(y));
+  sum = t;
+}
+
 // kinetic energy 0.5 m v^2 of slot i (FP64)
 __device__ __forceinline__ double kinetic(const DeviceState &s, int64_t i, int ti) {
   const double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
@@ -959,8 +968,7 @@ struct N3Acc {
   __device__ __forceinline__ void flush() {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      kahan_add(fs[c].x, fc[c].x, b[c].x);
-      kahan_add(fs[c].y, fc[c].y, b[c].y);
+      kahan_add2(fs[c], fc[c], b[c]);
       b[c] = make_float2(0.f, 0.f);
     }
   }
