@@ -174,6 +174,7 @@ struct pe_engine {
   DBuf<int64_t> sys_cl_range;
   DBuf<int64_t> chunks;        // (system, first cluster, end cluster) per reduction chunk
   DBuf<int32_t> sys_chunk0;    // first chunk of each system, [nsys+1]
+  DBuf<unsigned int> sys_done;  // chunks of each system reduced in the current evaluation (zero between them)
   DBuf<double> chunk_part;     // [nchunks*5]
   int nchunks = 0;  // a bound on the reduction chunks (their count is sys_chunk0[nsys] on the device)
   DBuf<int32_t> sys_tower_base;
@@ -531,7 +532,8 @@ __global__ void k_sys_ranges(const int32_t *__restrict__ tw_cl_start, const int3
 // (each system adds at most one partial chunk); entries beyond it are not written.
 __global__ void __launch_bounds__(1024) k_chunk_table(const int64_t *__restrict__ range, int nsys,
                                                       int64_t *__restrict__ chunks, int32_t *__restrict__ sys_chunk0,
-                                                      int max_chunks) {
+                                                      int max_chunks, double *__restrict__ sys_glob,
+                                                      long long *__restrict__ sys_hits) {
   __shared__ int32_t wsum[32];
   __shared__ int32_t base;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -565,6 +567,10 @@ __global__ void __launch_bounds__(1024) k_chunk_table(const int64_t *__restrict_
     __syncthreads();
     const int first = base + (wid > 0 ? wsum[wid - 1] : 0) + x - cnt;
     if (q < nsys) sys_chunk0[q] = first;
+    if (q < nsys && cnt == 0) {  // no chunk reduces this system: its globals are zero until the next rebuild
+      for (int g = 0; g < kSysGlob; ++g) sys_glob[kSysGlob * q + g] = 0.0;
+      sys_hits[q] = 0;
+    }
     __syncthreads();
     if (threadIdx.x == blockDim.x - 1) base = first + cnt;
     __syncthreads();
@@ -1200,9 +1206,11 @@ static int do_rebuild(pe_engine *h) {
     const int max_chunks = total_cl / kChunk + ns + 1;
     h->nchunks = max_chunks;
     if (!h->chunks.ensure(3 * (size_t)max_chunks) || !h->sys_chunk0.ensure(ns + 1) ||
-        !h->chunk_part.ensure((kGlob + 1) * (size_t)max_chunks))
+        !h->chunk_part.ensure((kGlob + 1) * (size_t)max_chunks) || !h->sys_done.ensure(ns))
       return h->fail(PE_ERR_OOM, "reduction chunks");
-    k_chunk_table<<<1, 1024, 0, st>>>(h->sys_cl_range.p, ns, h->chunks.p, h->sys_chunk0.p, max_chunks);
+    PE_CUDA(h, cudaMemsetAsync(h->sys_done.p, 0, sizeof(unsigned int) * ns, st));
+    k_chunk_table<<<1, 1024, 0, st>>>(h->sys_cl_range.p, ns, h->chunks.p, h->sys_chunk0.p, max_chunks,
+                                      h->sys_glob.p, h->sys_hits.p);
     h->launches += 1;
   }
   if (!h->own_reb.ensure((size_t)std::max<int64_t>(h->nslots, 1))) return h->fail(PE_ERR_OOM, "ownership record");
@@ -1297,8 +1305,8 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, b
   h->launches += 1;
   if (timed) h->force_launches += 1;
   if (h->cfg.calc_globals) {
-    launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->st);
-    h->launches += 2;
+    launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->sys_done.p, h->st);
+    h->launches += 1;
   }
   h->steps_since_rebuild += 1;
   h->forces_valid = true;
@@ -1538,6 +1546,7 @@ int pe_destroy(pe_engine *h) {
   for (auto *b : {&h->cp_start, &h->sys_cl_range, &h->dump_a, &h->dump_b, &h->chunks}) b->release();
   h->sys_chunk0.release();
   h->chunk_part.release();
+  h->sys_done.release();
   h->cp_list.release();
   h->cl_z.release();
   h->cl_bbf.release();

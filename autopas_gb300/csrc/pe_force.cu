@@ -1360,81 +1360,90 @@ __device__ __forceinline__ void warp_sum6(double (&g)[kGlob], long long &h) {
   }
 }
 
-// one warp per chunk of at most kChunk = 256 clusters: lane l sums clusters c0 + l + 32 m.  The grid covers a
-// bound on the chunk count; the count itself is sys_chunk0[nsys], written by the rebuild on the device.
+// One warp per chunk of at most kChunk = 256 clusters: lane l sums clusters c0 + l + 32 m into the chunk's partial.
+// The grid covers a bound on the chunk count; the count itself is sys_chunk0[nsys], written by the rebuild on the
+// device.  The warp that completes a system's last chunk (a counter per system, after a fence) then sums that
+// system's partials in index order (lane l takes partials l, l + 32, ...; a shuffle tree adds the lanes), writes the
+// system's globals and resets the counter: the result does not depend on which warp comes last, and no warp
+// waits.  Systems without particles have no chunk; the rebuild writes their globals (zero).
 __global__ void __launch_bounds__(kRedWarps * 32)
     k_reduce_chunks(DeviceState s, const int64_t *__restrict__ chunks, const int32_t *__restrict__ sys_chunk0,
-                    double *__restrict__ cpart) {
+                    double *__restrict__ cpart, unsigned int *__restrict__ sys_done) {
   const int k = blockIdx.x * kRedWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (k >= sys_chunk0[s.nsys]) return;  // a whole warp
   const int64_t c0 = chunks[3 * k + 1], c1 = chunks[3 * k + 2];
   double g[kGlob] = {0, 0, 0, 0, 0};
   long long h = 0;
-  for (int64_t c = c0 + lane; c < c1; c += 32) {
+  for (int64_t cb = c0 + lane; cb < c1; cb += 4 * 32) {  // four clusters per lane in flight at a time
+    double v[4][kGlob];
+    long long w[4];
 #pragma unroll
-    for (int q = 0; q < kGlob; ++q) g[q] += s.cl_glob[kGlob * c + q];
-    h += (long long)s.cl_hits[c];
+    for (int u = 0; u < 4; ++u) {
+      const int64_t c = cb + 32 * u;
+      const bool in = c < c1;
+#pragma unroll
+      for (int q = 0; q < kGlob; ++q) v[u][q] = in ? s.cl_glob[kGlob * c + q] : 0.0;
+      w[u] = in ? (long long)s.cl_hits[c] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int q = 0; q < kGlob; ++q) g[q] += v[u][q];
+      h += w[u];
+    }
   }
   warp_sum6(g, h);
+  const int sy = (int)chunks[3 * k];
+  int last = 0;
   if (lane == 0) {
     for (int q = 0; q < kGlob; ++q) cpart[(kGlob + 1) * k + q] = g[q];
     cpart[(kGlob + 1) * k + kGlob] = (double)h;
+    __threadfence();  // the partial before the count that announces it
+    const unsigned int nch = (unsigned int)(sys_chunk0[sy + 1] - sys_chunk0[sy]);
+    last = atomicAdd(&sys_done[sy], 1u) == nch - 1;
   }
-}
-
-// fixed-order sum of kGlob doubles and a count over a block: warp butterflies, then thread 0 over the warp sums
-__device__ __forceinline__ void block_sum6(double (&g)[kGlob], long long &h) {
-  __shared__ double wred[kRedWarps][kGlob];
-  __shared__ long long wh[kRedWarps];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  warp_sum6(g, h);
-  if (lane == 0) {
-    for (int q = 0; q < kGlob; ++q) wred[w][q] = g[q];
-    wh[w] = h;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < kGlob; ++q) g[q] = wred[0][q];
-    h = wh[0];
-    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-      for (int q = 0; q < kGlob; ++q) g[q] += wred[k][q];
-      h += wh[k];
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  __threadfence();  // the count seen before the partials are read
+  double t[kGlob] = {0, 0, 0, 0, 0};
+  long long hh = 0;
+  // four partials per lane in flight at a time (a system of 2M particles has about 1,000 chunks)
+  const int jend = sys_chunk0[sy + 1];
+  for (int j0 = sys_chunk0[sy] + lane; j0 < jend; j0 += 4 * 32) {
+    double v[4][kGlob + 1];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = j0 + 32 * u;
+#pragma unroll
+      for (int q = 0; q <= kGlob; ++q) v[u][q] = j < jend ? __ldcg(cpart + (kGlob + 1) * j + q) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int q = 0; q < kGlob; ++q) t[q] += v[u][q];
+      hh += (long long)v[u][kGlob];
     }
   }
-}
-
-// one block per system over its chunk partials (fixed assignment and tree), then the endTraversal scaling
-__global__ void __launch_bounds__(kRedWarps * 32)
-    k_reduce_systems(DeviceState s, const int32_t *__restrict__ sys_chunk0, const double *__restrict__ cpart) {
-  const int sy = blockIdx.x;
-  double g[kGlob] = {0, 0, 0, 0, 0};
-  long long hh = 0;
-  for (int k = sys_chunk0[sy] + threadIdx.x; k < sys_chunk0[sy + 1]; k += blockDim.x) {
-#pragma unroll
-    for (int q = 0; q < kGlob; ++q) g[q] += cpart[(kGlob + 1) * k + q];
-    hh += (long long)cpart[(kGlob + 1) * k + kGlob];
-  }
-  block_sum6(g, hh);
-  if (threadIdx.x != 0) return;
-  const double up = g[0] * 0.5 / 6.;
-  const double vx = g[1] * 0.5, vy = g[2] * 0.5, vz = g[3] * 0.5;
+  warp_sum6(t, hh);
+  if (lane != 0) return;
+  const double up = t[0] * 0.5 / 6.;
+  const double vx = t[1] * 0.5, vy = t[2] * 0.5, vz = t[3] * 0.5;
   s.sys_glob[kSysGlob * sy + 0] = up;
   s.sys_glob[kSysGlob * sy + 1] = vx + vy + vz;
   s.sys_glob[kSysGlob * sy + 2] = vx;
   s.sys_glob[kSysGlob * sy + 3] = vy;
   s.sys_glob[kSysGlob * sy + 4] = vz;
-  s.sys_glob[kSysGlob * sy + 5] = g[4];
+  s.sys_glob[kSysGlob * sy + 5] = t[4];
   const long long pairs = hh / 2;
   s.sys_hits[sy] = pairs;
   atomicAdd((unsigned long long *)s.pairs_acc, (unsigned long long)pairs);
+  sys_done[sy] = 0u;  // for the next evaluation (kernel boundaries order it before the next increments)
 }
 
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int max_chunks, const int32_t *sys_chunk0,
-                           double *cpart, cudaStream_t st) {
+                           double *cpart, unsigned int *sys_done, cudaStream_t st) {
   if (max_chunks > 0)
     k_reduce_chunks<<<(max_chunks + kRedWarps - 1) / kRedWarps, kRedWarps * 32, 0, st>>>(s, chunks, sys_chunk0,
-                                                                                        cpart);
-  if (s.nsys > 0) k_reduce_systems<<<s.nsys, kRedWarps * 32, 0, st>>>(s, sys_chunk0, cpart);
+                                                                                        cpart, sys_done);
 }
 
 }  // namespace pe

@@ -185,6 +185,6 @@ constexpr int kChunk = 256;  // clusters per globals-reduction chunk (8 per lane
 constexpr int kGlob = 5;      // per-cluster partials: 6*Upot, virial x, y, z, kinetic energy
 constexpr int kSysGlob = 6;   // per system: Upot, virial, virial x, y, z, kinetic energy
 void launch_reduce_globals(DeviceState &s, const int64_t *chunks, int max_chunks, const int32_t *sys_chunk0,
-                           double *cpart, cudaStream_t st);
+                           double *cpart, unsigned int *sys_done, cudaStream_t st);
 
 }  // namespace pe
