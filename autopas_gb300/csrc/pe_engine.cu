@@ -1302,7 +1302,7 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, b
     launch_prune_clear(s, h->st);
     h->launches += 1;
   }
-  h->launches += 1;
+  h->launches += (h->traversal == 2 && h->nslots > 0) ? 2 : 1;  // newton3: the force kernel and its finish
   if (timed) h->force_launches += 1;
   if (h->cfg.calc_globals) {
     launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->sys_done.p, h->st);
