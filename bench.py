@@ -701,7 +701,8 @@ def run_atm(args):
 
 # ---------------------------------------------------------------------------------------------- energy drift
 def run_drift(args):
-    """Energy drift of the FP32-mixed and FP64 forms over --steps steps (default 10^4) on the FCC case:
+    """Energy drift of the FP32-mixed (full lists, and newton3 pair-group lists) and FP64 forms over --steps steps
+    (default 10^4) on the FCC case:
     20^3 unit cells (32,000 particles), density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, rebuild every 10.
     Each form also runs from three more starts whose velocities differ by a relative 1e-10: MD is chaotic, so two
     trajectories part within a few thousand steps whatever their precision, and the spread of the drift over these
@@ -715,8 +716,8 @@ def run_drift(args):
     rng = np.random.default_rng(5)
     starts = [vel] + [vel * (1.0 + 1e-10 * rng.standard_normal(vel.shape)) for _ in range(3)]
 
-    def run(prec, v0):
-        e = E.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10)
+    def run(prec, v0, **kw):
+        e = E.PairEngine(2.5, 0.3, (bmin, bmax), periodic=True, precision=prec, rebuild_frequency=10, **kw)
         e.set_particles(pos, v0)
         g = e.compute_forces()[0]
         E0 = g["upot"] + g["ekin"]
@@ -734,23 +735,29 @@ def run_drift(args):
                 "slope_per_particle_per_time": float(slope), "steps": nsteps, "steps_per_s": nsteps / wall}
 
     out, spread = {}, {}
-    for name, prec in (("fp64", E.PRECISION_FP64), ("mixed", E.PRECISION_MIXED)):
-        runs = [run(prec, v0) for v0 in starts]
+    forms = (("fp64", E.PRECISION_FP64, {}), ("mixed", E.PRECISION_MIXED, {}),
+             ("mixed_newton3", E.PRECISION_MIXED, {"traversal": 2, "newton3": 1, "cluster_size": 8}))
+    for name, prec, kw in forms:
+        runs = [run(prec, v0, **kw) for v0 in starts]
         out[name] = runs[0]
         d = np.array([r["drift_rel"] for r in runs])
         spread[name] = {"drift_rel": d.tolist(), "mean": float(d.mean()), "std": float(d.std(ddof=1)),
                         "min": float(d.min()), "max": float(d.max())}
     gap = abs(spread["mixed"]["mean"] - spread["fp64"]["mean"])
+    gap_n3 = abs(spread["mixed_newton3"]["mean"] - spread["fp64"]["mean"])
     scale = spread["fp64"]["max"] - spread["fp64"]["min"]
     line = {"metric": "energy drift over MD steps, FP32-mixed vs FP64 (32,000-particle FCC LJ)",
             "value": out["mixed"]["drift_rel"], "unit": "relative total-energy change", "n_gpus": 1,
             "steps": nsteps, "warmup": 0, "higher_is_better": False, "data": "synthetic",
             "config": {"workload": "FCC 20^3 unit cells, density 0.8442, T* 0.72, rc 2.5, skin 0.3, dt 0.002, "
                                    "rebuild every 10, truncated LJ"},
-            "mixed": out["mixed"], "fp64": out["fp64"],
+            "mixed": out["mixed"], "fp64": out["fp64"], "mixed_newton3": out["mixed_newton3"],
             "starts": {"what": "drift_rel of each form from the same start and from three starts whose velocities "
                                "differ by a relative 1e-10 (seeded)", "fp64": spread["fp64"], "mixed": spread["mixed"],
-                       "mean_gap": gap, "fp64_range": scale, "mixed_within_fp64_range": bool(gap <= scale)}}
+                       "mixed_newton3": spread["mixed_newton3"],
+                       "mean_gap": gap, "mean_gap_newton3": gap_n3, "fp64_range": scale,
+                       "mixed_within_fp64_range": bool(gap <= scale),
+                       "mixed_newton3_within_fp64_range": bool(gap_n3 <= scale)}}
     print(json.dumps(line), flush=True)
     return 0
 
