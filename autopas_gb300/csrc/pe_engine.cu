@@ -1393,7 +1393,7 @@ static int tune(pe_engine *h, int samples) {
   const double per_step = 1.0 / std::max(1, h->cfg.rebuild_frequency);
   for (int C : Cs)
     for (int T : Ts) {
-      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : (T == 2 ? 3 : 1);
+      const int nv = T == 1 ? (h->precision == PE_PRECISION_FP64 ? 1 : 4) : (T == 2 ? 4 : 1);
       double reb_ms = 0;
       for (int v = 0; v < nv; ++v) {
         PE_TRY(apply_config(h, C, T, v));

@@ -976,9 +976,10 @@ struct N3Acc {
 
 // One group's force work: the group's own pair, its list walk, its own part into facc and the cluster globals.
 // Every thread of a warp calls it (the globals are reduced over the groups of a cluster with shuffles).
-template <int C, int GM, bool ONE_TYPE>
+template <int C, int GM, bool ONE_TYPE, bool SORTED = false>
 __device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &fa, int64_t g,
-                                         const float (*tab)[kMaxTypes * kMaxTypes]) {
+                                         const float (*tab)[kMaxTypes * kMaxTypes], float (*sg)[128] = nullptr,
+                                         int *sh = nullptr, int slot = 0) {
   constexpr int GL = C / 2;  // groups per cluster
   const int T = s.ntypes;
   const int64_t i0 = 2 * g;
@@ -1073,6 +1074,15 @@ __device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &
     float g0 = 2.f * (acc.pot.x + acc.pot.y);
     float g1 = -2.f * (acc.vx.x + acc.vx.y), g2 = -2.f * (acc.vy.x + acc.vy.y), g3 = -2.f * (acc.vz.x + acc.vz.y);
     int h = 2 * acc.hits;
+    if (SORTED) {
+      // the groups of a cluster are not in neighbouring lanes: the block sums them (k_lj_mixed_n3_sorted)
+      sg[0][slot] = g0;
+      sg[1][slot] = g1;
+      sg[2][slot] = g2;
+      sg[3][slot] = g3;
+      sh[slot] = h;
+      return;
+    }
 #pragma unroll
     for (int o = 1; o < GL; o <<= 1) {
       g0 += __shfl_xor_sync(0xffffffffu, g0, o);
@@ -1192,6 +1202,78 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceA
   n3_group<C, GM, ONE_TYPE>(s, fa, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, tab);
 }
 
+// The same with the block's 128 groups taken in decreasing order of list length: a warp runs as long as its
+// longest list, and list lengths fluctuate by ~20% from group to group, so warps of similar lengths keep more lanes
+// busy.  The permutation is a bitonic sort of (length, index) in shared memory; the cluster globals are summed by
+// the block in group order (the groups of a cluster no longer share a warp).
+template <int C, int GM, bool ONE_TYPE, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3_sorted(DeviceState s, ForceArgs fa) {
+  constexpr int GL = C / 2;
+  __shared__ float tab[3][kMaxTypes * kMaxTypes];
+  __shared__ unsigned int key[128];
+  __shared__ float sg[4][128];
+  __shared__ int sh[128];
+  const int t = threadIdx.x;
+  if (!ONE_TYPE) {
+    for (int q = t; q < s.ntypes * s.ntypes; q += blockDim.x) {
+      tab[0][q] = s.types->eps24f[q];
+      tab[1][q] = s.types->sig2f[q];
+      tab[2][q] = s.types->shrf[q];
+    }
+  }
+  const int64_t gb = blockIdx.x * (int64_t)128;
+  const int64_t ng = s.nslots / 2;
+  int n = 0;
+  if (gb + t < ng && pq_own(s.pq[2 * (gb + t)]) != 0) n = min(s.gl_count[gb + t], 0xFFFFFF);
+  key[t] = ((unsigned int)(0xFFFFFF - n) << 7) | (unsigned int)t;  // ascending key = decreasing length, then index
+  for (int size = 2; size <= 128; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      __syncthreads();
+      if (t < 64) {
+        const int lo = 2 * t - (t & (stride - 1)), hi = lo + stride;
+        const unsigned int a = key[lo], b = key[hi];
+        if ((a > b) == ((lo & size) == 0)) {
+          key[lo] = b;
+          key[hi] = a;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const int slot = (int)(key[t] & 127u);
+  n3_group<C, GM, ONE_TYPE, true>(s, fa, gb + slot, tab, sg, sh, slot);
+  if (GM > 0) {
+    __syncthreads();
+    if (t < 128 / GL) {
+      const int64_t cl = gb / GL + t;
+      if (cl * C < s.nslots) {
+        // the cluster's groups added pairwise, (g0 + g1) + (g2 + g3), the order of the unsorted kernel's xor
+        // butterflies, so that both variants give the same cluster sums
+        float v[4][GL];
+        int h = 0;
+#pragma unroll
+        for (int q = 0; q < GL; ++q) {
+          const int k = t * GL + q;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) v[c][q] = sg[c][k];
+          h += sh[k];
+        }
+#pragma unroll
+        for (int w = 1; w < GL; w <<= 1)
+#pragma unroll
+          for (int q = 0; q + w < GL; q += 2 * w)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) v[c][q] += v[c][q + w];
+        s.cl_glob[kGlob * cl + 0] = (double)v[0][0];
+        s.cl_glob[kGlob * cl + 1] = (double)v[1][0];
+        s.cl_glob[kGlob * cl + 2] = (double)v[2][0];
+        s.cl_glob[kGlob * cl + 3] = (double)v[3][0];
+        s.cl_hits[cl] = (unsigned long long)h;
+      }
+    }
+  }
+}
+
 // one thread per slot; a warp past the last slot leaves whole (the kinetic energy is reduced with shuffles)
 template <int C, bool GLOB>
 __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) {
@@ -1202,7 +1284,10 @@ __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) 
 
 template <int C, int GM, bool ONE_TYPE, int MINB>
 static void launch_n3(DeviceState &s, const ForceArgs &fa, int64_t ng, cudaStream_t st) {
-  k_lj_mixed_n3<C, GM, ONE_TYPE, MINB><<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(s, fa);
+  if (s.variant == 3)
+    k_lj_mixed_n3_sorted<C, GM, ONE_TYPE, MINB><<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(s, fa);
+  else
+    k_lj_mixed_n3<C, GM, ONE_TYPE, MINB><<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(s, fa);
 }
 
 template <int C, int MINB>
@@ -1222,7 +1307,7 @@ static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, int64_t ng, cu
 }
 
 // kernel variants (the tuner's choice): the register cap for 5 (variant 0), 6 (1) or 4 (2) resident blocks of
-// 128 threads per SM.  Then the finish of every slot.
+// 128 threads per SM, or (3) 5 blocks with each block's groups sorted by list length.  Then the finish of every slot.
 template <int C>
 static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st) {
   const int64_t ng = s.nslots / 2;

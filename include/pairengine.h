@@ -104,7 +104,8 @@ typedef struct {
                               4 entries): 0: 96 registers, 5 blocks per SM, 1: 80 registers, 6 blocks, 2: the
                               next batch gathered during the current one, 4 blocks, 3: as 1 with list entries
                               streamed past the caches.  Traversal 2: 0, 1, 2 cap the registers for 5, 6, 4
-                              blocks of 128 threads per SM.  The tuner picks its own. */
+                              blocks of 128 threads per SM; 3: 5 blocks, each block's pair groups taken in
+                              decreasing order of list length.  The tuner picks its own. */
 } pe_config;
 
 /* One particle system of the ensemble. */

@@ -179,3 +179,26 @@ def test_newton3_configuration_rules(eng_mod):
         with pytest.raises(eng_mod.EngineError) as ei:
             eng_mod.PairEngine(2.5, 0.3, box, **args)
         assert ei.value.code == -1, kw
+
+
+@pytest.mark.parametrize("C", [4, 8])
+def test_newton3_sorted_variant(eng_mod, orc, C):
+    """Kernel variant 3 takes each block's groups in decreasing order of list length; a group's accumulation does
+    not depend on its lane, and the block sums a cluster's groups in the butterflies' order, so Upot, virial and the
+    pair count are the unsorted variant's bit for bit, and the forces are the oracle's."""
+    pos, vel, bmin, bmax = liquid(8, seed=17)
+    rc, skin = 2.5, 0.3
+    out = {}
+    for v in (0, 3):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, cluster_size=C, traversal=2, newton3=1,
+                               kernel_variant=v)
+        e.set_particles(pos, vel)
+        out[v] = (e.compute_forces()[0], e.forces())
+        e.close()
+    (g0, F0), (g3, F3) = out[0], out[3]
+    assert (g3["upot"], g3["virial"], g3["num_pairs"]) == (g0["upot"], g0["virial"], g0["num_pairs"])
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+    R = R[: len(pos)]
+    assert rel_rms(F3, R) <= 1e-6
+    assert g3["upot"] == pytest.approx(glob[0], rel=1e-6)
