@@ -314,9 +314,17 @@ __global__ void k_cluster_bbox(DeviceState s) {
   if (c >= clusters_bound(s)) return;
   const int C = s.C;
   double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  // the z window of the tower search spans every particle of the caller's (dummies too: they are z-sorted with
+  // the others), so that the windows of a tower's clusters stay monotone even where a cluster holds dummies only;
+  // cluster padding sits outside every window
+  double wlo = INFINITY, whi = -INFINITY;
   int flags = 0;
   for (int q = 0; q < C; ++q) {
     const int64_t i = c * C + q;
+    if (s.orig[i] >= 0) {
+      wlo = fmin(wlo, s.z[i]);
+      whi = fmax(whi, s.z[i]);
+    }
     const int o = s.own[i];
     if (o == 0) continue;
     flags |= 2;
@@ -335,7 +343,7 @@ __global__ void k_cluster_bbox(DeviceState s) {
   const float4 hif = make_float4(__double2float_ru(hi[0]), __double2float_ru(hi[1]), __double2float_ru(hi[2]), 0.f);
   s.cl_bbf[2 * c] = lof;
   s.cl_bbf[2 * c + 1] = hif;
-  s.cl_z[c] = make_float2(lof.z, hif.z);
+  s.cl_z[c] = make_float2(__double2float_rd(wlo), __double2float_ru(whi));
   s.cl_flags[c] = flags;
   s.cl_sys[c] = s.sys[c * C];
 }
@@ -719,8 +727,8 @@ template <int C>
 __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
   constexpr int GL = C / 2;   // groups (lanes) per cluster
   constexpr int G = 32 / GL;  // clusters per warp
-  // the current j-cluster of each cluster of the warp, hi parts negated, one float4 (x, y, z, -) per particle; one
-  // float4 of padding per row puts the rows of the warp's clusters in different banks
+  // the current j-cluster of each cluster of the warp, hi parts negated, one float4 (x, y, z, ownership) per
+  // particle; one float4 of padding per row puts the rows of the warp's clusters in different banks
   __shared__ float4 sj[4][G][C + 1];
   // each lane's last two blocks of entries (a ring of 16; up to C <= 8 appends per cluster pair complete at most one
   // block); 17 words per lane keep lanes that append at the same ring position in different banks
@@ -747,16 +755,20 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
   float2 hy = make_float2(pq_hi(q0.y, eb), pq_hi(q1.y, eb));
   float2 hz = make_float2(pq_hi(q0.z, eb), pq_hi(q1.z, eb));
   const float r2max = S.plist_r2max;
-  // padding dummies close a cluster, so a group whose first member is a dummy has a dummy second member too
-  const bool real = validA && pq_own(q0) != 0;
-  if (pq_own(q1) == 0) {
-    // a dummy second member: moved to 4x the first member's coordinates (encoded positions lie in [B, 2B), so
-    // this is at least 2B from every record), where no distance test keeps anything.  With the group's own
-    // pair excluded by index (jfirst), no test then needs r2 > 0: only dummies share a position.
-    const float far = 4.f * hx.x;
-    hx.y = far;
-    hy.y = far;
-    hz.y = far;
+  // a group with a real member (padding dummies close a cluster; a particle the caller marked as a dummy may sit
+  // anywhere in it)
+  const bool real = validA && (pq_own(q0) != 0 || pq_own(q1) != 0);
+  // with explicit halos, a group of halo particles keeps only owned j (a halo-halo pair counts for nothing)
+  const bool halo_group = s.any_halo_sys && pq_own(q0) != 1 && pq_own(q1) != 1;
+  if (pq_own(q0) == 0 || pq_own(q1) == 0) {
+    // a dummy member: moved to 4x the other member's coordinates (encoded positions lie in [B, 2B), so this is
+    // at least 2B from every record), where no distance test keeps anything.  Dummy j are not kept and the
+    // group's own pair is excluded by index (jfirst), so no test needs r2 > 0.
+    const bool d0 = pq_own(q0) == 0;
+    const float far = 4.f * (d0 ? hx.y : hx.x);
+    (d0 ? hx.x : hx.y) = far;
+    (d0 ? hy.x : hy.y) = far;
+    (d0 ? hz.x : hz.y) = far;
   }
   int nmax = n;
 #pragma unroll
@@ -798,7 +810,8 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
     if (fwd) {
 #pragma unroll
       for (int u = 0; u < 2; ++u)
-        sj[w][cg][2 * gl + u] = make_float4(pq_nhi(pc[u].x, eb), pq_nhi(pc[u].y, eb), pq_nhi(pc[u].z, eb), 0.f);
+        sj[w][cg][2 * gl + u] = make_float4(pq_nhi(pc[u].x, eb), pq_nhi(pc[u].y, eb), pq_nhi(pc[u].z, eb),
+                                            (float)pq_own(pc[u]));
     }
     __syncwarp();
     if (fwd && real) {
@@ -819,7 +832,8 @@ __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
         const float2 dy = add2(yh, dup2(hj.y));
         const float2 dz = add2(zh, dup2(hj.z));
         const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-        const bool keep = jj >= jfirst && (r2.x <= r2max || r2.y <= r2max);
+        const bool keep = jj >= jfirst && (r2.x <= r2max || r2.y <= r2max) && hj.w != 0.f &&
+                          (!halo_group || hj.w == 1.f);
         if (keep) stg[cnt & (2 * kPlistBlock - 1)] = ebase + ((uint32_t)jj << 5);
         cnt += keep ? 1 : 0;
       }
@@ -1121,16 +1135,21 @@ __global__ void k_pair_dump_glist(DeviceState s, int which, int64_t cap, int64_t
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (2 * g >= s.nslots) return;
   const int64_t i0 = 2 * g, i1 = 2 * g + 1;
-  if (s.own[i0] == 0) return;
-  const SysDev &S = s.sysd[s.sys[i0]];
-  if (s.own[i1] != 0) dump_one(s, S, which, cap, i0, i1, kShiftNone, oa, ob, oc, count);
+  const int o0 = s.own[i0], o1 = s.own[i1];
+  if (o0 == 0 && o1 == 0) return;
+  const SysDev &S = s.sysd[s.sys[o0 != 0 ? i0 : i1]];
+  // dummies take part in no pair, and a pair of two explicit halo particles is not a pair of the container (the
+  // force kernel gives it no weight)
+  if (o0 != 0 && o1 != 0 && (o0 == 1 || o1 == 1)) dump_one(s, S, which, cap, i0, i1, kShiftNone, oa, ob, oc, count);
   const int n = min(s.gl_count[g], s.gl_cap);
   for (int k = 0; k < n; ++k) {
     const uint32_t ent = s.gl_list[plist_index(s.gl_stride, g, k)];
     const int64_t j = ent >> 5;
     const int code = ent & 31;
-    dump_one(s, S, which, cap, i0, j, code, oa, ob, oc, count);
-    if (s.own[i1] != 0) dump_one(s, S, which, cap, i1, j, code, oa, ob, oc, count);
+    const int oj = s.own[j];
+    if (oj == 0) continue;
+    if (o0 != 0 && (o0 == 1 || oj == 1)) dump_one(s, S, which, cap, i0, j, code, oa, ob, oc, count);
+    if (o1 != 0 && (o1 == 1 || oj == 1)) dump_one(s, S, which, cap, i1, j, code, oa, ob, oc, count);
   }
 }
 

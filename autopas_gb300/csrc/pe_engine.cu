@@ -704,7 +704,10 @@ __global__ void k_update_own(DeviceState s, int64_t n, const int8_t *__restrict_
   if (u >= n) return;
   const int32_t q = s.slot_of[u];
   const int o = own[u];
-  if (o != 0 && own_reb[q] == 0) atomicOr(flag, 1);
+  // a particle that was a dummy at the rebuild is in no list; one that was a halo has no list of its own and no
+  // entries towards other halos: a dummy becoming real, or a halo becoming owned, needs new lists
+  const int r = own_reb[q];
+  if ((o != 0 && r == 0) || (o == 1 && r != 1)) atomicOr(flag, 1);
   if (o == s.own[q]) return;
   s.own[q] = (int8_t)o;
   pack_one(s, q);
@@ -1253,14 +1256,12 @@ static bool fused_positions_ok(const pe_engine *h) {
          !(h->cfg.atm_nu > 0) && !(h->force_cap > 0);
 }
 
-// The newton3 traversal (pair-group half lists) serves the mixed form on periodic systems without three-body
-// forces or rolling pruning, when the configuration allows newton3.
+// The newton3 traversal (pair-group half lists) serves the mixed form without three-body forces or rolling
+// pruning, when the configuration allows newton3; periodic systems and systems with explicit halo particles alike
+// (a pair with a halo endpoint weighs its owned endpoints, as the reference's newton3 energy factor does).
 static bool newton3_allowed(const pe_engine *h) {
-  if (h->cfg.newton3 == 0 || h->precision != PE_PRECISION_MIXED || h->cfg.atm_nu > 0 || h->cfg.prune_buffer > 0)
-    return false;
-  for (const auto &S : h->sys)
-    if (!S.desc.periodic) return false;
-  return true;
+  return h->cfg.newton3 != 0 && h->precision == PE_PRECISION_MIXED && !(h->cfg.atm_nu > 0) &&
+         !(h->cfg.prune_buffer > 0);
 }
 
 static VVFactors vv_factors(const pe_engine *h, double dt) {
@@ -1456,13 +1457,11 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->atm_nu > 0 && !(cfg->atm_cutoff > 0 && cfg->atm_cutoff <= cfg->cutoff + cfg->skin)) return PE_ERR_ARG;
   if (cfg->prune_buffer < 0 || cfg->prune_buffer > cfg->skin) return PE_ERR_ARG;
   if (cfg->kernel_variant < 0 || cfg->kernel_variant > 3) return PE_ERR_ARG;
-  // newton3 (pair-group half lists): the mixed form, periodic systems, no three-body forces or pruning
+  // newton3 (pair-group half lists): the mixed form, no three-body forces or pruning
   if (cfg->newton3 == 1 || cfg->traversal == 2) {
     if (cfg->precision != PE_PRECISION_MIXED || cfg->atm_nu > 0 || cfg->prune_buffer > 0 || cfg->newton3 == 0)
       return PE_ERR_ARG;
     if (cfg->traversal == 0 || cfg->traversal == 1) return PE_ERR_ARG;
-    for (int q = 0; q < num_systems; ++q)
-      if (!systems[q].periodic) return PE_ERR_ARG;
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PE_ERR_NO_DEVICE;
@@ -1725,7 +1724,7 @@ int pe_update_ownership(pe_engine *h, const int8_t *ownership, int *lists_valid)
       PE_CUDA(h, cudaStreamSynchronize(st));
     }
   } else if (w->pad & 1) {
-    h->lists_valid = false;  // a particle that was a dummy at the rebuild became real
+    h->lists_valid = false;  // a dummy at the rebuild became real, or a halo became owned
   }
   h->forces_valid = false;
   if (lists_valid) *lists_valid = h->lists_valid ? 1 : 0;

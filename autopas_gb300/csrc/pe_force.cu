@@ -886,14 +886,17 @@ struct N3Acc {
   float2 b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   float2 pot = {0.f, 0.f}, vx = {0.f, 0.f}, vy = {0.f, 0.f}, vz = {0.f, 0.f};
   int hits = 0;
+  // GM == 2 (systems with explicit halo particles): 1 for an owned member, 0 for a halo one
+  float2 oi = {1.f, 1.f};
 
   // LJ of the two pairs (i0, j) and (i1, j) from their displacements; returns minus the forces on i0, i1 (the
   // forces on j summed over the two are their sum) with the cutoff masks applied.  k0, k1: type-pair indices.
+  // oj: 1 when j is owned (used with GM == 2).
   __device__ __forceinline__ void lj2(const DeviceState &s, const SysDev &S, const ForceArgs &fa, int64_t i0,
                                       int64_t j, int code, float2 dx, float2 dy, float2 dz, float2 r2, bool live1,
                                       int k0, int k1, float eps24, float sig2, float shr,
                                       const float (*tab)[kMaxTypes * kMaxTypes], float band, float2 &px, float2 &py,
-                                      float2 &pz, bool &any) {
+                                      float2 &pz, bool &any, float oj = 1.f) {
     bool m0 = r2.x <= fa.rc2f, m1 = live1 && r2.y <= fa.rc2f;
     const float2 off = add2(r2, dup2(-fa.rc2f));
     const bool n0 = fabsf(off.x) <= band, n1 = live1 && fabsf(off.y) <= band;
@@ -918,7 +921,16 @@ struct N3Acc {
     px = mul2(dx, nfac);
     py = mul2(dy, nfac);
     pz = mul2(dz, nfac);
-    if (GM > 0) {
+    if (GM == 2) {
+      // explicit halos: a pair weighs its owned endpoints (the newton3 energy factor, LJFunctor.h:327-345), and
+      // counts when one of them is owned
+      const float2 w = add2(oi, dup2(oj));
+      pot = fma2(mul2(em, w), add2(lj12m6, sh), pot);
+      vx = fma2(mul2(px, w), dx, vx);
+      vy = fma2(mul2(py, w), dy, vy);
+      vz = fma2(mul2(pz, w), dz, vz);
+      hits += ((m0 && w.x > 0.f) ? 1 : 0) + ((m1 && w.y > 0.f) ? 1 : 0);
+    } else if (GM > 0) {
       pot = fma2(em, add2(lj12m6, sh), pot);
       vx = fma2(px, dx, vx);
       vy = fma2(py, dy, vy);
@@ -957,7 +969,7 @@ struct N3Acc {
     float2 px, py, pz;
     bool any;
     lj2(s, S, fa, i0, j, code, dx, dy, dz, r2, live1, ti.x * T + tj, ti.y * T + tj, eps24, sig2, shr, tab, band, px,
-        py, pz, any);
+        py, pz, any, GM == 2 ? (pq_own(qj) == 1 ? 1.f : 0.f) : 1.f);
     b[0] = add2(b[0], px);
     b[1] = add2(b[1], py);
     b[2] = add2(b[2], pz);
@@ -990,15 +1002,32 @@ __device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &
     q0 = s.pq[i0];
     q1 = s.pq[i0 + 1];
     sy = s.sys[i0];
-    if (pq_own(q0) != 0) n = s.gl_count[g];
+    n = s.gl_count[g];  // 0 for a group of padding dummies
   }
-  const bool live0 = pq_own(q0) == 1, live1 = pq_own(q1) == 1;
+  // members that take part: owned ones, and where some system has explicit halos, halo ones too (their pairs
+  // with owned particles count; their own forces are dropped by the finish)
+  const bool halos = GM == 2 || (GM == 0 && s.any_halo_sys != 0);
+  const bool live0 = halos ? pq_own(q0) != 0 : pq_own(q0) == 1;
+  const bool live1 = halos ? pq_own(q1) != 0 : pq_own(q1) == 1;
   const SysDev &S = s.sysd[sy];
   const unsigned int eb = S.pq_expb;
   const float u = S.pq_unit;
   float2 iq[6] = {make_float2(pq_hi(q0.x, eb), pq_hi(q1.x, eb)), make_float2(pq_hi(q0.y, eb), pq_hi(q1.y, eb)),
                   make_float2(pq_hi(q0.z, eb), pq_hi(q1.z, eb)), make_float2(pq_lox(q0), pq_lox(q1)),
                   make_float2(pq_loy(q0), pq_loy(q1)), make_float2(pq_loz(q0), pq_loz(q1))};
+  if (!live0) {
+    // a member that takes no part (a dummy, possibly one since the lists were built, where other dummies sit):
+    // 4x its coordinates lie at least 2B from every record (encoded positions lie in [B, 2B)), so every pair of
+    // it is beyond the cutoff and finite, and the cutoff masks drop it
+    iq[0].x *= 4.f;
+    iq[1].x *= 4.f;
+    iq[2].x *= 4.f;
+  }
+  if (!live1) {
+    iq[0].y *= 4.f;
+    iq[1].y *= 4.f;
+    iq[2].y *= 4.f;
+  }
   const int2 ti = make_int2(pq_type(q0), pq_type(q1));
   float eps24 = 0.f, sig2 = 0.f, shr = 0.f;
   if (ONE_TYPE) {
@@ -1011,6 +1040,7 @@ __device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &
   asm volatile("" : "+f"(eps24), "+f"(sig2), "+f"(shr));
   const float band = fa.rc2f * 2e-6f;
   N3Acc<GM, ONE_TYPE> acc;
+  if (GM == 2) acc.oi = make_float2(pq_own(q0) == 1 ? 1.f : 0.f, pq_own(q1) == 1 ? 1.f : 0.f);
   // the group's own pair (i0, i1), once
   if (live0 && live1) {
     const float ax = iq[0].x - iq[0].y, ay = iq[1].x - iq[1].y, az = iq[2].x - iq[2].y;
@@ -1020,7 +1050,8 @@ __device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &
     float2 px, py, pz;
     bool any;
     acc.lj2(s, S, fa, i0, i0 + 1, kShiftNone, make_float2(dx, dx), make_float2(dy, dy), make_float2(dz, dz),
-            make_float2(r2, r2), false, ti.x * T + ti.y, ti.x * T + ti.y, eps24, sig2, shr, tab, band, px, py, pz, any);
+            make_float2(r2, r2), false, ti.x * T + ti.y, ti.x * T + ti.y, eps24, sig2, shr, tab, band, px, py, pz, any,
+            acc.oi.y);
     // .x holds minus the force on i0; i1 gets the opposite
     acc.b[0] = make_float2(px.x, -px.x);
     acc.b[1] = make_float2(py.x, -py.x);
@@ -1070,9 +1101,11 @@ __device__ __forceinline__ void n3_group(const DeviceState &s, const ForceArgs &
                                              acc.fc[2].y - acc.fs[2].y, 0.f));
   }
   if (GM > 0) {
-    // newton3 energy factor 2 (both members and j owned: the engine runs this path on periodic systems only)
-    float g0 = 2.f * (acc.pot.x + acc.pot.y);
-    float g1 = -2.f * (acc.vx.x + acc.vx.y), g2 = -2.f * (acc.vy.x + acc.vy.y), g3 = -2.f * (acc.vz.x + acc.vz.y);
+    // the newton3 energy factor: 2 for a periodic system (every particle owned); with explicit halos (GM == 2)
+    // each pair already carries its owned endpoints
+    constexpr float ef = GM == 2 ? 1.f : 2.f;
+    float g0 = ef * (acc.pot.x + acc.pot.y);
+    float g1 = -ef * (acc.vx.x + acc.vx.y), g2 = -ef * (acc.vy.x + acc.vy.y), g3 = -ef * (acc.vz.x + acc.vz.y);
     int h = 2 * acc.hits;
     if (SORTED) {
       // the groups of a cluster are not in neighbouring lanes: the block sums them (k_lj_mixed_n3_sorted)
@@ -1224,7 +1257,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3_sorted(DeviceState s,
   const int64_t gb = blockIdx.x * (int64_t)128;
   const int64_t ng = s.nslots / 2;
   int n = 0;
-  if (gb + t < ng && pq_own(s.pq[2 * (gb + t)]) != 0) n = min(s.gl_count[gb + t], 0xFFFFFF);
+  if (gb + t < ng) n = min(s.gl_count[gb + t], 0xFFFFFF);
   key[t] = ((unsigned int)(0xFFFFFF - n) << 7) | (unsigned int)t;  // ascending key = decreasing length, then index
   for (int size = 2; size <= 128; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -1292,14 +1325,19 @@ static void launch_n3(DeviceState &s, const ForceArgs &fa, int64_t ng, cudaStrea
 
 template <int C, int MINB>
 static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, int64_t ng, cudaStream_t st) {
-  const bool glob = fa.calc_globals != 0;
+  // globals: 1, or 2 when some system has explicit halo particles (per-pair energy factors, owned-pair counts)
+  const int gm = fa.calc_globals ? (s.any_halo_sys ? 2 : 1) : 0;
   if (s.ntypes == 1) {
-    if (glob)
+    if (gm == 2)
+      launch_n3<C, 2, true, MINB>(s, fa, ng, st);
+    else if (gm == 1)
       launch_n3<C, 1, true, MINB>(s, fa, ng, st);
     else
       launch_n3<C, 0, true, MINB>(s, fa, ng, st);
   } else {
-    if (glob)
+    if (gm == 2)
+      launch_n3<C, 2, false, MINB>(s, fa, ng, st);
+    else if (gm == 1)
       launch_n3<C, 1, false, MINB>(s, fa, ng, st);
     else
       launch_n3<C, 0, false, MINB>(s, fa, ng, st);

@@ -35,17 +35,20 @@ namespace autopas_gb300 {
 template <class Functor>
 class GPUTraversal {
  public:
-  GPUTraversal(Functor *f, TraversalOption option, bool newton3 = false) : _functor(f), _option(option) {
-    if (newton3)
-      throw GpuEngineException(PE_ERR_ARG,
-                               "GPUTraversal: a container with explicit halo copies evaluates pairs without newton3");
+  /** newton3: the pair-group half lists (gpu_newton3_pair_groups, or gpu_tuned restricted to them) evaluate
+   *  each pair once; the full-list traversals evaluate every pair from both sides and take newton3 = false. */
+  GPUTraversal(Functor *f, TraversalOption option, bool newton3 = false)
+      : _functor(f), _option(option), _newton3(newton3) {
+    if (newton3 && option != TraversalOption::gpu_newton3_pair_groups && option != TraversalOption::gpu_tuned)
+      throw GpuEngineException(PE_ERR_ARG, "GPUTraversal: the full-list traversals evaluate pairs without newton3");
+    if (!newton3 && option == TraversalOption::gpu_newton3_pair_groups)
+      throw GpuEngineException(PE_ERR_ARG, "GPUTraversal: the pair-group half lists evaluate pairs with newton3");
   }
   TraversalOption getTraversalType() const { return _option; }
-  // The newton3 pair-group traversal serves periodic systems, whose images the engine forms itself; this container
-  // receives explicit halo copies from AutoPas, so the tuner is told it does not apply here
-  // (TraversalInterface.h:18-83, isApplicable).
-  bool isApplicableToDomain() const { return _option != TraversalOption::gpu_newton3_pair_groups; }
-  bool getUseNewton3() const { return false; }
+  // Every traversal serves a container of owned particles with explicit halo copies (TraversalInterface.h:18-83,
+  // isApplicable); the newton3 pair groups weigh a pair with a halo endpoint by its owned endpoints.
+  bool isApplicableToDomain() const { return true; }
+  bool getUseNewton3() const { return _newton3; }
   void initTraversal() {}
   void traverseParticles() {}
   void endTraversal() {}
@@ -54,6 +57,7 @@ class GPUTraversal {
  private:
   Functor *_functor;
   TraversalOption _option;
+  bool _newton3;
 };
 
 template <class Particle_T>
@@ -177,7 +181,7 @@ class GPUClusterLists {
    *  particles join the container first. */
   template <class Functor>
   void rebuildNeighborLists(GPUTraversal<Functor> *traversal) {
-    ensureEngine(*traversal->functor(), traversal->getTraversalType());
+    ensureEngine(*traversal->functor(), traversal->getTraversalType(), traversal->getUseNewton3());
     for (auto &p : _ownedBuffer) _owned.push_back(p);
     for (auto &p : _haloBuffer) {
       _haloIndex.emplace(p.getID(), _halo.size());
@@ -200,7 +204,7 @@ class GPUClusterLists {
     if (!_listsValid) rebuildNeighborLists(traversal);
     if (_ownershipDirty) {
       ownershipStates();
-      // a particle that was a dummy at the last rebuild cannot rejoin the lists: the engine then rebuilds
+      // a dummy at the last rebuild cannot rejoin the lists (nor a halo turn owned): the engine then rebuilds
       if (!_engine->updateOwnership(_own.data())) _rebuildsRequested += 1;
       _ownershipDirty = false;
     }
@@ -289,19 +293,20 @@ class GPUClusterLists {
     return true;
   }
 
+  // The engine is configured by the first traversal that reaches the container (its option and newton3).
   template <class Functor>
-  void ensureEngine(const Functor &f, TraversalOption t) {
+  void ensureEngine(const Functor &f, TraversalOption t, bool newton3) {
     if (_engine) return;
     pe_config cfg{};
     f.fillConfig(cfg, _eps, _sig, _mass);
     cfg.skin = _skin;
     cfg.precision = _precision;
     cfg.cluster_size = (int)_clusterSize;
-    cfg.newton3 = 0;  // explicit halo particles: the full lists (the newton3 pair groups serve periodic systems)
+    cfg.newton3 = newton3 ? 1 : 0;
     cfg.dist_mode = PE_DIST_FMA_SOA;
     cfg.rebuild_frequency = 1;
     cfg.tower_sizing = 1;
-    cfg.traversal = t == TraversalOption::gpu_newton3_pair_groups ? -1 : toEngineTraversal(t);
+    cfg.traversal = toEngineTraversal(t);
     _engine = std::make_unique<Engine>(cfg, std::vector<Engine::System>{{_boxMin, _boxMax, false}});
   }
 
@@ -417,12 +422,12 @@ class GPUClusterLists {
 /** LogicHandler::computeInteractions for the GPU container (LogicHandler.h:1064-1141). */
 template <class Particle_T, class Functor>
 void computeInteractionsPipeline(GPUClusterLists<Particle_T> &container, Functor &functor,
-                                 TraversalOption option = TraversalOption::gpu_tuned) {
-  GPUTraversal<Functor> traversal(&functor, option, false);
+                                 TraversalOption option = TraversalOption::gpu_tuned, bool newton3 = false) {
+  GPUTraversal<Functor> traversal(&functor, option, newton3);
   functor.initTraversal();
   if (!container.neighborListsAreValid()) container.rebuildNeighborLists(&traversal);
   container.computeInteractions(&traversal);
-  functor.endTraversal(false);
+  functor.endTraversal(newton3);
 }
 
 /** A particle with the MoleculeLJ members the container uses

@@ -101,8 +101,8 @@ class LJFunctorGPU {
 
   std::string getName() const { return "LJFunctorGPU"; }
   bool isRelevantForTuning() const { return true; }
-  /** The device kernels evaluate every pair from both sides. */
-  bool allowsNewton3() const { return false; }
+  /** The full-list kernels evaluate every pair from both sides, the pair-group kernels each pair once. */
+  bool allowsNewton3() const { return true; }
   bool allowsNonNewton3() const { return true; }
 
   /** LJFunctor::setParticleProperties(epsilon24, sigmaSquared) (LJFunctor.h:583-590).  The engine receives

@@ -18,7 +18,7 @@ namespace autopas_gb300 {
 enum class ContainerOption { gpuClusterLists };
 
 /** The traversal options the engine registers; gpu_tuned lets the engine's tuner pick among the others (the
- *  newton3 pair-group lists serve periodic systems of the mixed form only). */
+ *  newton3 pair-group lists serve the mixed form only). */
 enum class TraversalOption { gpu_cluster_pairs, gpu_particle_lists, gpu_newton3_pair_groups, gpu_tuned };
 
 inline std::string toString(ContainerOption) { return "GPUClusterLists"; }

@@ -77,8 +77,9 @@ typedef struct {
   int precision;           /* PE_PRECISION_* */
   int cluster_size;        /* 4 or 8; 0 lets the engine's tuner decide */
   int newton3;             /* 0: full lists, each pair evaluated from both sides; 1: Newton-3, each pair once
-                              (traversal 2; mixed precision on periodic systems without ATM or pruning, else
-                              PE_ERR_ARG), as the reference's newton3 functor calls (LJFunctor.h:369-559);
+                              (traversal 2; the mixed form without ATM or pruning, else PE_ERR_ARG; periodic and
+                              explicit-halo systems, a pair with a halo endpoint weighing its owned endpoints), as
+                              the reference's newton3 functor calls (LJFunctor.h:369-559);
                               -1: the tuner may pick either where newton3 is allowed */
   int dist_mode;           /* PE_DIST_* for every FP64 distance test */
   int rebuild_frequency;   /* steps between list rebuilds inside pe_step (verletRebuildFrequency) */
@@ -147,8 +148,9 @@ int pe_update_positions(pe_engine *h, const double *x, const double *y, const do
  * (src/autopas/containers/LeavingParticleCollector.h:85-118) -- and reviving a halo particle in place
  * (ParticleContainerInterface::updateHaloParticle, VerletClusterLists.h:194-212).  ownership: new
  * OwnershipState of every particle of the last pe_set_particles, in that order.  The lists stay valid, except
- * when a particle that was a dummy at the last rebuild becomes owned or halo (it is in no list): then the next
- * force evaluation rebuilds them.  *lists_valid (may be NULL) receives whether they stayed valid. */
+ * when a particle that was a dummy at the last rebuild becomes owned or halo (it is in no list), or one that was
+ * a halo becomes owned (it has no list of its own): then the next force evaluation rebuilds them.
+ * *lists_valid (may be NULL) receives whether they stayed valid. */
 int pe_update_ownership(pe_engine *h, const int8_t *ownership, int *lists_valid);
 
 /* Replaces: VerletClusterLists::rebuildNeighborLists (VerletClusterLists.h:779-800) -- binning by radix

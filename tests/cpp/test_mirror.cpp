@@ -85,20 +85,26 @@ static void cpu_tests() {
   CHECK(toEngineTraversal(TraversalOption::gpu_tuned) == -1, "tuned traversal");
   CHECK(toEngineTraversal(TraversalOption::gpu_newton3_pair_groups) == 2, "newton3 traversal");
   {
-    // the container receives explicit halo copies: the newton3 pair-group traversal (periodic systems only) must
-    // not look applicable to the AutoTuner, the others must
+    // every traversal applies to the explicit-halo container; newton3 goes with the pair-group half lists only
     Functor fa(1.1);
-    CHECK(!GPUTraversal<Functor>(&fa, TraversalOption::gpu_newton3_pair_groups).isApplicableToDomain(),
-          "newton3 traversal must not apply to an explicit-halo container");
+    CHECK(fa.allowsNewton3() && fa.allowsNonNewton3(), "functor allows both newton3 modes");
+    GPUTraversal<Functor> n3(&fa, TraversalOption::gpu_newton3_pair_groups, true);
+    CHECK(n3.isApplicableToDomain() && n3.getUseNewton3(), "newton3 traversal applies with newton3");
     CHECK(GPUTraversal<Functor>(&fa, TraversalOption::gpu_particle_lists).isApplicableToDomain(),
           "particle-list traversal applies");
-    bool n3threw = false;
-    try {
-      GPUTraversal<Functor> t(&fa, TraversalOption::gpu_particle_lists, true);
-    } catch (const GpuEngineException &) {
-      n3threw = true;
+    CHECK(GPUTraversal<Functor>(&fa, TraversalOption::gpu_tuned, true).getUseNewton3(), "tuned with newton3");
+    for (int k = 0; k < 2; ++k) {
+      bool threw = false;
+      try {
+        if (k == 0)
+          GPUTraversal<Functor> t(&fa, TraversalOption::gpu_particle_lists, true);
+        else
+          GPUTraversal<Functor> t(&fa, TraversalOption::gpu_newton3_pair_groups, false);
+      } catch (const GpuEngineException &) {
+        threw = true;
+      }
+      CHECK(threw, "traversal %d: a newton3 mode the traversal does not serve must be refused", k);
     }
-    CHECK(n3threw, "a newton3 traversal object must be refused");
   }
   GPUClusterLists<MoleculeLJ> c({0, 0, 0}, {3, 3, 3}, 1.1, 0.2);
   bool threw = false;
@@ -212,8 +218,11 @@ static void mixed_vs_fp64() {
           for (auto &v : r) v = std::fmod(v + jit(rng) + box, box);
           pos.push_back(r);
         }
-  std::vector<std::vector<std::array<double, 3>>> forces(2);
-  for (int prec = 0; prec < 2; ++prec) {
+  // run 0: FP64 full lists; 1: mixed, tuned full lists; 2: mixed, newton3 pair groups
+  std::vector<std::vector<std::array<double, 3>>> forces(3);
+  std::vector<double> upot(3);
+  std::vector<int64_t> pairs(3);
+  for (int prec = 0; prec < 3; ++prec) {
     GPUClusterLists<MoleculeLJ> c({0, 0, 0}, {box, box, box}, rc, skin, 0, prec == 0 ? PE_PRECISION_FP64 : PE_PRECISION_MIXED);
     uint64_t id = 0;
     for (auto &r : pos) c.addParticle(MoleculeLJ(r, {0, 0, 0}, id++));
@@ -229,19 +238,29 @@ static void mixed_vs_fp64() {
           }
     Functor f(rc);
     f.setParticleProperties(24, 1);
-    computeInteractionsPipeline(c, f);
+    if (prec == 2)
+      computeInteractionsPipeline(c, f, TraversalOption::gpu_newton3_pair_groups, true);
+    else
+      computeInteractionsPipeline(c, f);
     c.forEach([&](MoleculeLJ &p) { forces[prec].push_back(p.getF()); }, IteratorBehavior::owned);
+    upot[prec] = f.getPotentialEnergy();
+    pairs[prec] = f.getNumInteractingPairs();
   }
-  double e2 = 0, f2 = 0;
-  for (size_t i = 0; i < forces[0].size(); ++i)
-    for (int d = 0; d < 3; ++d) {
-      const double df = forces[1][i][d] - forces[0][i][d];
-      e2 += df * df;
-      f2 += forces[0][i][d] * forces[0][i][d];
-    }
-  const double rel = std::sqrt(e2 / f2);
-  CHECK(rel <= 1e-6, "mixed vs FP64 force RMS %.3g", rel);
-  std::printf("mixed vs FP64 force RMS relative error: %.3e\n", rel);
+  for (int run = 1; run < 3; ++run) {
+    double e2 = 0, f2 = 0;
+    for (size_t i = 0; i < forces[0].size(); ++i)
+      for (int d = 0; d < 3; ++d) {
+        const double df = forces[run][i][d] - forces[0][i][d];
+        e2 += df * df;
+        f2 += forces[0][i][d] * forces[0][i][d];
+      }
+    const double rel = std::sqrt(e2 / f2);
+    CHECK(rel <= 1e-6, "run %d: mixed vs FP64 force RMS %.3g", run, rel);
+    CHECK(std::fabs(upot[run] - upot[0]) <= 1e-6 * std::fabs(upot[0]), "run %d: Upot %.12g vs %.12g", run, upot[run],
+          upot[0]);
+    CHECK(pairs[run] == pairs[0], "run %d: %lld pairs vs %lld", run, (long long)pairs[run], (long long)pairs[0]);
+    std::printf("%s vs FP64 force RMS relative error: %.3e\n", run == 1 ? "mixed" : "mixed newton3", rel);
+  }
 }
 
 // md-flexible's periodic halo copies of an owned particle: one image per shift whose coordinates lie within the

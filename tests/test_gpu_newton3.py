@@ -169,11 +169,14 @@ def test_newton3_ensemble(eng_mod, orc):
 
 
 def test_newton3_configuration_rules(eng_mod):
-    """Newton3 serves the mixed form on periodic systems: the FP64 form, explicit halo systems and a full-list
-    traversal with newton3 required are refused."""
+    """Newton3 serves the mixed form: the FP64 form and a full-list traversal with newton3 required are refused;
+    systems with explicit halo particles are accepted."""
     box = ([0, 0, 0], [12, 12, 12])
-    for kw in (dict(newton3=1, precision=eng_mod.PRECISION_FP64), dict(newton3=1, periodic=False),
-               dict(newton3=1, traversal=1), dict(traversal=2, newton3=0)):
+    e = eng_mod.PairEngine(2.5, 0.3, box, periodic=False, traversal=2, newton3=1)
+    assert e.info()["traversal"] == 2 and e.info()["newton3"] == 1
+    e.close()
+    for kw in (dict(newton3=1, precision=eng_mod.PRECISION_FP64), dict(newton3=1, traversal=1),
+               dict(traversal=2, newton3=0)):
         args = dict(periodic=True, traversal=-1)
         args.update(kw)
         with pytest.raises(eng_mod.EngineError) as ei:
@@ -202,3 +205,106 @@ def test_newton3_sorted_variant(eng_mod, orc, C):
     R = R[: len(pos)]
     assert rel_rms(F3, R) <= 1e-6
     assert g3["upot"] == pytest.approx(glob[0], rel=1e-6)
+
+
+@pytest.mark.parametrize("C", [4, 8])
+def test_newton3_explicit_halo_matches_oracle(eng_mod, orc, C):
+    """Container mode with newton3 (the caller hands owned + halo particles, AutoPas addHaloParticle semantics):
+    every pair with an owned endpoint is covered by exactly one group (pairs of two halos are not pairs of the
+    container), a pair's energy and virial weigh its owned endpoints (LJFunctor.h:327-345), the forces on owned
+    particles are the oracle's, halo particles get none, and the pair count is the oracle's."""
+    pos, vel, bmin, bmax = liquid(6, seed=3)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    n = len(pos)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, cluster_size=C, traversal=2, newton3=1)
+    e.set_particles(allpos, ownership=own)
+    g = e.compute_forces()[0]
+    F = e.forces()
+    for which in (0, 1):
+        a, b, c = e.pair_set(which)
+        assert np.all(c == 13)
+        dev = np.unique(np.stack([np.minimum(a, b), np.maximum(a, b)], 1), axis=0)
+        assert len(dev) == len(a), "a pair is covered by two groups"
+        if which == 0:
+            ra, rb = orc.pair_set(allpos, rc + skin, own=own)
+        else:
+            ra, rb = orc.interacting_set(allpos, rc, own=own)
+        ref = np.unique(np.stack([np.minimum(ra, rb), np.maximum(ra, rb)], 1), axis=0)
+        assert np.array_equal(dev, ref)
+    e.close()
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=own)
+    assert rel_rms(F[:n], R[:n]) <= 1e-6
+    assert np.all(F[n:] == 0)
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
+    assert g["virial"] == pytest.approx(glob[1], rel=1e-6)
+    ia, ib = orc.interacting_set(allpos, rc, own=own)
+    assert g["num_pairs"] == len(ia)
+
+
+def test_newton3_explicit_halo_md_follows_the_full_list_path(eng_mod, orc):
+    """Steps with explicit halos (fused position update, rebuilds): the halos stay where the caller put them and
+    the newton3 trajectory stays within FP32 rounding of the full-list one."""
+    pos, vel, bmin, bmax = liquid(5, seed=37, jitter=0.02)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    n = len(pos)
+    allvel = np.zeros_like(allpos)
+    allvel[:n] = vel * 0.1
+    out = {}
+    for t, n3 in ((1, 0), (2, 1)):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, traversal=t, newton3=n3, rebuild_frequency=5)
+        e.set_particles(allpos, allvel, ownership=own)
+        e.compute_forces()
+        g = e.step(0.002, 18)[0]
+        P, V = e.state()
+        e.close()
+        assert np.array_equal(P[n:], allpos[n:])
+        out[t] = (P, V, g)
+    (P1, V1, g1), (P2, V2, g2) = out[1], out[2]
+    assert np.abs(P1 - P2).max() < 1e-6
+    assert np.abs(V1 - V2).max() < 1e-4
+    assert g2["upot"] == pytest.approx(g1["upot"], rel=1e-6)
+    assert g2["num_pairs"] == g1["num_pairs"]
+
+
+@pytest.mark.parametrize("traversal,n3", [(1, 0), (2, 1)])
+def test_ownership_changes_in_place(eng_mod, orc, traversal, n3):
+    """pe_update_ownership (updateContainer with kept lists, updateHaloParticle): owned and halo particles that
+    become dummies keep the lists valid and drop out of the forces and globals; a halo that becomes owned (it has
+    no list of its own, and a group of halos has no entries towards other halos) makes the next evaluation
+    rebuild.  Forces on owned particles, Upot and the pair count follow the oracle for each ownership state."""
+    pos, vel, bmin, bmax = liquid(5, seed=41)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    n, m = len(pos), len(allpos)
+    rng = np.random.default_rng(3)
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, traversal=traversal, newton3=n3)
+    e.set_particles(allpos, ownership=own)
+    e.compute_forces()
+    r0 = e.stats(reset=False)["rebuilds"]
+
+    def check(o):
+        g = e.compute_forces()[0]
+        F = e.forces()
+        R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=o)
+        real = o == 1
+        assert rel_rms(F[real], R[real]) <= 1e-6
+        assert np.all(F[~real] == 0)
+        assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
+        ia, _ = orc.interacting_set(allpos, rc, own=o)
+        assert g["num_pairs"] == len(ia)
+
+    o1 = own.copy()
+    o1[rng.choice(n, 25, replace=False)] = 0
+    o1[n + rng.choice(m - n, 40, replace=False)] = 0
+    assert e.update_ownership(o1)
+    check(o1)
+    assert e.stats(reset=False)["rebuilds"] == r0
+    o2 = o1.copy()
+    halos = np.flatnonzero(o1 == 2)
+    o2[halos[rng.choice(len(halos), 10, replace=False)]] = 1
+    assert not e.update_ownership(o2)
+    check(o2)
+    assert e.stats(reset=False)["rebuilds"] == r0 + 1
+    e.close()

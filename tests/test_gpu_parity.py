@@ -693,3 +693,34 @@ def test_page_locked_host_buffers_are_read_and_written_directly(eng_mod):
     np.testing.assert_array_equal(np.stack([fx, fy, fz], 1), f_ref)
     P, _ = e.state()
     np.testing.assert_array_equal(P, moved)
+
+
+@pytest.mark.parametrize("traversal,n3", [(0, 0), (1, 0), (2, 1)])
+def test_dummies_at_the_top_of_towers(eng_mod, orc, traversal, n3):
+    """Particles the caller marks as dummies keep their slots and are z-sorted with the others; where they are the
+    highest particles of their towers, whole clusters hold dummies only.  The tower search still sees every
+    cluster below them: the pair sets (rc+skin and rc) are the oracle's bit for bit and the forces match."""
+    pos, vel, bmin, bmax = liquid(5, seed=43)
+    rc, skin = 2.5, 0.3
+    allpos, own, _, _, _ = orc.periodic_system(pos, bmin, bmax, rc, skin)
+    o = own.copy()
+    o[allpos[:, 2] > bmax[2] + 0.5] = 0
+    assert (o == 0).sum() > 100
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=False, traversal=traversal, newton3=n3)
+    e.set_particles(allpos, ownership=o)
+    g = e.compute_forces()[0]
+    F = e.forces()
+    for which in (0, 1):
+        a, b, _ = e.pair_set(which)
+        dev = np.unique(np.stack([np.minimum(a, b), np.maximum(a, b)], 1), axis=0)
+        if which == 0:
+            ra, rb = orc.pair_set(allpos, rc + skin, own=o)
+        else:
+            ra, rb = orc.interacting_set(allpos, rc, own=o)
+        ref = np.unique(np.stack([np.minimum(ra, rb), np.maximum(ra, rb)], 1), axis=0)
+        assert np.array_equal(dev, ref)
+    e.close()
+    R, glob, _ = orc.lj_forces(allpos, orc.LJ(rc), own=o)
+    real = o == 1
+    assert rel_rms(F[real], R[real]) <= 1e-6
+    assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
