@@ -121,6 +121,38 @@ __device__ __forceinline__ uint4 pq_pack(const SysDev &S, double x, double y, do
   return pq_encode(xp, type, own);
 }
 
+// Conversions between float and double on the integer pipes.  This GPU issues FP64 instructions, conversions to
+// and from double included, at 1/64 of the FP32 rate, which bounds the per-slot epilogues; these give the
+// converter's results (IEEE: float to double exact, double to float rounded to nearest even) from the bit
+// fields for normal numbers and zeros, and leave the rare rest (subnormals, infinities, NaN, out-of-range
+// exponents) to the converter.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  if (e - 1u < 254u) {
+    // exponent rebiased 127 -> 1023; the 23 fraction bits become the top of the 52
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+  }
+  if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)b, 0);  // signed zero
+  return (double)f;
+}
+
+__device__ __forceinline__ float d2f_rn(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned E = (hi >> 20) & 0x7FFu;
+  if (E - 897u < 254u) {
+    // float exponent 1..254: the top 23 of the 52 fraction bits, then round to nearest even on the 29 dropped
+    // ones (a carry out of the fraction moves the exponent up, to infinity past the largest float)
+    unsigned f = (hi & 0x80000000u) | ((E - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1FFFFFFFu;
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    return __uint_as_float(f);
+  }
+  if (((hi & 0x7FFFFFFFu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // signed zero
+  return __double2float_rn(d);
+}
+
 // Packed FP32 pairs: the Blackwell f32x2 instructions evaluate two operations (.x and .y) per instruction,
 // each lane an IEEE round-to-nearest operation, so a packed pair gives the bits of two scalar ones.
 __device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }

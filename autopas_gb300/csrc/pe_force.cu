@@ -691,9 +691,10 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
   }
   // Epilogue.  The FP64 pipe of this GPU (conversions included) issues 2 lanes per clock per SM, so the
   // epilogue keeps to the FP64 work the state needs: the force rounded once from its compensated sum, the
-  // velocity half in FP64 with the reference's operation order.  Per-particle globals, the kinetic energy
-  // included, are float values summed over the cluster's lanes in float and widened once per cluster.
-  const double Fx = (double)acc.force_x(), Fy = (double)acc.force_y(), Fz = (double)acc.force_z();
+  // velocity half in FP64 with the reference's operation order; the conversions between float and double run on
+  // the integer pipes (f2d_exact, d2f_rn).  Per-particle globals, the kinetic energy included, are float values
+  // summed over the cluster's lanes in float and widened once per cluster.
+  const double Fx = f2d_exact(acc.force_x()), Fy = f2d_exact(acc.force_y()), Fz = f2d_exact(acc.force_z());
   float ek = 0.f;
   if (oi == 1) {
     // every load of the epilogue before its first store (through plain pointers a load after a store is issued
@@ -742,7 +743,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_plist(DeviceState s, For
       }
     }
     if (GLOB) {
-      const float ux = (float)vx, uy = (float)vy, uz = (float)vz;
+      const float ux = d2f_rn(vx), uy = d2f_rn(vy), uz = d2f_rn(vz);
       ek = fa.vv.half_mass[ti] * fmaf(uz, uz, fmaf(uy, uy, ux * ux));
     }
   } else if (inrange && fa.fuse_positions) {
@@ -1166,7 +1167,7 @@ __device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const Force
     }
     __stcg(s.facc + k, make_float4(0.f, 0.f, 0.f, 0.f));
     if (oi == 1) {
-      const double Fx = (double)r.x, Fy = (double)r.y, Fz = (double)r.z;
+      const double Fx = f2d_exact(r.x), Fy = f2d_exact(r.y), Fz = f2d_exact(r.z);
       if (!fa.fuse_positions) {  // fused: the force goes to the old-force arrays (as in the particle-list kernel)
         s.fx[k] = Fx;
         s.fy[k] = Fy;
@@ -1196,7 +1197,7 @@ __device__ __forceinline__ void n3_finish_slot(const DeviceState &s, const Force
         }
       }
       if (GLOB) {
-        const float ux = (float)vx, uy = (float)vy, uz = (float)vz;
+        const float ux = d2f_rn(vx), uy = d2f_rn(vy), uz = d2f_rn(vz);
         ek = fa.vv.half_mass[ti] * fmaf(uz, uz, fmaf(uy, uy, ux * ux));
       }
     } else if (fa.fuse_positions) {

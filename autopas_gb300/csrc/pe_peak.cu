@@ -1,12 +1,19 @@
 // pe_peak.cu -- the FP32 CUDA-core throughput of this GPU, measured: the denominator of the force kernels'
-// roofline (their work is FP32 arithmetic on the CUDA cores, not tensor-core contractions).
+// roofline (their work is FP32 arithmetic on the CUDA cores, not tensor-core contractions); and a device
+// self-check of the engine's integer-pipe float/double conversions.
 //
 // Every thread runs 8 independent chains of packed FP32x2 fused multiply-adds (16 FLOP per instruction pair of
 // lanes), enough independent work per warp to keep the FMA pipes issuing back to back; the grid fills every SM
 // with 8 blocks of 256 threads.  Timed with CUDA events after a warm-up launch.
+//
+// pe_check_conversions compares the engine's integer-pipe conversions between float and double (pe_common.cuh)
+// with the hardware converter: every float bit pattern widened, and for every float bit pattern the double that
+// equals it, the double halfway to the next float up (a rounding tie) and the doubles one unit on either side
+// of that tie, narrowed.
 #include <cuda_runtime.h>
 
 #include "../../include/pairengine.h"
+#include "pe_common.cuh"
 
 namespace {
 
@@ -44,7 +51,52 @@ __global__ void __launch_bounds__(256) k_dfma_peak(double *out, int iters, doubl
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+constexpr int kPatternsPerThread = 16;
+
+// the 2^32 float bit patterns, kPatternsPerThread consecutive ones per thread
+__global__ void __launch_bounds__(256) k_check_conversions(unsigned long long *bad) {
+  const unsigned long long first =
+      ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) * (unsigned long long)kPatternsPerThread;
+  unsigned long long nbad = 0;
+  for (int k = 0; k < kPatternsPerThread; ++k) {
+    const unsigned bits = (unsigned)(first + k);
+    const float f = __uint_as_float(bits);
+    const double w = pe::f2d_exact(f), wr = (double)f;
+    const bool same = (__double_as_longlong(w) == __double_as_longlong(wr)) || (wr != wr && w != w);
+    nbad += same ? 0 : 1;
+    // narrowing: the float itself, the tie halfway to the next float up (2^28 units of the double's last place),
+    // and its two neighbours
+    const long long e = __double_as_longlong(wr);
+    const long long tie = e + (1ll << 28);
+    const long long cand[4] = {e, tie - 1, tie, tie + 1};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double d = __longlong_as_double(cand[c]);
+      const float n = pe::d2f_rn(d), nr = __double2float_rn(d);
+      nbad += (__float_as_uint(n) == __float_as_uint(nr) || (nr != nr && n != n)) ? 0 : 1;
+    }
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
 }  // namespace
+
+extern "C" int pe_check_conversions(int64_t *mismatches) {
+  if (!mismatches) return PE_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PE_ERR_NO_DEVICE;
+  unsigned long long *bad = nullptr;
+  if (cudaMalloc(&bad, sizeof(unsigned long long)) != cudaSuccess) return PE_ERR_OOM;
+  cudaMemset(bad, 0, sizeof(unsigned long long));
+  const unsigned blocks = (unsigned)((1ull << 32) / (256ull * kPatternsPerThread));
+  k_check_conversions<<<blocks, 256>>>(bad);
+  unsigned long long h = 0;
+  const cudaError_t e = cudaMemcpy(&h, bad, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) return PE_ERR_CUDA;
+  *mismatches = (int64_t)h;
+  return PE_OK;
+}
 
 extern "C" int pe_measure_fp64_peak(double *tflops) {
   if (!tflops) return PE_ERR_ARG;

@@ -29,7 +29,7 @@ EXPORTS = [
     "pe_compute_forces", "pe_get_forces", "pe_get_state", "pe_step", "pe_get_info", "pe_get_tower_grid",
     "pe_pair_set", "pe_get_stats", "pe_device_timer", "pe_tune", "pe_get_tuning", "pe_lj_forces_noalloc",
     "pe_compute_atm", "pe_update_ownership", "pe_set_force_cap", "pe_scale_velocities", "pe_measure_fp32_peak",
-    "pe_measure_fp64_peak",
+    "pe_measure_fp64_peak", "pe_check_conversions",
 ]
 
 
@@ -100,6 +100,7 @@ def load(path: str | None = None):
     L.pe_set_force_cap.argtypes = [vp, C.c_double]
     L.pe_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
     L.pe_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    L.pe_check_conversions.argtypes = [C.POINTER(C.c_int64)]
     L.pe_scale_velocities.argtypes = [vp, vp]
     L.pe_compute_forces.argtypes = [vp, vp]
     L.pe_get_forces.argtypes = [vp, vp, vp, vp]
@@ -364,6 +365,16 @@ def measure_fp64_peak():
     rc = load().pe_measure_fp64_peak(C.byref(v))
     if rc != PE_OK:
         raise EngineError(rc, "pe_measure_fp64_peak failed")
+    return v.value
+
+
+def check_conversions():
+    """Mismatches of the engine's integer-pipe float<->double conversions against the hardware converter
+    (pe_check_conversions); 0 expected."""
+    v = C.c_int64()
+    rc = load().pe_check_conversions(C.byref(v))
+    if rc != PE_OK:
+        raise EngineError(rc, "pe_check_conversions failed")
     return v.value
 
 

@@ -286,6 +286,11 @@ int pe_lj_forces_noalloc(const pe_config *cfg, int64_t n, const double *x, const
 int pe_measure_fp32_peak(double *tflops);
 /* The same for FP64 fused multiply-adds (the FP64 form's roofline denominator). */
 int pe_measure_fp64_peak(double *tflops);
+/* A device self-check with no counterpart in the reference: the engine's float<->double conversions on the
+ * integer pipes (used in the per-slot epilogues, where the FP64 pipe bounds the time) against the hardware
+ * converter, over every float bit pattern widened and the rounding ties of every float narrowed.  *mismatches
+ * receives the number of differing results (0 expected).  About 20 G conversions. */
+int pe_check_conversions(int64_t *mismatches);
 
 /* Device timer on the engine's stream: op 0 records a start event; op 1 records a stop event, waits for it and
  * returns the elapsed milliseconds between the two in *ms. */

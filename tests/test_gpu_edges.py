@@ -199,3 +199,9 @@ def test_rebuild_on_previous_sizes_and_its_redo(eng_mod, orc):
     assert e.info()["max_tower_size"] >= 160
     assert check(pos2) == 0                # the new sizes are assumed next time
     e.close()
+
+
+def test_integer_pipe_conversions_match_the_converter(eng_mod):
+    """The per-slot epilogues widen forces and narrow velocities with integer-pipe conversions; every float bit
+    pattern widened and the rounding ties of every float narrowed give the hardware converter's bits."""
+    assert eng_mod.check_conversions() == 0
