@@ -125,6 +125,7 @@ struct pe_engine {
   std::vector<SysHost> sys;
   TypeTable table;
   cudaStream_t st = nullptr;
+  N3Pipe n3pipe;  // the newton3 evaluation's second force stream, finish stream and events
   int device = 0;
   int C = 8;
   int newton3 = 0;
@@ -1294,7 +1295,7 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, b
     cudaEventRecord(e0, h->st);
   }
   const VVFactors vv = vv_factors(h, dt);
-  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st, &vv, fuse_positions);
+  launch_force(s, h->precision, h->cfg.calc_globals, fuse_velocity, dt, h->st, &vv, fuse_positions, &h->n3pipe);
   if (timed) {
     cudaEventRecord(e1, h->st);
     h->force_ev.push_back({i0, i0 + 1});
@@ -1303,7 +1304,8 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, b
     launch_prune_clear(s, h->st);
     h->launches += 1;
   }
-  h->launches += (h->traversal == 2 && h->nslots > 0) ? 2 : 1;  // newton3: the force kernel and its finish
+  // newton3: a force kernel and a finish per piece
+  h->launches += (h->traversal == 2 && h->nslots > 0) ? 2 * n3_pieces(h->nslots) : 1;
   if (timed) h->force_launches += 1;
   if (h->cfg.calc_globals) {
     launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->sys_done.p, h->st);
@@ -1411,7 +1413,7 @@ static int tune(pe_engine *h, int samples) {
           cudaEvent_t a = h->ev(), b = h->ev();
           cudaEventRecord(a, h->st);
           DeviceState ds = h->state();
-          launch_force(ds, h->precision, h->cfg.calc_globals, false, 0.0, h->st);
+          launch_force(ds, h->precision, h->cfg.calc_globals, false, 0.0, h->st, nullptr, false, &h->n3pipe);
           cudaEventRecord(b, h->st);
           PE_CUDA(h, cudaEventSynchronize(b));
           float ms = 0;
@@ -1480,8 +1482,16 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   h->precision = cfg->precision;
   h->variant = cfg->kernel_variant;
   cudaGetDevice(&h->device);
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
-    delete h;
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  h->n3pipe.finish_priority = prio_greatest;
+  bool streams_ok = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) == cudaSuccess;
+  streams_ok = streams_ok && cudaStreamCreateWithFlags(&h->n3pipe.st[0], cudaStreamNonBlocking) == cudaSuccess;
+  streams_ok = streams_ok && cudaStreamCreateWithPriority(&h->n3pipe.st[1], cudaStreamNonBlocking, prio_greatest) ==
+                                 cudaSuccess;
+  for (auto &x : h->n3pipe.ev) streams_ok = streams_ok && cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess;
+  if (!streams_ok) {
+    pe_destroy(h);
     return PE_ERR_CUDA;
   }
   // ParticlePropertiesLibrary::calculateMixingCoefficients (ParticlePropertiesLibrary.h:444-473, 576-582)
@@ -1582,6 +1592,10 @@ int pe_destroy(pe_engine *h) {
   h->atm_out.release();
   h->atm_err.release();
   if (h->st) cudaStreamDestroy(h->st);
+  for (auto x : h->n3pipe.st)
+    if (x) cudaStreamDestroy(x);
+  for (auto x : h->n3pipe.ev)
+    if (x) cudaEventDestroy(x);
   delete h;
   return PE_OK;
 }

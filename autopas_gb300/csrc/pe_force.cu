@@ -38,6 +38,7 @@ struct ForceArgs {
   int fuse_positions;  // with fuse_velocity: also the next step's position half, into xn/yn/zn/pqn
   int calc_globals;
   VVFactors vv;
+  int64_t g_first;  // newton3: the first pair group of the launch (the finish: its first slot is 2 g_first)
 };
 
 // Reciprocal: hardware approximation refined by one Newton-Raphson step r' = r + r(1 - x r).
@@ -1233,7 +1234,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3(DeviceState s, ForceA
     }
     __syncthreads();
   }
-  n3_group<C, GM, ONE_TYPE>(s, fa, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, tab);
+  n3_group<C, GM, ONE_TYPE>(s, fa, fa.g_first + blockIdx.x * (int64_t)blockDim.x + threadIdx.x, tab);
 }
 
 // The same with the block's 128 groups taken in decreasing order of list length: a warp runs as long as its
@@ -1255,7 +1256,7 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3_sorted(DeviceState s,
       tab[2][q] = s.types->shrf[q];
     }
   }
-  const int64_t gb = blockIdx.x * (int64_t)128;
+  const int64_t gb = fa.g_first + blockIdx.x * (int64_t)128;
   const int64_t ng = s.nslots / 2;
   int n = 0;
   if (gb + t < ng) n = min(s.gl_count[gb + t], 0xFFFFFF);
@@ -1308,10 +1309,11 @@ __global__ void __launch_bounds__(128, MINB) k_lj_mixed_n3_sorted(DeviceState s,
   }
 }
 
-// one thread per slot; a warp past the last slot leaves whole (the kinetic energy is reduced with shuffles)
+// one thread per slot from slot 2 g_first; a warp past the last slot leaves whole (the kinetic energy is reduced
+// with shuffles)
 template <int C, bool GLOB>
 __global__ void __launch_bounds__(256) k_n3_finish(DeviceState s, ForceArgs fa) {
-  const int64_t w0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31u);
+  const int64_t w0 = 2 * fa.g_first + blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31u);
   if (w0 >= s.nslots) return;
   n3_finish_slot<C, GLOB>(s, fa, w0 + (threadIdx.x & 31));
 }
@@ -1346,22 +1348,75 @@ static void launch_n3_kernel(DeviceState &s, const ForceArgs &fa, int64_t ng, cu
 }
 
 // kernel variants (the tuner's choice): the register cap for 5 (variant 0), 6 (1) or 4 (2) resident blocks of
-// 128 threads per SM, or (3) 5 blocks with each block's groups sorted by list length.  Then the finish of every slot.
+// 128 threads per SM, or (3) 5 blocks with each block's groups sorted by list length.  Groups [g0, g1).
 template <int C>
-static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st) {
+static void launch_n3_piece(DeviceState &s, ForceArgs fa, int64_t g0, int64_t g1, cudaStream_t st) {
+  fa.g_first = g0;
+  if (s.variant == 1)
+    launch_n3_kernel<C, 6>(s, fa, g1 - g0, st);
+  else if (s.variant == 2)
+    launch_n3_kernel<C, 4>(s, fa, g1 - g0, st);
+  else
+    launch_n3_kernel<C, 5>(s, fa, g1 - g0, st);
+}
+
+// the finish of the slots of groups [g0, g1), launched with the given scheduling priority (kept by graph capture)
+template <int C>
+static void launch_n3_finish(DeviceState &s, ForceArgs fa, int64_t g0, int64_t g1, cudaStream_t st,
+                             int priority = 0) {
+  fa.g_first = g0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned int)((2 * (g1 - g0) + 255) / 256));
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = priority;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (fa.calc_globals)
+    cudaLaunchKernelEx(&cfg, k_n3_finish<C, true>, s, fa);
+  else
+    cudaLaunchKernelEx(&cfg, k_n3_finish<C, false>, s, fa);
+}
+
+// a piece holds at least about two waves of the force kernel (152 SMs x 5 blocks x 128 groups)
+constexpr int64_t kN3PieceGroups = 2 * 152 * 5 * 128;
+
+int n3_pieces(int64_t nslots) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(kN3PiecesMax, nslots / 2 / kN3PieceGroups));
+}
+
+template <int C>
+static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st, const N3Pipe *pipe) {
   const int64_t ng = s.nslots / 2;
   if (ng == 0) return;
-  if (s.variant == 1)
-    launch_n3_kernel<C, 6>(s, fa, ng, st);
-  else if (s.variant == 2)
-    launch_n3_kernel<C, 4>(s, fa, ng, st);
-  else
-    launch_n3_kernel<C, 5>(s, fa, ng, st);
-  const unsigned int grid = (unsigned int)((s.nslots + 255) / 256);
-  if (fa.calc_globals)
-    k_n3_finish<C, true><<<grid, 256, 0, st>>>(s, fa);
-  else
-    k_n3_finish<C, false><<<grid, 256, 0, st>>>(s, fa);
+  const int P = pipe ? n3_pieces(s.nslots) : 1;
+  if (P == 1) {
+    launch_n3_piece<C>(s, fa, 0, ng, st);
+    launch_n3_finish<C>(s, fa, 0, ng, st);
+    return;
+  }
+  // pieces on whole blocks of 128 groups (the sorted variant permutes within a block); the finish stream runs the
+  // finishes in piece order, each after the event of its own force piece (the earlier pieces' events it waited on
+  // before the earlier finishes)
+  const int64_t gp = ((ng + P - 1) / P + 127) / 128 * 128;
+  cudaEventRecord(pipe->ev[0], st);
+  cudaStreamWaitEvent(pipe->st[0], pipe->ev[0], 0);
+  cudaStreamWaitEvent(pipe->st[1], pipe->ev[0], 0);
+  for (int k = 0; k < P; ++k) {
+    const int64_t g0 = k * gp, g1 = std::min<int64_t>(ng, g0 + gp);
+    if (g0 >= g1) break;
+    cudaStream_t fs = (k & 1) ? pipe->st[0] : st;
+    launch_n3_piece<C>(s, fa, g0, g1, fs);
+    cudaEventRecord(pipe->ev[3 + k], fs);
+    cudaStreamWaitEvent(pipe->st[1], pipe->ev[3 + k], 0);
+    launch_n3_finish<C>(s, fa, g0, g1, pipe->st[1], pipe->finish_priority);
+  }
+  cudaEventRecord(pipe->ev[1], pipe->st[0]);
+  cudaStreamWaitEvent(st, pipe->ev[1], 0);
+  cudaEventRecord(pipe->ev[2], pipe->st[1]);
+  cudaStreamWaitEvent(st, pipe->ev[2], 0);
 }
 
 template <int C>
@@ -1416,9 +1471,9 @@ static void launch_force_plist(DeviceState &s, int precision, const ForceArgs &f
 }
 
 template <int C>
-static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st) {
+static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, cudaStream_t st, const N3Pipe *pipe) {
   if (s.traversal == 2) {
-    launch_force_n3<C>(s, fa, st);  // the engine allows this traversal for the mixed form only
+    launch_force_n3<C>(s, fa, st, pipe);  // the engine allows this traversal for the mixed form only
     return;
   }
   if (s.traversal == 1) {
@@ -1450,7 +1505,7 @@ static void launch_force_c(DeviceState &s, int precision, const ForceArgs &fa, c
 }
 
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
-                  const VVFactors *vv, bool fuse_positions) {
+                  const VVFactors *vv, bool fuse_positions, const N3Pipe *pipe) {
   ForceArgs fa{};
   if (vv) fa.vv = *vv;
   fa.rc2 = s.cutoff * s.cutoff;
@@ -1460,9 +1515,9 @@ void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_vel
   fa.fuse_positions = (fuse_velocity && fuse_positions) ? 1 : 0;
   fa.calc_globals = calc_globals;
   if (s.C == 4)
-    launch_force_c<4>(s, precision, fa, st);
+    launch_force_c<4>(s, precision, fa, st, pipe);
   else
-    launch_force_c<8>(s, precision, fa, st);
+    launch_force_c<8>(s, precision, fa, st, pipe);
 }
 
 // ---------------------------------------------------------------------------------------------

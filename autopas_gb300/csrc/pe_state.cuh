@@ -179,8 +179,20 @@ void launch_atm(DeviceState &s, int precision, double nu, double cutoff, double 
                 const int64_t *sys_cl_range, double *out, int *err, cudaStream_t st);
 
 // forces (pe_force.cu)
+// The newton3 evaluation in pieces of consecutive pair groups: the force kernel of piece k on one of two streams in
+// turn, and the finish of piece k on a third stream once the force pieces up to k are complete (a slot receives
+// reactions only from groups of clusters up to its own), so that the FP64-bound finish of one piece runs beside the
+// FP32 force work of the next.  The streams and events belong to the engine.
+constexpr int kN3PiecesMax = 4;
+struct N3Pipe {
+  cudaStream_t st[2] = {nullptr, nullptr};  // the second force stream and the finish stream
+  cudaEvent_t ev[kN3PiecesMax + 3] = {};    // fork, two joins, one per force piece
+  int finish_priority = 0;                  // the device's greatest stream priority: a finish whose piece is
+                                            // complete takes SM slots before force blocks still queued
+};
+int n3_pieces(int64_t nslots);  // pieces of an evaluation of this many slots (1: one force kernel, one finish)
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
-                  const VVFactors *vv = nullptr, bool fuse_positions = false);
+                  const VVFactors *vv = nullptr, bool fuse_positions = false, const N3Pipe *pipe = nullptr);
 constexpr int kChunk = 256;  // clusters per globals-reduction chunk (8 per lane of a reduction warp)
 constexpr int kGlob = 5;      // per-cluster partials: 6*Upot, virial x, y, z, kinetic energy
 constexpr int kSysGlob = 6;   // per system: Upot, virial, virial x, y, z, kinetic energy

@@ -95,6 +95,43 @@ def test_slab_2m_matches_oracle(eng_mod, orc, slab):
         assert g["virial"] == pytest.approx(glob[1], rel=tol), what
 
 
+def test_slab_2m_newton3_steps_in_pieces(eng_mod, slab):
+    """At 2M particles the newton3 evaluation runs in pieces (force kernels on two streams, each piece's finish
+    on a third as soon as the pieces up to it are complete), replayed from CUDA graphs with the velocity and
+    position halves fused.  After thirty velocity-Verlet steps with a rebuild at step 20, the forces of the last
+    evaluation match the FP64 form's at the same positions (force RMS error <= 1e-6, Upot 1e-6, the same
+    interacting pairs), and the trajectory stays near the particle-list one: the slab starts from random
+    sequential addition with forces up to ~10^3, so FP32 differences of ~1e-3 in them move positions by ~1e-6
+    over these steps; a lost or doubled reaction would move them by orders of magnitude more."""
+    pos, vel, bmin, bmax = slab
+    rc, skin, dt = 3.0, 0.4, 0.002
+    out = {}
+    for traversal in (1, 2):
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, cluster_size=8, traversal=traversal,
+                               newton3=1 if traversal == 2 else 0, rebuild_frequency=20, use_graphs=True)
+        e.set_particles(pos, vel)
+        e.compute_forces()
+        g = e.step(dt, 30)[0]
+        P, V = e.state()
+        out[traversal] = (P, V, g, e.forces())
+        e.close()
+    P2, V2, g2, F2 = out[2]
+    e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, precision=eng_mod.PRECISION_FP64,
+                           cluster_size=8, traversal=1)
+    e.set_particles(P2, V2)
+    g64 = e.compute_forces()[0]
+    F64 = e.forces()
+    e.close()
+    assert rel_rms(F2, F64) <= 1e-6
+    assert g2["num_pairs"] == g64["num_pairs"]
+    assert g2["upot"] == pytest.approx(g64["upot"], rel=1e-6)
+    P1 = out[1][0]
+    d = P1 - P2
+    d -= (bmax - bmin) * np.round(d / (bmax - bmin))
+    print(f"newton3 in pieces against particle lists after 30 steps: max position difference {np.abs(d).max():.3g}")
+    assert np.abs(d).max() < 1e-4
+
+
 def test_mixture_4m_matches_oracle(eng_mod, orc):
     from autopas_gb300 import workloads
     n, rho, rc, skin = 4_000_000, 0.7, 3.0, 0.3
