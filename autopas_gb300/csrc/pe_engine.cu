@@ -1305,7 +1305,7 @@ static int force_eval(pe_engine *h, bool fuse_velocity, double dt, bool timed, b
     h->launches += 1;
   }
   // newton3: a force kernel and a finish per piece
-  h->launches += (h->traversal == 2 && h->nslots > 0) ? 2 * n3_pieces(h->nslots) : 1;
+  h->launches += (h->traversal == 2 && h->nslots > 0) ? 2 * n3_pieces(h->nslots, h->n3pipe.pieces) : 1;
   if (timed) h->force_launches += 1;
   if (h->cfg.calc_globals) {
     launch_reduce_globals(s, h->chunks.p, h->nchunks, h->sys_chunk0.p, h->chunk_part.p, h->sys_done.p, h->st);
@@ -1459,6 +1459,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   if (cfg->atm_nu > 0 && !(cfg->atm_cutoff > 0 && cfg->atm_cutoff <= cfg->cutoff + cfg->skin)) return PE_ERR_ARG;
   if (cfg->prune_buffer < 0 || cfg->prune_buffer > cfg->skin) return PE_ERR_ARG;
   if (cfg->kernel_variant < 0 || cfg->kernel_variant > 3) return PE_ERR_ARG;
+  if (cfg->n3_pieces < 0 || cfg->n3_pieces > kN3PiecesMax) return PE_ERR_ARG;
   // newton3 (pair-group half lists): the mixed form, no three-body forces or pruning
   if (cfg->newton3 == 1 || cfg->traversal == 2) {
     if (cfg->precision != PE_PRECISION_MIXED || cfg->atm_nu > 0 || cfg->prune_buffer > 0 || cfg->newton3 == 0)
@@ -1485,6 +1486,7 @@ int pe_create(const pe_config *cfg, int num_systems, const pe_system_desc *syste
   int prio_least = 0, prio_greatest = 0;
   cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
   h->n3pipe.finish_priority = prio_greatest;
+  h->n3pipe.pieces = cfg->n3_pieces;
   bool streams_ok = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) == cudaSuccess;
   streams_ok = streams_ok && cudaStreamCreateWithFlags(&h->n3pipe.st[0], cudaStreamNonBlocking) == cudaSuccess;
   streams_ok = streams_ok && cudaStreamCreateWithPriority(&h->n3pipe.st[1], cudaStreamNonBlocking, prio_greatest) ==

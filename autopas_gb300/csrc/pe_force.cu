@@ -1380,33 +1380,41 @@ static void launch_n3_finish(DeviceState &s, ForceArgs fa, int64_t g0, int64_t g
     cudaLaunchKernelEx(&cfg, k_n3_finish<C, false>, s, fa);
 }
 
-// a piece holds at least about two waves of the force kernel (152 SMs x 5 blocks x 128 groups)
-constexpr int64_t kN3PieceGroups = 2 * 152 * 5 * 128;
+// a piece holds at least about 1.6 waves of the force kernel (152 SMs x 5 blocks x 128 groups = 97,280 groups): 6
+// pieces on the 2M-particle slab, where 4 to 8 pieces measured within 1% of each other and one piece 1.5% slower
+constexpr int64_t kN3PieceGroups = 160000;
 
-int n3_pieces(int64_t nslots) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>(kN3PiecesMax, nslots / 2 / kN3PieceGroups));
+// groups per piece: whole blocks of 128 groups (the sorted variant permutes within a block)
+static int64_t n3_piece_groups(int64_t nslots, int forced) {
+  const int64_t ng = nslots / 2;
+  const int64_t P = forced > 0 ? std::min(forced, kN3PiecesMax)
+                               : std::max<int64_t>(1, std::min<int64_t>(kN3PiecesMax, ng / kN3PieceGroups));
+  return std::max<int64_t>(128, ((ng + P - 1) / P + 127) / 128 * 128);
+}
+
+int n3_pieces(int64_t nslots, int forced) {
+  const int64_t ng = nslots / 2;
+  return ng > 0 ? (int)((ng + n3_piece_groups(nslots, forced) - 1) / n3_piece_groups(nslots, forced)) : 0;
 }
 
 template <int C>
 static void launch_force_n3(DeviceState &s, const ForceArgs &fa, cudaStream_t st, const N3Pipe *pipe) {
   const int64_t ng = s.nslots / 2;
   if (ng == 0) return;
-  const int P = pipe ? n3_pieces(s.nslots) : 1;
+  const int P = pipe ? n3_pieces(s.nslots, pipe->pieces) : 1;
   if (P == 1) {
     launch_n3_piece<C>(s, fa, 0, ng, st);
     launch_n3_finish<C>(s, fa, 0, ng, st);
     return;
   }
-  // pieces on whole blocks of 128 groups (the sorted variant permutes within a block); the finish stream runs the
-  // finishes in piece order, each after the event of its own force piece (the earlier pieces' events it waited on
-  // before the earlier finishes)
-  const int64_t gp = ((ng + P - 1) / P + 127) / 128 * 128;
+  // the finish stream runs the finishes in piece order, each after the event of its own force piece (the earlier
+  // pieces' events it waited on before the earlier finishes)
+  const int64_t gp = n3_piece_groups(s.nslots, pipe->pieces);
   cudaEventRecord(pipe->ev[0], st);
   cudaStreamWaitEvent(pipe->st[0], pipe->ev[0], 0);
   cudaStreamWaitEvent(pipe->st[1], pipe->ev[0], 0);
   for (int k = 0; k < P; ++k) {
     const int64_t g0 = k * gp, g1 = std::min<int64_t>(ng, g0 + gp);
-    if (g0 >= g1) break;
     cudaStream_t fs = (k & 1) ? pipe->st[0] : st;
     launch_n3_piece<C>(s, fa, g0, g1, fs);
     cudaEventRecord(pipe->ev[3 + k], fs);

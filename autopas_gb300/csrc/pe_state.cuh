@@ -183,14 +183,17 @@ void launch_atm(DeviceState &s, int precision, double nu, double cutoff, double 
 // turn, and the finish of piece k on a third stream once the force pieces up to k are complete (a slot receives
 // reactions only from groups of clusters up to its own), so that the FP64-bound finish of one piece runs beside the
 // FP32 force work of the next.  The streams and events belong to the engine.
-constexpr int kN3PiecesMax = 4;
+constexpr int kN3PiecesMax = 8;
 struct N3Pipe {
   cudaStream_t st[2] = {nullptr, nullptr};  // the second force stream and the finish stream
   cudaEvent_t ev[kN3PiecesMax + 3] = {};    // fork, two joins, one per force piece
   int finish_priority = 0;                  // the device's greatest stream priority: a finish whose piece is
                                             // complete takes SM slots before force blocks still queued
+  int pieces = 0;                           // pieces per evaluation; 0: by size
 };
-int n3_pieces(int64_t nslots);  // pieces of an evaluation of this many slots (1: one force kernel, one finish)
+// non-empty pieces of an evaluation of this many slots (1: one force kernel, one finish); forced > 0 asks for that
+// many (fewer when the pair groups do not fill that many blocks of 128)
+int n3_pieces(int64_t nslots, int forced);
 void launch_force(DeviceState &s, int precision, int calc_globals, bool fuse_velocity, double dt, cudaStream_t st,
                   const VVFactors *vv = nullptr, bool fuse_positions = false, const N3Pipe *pipe = nullptr);
 constexpr int kChunk = 256;  // clusters per globals-reduction chunk (8 per lane of a reduction warp)

@@ -40,7 +40,7 @@ class PeConfig(C.Structure):
         ("apply_shift", C.c_int), ("precision", C.c_int), ("cluster_size", C.c_int), ("newton3", C.c_int),
         ("dist_mode", C.c_int), ("rebuild_frequency", C.c_int), ("calc_globals", C.c_int),
         ("tower_sizing", C.c_int), ("traversal", C.c_int), ("atm_nu", C.c_double), ("atm_cutoff", C.c_double),
-        ("use_graphs", C.c_int), ("prune_buffer", C.c_double), ("kernel_variant", C.c_int),
+        ("use_graphs", C.c_int), ("prune_buffer", C.c_double), ("kernel_variant", C.c_int), ("n3_pieces", C.c_int),
     ]
 
 
@@ -138,7 +138,7 @@ class PairEngine:
     def __init__(self, cutoff, skin, boxes, periodic=True, epsilon=(1.0,), sigma=(1.0,), mass=(1.0,),
                  shift=False, precision=PRECISION_MIXED, cluster_size=8, newton3=0, dist_mode=DIST_FMA_SOA,
                  rebuild_frequency=10, calc_globals=True, tower_sizing=1, traversal=1, atm_nu=0.0, atm_cutoff=0.0,
-                 use_graphs=True, prune_buffer=0.0, kernel_variant=0):
+                 use_graphs=True, prune_buffer=0.0, kernel_variant=0, n3_pieces=0):
         L = load()
         self._L = L
         self._eps = np.ascontiguousarray(epsilon, np.float64)
@@ -150,7 +150,7 @@ class PairEngine:
                        self._mass.ctypes.data_as(dp), int(shift), int(precision), int(cluster_size), int(newton3),
                        int(dist_mode), int(rebuild_frequency), int(calc_globals), int(tower_sizing),
                        int(traversal), float(atm_nu), float(atm_cutoff), int(use_graphs), float(prune_buffer),
-                       int(kernel_variant))
+                       int(kernel_variant), int(n3_pieces))
         boxes = list(boxes)
         if np.ndim(boxes[0]) == 1:  # single (bmin, bmax)
             boxes = [boxes]

@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--newton3", type=int, default=-1, help="-1: the tuner may pick newton3; 0 off; 1 required")
     p.add_argument("--prune", type=float, default=0.0, help="rolling-prune buffer of the particle lists (0: off)")
     p.add_argument("--variant", type=int, default=0, help="particle-list kernel variant when the tuner is off")
+    p.add_argument("--n3-pieces", type=int, default=0, help="newton3 evaluation pieces (0: by size)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile", action="store_true", help="small run for ncu: no fp64 leg, no baselines")
@@ -260,7 +261,8 @@ def run_ours(args):
                          newton3=args.newton3 if prec == E.PRECISION_MIXED else 0, rebuild_frequency=REBUILD,
                          calc_globals=True,
                          traversal=args.traversal if prec == E.PRECISION_MIXED or args.traversal < 2 else -1,
-                         prune_buffer=args.prune, use_graphs=use_graphs, kernel_variant=args.variant)
+                         prune_buffer=args.prune, use_graphs=use_graphs, kernel_variant=args.variant,
+                         n3_pieces=args.n3_pieces)
         e.set_particles(pos, vel)
         return e
 
@@ -416,6 +418,10 @@ def run_ours(args):
     fp32_peak = max(E.measure_fp32_peak() for _ in range(3))
     achieved = FLOP_PER_PAIR * pairs_per_launch / (force_ms_per_launch * 1e-3) / 1e12
     kernel = {0: "k_lj_mixed_full", 1: "k_lj_mixed_plist", 2: "k_lj_mixed_n3 + k_n3_finish"}[info["traversal"]]
+    chosen = tuning["chosen"]
+    variant = tuning["candidates"][chosen]["variant"] if chosen >= 0 else args.variant
+    if info["traversal"] == 2 and variant == 3:
+        kernel = "k_lj_mixed_n3_sorted + k_n3_finish"  # each block's pair groups in decreasing order of list length
     line = {
         "metric": metric_name(), "value": value, "unit": "pair interactions/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,

@@ -107,6 +107,9 @@ typedef struct {
                               streamed past the caches.  Traversal 2: 0, 1, 2 cap the registers for 5, 6, 4
                               blocks of 128 threads per SM; 3: 5 blocks, each block's pair groups taken in
                               decreasing order of list length.  The tuner picks its own. */
+  int n3_pieces;           /* newton3: the evaluation in this many pieces of consecutive pair groups (1-8), each
+                              piece's finish (FP64 velocity and position halves) running beside the next pieces'
+                              force kernels; 0: one piece per 160,000 pair groups, at most 8 */
 } pe_config;
 
 /* One particle system of the ensemble. */

@@ -125,14 +125,17 @@ def test_newton3_mixture_with_shift(eng_mod, orc):
     assert g["upot"] == pytest.approx(glob[0], rel=1e-6)
 
 
-def test_newton3_md_steps_follow_the_full_list_path(eng_mod):
+@pytest.mark.parametrize("pieces", [0, 4])
+def test_newton3_md_steps_follow_the_full_list_path(eng_mod, pieces):
     """Forty velocity-Verlet steps with rebuilds, CUDA-graph replay and the fused position update: the newton3
-    trajectory stays within FP32 rounding of the full-list one."""
+    trajectory stays within FP32 rounding of the full-list one, with the evaluation in one piece or in four
+    (force pieces on two streams, each piece's finish on a third after the force pieces up to it)."""
     pos, vel, bmin, bmax = liquid(6, seed=13, jitter=0.02)
     rc, skin, dt = 2.5, 0.3, 0.002
     out = {}
     for t, n3 in ((1, 0), (2, 1)):
-        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, traversal=t, newton3=n3, rebuild_frequency=10)
+        e = eng_mod.PairEngine(rc, skin, (bmin, bmax), periodic=True, traversal=t, newton3=n3, rebuild_frequency=10,
+                               n3_pieces=pieces)
         e.set_particles(pos, vel)
         e.compute_forces()
         g = e.step(dt, 40)[0]
@@ -176,7 +179,8 @@ def test_newton3_configuration_rules(eng_mod):
     assert e.info()["traversal"] == 2 and e.info()["newton3"] == 1
     e.close()
     for kw in (dict(newton3=1, precision=eng_mod.PRECISION_FP64), dict(newton3=1, traversal=1),
-               dict(traversal=2, newton3=0)):
+               dict(traversal=2, newton3=0), dict(traversal=2, newton3=1, n3_pieces=9),
+               dict(traversal=2, newton3=1, n3_pieces=-1)):
         args = dict(periodic=True, traversal=-1)
         args.update(kw)
         with pytest.raises(eng_mod.EngineError) as ei:
