@@ -721,7 +721,8 @@ void launch_plist_build(DeviceState &s, cudaStream_t st) {
 //     only beyond the group (the group's own pair needs no entry); of an image of the same cluster, only for
 //     image codes above kShiftNone (the opposite code gives the same pair).  A j is kept when it lies within the
 //     widened rc+skin threshold of either member, both tested in one packed instruction on the hi parts.
-//     Systems with explicit halo particles use the full lists; this traversal serves periodic systems.
+//     With explicit halo particles, a group of two halos keeps only owned j (a pair of two halos is no pair of the
+//     container); a group with an owned member keeps halo j too.
 // ---------------------------------------------------------------------------------------------
 template <int C>
 __global__ void __launch_bounds__(128) k_glist_build(DeviceState s) {
