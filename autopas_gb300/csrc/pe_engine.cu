@@ -160,6 +160,7 @@ struct pe_engine {
   // towers / clusters
   int64_t ntowers = 0, nclusters = 0;
   DBuf<int32_t> tw_count, tw_start, tw_cl_start, tw_ncl, tw_fill;
+  DBuf<int4> tw_part;  // per tile of 1024 towers: particles, clusters, largest tower
   DBuf<float4> tw_bbf;
   DBuf<double> cl_bb;
   DBuf<float4> cl_bbf;
@@ -928,7 +929,8 @@ static int setup_grids(pe_engine *h) {
                              cudaMemcpyHostToDevice, h->st));
   const size_t nt = (size_t)h->ntowers;
   if (!h->tw_count.ensure(nt) || !h->tw_start.ensure(nt + 1) || !h->tw_cl_start.ensure(nt + 1) ||
-      !h->tw_ncl.ensure(nt) || !h->tw_fill.ensure(nt) || !h->tw_bbf.ensure(nt))
+      !h->tw_ncl.ensure(nt) || !h->tw_fill.ensure(nt) || !h->tw_bbf.ensure(nt) ||
+      !h->tw_part.ensure(nt / 1024 + 1))
     return h->fail(PE_ERR_OOM, "tower arrays (%lld towers)", (long long)nt);
   // slot capacity: every tower can add at most C-1 padding dummies
   h->pcap = h->nuser + (int64_t)nt * (h->C - 1) + 64;
@@ -1080,8 +1082,8 @@ static int do_rebuild(pe_engine *h) {
   PE_CUDA(h, cudaMemcpyAsync(&w->e_steps, h->derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   PE_CUDA(h, cudaMemsetAsync(h->derr.p, 0, sizeof(int), st));
   launch_bin(s, nold, h->key.p, h->tower_of.p, st);
-  if (launch_tower_tables(s, h->tw_ncl.p, h->dmax.p, st)) {
-    h->launches += 2;
+  if (launch_tower_tables(s, h->tw_ncl.p, h->dmax.p, h->tw_part.p, st)) {
+    h->launches += 3;
   } else {
     scan_exclusive_i32(h->tw_count.p, h->tw_start.p, h->ntowers, st);
     launch_clusters_per_tower(s, h->tw_ncl.p, st);
@@ -1562,6 +1564,7 @@ int pe_destroy(pe_engine *h) {
   h->cl_z.release();
   h->cl_bbf.release();
   h->tw_bbf.release();
+  h->tw_part.release();
   h->cp_total.release();
   h->cl_hits.release();
   h->dump_n.release();

@@ -153,11 +153,11 @@ void scan_exclusive_i32(const int32_t *in, int32_t *out, int64_t n, cudaStream_t
 // rebuild (pe_build.cu)
 void launch_bin(DeviceState &s, int64_t nslots_old, uint64_t *key, int32_t *tower_of, cudaStream_t st);
 void launch_clusters_per_tower(DeviceState &s, int32_t *ncl, cudaStream_t st);
-// the tower tables of a rebuild in one single-block launch (tower starts, clusters per tower, cluster starts with
-// the totals at index ntowers, the largest tower into *maxc); false beyond kTowerTablesMax towers, where the
-// caller uses the scans
-constexpr int64_t kTowerTablesMax = 262144;  // 256 towers per thread at most
-bool launch_tower_tables(DeviceState &s, int32_t *ncl, int *maxc, cudaStream_t st);
+// the tower tables of a rebuild in two launches over tiles of 1024 towers (tower starts, clusters per tower,
+// cluster starts with the totals at index ntowers, the largest tower into *maxc); part holds one int4 per tile;
+// false beyond kTowerTablesMax towers, where the caller uses the scans
+constexpr int64_t kTowerTablesMax = 262144;  // 256 tiles at most
+bool launch_tower_tables(DeviceState &s, int32_t *ncl, int *maxc, int4 *part, cudaStream_t st);
 void launch_scatter(DeviceState &s, int64_t nslots_old, const int32_t *tower_of, const uint64_t *key,
                     int32_t *fill, uint64_t *skey, int32_t *sval, cudaStream_t st);
 int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *perm_src, int max_tower,
