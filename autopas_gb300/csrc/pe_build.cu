@@ -357,7 +357,9 @@ int launch_tower_sort(DeviceState &s, uint64_t *skey, int32_t *sval, int32_t *pe
     cudaFuncSetAttribute(k_tower_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, kTowerSortMax * 16);
     attr_set = true;
   }
-  if (s.ntowers > 0) k_tower_sort<<<(unsigned)s.ntowers, 256, sm, st>>>(s, skey, sval, perm_src, p2);
+  // 128 threads: a tower of up to 256 particles takes one pass per bitonic stage, and twice as many towers are
+  // resident per SM as with 256 threads (most threads of which waited at every stage's barrier)
+  if (s.ntowers > 0) k_tower_sort<<<(unsigned)s.ntowers, 128, sm, st>>>(s, skey, sval, perm_src, p2);
   return 0;
 }
 
